@@ -1,0 +1,217 @@
+// sflow_capi.cpp -- the extern "C" boundary declared in include/sflow.h.
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/sflow.h"
+#include "sflow_host.h"
+
+using sflow::HostSetup;
+using sflow::SolverBase;
+
+struct sflow_handle {
+  SolverBase* solver = nullptr;
+  int nx = 0, ny = 0, nv = 0;
+  int precision = 0;
+};
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CHECK_HANDLE(h)                                         \
+  do {                                                          \
+    if (!(h) || !(h)->solver) return fail(SFLOW_EINVAL, "null handle"); \
+  } while (0)
+
+static std::string last_solver_error(const sflow_handle* h);
+
+extern "C" {
+
+const char* sflow_last_error(void) { return g_err.c_str(); }
+
+const char* sflow_build_info(void) {
+  return "sflow GB300: FP64 plain form + FP32 bulk form, N_RK=2, KT fluxes, sm_103a";
+}
+
+void sflow_default_params(SflowParams* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->abi_version = SFLOW_ABI_VERSION;
+  p->precision = SFLOW_PREC_FP64;
+  p->comp_cells_x = 1000;
+  p->comp_cells_y = 1;
+  p->cell_size = 1.0e-3;
+  p->gas_flag = 1;
+  p->solver_scheme = SFLOW_SCHEME_KT;
+  p->n_rk = 2;
+  p->dt0 = 1.0e-4;
+  p->max_dt = 1.0e-3;
+  p->cfl = 0.24;
+  p->theta = 1.0;
+  p->reconstr_coeff = 1.0;
+  for (int i = 0; i < SFLOW_MAX_VARS; ++i) p->limiter[i] = 1;
+  for (int s = 0; s < 4; ++s)
+    for (int i = 0; i < SFLOW_MAX_VARS; ++i) {
+      p->bc[s][i].flag = 1;
+      p->bc[s][i].value = 0.0;
+    }
+  p->grav = 9.81;
+  p->maximum_solid_packing = 0.64;
+  p->A_drag = -1.0;
+  p->B_drag = -1.0;
+  p->r2_source = -1.0;
+  p->arc_width_source = 360.0;
+  p->h_source = -1.0;
+  p->mfr_source = -1.0;
+  for (int i = 0; i < 4; ++i) p->time_param[i] = -1.0;
+  p->t_end = 5.0e-2;
+  p->dt_output = 5.0e-3;
+}
+
+int sflow_create(const SflowParams* p, const double* B_cent, sflow_handle** out) {
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  *out = nullptr;
+  HostSetup s;
+  std::string err;
+  int rc = sflow::host_setup(p, B_cent, s, err);
+  if (rc != SFLOW_OK) return fail(rc, err);
+  SolverBase* sv = (p->precision == SFLOW_PREC_FP32) ? sflow::make_solver_fp32(s, err)
+                                                     : sflow::make_solver_fp64(s, err);
+  if (!sv) return fail(SFLOW_ECUDA, err.empty() ? "device set-up failed" : err);
+  sflow_handle* h = new (std::nothrow) sflow_handle;
+  if (!h) {
+    delete sv;
+    return fail(SFLOW_ENOMEM, "out of host memory");
+  }
+  h->solver = sv;
+  h->nx = s.nx;
+  h->ny = s.ny;
+  h->nv = s.nv;
+  h->precision = p->precision;
+  *out = h;
+  g_err.clear();
+  return SFLOW_OK;
+}
+
+void sflow_destroy(sflow_handle* h) {
+  if (!h) return;
+  delete h->solver;
+  delete h;
+}
+
+#define FORWARD(expr)                                                  \
+  do {                                                                 \
+    int rc_ = (expr);                                                  \
+    if (rc_ < 0) return fail(rc_, last_solver_error(h));               \
+    return rc_;                                                        \
+  } while (0)
+
+}  // extern "C"
+
+static std::string last_solver_error(const sflow_handle* h) {
+  const char* e = h->solver->error();
+  return (e && *e) ? std::string(e) : std::string("solver error");
+}
+
+extern "C" {
+
+int sflow_upload_q(sflow_handle* h, const double* q) {
+  CHECK_HANDLE(h);
+  if (!q) return fail(SFLOW_EINVAL, "q is NULL");
+  FORWARD(h->solver->upload(q));
+}
+int sflow_download_q(sflow_handle* h, double* q) {
+  CHECK_HANDLE(h);
+  if (!q) return fail(SFLOW_EINVAL, "q is NULL");
+  FORWARD(h->solver->download(q));
+}
+int sflow_download_qp(sflow_handle* h, double* qp) {
+  CHECK_HANDLE(h);
+  if (!qp) return fail(SFLOW_EINVAL, "qp is NULL");
+  FORWARD(h->solver->download_qp(qp));
+}
+int sflow_download_maps(sflow_handle* h, double* a, double* b, double* c) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->download_maps(a, b, c));
+}
+int sflow_check_solve(sflow_handle* h, int32_t solve_all) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->check_solve(solve_all));
+}
+int sflow_timestep(sflow_handle* h, double* dt) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->timestep(dt));
+}
+int sflow_imex_rk(sflow_handle* h, double t, double dt) {
+  CHECK_HANDLE(h);
+  if (!(dt > 0.0)) return fail(SFLOW_EINVAL, "dt must be > 0");
+  FORWARD(h->solver->imex_rk(t, dt));
+}
+int sflow_erosion_deposition(sflow_handle* h, double dt) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->erosion_deposition(dt));
+}
+int sflow_post_step(sflow_handle* h, SflowStepStats* s) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->post_step(s));
+}
+int sflow_step(sflow_handle* h) {
+  CHECK_HANDLE(h);
+  int rc = h->solver->step();
+  if (rc < 0) return fail(rc, last_solver_error(h));
+  uint32_t f = 0;
+  rc = h->solver->status(&f);
+  if (rc < 0) return fail(rc, last_solver_error(h));
+  return (int)f;
+}
+int sflow_advance(sflow_handle* h, double t_stop, int64_t max_steps, SflowStepStats* s) {
+  CHECK_HANDLE(h);
+  int rc = h->solver->advance(t_stop, max_steps, s);
+  if (rc < 0) return fail(rc, last_solver_error(h));
+  uint32_t f = 0;
+  rc = h->solver->status(&f);
+  if (rc < 0) return fail(rc, last_solver_error(h));
+  return (int)f;
+}
+int sflow_get_stats(sflow_handle* h, SflowStepStats* s) {
+  CHECK_HANDLE(h);
+  if (!s) return fail(SFLOW_EINVAL, "stats is NULL");
+  FORWARD(h->solver->stats(s));
+}
+int sflow_status(sflow_handle* h, uint32_t* f) {
+  CHECK_HANDLE(h);
+  if (!f) return fail(SFLOW_EINVAL, "flags is NULL");
+  FORWARD(h->solver->status(f));
+}
+int sflow_clear_status(sflow_handle* h) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->clear_status());
+}
+int64_t sflow_launch_count(const sflow_handle* h) {
+  return (h && h->solver) ? h->solver->launches() : -1;
+}
+int64_t sflow_device_bytes(const sflow_handle* h) {
+  return (h && h->solver) ? h->solver->device_bytes() : -1;
+}
+int sflow_counters(sflow_handle* h, int64_t* cell_updates, int64_t* steps, int64_t* newton_iters,
+                   int32_t* newton_max) {
+  CHECK_HANDLE(h);
+  SflowStepStats s;
+  int rc = h->solver->stats(&s);
+  if (rc < 0) return fail(rc, last_solver_error(h));
+  int64_t tot = 0;
+  int mx = 0;
+  rc = h->solver->newton_stats(&tot, &mx);
+  if (rc < 0) return fail(rc, last_solver_error(h));
+  if (cell_updates) *cell_updates = h->solver->cells_total();
+  if (steps) *steps = s.steps;
+  if (newton_iters) *newton_iters = tot;
+  if (newton_max) *newton_max = mx;
+  return SFLOW_OK;
+}
+
+}  // extern "C"

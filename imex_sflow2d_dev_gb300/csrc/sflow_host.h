@@ -1,0 +1,70 @@
+// sflow_host.h -- host-side set-up shared by the FP64 and FP32 solvers.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/sflow.h"
+
+namespace sflow {
+
+// Everything the device solver needs, derived on the host from
+// SflowParams + B_cent the way the reference's init sequence does
+// (read_param, init_grid, topography_reconstruction, init_source).
+struct HostSetup {
+  SflowParams p;
+  int nx = 0, ny = 0, nv = 0, ns = 0, nrk = 0;
+  double dx = 0, dy = 0, eps_sing = 0, eps_sing4 = 0;
+  double rho_a_amb = 0, kin_visc_c = 0, rho_c_sub = 0, T_erodible = 300.0;
+  double h_source = 0, time_param[4] = {0, 0, 0, 0};
+  double src_rho_m = 0, src_cp_mix = 0;
+  double pi_g = 0;
+  // tableau (solver_2d.f90:399-487), row-major [i][j] of a 4x4 block
+  double a_tilde[16] = {0}, a_dirk[16] = {0}, omega_tilde[4] = {0}, omega[4] = {0};
+  int take_last = 0;
+  // per-cell fields, row-major [k][j] (k = y index)
+  std::vector<double> Bx, By, Bxx, Bxy, Byy, gc, dgcx, dgcy;
+  std::vector<uint8_t> cflags;                 // source_cell | E<<2 | W<<3 | N<<4 | S<<5
+  std::vector<double> arc_perim, arc_nx, arc_ny;
+  int64_t ring_cells = 0;
+};
+
+// Validates p and fills s; returns 0 or SFLOW_EINVAL with a message in err.
+int host_setup(const SflowParams* p, const double* B_cent, HostSetup& s, std::string& err);
+
+// Reference mixt_var (constitutive_2d.f90:1342-1492) in FP64 on the host,
+// used for constants of the run (inlet state).
+void host_mixt_var(const HostSetup& s, const double* qp, double* rho_m, double* cp_mix);
+
+// Largest float not greater than x: `f > thr` on floats equals the FP64
+// test `(double)f > x`.
+float float_below(double x);
+
+class SolverBase {
+ public:
+  virtual ~SolverBase() {}
+  virtual int upload(const double* q_aos) = 0;
+  virtual int download(double* q_aos) = 0;
+  virtual int download_qp(double* qp_aos) = 0;
+  virtual int download_maps(double* h, double* p, double* v) = 0;
+  virtual int check_solve(int solve_all) = 0;
+  virtual int timestep(double* dt_out) = 0;
+  virtual int imex_rk(double t, double dt) = 0;
+  virtual int erosion_deposition(double dt) = 0;
+  virtual int post_step(SflowStepStats* s) = 0;
+  virtual int step() = 0;
+  virtual int advance(double t_stop, int64_t max_steps, SflowStepStats* s) = 0;
+  virtual int stats(SflowStepStats* s) = 0;
+  virtual int status(uint32_t* f) = 0;
+  virtual int clear_status() = 0;
+  virtual int64_t launches() const = 0;
+  virtual int64_t device_bytes() const = 0;
+  virtual int newton_stats(int64_t* total, int* maxit) = 0;
+  virtual int64_t cells_total() = 0;
+  virtual const char* error() const = 0;
+};
+
+SolverBase* make_solver_fp64(const HostSetup& s, std::string& err);
+SolverBase* make_solver_fp32(const HostSetup& s, std::string& err);
+
+}  // namespace sflow

@@ -1,0 +1,811 @@
+// sflow_physics.cuh -- per-cell and per-face physics of the IMEX_SfloW2D
+// time step as device functions, templated on the bulk arithmetic type.
+//
+//   Real = double : plain FP64 form.  Operation order follows the reference
+//                   routine by routine; the translation unit is compiled with
+//                   --fmad=false so no FMA changes the rounding.
+//   Real = float  : FP32 bulk form.  State, reconstruction, fluxes and
+//                   explicit sources in FP32; the implicit Newton solve, the
+//                   wet/dry thresholds and the mass sums stay FP64.
+//
+// Each function cites the reference routine (path:line inside the reference
+// project) it restates.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "sflow_types.cuh"
+
+namespace sflow {
+
+constexpr double kEps = DBL_EPSILON;  // EPSILON(1.0_wp)
+
+template <class R>
+__device__ __forceinline__ R cst(double x) { return static_cast<R>(x); }
+
+template <class R>
+__device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
+template <class R>
+__device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+template <class R>
+__device__ __forceinline__ R sq(R a) { return a * a; }
+
+// ---------------------------------------------------------------------------
+// geometry_2d.f90:1855-1876 minmod, 1878-1897 maxmod, 1776-1841 limit
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ R minmod(R a, R b) {
+  R aa = fabs(a), ab = fabs(b);
+  if (rmin(aa, ab) <= R(0)) return R(0);
+  R sa = a / aa, sb = b / ab;
+  return cst<R>(0.5) * (sa + sb) * rmin(aa, ab);
+}
+template <class R>
+__device__ __forceinline__ R maxmod(R a, R b) {
+  if (fabs(a * b) <= R(0)) return R(0);
+  R sa = a / fabs(a), sb = b / fabs(b);
+  return cst<R>(0.5) * (sa + sb) * rmax(fabs(a), fabs(b));
+}
+template <class R>
+__device__ __forceinline__ R limit(R v0, R v1, R v2, R z0, R z1, R z2, int lim, R theta) {
+  R a = (v2 - v1) / (z2 - z1);
+  R b = (v1 - v0) / (z1 - z0);
+  switch (lim) {
+    case 0: return R(0);
+    case 1: return minmod(a, b);
+    case 2: return maxmod(minmod(a, cst<R>(2.0) * b), minmod(cst<R>(2.0) * a, b));
+    case 3: { R c = (v2 - v0) / (z2 - z0); return minmod(c, theta * minmod(a, b)); }
+    case 4: { R c = (v2 - v0) / (z2 - z0); return minmod(c, cst<R>(2.0) * minmod(a, b)); }
+    case 5: return (v2 - v0) / (z2 - z0);
+    case 6: return a;
+    case 7: return b;
+  }
+  return R(0);
+}
+
+// ---------------------------------------------------------------------------
+// constitutive_2d.f90:550-976 r_phys_var + 1637-1690 qc_to_qp
+// qp = (h, hu, hv, T, alphas or h*alphas ..., u, v); returns p_dyn
+// ---------------------------------------------------------------------------
+template <class R, int NS>
+__device__ __forceinline__ R qc_to_qp(const Phys<R>& P, const R* q, R* qp) {
+  constexpr int ns = NS, nv = 4 + NS;
+  R xs[kMaxSolid];
+  R inv_qj1;
+  if (q[0] > P.thr_eps) {
+    inv_qj1 = R(1) / q[0];
+    R sq_ = R(0);
+    for (int i = 0; i < ns; ++i) { xs[i] = q[4 + i] * inv_qj1; sq_ += q[4 + i]; }
+    if (sq_ == q[0]) {
+      R s = R(0);
+      for (int i = 0; i < ns; ++i) s += xs[i];
+      for (int i = 0; i < ns; ++i) xs[i] = xs[i] / s;
+    }
+  } else {
+    for (int i = 0; i < nv + 2; ++i) qp[i] = R(0);
+    qp[3] = P.T_ambient;
+    return R(0);
+  }
+  R xs_tot = R(0);
+  for (int i = 0; i < ns; ++i) xs_tot += xs[i];
+  R xc = R(1) - xs_tot;
+  R cbyxc = P.gas ? ((xc - R(0)) * P.sp_heat_a + R(0)) : P.sp_heat_l * xc;
+  R dcp = R(0);
+  for (int i = 0; i < ns; ++i) dcp += xs[i] * P.sp_heat_s[i];
+  R cmix = dcp + cbyxc;
+  R T;
+  if (q[0] > P.thr_eps_sing) {
+    if (P.energy) T = (q[3] - cst<R>(0.5) * (sq(q[1]) + sq(q[2])) * inv_qj1) / (q[0] * cmix);
+    else T = q[3] / (q[0] * cmix);
+    if (T <= R(0)) T = P.T_ambient;
+  } else {
+    T = P.T_ambient;
+  }
+  R inv_rho_c;
+  if (P.gas) {
+    R Rc = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_gas_const_a + R(0)) / xc : P.sp_gas_const_a;
+    inv_rho_c = Rc * T * P.inv_pres;
+  } else {
+    inv_rho_c = P.inv_rho_l;
+  }
+  R dinv = R(0);
+  for (int i = 0; i < ns; ++i) dinv += xs[i] * P.inv_rho_s[i];
+  R inv_rhom = dinv + xc * inv_rho_c;
+  R rho_m = R(1) / inv_rhom;
+  R h = q[0] * inv_rhom;
+  R u, v;
+  if (q[0] > P.thr_eps_sing) {
+    u = q[1] * inv_qj1;
+    v = q[2] * inv_qj1;
+  } else {
+    R q12 = q[0] * q[0];
+    R den = sqrt(q12 * q12 + P.eps_sing4);
+    u = P.sqrt2 * q[0] * q[1] / den;
+    v = P.sqrt2 * q[0] * q[2] / den;
+  }
+  qp[0] = h;
+  qp[1] = h * u;
+  qp[2] = h * v;
+  qp[3] = T;
+  for (int i = 0; i < ns; ++i) {
+    R al = xs[i] * rho_m * P.inv_rho_s[i];
+    qp[4 + i] = P.alpha ? al : al * h;
+  }
+  qp[nv] = u;
+  qp[nv + 1] = v;
+  return cst<R>(0.5) * rho_m * (sq(u) + sq(v));
+}
+
+// constitutive_2d.f90:1718-2149 qp_to_qc (vertical profiles off)
+template <class R, int NS>
+__device__ __forceinline__ void qp_to_qc(const Phys<R>& P, const R* qp, R* qc) {
+  constexpr int ns = NS, nv = 4 + NS;
+  R r_h = qp[0];
+  if (!(r_h > P.thr_eps)) {
+    for (int i = 0; i < nv; ++i) qc[i] = R(0);
+    return;
+  }
+  R r_hu = qp[1], r_hv = qp[2], r_u = qp[nv], r_v = qp[nv + 1], r_T = qp[3];
+  R arhos[kMaxSolid];
+  R at = R(0);
+  for (int i = 0; i < ns; ++i) {
+    R al = P.alpha ? qp[4 + i] : qp[4 + i] / qp[0];
+    at += al;
+    arhos[i] = al * P.rho_s[i];
+  }
+  R rho_c;
+  if (P.gas) {
+    R rho_a = P.pres / (P.sp_gas_const_a * r_T);
+    rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
+  } else {
+    rho_c = P.rho_l;
+  }
+  R alphac = R(1) - at;
+  R sa = R(0);
+  for (int i = 0; i < ns; ++i) sa += arhos[i];
+  R rho_m = alphac * rho_c + sa;
+  R inv_rhom = R(1) / rho_m;
+  R xc = alphac * rho_c * inv_rhom;
+  R cp_c;
+  if (P.gas) cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
+  else cp_c = P.sp_heat_l;
+  R dcp = R(0);
+  for (int i = 0; i < ns; ++i) dcp += (arhos[i] * inv_rhom) * P.sp_heat_s[i];
+  R cmix = dcp + xc * cp_c;
+  qc[0] = rho_m * r_h;
+  qc[1] = rho_m * r_hu;
+  qc[2] = rho_m * r_hv;
+  if (P.energy) {
+    qc[3] = (r_h > R(0)) ? r_h * rho_m * (cmix * r_T + cst<R>(0.5) * (sq(r_u) + sq(r_v))) : R(0);
+  } else {
+    qc[3] = r_h * rho_m * cmix * r_T;
+  }
+  for (int i = 0; i < ns; ++i) qc[4 + i] = (arhos[i] * inv_rhom) * qc[0];
+}
+
+// constitutive_2d.f90:1342-1492 mixt_var (+1513-1607 eval_sp_heat)
+template <class R>
+struct Mixt {
+  R Ri, rho_m, rho_c, red_grav, cp_c, cp_mix;
+};
+
+template <class R, int NS>
+__device__ __forceinline__ Mixt<R> mixt_var(const Phys<R>& P, const R* qpj, bool sp_heat_flag) {
+  constexpr int ns = NS, nv = 4 + NS;
+  Mixt<R> m;
+  R r_h = qpj[0];
+  if (!(qpj[0] > P.thr_eps)) {
+    m.red_grav = R(0); m.rho_m = P.rho_a_amb; m.rho_c = P.rho_a_amb;
+    m.cp_c = P.liquid ? P.sp_heat_l : P.sp_heat_a;
+    m.cp_mix = m.cp_c;
+    m.Ri = R(0);
+    return m;
+  }
+  R r_u = qpj[nv], r_v = qpj[nv + 1], r_T = qpj[3];
+  R al[kMaxSolid];
+  R at = R(0);
+  for (int i = 0; i < ns; ++i) { al[i] = P.alpha ? qpj[4 + i] : qpj[4 + i] / qpj[0]; at += al[i]; }
+  R rho_c;
+  if (P.gas) {
+    R rho_a = P.pres / (P.sp_gas_const_a * r_T);
+    rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
+  } else {
+    rho_c = P.rho_l;
+  }
+  R d = R(0);
+  for (int i = 0; i < ns; ++i) d += al[i] * P.rho_s[i];
+  R rho_m = (R(1) - at) * rho_c + d;
+  R inv_rhom = R(1) / rho_m;
+  R red_grav = (rho_m - P.rho_a_amb) / rho_m * P.grav;
+  R u2 = sq(r_u) + sq(r_v);
+  m.Ri = (u2 > R(0)) ? rmin(cst<R>(1.0e15), red_grav * r_h / u2) : R(0);
+  m.rho_m = rho_m;
+  m.rho_c = rho_c;
+  m.red_grav = red_grav;
+  m.cp_c = R(0);
+  m.cp_mix = R(0);
+  if (sp_heat_flag) {
+    R xs[kMaxSolid];
+    R sxs = R(0);
+    for (int i = 0; i < ns; ++i) { xs[i] = al[i] * P.rho_s[i] * inv_rhom; sxs += xs[i]; }
+    R xc = R(1) - sxs;
+    R cp_c;
+    if (P.gas) cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
+    else cp_c = P.sp_heat_l;
+    R dcp = R(0);
+    for (int i = 0; i < ns; ++i) dcp += xs[i] * P.sp_heat_s[i];
+    m.cp_c = cp_c;
+    m.cp_mix = dcp + xc * cp_c;
+  }
+  return m;
+}
+
+// constitutive_2d.f90:2203-2307 eval_local_speeds_x / _y.  dir 1 = x, 2 = y.
+template <class R, int NS>
+__device__ __forceinline__ void local_speeds(const Phys<R>& P, const R* qpj, R red_grav, R gc,
+                                             int dir, R& vmin, R& vmax) {
+  constexpr int nv = 4 + NS;
+  R r_h = qpj[0];
+  R vel = (dir == 1) ? qpj[nv] : qpj[nv + 1];
+  if (red_grav * r_h < R(0)) {
+    vmin = vel; vmax = vel;
+  } else {
+    R c = (dir == 1) ? sqrt(red_grav * r_h * gc) : sqrt(gc * red_grav * r_h);
+    vmin = vel - c; vmax = vel + c;
+  }
+}
+
+// constitutive_2d.f90:2325-2518 eval_fluxes (vertical profiles off); the
+// mixture state m is the mixt_var of qpj (only evaluated when h > eps).
+template <class R, int NS>
+__device__ __forceinline__ void eval_fluxes(const Phys<R>& P, const R* qcj, const R* qpj,
+                                            const Mixt<R>& m, R gc, int dir, R* flux) {
+  constexpr int ns = NS, nv = 4 + NS;
+  if (qpj[0] > P.thr_eps) {
+    R r_h = qpj[0];
+    R vel = (dir == 1) ? qpj[nv] : qpj[nv + 1];
+    R pterm = cst<R>(0.5) * m.rho_m * gc * m.red_grav * sq(r_h);
+    flux[0] = vel * qcj[0] * R(1);
+    if (dir == 1) {
+      flux[1] = vel * qcj[1] * R(1) + pterm;
+      flux[2] = vel * qcj[2] * R(1);
+    } else {
+      flux[1] = vel * qcj[1] * R(1);
+      flux[2] = vel * qcj[2] * R(1) + pterm;
+    }
+    flux[3] = P.energy ? vel * (qcj[3] * R(1) + pterm) : vel * qcj[3] * R(1);
+    for (int i = 0; i < ns; ++i) flux[4 + i] = vel * qcj[4 + i] * R(1);
+    if (ns > 0 && flux[0] > R(0)) {
+      R s = R(0);
+      for (int i = 0; i < ns; ++i) s += flux[4 + i];
+      if (s / flux[0] > R(1))
+        for (int i = 0; i < ns; ++i) flux[4 + i] = flux[4 + i] / s * flux[0];
+    }
+  } else {
+    for (int i = 0; i < nv; ++i) flux[i] = R(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// constitutive_2d.f90:3024-3431 eval_expl_terms (gravity/slope terms and the
+// lateral ring inlet; no bottom radial source)
+// ---------------------------------------------------------------------------
+template <class R, int NS>
+__device__ __forceinline__ void expl_terms(const Phys<R>& P, const Geo<R>& g, const R* qpj,
+                                           R t_coeff_src, R arc_perim, R arc_nx, R arc_ny,
+                                           R* e) {
+  constexpr int ns = NS, nv = 4 + NS;
+  for (int i = 0; i < nv; ++i) e[i] = R(0);
+  if (!(qpj[0] > P.thr_eps) && arc_perim == R(0)) return;
+  if (qpj[0] > P.thr_eps) {
+    R r_h = qpj[0], r_u = qpj[nv], r_v = qpj[nv + 1];
+    Mixt<R> m = mixt_var<R, NS>(P, qpj, true);
+    R centr = P.curv ? (g.Bxx * sq(r_u) + cst<R>(2.0) * g.Bxy * r_u * r_v + g.Byy * sq(r_v)) : R(0);
+    R tg = m.red_grav + centr;
+    e[1] = -g.gc * m.rho_m * tg * r_h * g.Bx + cst<R>(0.5) * m.rho_m * m.red_grav * sq(r_h) * g.dgcx;
+    e[2] = -g.gc * m.rho_m * tg * r_h * g.By + cst<R>(0.5) * m.rho_m * m.red_grav * sq(r_h) * g.dgcy;
+    e[3] = P.energy ? (e[1] * r_u + e[2] * r_v) : R(0);
+  }
+  if (P.radial_source && arc_perim > R(0) && P.h_source > R(0)) {
+    R t_coeff = t_coeff_src;
+    if (t_coeff > R(0)) {
+      R h_dot = P.h_source * P.vel_source * arc_perim / P.cell_area;
+      e[0] = e[0] + t_coeff * h_dot * P.src_rho_m;
+      e[1] = e[1] + t_coeff * h_dot * P.src_rho_m * P.vel_source * arc_nx;
+      e[2] = e[2] + t_coeff * h_dot * P.src_rho_m * P.vel_source * arc_ny;
+      e[3] = e[3] + t_coeff * h_dot * P.src_rho_m * P.src_cp_mix * P.T_source;
+      for (int i = 0; i < ns; ++i)
+        e[4 + i] = e[4 + i] + t_coeff * h_dot * P.alphas_source[i] * P.rho_s[i];
+    }
+  }
+}
+
+// time factor of the ring inlet (constitutive_2d.f90:3320-3349), FP64
+__device__ __forceinline__ double source_time_coeff(const double* tp, double pi_g, double time) {
+  double t_coeff;
+  if (time >= tp[3]) {
+    if (tp[2] > 0.0 && time < tp[3] + tp[2]) t_coeff = 0.5 * (1.0 + cos(pi_g * (time - tp[3]) / tp[2]));
+    else t_coeff = 0.0;
+  } else {
+    double t_rem = fmod(time, tp[0]);
+    t_coeff = 0.0;
+    if (tp[2] == 0.0) {
+      if (t_rem <= tp[1]) t_coeff = 1.0;
+    } else {
+      if (t_rem < tp[2]) t_coeff = 0.5 * (1.0 - cos(pi_g * t_rem / tp[2]));
+      else if (t_rem <= tp[1] - tp[2]) t_coeff = 1.0;
+      else if (t_rem <= tp[1]) t_coeff = 0.5 * (1.0 + cos(pi_g * ((t_rem - tp[1]) / tp[2] + 1.0)));
+    }
+  }
+  return t_coeff;
+}
+
+// ---------------------------------------------------------------------------
+// constitutive_2d.f90:4027-4547 eval_nh_semi_impl_terms (rheology 1); FP64
+// ---------------------------------------------------------------------------
+template <class R, int NS>
+__device__ __forceinline__ void semi_impl_terms(const Phys<R>& P, const Geo<R>& g, const R* qpj,
+                                                R* si) {
+  constexpr int nv = 4 + NS;
+  for (int i = 0; i < nv; ++i) si[i] = R(0);
+  if (!P.rheo) return;
+  R r_h = qpj[0], r_u = qpj[nv], r_v = qpj[nv + 1];
+  Mixt<R> m = mixt_var<R, NS>(P, qpj, false);
+  R r_w = P.slope_corr ? (r_u * g.Bx + r_v * g.By) : R(0);
+  R mod_vel = sqrt(sq(r_u) + sq(r_v) + sq(r_w));
+  if (P.rheo_model == 1 && mod_vel > R(0)) {
+    R centr = P.curv ? (g.Bxx * sq(r_u) + cst<R>(2.0) * g.Bxy * r_u * r_v + g.Byy * sq(r_v)) : R(0);
+    R tt = P.mu * m.rho_m * (m.red_grav + centr) * r_h * sqrt(g.gc);
+    tt = rmax(R(0), tt);
+    si[1] = si[1] - tt * r_u / mod_vel;
+    si[2] = si[2] - tt * r_v / mod_vel;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Implicit friction (constitutive_2d.f90:3513-4009, rheology 1 and 6) with
+// the gas-density / temperature closure of c_phys_var (1154-1322), written
+// once over a number type N: double for the residual, Dual2 for the two
+// Jacobian columns d/d(hu), d/d(hv).  This replaces the complex-step
+// derivative of solver_2d.f90:2302-2367: forward-mode derivatives are exact
+// for these rational/sqrt expressions, as the complex step is.
+// ---------------------------------------------------------------------------
+struct Dual2 {
+  double v, d0, d1;
+  __device__ Dual2() {}
+  __device__ Dual2(double x) : v(x), d0(0.0), d1(0.0) {}
+  __device__ Dual2(double x, double a, double b) : v(x), d0(a), d1(b) {}
+};
+__device__ __forceinline__ Dual2 operator+(Dual2 a, Dual2 b) { return Dual2(a.v + b.v, a.d0 + b.d0, a.d1 + b.d1); }
+__device__ __forceinline__ Dual2 operator-(Dual2 a, Dual2 b) { return Dual2(a.v - b.v, a.d0 - b.d0, a.d1 - b.d1); }
+__device__ __forceinline__ Dual2 operator-(Dual2 a) { return Dual2(-a.v, -a.d0, -a.d1); }
+__device__ __forceinline__ Dual2 operator*(Dual2 a, Dual2 b) {
+  return Dual2(a.v * b.v, a.d0 * b.v + a.v * b.d0, a.d1 * b.v + a.v * b.d1);
+}
+__device__ __forceinline__ Dual2 operator/(Dual2 a, Dual2 b) {
+  double r = a.v / b.v;
+  double ib = 1.0 / b.v;
+  return Dual2(r, (a.d0 - r * b.d0) * ib, (a.d1 - r * b.d1) * ib);
+}
+__device__ __forceinline__ Dual2 dsqrt(Dual2 a) {
+  double s = sqrt(a.v);
+  double h = (s > 0.0) ? 0.5 / s : 0.0;
+  return Dual2(s, a.d0 * h, a.d1 * h);
+}
+__device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ double val(double a) { return a; }
+__device__ __forceinline__ double val(Dual2 a) { return a.v; }
+
+template <class N, int NS>
+__device__ __forceinline__ void implicit_terms(const Phys<double>& P, double Bx, double By,
+                                               const N* q, N& nh1, N& nh2) {
+  nh1 = N(0.0);
+  nh2 = N(0.0);
+  if (!P.rheo) return;
+  constexpr int ns = NS;
+  // c_phys_var
+  N h, u, v, T, rho_m;
+  if (val(q[0]) > kEps) {
+    N inv_cqj1 = N(1.0) / q[0];
+    N xs_tot = N(0.0), dcp = N(0.0), dinv = N(0.0);
+    for (int i = 0; i < ns; ++i) {
+      N xs = q[4 + i] * inv_cqj1;
+      xs_tot = xs_tot + xs;
+    }
+    for (int i = 0; i < ns; ++i) {
+      N xs = q[4 + i] * inv_cqj1;
+      dcp = dcp + xs * N(P.sp_heat_s[i]);
+      dinv = dinv + xs * N(P.inv_rho_s[i]);
+    }
+    N xc = N(1.0) - xs_tot;
+    N cp_c = P.gas ? ((xc - N(0.0)) * N(P.sp_heat_a) + N(0.0)) / xc : N(P.sp_heat_l);
+    N cmix = dcp + xc * cp_c;
+    if (val(q[0]) > P.eps_sing_d) {
+      if (P.energy) T = (q[3] - N(0.5) * (q[1] * q[1] + q[2] * q[2]) * inv_cqj1) / (q[0] * cmix);
+      else T = q[3] / (q[0] * cmix);
+      if (val(T) <= 0.0) T = N(P.T_ambient);
+    } else {
+      T = N(P.T_ambient);
+    }
+    N inv_rho_c;
+    if (P.gas) {
+      N Rc = ((xc - N(0.0)) * N(P.sp_gas_const_a) + N(0.0)) / xc;
+      inv_rho_c = Rc * T * N(P.inv_pres);
+    } else {
+      inv_rho_c = N(P.inv_rho_l);
+    }
+    N inv_rhom = dinv + xc * inv_rho_c;
+    rho_m = N(1.0) / inv_rhom;
+    h = q[0] * inv_rhom;
+    if (val(q[0]) > P.eps_sing_d) {
+      u = q[1] * inv_cqj1;
+      v = q[2] * inv_cqj1;
+    } else {
+      N q4 = q[0] * q[0];
+      q4 = q4 * q4;
+      N den = dsqrt(q4 + N(P.eps_sing4));
+      u = N(P.sqrt2) * q[0] * q[1] / den;
+      v = N(P.sqrt2) * q[0] * q[2] / den;
+    }
+  } else {
+    return;  // h = u = v = 0: mod_vel = 0, no friction
+  }
+  N red_grav = (rho_m - N(P.rho_a_amb)) / rho_m * N(P.grav);
+  N w = P.slope_corr ? (u * N(Bx) + v * N(By)) : N(0.0);
+  N mod_vel2 = u * u + v * v + w * w;
+  N mod_vel = dsqrt(mod_vel2);
+  if (val(mod_vel) != 0.0) {
+    if (P.rheo_model == 1) {
+      N turb = rho_m * red_grav / N(P.xi) * mod_vel2;
+      nh1 = nh1 - turb * (u / mod_vel);
+      nh2 = nh2 - turb * (v / mod_vel);
+    } else if (P.rheo_model == 6) {
+      N mod_vel_hor = dsqrt(u * u + v * v);
+      nh1 = nh1 - rho_m * (u / mod_vel_hor) * N(P.friction_factor) * mod_vel2;
+      nh2 = nh2 - rho_m * (v / mod_vel_hor) * N(P.friction_factor) * mod_vel2;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// solver_2d.f90:1662-1996 solve_rk_step, 2021-2226 lnsrch, 2245-2284 eval_f
+// (normalize_q = T, normalize_f = F, opt_search_NL = T; implicit set {hu,hv})
+// ---------------------------------------------------------------------------
+struct NewtonCtx {
+  const Phys<double>* P;
+  double dt, a_diag, Bx, By;
+  const double* q_old;
+  const double* Rj;
+};
+
+template <int NS>
+__device__ __forceinline__ void newton_eval_f(const NewtonCtx& c, const double* qj, double* f,
+                                              double& scal_f) {
+  constexpr int nv = 4 + NS;
+  double nh1, nh2;
+  implicit_terms<double, NS>(*c.P, c.Bx, c.By, qj, nh1, nh2);
+  double s = 0.0;
+  for (int i = 0; i < nv; ++i) {
+    double nh = (i == 1) ? nh1 : (i == 2) ? nh2 : 0.0;
+    double Rj = c.Rj[i] - c.a_diag * nh;
+    f[i] = qj[i] - c.q_old[i] + c.dt * Rj;
+  }
+  for (int i = 0; i < nv; ++i) s += f[i] * f[i];
+  scal_f = 0.5 * s;
+}
+
+// Jacobian of f with respect to qj_rel for the implicit columns 1, 2:
+// J(k,i) = d f_k / d qrel_i = qj_org_i * (delta_ki - dt a_diag dNH_k/dq_i)
+template <int NS>
+__device__ __forceinline__ void newton_jacobian(const NewtonCtx& c, const double* qj,
+                                                const double* qj_org, double& s11, double& s12,
+                                                double& s21, double& s22) {
+  constexpr int nv = 4 + NS;
+  Dual2 qd[kMaxVars];
+  for (int i = 0; i < nv; ++i) qd[i] = Dual2(qj[i]);
+  qd[1].d0 = 1.0;
+  qd[2].d1 = 1.0;
+  Dual2 n1, n2;
+  implicit_terms<Dual2, NS>(*c.P, c.Bx, c.By, qd, n1, n2);
+  const double k = c.dt * c.a_diag;
+  s11 = qj_org[1] - k * (n1.d0 * qj_org[1]);
+  s12 = -k * (n1.d1 * qj_org[2]);
+  s21 = -k * (n2.d0 * qj_org[1]);
+  s22 = qj_org[2] - k * (n2.d1 * qj_org[2]);
+}
+
+// returns iterations used (kMaxNewton+1 when the limit was reached)
+template <int NS>
+__device__ int solve_rk_step(const NewtonCtx& c, double* qj) {
+  constexpr int nv = 4 + NS;
+  const double STPMX = 100.0, TOLF = 1.0e-10, TOLMIN = 1.0e-6, TOLX = kEps;
+  double qj_org[kMaxVars], qj_rel[kMaxVars], f[kMaxVars], p[kMaxVars], g[kMaxVars],
+      x_old[kMaxVars], qt[kMaxVars];
+  double scal_f, scal_f_old;
+  bool check = false;
+  for (int i = 0; i < nv; ++i) {
+    g[i] = 0.0;
+    qj_org[i] = rmax(fabs(qj[i]), 1.0e-3);
+    qj_rel[i] = qj[i] / qj_org[i];
+  }
+  for (int it = 1; it <= kMaxNewton; ++it) {
+    newton_eval_f<NS>(c, qj, f, scal_f);
+    double mf = 0.0;
+    for (int i = 0; i < nv; ++i) mf = rmax(mf, fabs(f[i]));
+    if (mf < TOLF) return it;
+    double s11, s12, s21, s22;
+    newton_jacobian<NS>(c, qj, qj_org, s11, s12, s21, s22);
+    // explicit rows: diagonal qj_org (mask11); coupling mask21 is zero
+    for (int i = 0; i < nv; ++i) p[i] = (i == 1 || i == 2) ? 0.0 : -(f[i] / qj_org[i]) + 0.0;
+    double d2a = f[1], d2b = f[2];
+    for (int i = 0; i < nv; ++i) {
+      if (i == 1 || i == 2) continue;
+      d2a = d2a - (f[i] / qj_org[i]) * 0.0;
+      d2b = d2b - (f[i] / qj_org[i]) * 0.0;
+    }
+    double inv_det = 1.0 / (s11 * s22 - s21 * s12);
+    p[1] = -((d2a * s22 - d2b * s12) * inv_det) + 0.0;
+    p[2] = -((s11 * d2b - s21 * d2a) * inv_det) + 0.0;
+    for (int i = 0; i < nv; ++i) x_old[i] = qj_rel[i];
+    scal_f_old = scal_f;
+    if (it > 1) {
+      double nr = 0.0;
+      for (int i = 0; i < nv; ++i) nr += qj_rel[i] * qj_rel[i];
+      double stpmax = STPMX * rmax(sqrt(nr), double(nv));
+      // grad_f = right_term . left_matrix: explicit columns diag qj_org
+      for (int i = 0; i < nv; ++i) g[i] = (i == 1 || i == 2) ? 0.0 : f[i] * qj_org[i];
+      g[1] = f[1] * s11 + f[2] * s21;
+      g[2] = f[1] * s12 + f[2] * s22;
+      // lnsrch
+      check = false;
+      double nrm = 0.0;
+      for (int i = 0; i < nv; ++i) nrm += p[i] * p[i];
+      nrm = sqrt(nrm);
+      if (nrm > stpmax)
+        for (int i = 0; i < nv; ++i) p[i] = p[i] * stpmax / nrm;
+      double slope = 0.0;
+      for (int i = 0; i < nv; ++i) slope += g[i] * p[i];
+      double mx = 0.0;
+      for (int i = 0; i < nv; ++i) {
+        double t = fabs(p[i]) / rmax(fabs(x_old[i]), 1.0);
+        if (i == 0 || t > mx) mx = t;
+      }
+      double alamin = TOLX / mx;
+      if (alamin == 0.0) {
+        for (int i = 0; i < nv; ++i) qj_rel[i] = x_old[i];
+      } else {
+        double alam = 1.0, alam2 = 0.0, f2 = 0.0, tmplam = 0.0;
+        for (int ls = 0; ls < 4096; ++ls) {
+          for (int i = 0; i < nv; ++i) {
+            qj_rel[i] = x_old[i] + alam * p[i];
+            qt[i] = qj_rel[i] * qj_org[i];
+          }
+          newton_eval_f<NS>(c, qt, f, scal_f);
+          if (scal_f <= 0.9 * scal_f_old) break;
+          if (alam < alamin) {
+            for (int i = 0; i < nv; ++i) qj_rel[i] = x_old[i];
+            scal_f = scal_f_old;
+            check = true;
+            break;
+          }
+          if (alam == 1.0) {
+            tmplam = -slope / (2.0 * (scal_f - scal_f_old - slope));
+          } else {
+            double rhs1 = scal_f - scal_f_old - alam * slope;
+            double rhs2 = f2 - scal_f_old - alam2 * slope;
+            double a = (rhs1 / sq(alam) - rhs2 / sq(alam2)) / (alam - alam2);
+            double b = (-alam2 * rhs1 / sq(alam) + alam * rhs2 / sq(alam2)) / (alam - alam2);
+            if (a == 0.0) {
+              tmplam = -slope / (2.0 * b);
+            } else {
+              double disc = b * b - 3.0 * a * slope;
+              if (disc < 0.0) tmplam = 0.5 * alam;
+              else if (b <= 0.0) tmplam = (-b + sqrt(disc)) / (3.0 * a);
+              else tmplam = -slope / (b + sqrt(disc));
+            }
+            if (tmplam > 0.5 * alam) tmplam = 0.5 * alam;
+          }
+          alam2 = alam;
+          f2 = scal_f;
+          alam = rmax(tmplam, 0.5 * alam);
+        }
+      }
+    } else {
+      for (int i = 0; i < nv; ++i) {
+        qj_rel[i] = x_old[i] + p[i];
+        qj[i] = qj_rel[i] * qj_org[i];
+      }
+      newton_eval_f<NS>(c, qj, f, scal_f);
+    }
+    for (int i = 0; i < nv; ++i) qj[i] = qj_rel[i] * qj_org[i];
+    mf = 0.0;
+    for (int i = 0; i < nv; ++i) mf = rmax(mf, fabs(f[i]));
+    if (mf < TOLF) return it;
+    if (check) {
+      double mc = 0.0;
+      for (int i = 0; i < nv; ++i)
+        mc = rmax(mc, fabs(g[i]) * rmax(fabs(qj_rel[i]), 1.0) / rmax(scal_f, 0.5 * nv));
+      check = mc < TOLMIN;
+    }
+    double mx = 0.0;
+    for (int i = 0; i < nv; ++i) mx = rmax(mx, fabs(qj_rel[i] - x_old[i]) / rmax(fabs(qj_rel[i]), 1.0));
+    if (mx < TOLX) return it;
+  }
+  return kMaxNewton + 1;
+}
+
+// ---------------------------------------------------------------------------
+// constitutive_2d.f90:5326-5404 settling_velocity and 4574-5153
+// eval_mass_exchange_terms (no erosion / pore pressure / vaporisation); FP64
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ R settling_velocity(const Phys<R>& P, R diam, R rhos, R rhoc,
+                                               R inv_kin_visc) {
+  R inv_sqrt_C_D = R(1);
+  if (rhos <= rhoc) return R(0);
+  R const_part = sqrt((cst<R>(4.0) / cst<R>(3.0)) * (rhos / rhoc - R(1)) * diam * P.grav);
+  R sv = const_part * inv_sqrt_C_D;
+  R Rey = diam * sv * inv_kin_visc;
+  if (Rey <= cst<R>(1000.0)) {
+    for (int i = 1; i <= 20; ++i) {
+      R sv_old = sv;
+      if (P.collective)
+        inv_sqrt_C_D = sqrt(R(1) / (cst<R>(24.0) * (R(1) + cst<R>(0.15) * pow(Rey, cst<R>(0.687))) / Rey +
+                                    P.A_drag * (log(Rey) - P.B_drag)));
+      else
+        inv_sqrt_C_D = sqrt(Rey / (cst<R>(24.0) * (R(1) + cst<R>(0.15) * pow(Rey, cst<R>(0.687)))));
+      sv = const_part * inv_sqrt_C_D;
+      if (fabs(sv_old - sv) / sv_old < cst<R>(1.0e-6)) return sv;
+      Rey = diam * sv * inv_kin_visc;
+    }
+  }
+  return sv;
+}
+
+template <class R, int NS>
+__device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R Bx, R By, R dt,
+                                              R* dep, R* eqn) {
+  constexpr int ns = NS, nv = 4 + NS;
+  for (int i = 0; i < ns; ++i) dep[i] = R(0);
+  for (int i = 0; i < nv; ++i) eqn[i] = R(0);
+  if (!(qpj[0] > P.thr_eps)) return;
+  const R alpha_max = cst<R>(0.6), hind_exp = cst<R>(4.65);
+  R r_h = qpj[0], r_u = qpj[nv], r_v = qpj[nv + 1];
+  R al[kMaxSolid];
+  R at = R(0);
+  for (int i = 0; i < ns; ++i) { al[i] = P.alpha ? qpj[4 + i] : qpj[4 + i] / qpj[0]; at += al[i]; }
+  R r_w = P.slope_corr ? (r_u * Bx + r_v * By) : R(0);
+  R mod_vel2 = sq(r_u) + sq(r_v) + sq(r_w);
+  R tot_erosion = R(0) / (R(1) - P.erodible_porosity);
+  R cont_erosion = tot_erosion * P.erodible_porosity;
+  if (at <= P.alphastot_min) return;
+  R r_T = qpj[3];
+  Mixt<R> m = mixt_var<R, NS>(P, qpj, true);
+  R inv_kin_visc = R(1) / P.kin_visc_c;
+  R sdep = R(0);
+  for (int i = 0; i < ns; ++i) {
+    if (al[i] > R(0) && P.settling) {
+      R sv = settling_velocity<R>(P, P.diam_s[i], P.rho_s[i], m.rho_c, inv_kin_visc);
+      dep[i] = al[i] * sv * R(1);
+      dep[i] = dep[i] * pow(R(1) - rmin(R(1), at / alpha_max), hind_exp);
+      dep[i] = rmin(dep[i], r_h * al[i] / dt);
+    }
+  }
+  for (int i = 0; i < ns; ++i) sdep += dep[i];
+  R sal = R(0);
+  for (int i = 0; i < ns; ++i) sal += al[i];
+  R cpl = P.liquid ? P.loss_rate : R(0);
+  cpl = cpl + P.coeff_porosity * sdep;
+  cpl = rmin(cpl, r_h * rmax(R(0), P.max_packing - sal) / dt);
+  cpl = rmin(cpl, (r_h * (R(1) - sal) - P.coeff_porosity * (r_h * sal - dt * sdep)) / dt);
+  R air_entr = R(0);
+  if (P.entrain && r_h > R(0) && m.Ri > R(0)) {
+    R entr_coeff = cst<R>(0.075) / sqrt(R(1) + cst<R>(718.0) * pow(m.Ri, cst<R>(2.4)));
+    air_entr = entr_coeff * sqrt(mod_vel2);
+  }
+  R rho_dep_tot = R(0), rho_ers_tot = R(0), s_dep = R(0), s_ers = R(0);
+  for (int i = 0; i < ns; ++i) rho_dep_tot += P.rho_s[i] * dep[i];
+  for (int i = 0; i < ns; ++i) rho_ers_tot += P.rho_s[i] * R(0);
+  for (int i = 0; i < ns; ++i) s_dep += P.rho_s[i] * P.sp_heat_s[i] * dep[i];
+  for (int i = 0; i < ns; ++i) s_ers += P.rho_s[i] * P.sp_heat_s[i] * R(0);
+  eqn[0] = P.rho_a_amb * air_entr + rho_ers_tot - rho_dep_tot + P.rho_c_sub * cont_erosion -
+           m.rho_c * cpl;
+  eqn[1] = -r_u * (rho_dep_tot + m.rho_c * cpl);
+  eqn[2] = -r_v * (rho_dep_tot + m.rho_c * cpl);
+  if (P.energy)
+    eqn[3] = -r_T * (s_dep + m.rho_c * m.cp_c * cpl) - cst<R>(0.5) * mod_vel2 * (rho_dep_tot + m.rho_c * cpl) +
+             P.T_erodible * (s_ers + P.rho_c_sub * m.cp_c * cont_erosion) +
+             P.T_ambient * P.sp_heat_a * P.rho_a_amb * air_entr;
+  else
+    eqn[3] = -r_T * (s_dep + m.rho_c * m.cp_c * cpl) +
+             P.T_erodible * (s_ers + P.rho_c_sub * m.cp_c * cont_erosion) +
+             P.T_ambient * P.sp_heat_a * P.rho_a_amb * air_entr;
+  for (int i = 0; i < ns; ++i) eqn[4 + i] = P.rho_s[i] * (R(0) - dep[i]);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 form: the implicit friction step solved as a scalar FP64 Newton.
+// With the non-momentum components fixed, q_h = q_si_h + dt*a*NH_h(q) and
+// NH_h is antiparallel to q_h (both rheologies 1 and 6), so the solution is
+// s*e with e = q_si_h/|q_si_h| and s >= 0 the root of
+//     g(s) = s + dt*a*K(s)*s^2 - S,   S = |q_si_h|,
+// K = rho_m g' kappa phi^2 / xi (Voellmy) or rho_m ff kappa^2 phi^2 (6),
+// kappa = sqrt(1+(e.grad B)^2) with slope correction, phi = u/hu.  K depends
+// on s only through T (energy equation: kinetic energy is subtracted) and
+// the gas density.  This is the same fixed point the reference's 2x2
+// Newton (solver_2d.f90:1662-1996) converges to, computed in FP64 with an
+// analytic derivative.  Returns s; writes e.
+// ---------------------------------------------------------------------------
+template <int NS>
+__device__ __forceinline__ double reduced_friction_solve(const Phys<double>& P, double Bx,
+                                                         double By, const double* q, double dta,
+                                                         double& e1, double& e2, int& iters) {
+  constexpr int ns = NS;
+  iters = 0;
+  double S = sqrt(q[1] * q[1] + q[2] * q[2]);
+  if (S == 0.0) { e1 = 0.0; e2 = 0.0; return 0.0; }
+  e1 = q[1] / S;
+  e2 = q[2] / S;
+  if (!P.rheo || !(q[0] > kEps)) return S;
+  const double q1 = q[0];
+  const double inv_q1 = 1.0 / q1;
+  double xs_tot = 0.0, dcp = 0.0, dinv = 0.0;
+  for (int i = 0; i < ns; ++i) {
+    double xs = q[4 + i] * inv_q1;
+    xs_tot += xs;
+    dcp += xs * P.sp_heat_s[i];
+    dinv += xs * P.inv_rho_s[i];
+  }
+  const double xc = 1.0 - xs_tot;
+  const double cp_c = P.gas ? P.sp_heat_a : P.sp_heat_l;
+  const double cmix = dcp + xc * cp_c;
+  const double phi = (q1 > P.eps_sing_d) ? inv_q1 : P.sqrt2 * q1 / sqrt(q1 * q1 * q1 * q1 + P.eps_sing4);
+  double kappa2 = 1.0;
+  if (P.slope_corr) { double w = e1 * Bx + e2 * By; kappa2 = 1.0 + w * w; }
+  const double kappa = sqrt(kappa2);
+  const double cgeo = (P.rheo_model == 1) ? P.grav * kappa * phi * phi / P.xi
+                                          : P.friction_factor * kappa2 * phi * phi;
+  // rho_m(s) through T(s); for rheology 1 K uses (rho_m - rho_a) g, for 6 rho_m
+  const bool varT = P.gas && P.energy && (q1 > P.eps_sing_d);
+  const double a_T = q[3] / (q1 * cmix), b_T = 0.5 * inv_q1 / (q1 * cmix);
+  const double c_inv = xc * P.sp_gas_const_a * P.inv_pres;
+  auto K_of = [&](double s, double& dK) -> double {
+    double T, dT;
+    if (P.gas) {
+      if (varT) { T = a_T - b_T * s * s; dT = -2.0 * b_T * s; }
+      else if (q1 > P.eps_sing_d) { T = P.energy ? a_T : q[3] / (q1 * cmix); dT = 0.0; }
+      else { T = P.T_ambient; dT = 0.0; }
+      if (T <= 0.0) { T = P.T_ambient; dT = 0.0; }
+      double inv_rhom = dinv + c_inv * T;
+      double rho_m = 1.0 / inv_rhom;
+      double drho = -rho_m * rho_m * c_inv * dT;
+      double base = (P.rheo_model == 1) ? (rho_m - P.rho_a_amb) : rho_m;
+      dK = cgeo * drho;
+      return cgeo * base;
+    } else {
+      double rho_m = 1.0 / (dinv + xc * P.inv_rho_l);
+      dK = 0.0;
+      return cgeo * ((P.rheo_model == 1) ? (rho_m - P.rho_a_amb) : rho_m);
+    }
+  };
+  double dK;
+  double K = K_of(S, dK);
+  double disc = 1.0 + 4.0 * dta * K * S;
+  double s = (disc >= 0.0) ? 2.0 * S / (1.0 + sqrt(disc)) : S;
+  if (varT) {
+    for (int it = 0; it < 20; ++it) {
+      K = K_of(s, dK);
+      double gv = s + dta * K * s * s - S;
+      double gd = 1.0 + dta * (dK * s * s + 2.0 * K * s);
+      double ds = gv / gd;
+      s = s - ds;
+      ++iters;
+      if (!(fabs(ds) > 1.0e-15 * s)) break;
+    }
+  } else {
+    iters = 1;
+  }
+  return s > 0.0 ? s : 0.0;
+}
+
+}  // namespace sflow

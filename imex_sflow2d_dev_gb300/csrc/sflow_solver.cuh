@@ -1,0 +1,577 @@
+// sflow_solver.cuh -- device-resident solver of one domain, templated on the
+// bulk arithmetic type (double: plain FP64 form, float: FP32 bulk form).
+// Included by sflow_fp64.cu and sflow_fp32.cu only.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sflow_host.h"
+#include "sflow_kernels.cuh"
+#include "sflow_table.h"
+
+namespace sflow {
+
+// ---------------------------------------------------------------------------
+// layout kernels: host layout q(1:n,1:nx,1:ny) (variable fastest) <-> planes
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void k_aos_to_planes(const double* __restrict__ aos, R* __restrict__ q, int nv, int nx,
+                                int ny, int pitch, int64_t plane) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)nx * ny) return;
+  int j = (int)(c % nx), k = (int)(c / nx);
+  for (int i = 0; i < nv; ++i) q[i * plane + (int64_t)k * pitch + j] = (R)aos[c * nv + i];
+}
+
+template <class R>
+__global__ void k_planes_to_aos(const R* __restrict__ q, double* __restrict__ aos, int nv, int nx,
+                                int ny, int pitch, int64_t plane) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)nx * ny) return;
+  int j = (int)(c % nx), k = (int)(c / nx);
+  for (int i = 0; i < nv; ++i) aos[c * nv + i] = (double)q[i * plane + (int64_t)k * pitch + j];
+}
+
+template <class R>
+__global__ void k_map_to_host(const R* __restrict__ m, double* __restrict__ out, int nx, int ny,
+                              int pitch) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)nx * ny) return;
+  int j = (int)(c % nx), k = (int)(c / nx);
+  out[c] = (double)m[(int64_t)k * pitch + j];
+}
+
+static __global__ void k_stats_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+  // Neumaier-compensated sum over the block partials, in block order
+  if (threadIdx.x >= 4) return;
+  int m = threadIdx.x;
+  double s = 0.0, cmp = 0.0;
+  for (int b = 0; b < nblk; ++b) {
+    double x = part[b * 4 + m];
+    double t = s + x;
+    if (fabs(s) >= fabs(x)) cmp += (s - t) + x;
+    else cmp += (x - t) + s;
+    s = t;
+  }
+  out[m] = s + cmp;
+}
+
+// ---------------------------------------------------------------------------
+// host driver of one domain
+// ---------------------------------------------------------------------------
+#define SFLOW_CU(call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      err_ = std::string(#call) + ": " + cudaGetErrorString(e_);              \
+      return SFLOW_ECUDA;                                                     \
+    }                                                                         \
+  } while (0)
+
+template <class R>
+class Solver : public SolverBase {
+ public:
+  explicit Solver(const HostSetup& s) : hs_(s) { tab_ = kernel_table<R>(s.ns); }
+  ~Solver() override { release(); }
+
+  std::string err_;
+
+  int init() {
+    if (!tab_.flux) { err_ = "no kernels built for this number of solid classes"; return SFLOW_EINVAL; }
+    const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
+    pitch_ = (nx + 31) / 32 * 32;
+    plane_ = (int64_t)pitch_ * ny;
+    tiles_x_ = (nx + TX - 1) / TX;
+    tiles_y_ = (ny + TY - 1) / TY;
+    SFLOW_CU(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    SFLOW_CU(alloc((void**)&q_, sizeof(R) * plane_ * nv));
+    SFLOW_CU(alloc((void**)&rd_, sizeof(R) * plane_ * nv));
+    for (int i = 0; i < 8; ++i) geo_[i] = nullptr;
+    const std::vector<double>* gsrc[8] = {&hs_.Bx, &hs_.By, &hs_.Bxx, &hs_.Bxy, &hs_.Byy, &hs_.gc, &hs_.dgcx, &hs_.dgcy};
+    for (int i = 0; i < 8; ++i) {
+      if ((i >= 2 && i <= 4) && !hs_.p.curvature_term_flag) continue;
+      SFLOW_CU(alloc((void**)&geo_[i], sizeof(R) * plane_));
+      SFLOW_CU(put_plane(geo_[i], *gsrc[i]));
+    }
+    SFLOW_CU(alloc((void**)&cflags_, plane_));
+    {
+      std::vector<uint8_t> f((size_t)plane_, 0);
+      for (int k = 0; k < ny; ++k)
+        for (int j = 0; j < nx; ++j) f[(size_t)k * pitch_ + j] = hs_.cflags[(size_t)k * nx + j];
+      SFLOW_CU(cudaMemcpy(cflags_, f.data(), plane_, cudaMemcpyHostToDevice));
+    }
+    SFLOW_CU(alloc((void**)&arc_, sizeof(R) * plane_ * 3));
+    SFLOW_CU(put_plane(arc_, hs_.arc_perim));
+    SFLOW_CU(put_plane(arc_ + plane_, hs_.arc_nx));
+    SFLOW_CU(put_plane(arc_ + 2 * plane_, hs_.arc_ny));
+    SFLOW_CU(alloc((void**)&mask_, plane_));
+    SFLOW_CU(cudaMemset(mask_, 0, plane_));
+    SFLOW_CU(alloc((void**)&tile_active_, (size_t)tiles_x_ * tiles_y_));
+    SFLOW_CU(alloc((void**)&hmax_, sizeof(R) * plane_));
+    SFLOW_CU(alloc((void**)&pdynmax_, sizeof(R) * plane_));
+    SFLOW_CU(alloc((void**)&mvmax_, sizeof(R) * plane_));
+    SFLOW_CU(alloc((void**)&st_, sizeof(RunState)));
+    SFLOW_CU(alloc((void**)&stage_aos_, sizeof(double) * (size_t)nx * ny * (nv + 2)));
+    nstat_blocks_ = 1024;
+    SFLOW_CU(alloc((void**)&stat_part_, sizeof(double) * 4 * nstat_blocks_));
+    SFLOW_CU(alloc((void**)&stat_out_, sizeof(double) * 4));
+    SFLOW_CU(cudaMemset(q_, 0, sizeof(R) * plane_ * nv));
+    SFLOW_CU(cudaMemset(rd_, 0, sizeof(R) * plane_ * nv));
+    fill_args();
+    // shared memory of the flux kernel
+    smem_flux_ = flux_smem_bytes();
+    SFLOW_CU(set_smem_attr());
+    std::memset(&hst_, 0, sizeof(hst_));
+    init_state_host();
+    SFLOW_CU(cudaMemcpy(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice));
+    return SFLOW_OK;
+  }
+
+  // --- SolverBase -----------------------------------------------------------
+  int upload(const double* q_aos) override {
+    const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
+    const size_t N = (size_t)nx * ny;
+    SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
+    k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
+    ++launches_;
+    SFLOW_CU(cudaGetLastError());
+    init_state_host();
+    SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
+    SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    uploaded_ = true;
+    return SFLOW_OK;
+  }
+
+  int download(double* q_aos) override {
+    const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
+    const size_t N = (size_t)nx * ny;
+    k_planes_to_aos<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(q_, stage_aos_, nv, nx, ny, pitch_, plane_);
+    ++launches_;
+    SFLOW_CU(cudaGetLastError());
+    SFLOW_CU(cudaMemcpyAsync(q_aos, stage_aos_, sizeof(double) * N * nv, cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+
+  int download_qp(double* qp_aos) override {
+    const size_t N = (size_t)hs_.nx * hs_.ny;
+    SFLOW_CU(dispatch_qp((unsigned)((N + 255) / 256)));
+    SFLOW_CU(cudaMemcpyAsync(qp_aos, stage_aos_, sizeof(double) * N * (hs_.nv + 2), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+
+  int download_maps(double* h, double* p, double* v) override {
+    const int nx = hs_.nx, ny = hs_.ny;
+    const size_t N = (size_t)nx * ny;
+    R* src[3] = {hmax_, pdynmax_, mvmax_};
+    double* dst[3] = {h, p, v};
+    for (int m = 0; m < 3; ++m) {
+      if (!dst[m]) continue;
+      k_map_to_host<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(src[m], stage_aos_, nx, ny, pitch_);
+      ++launches_;
+      SFLOW_CU(cudaGetLastError());
+      SFLOW_CU(cudaMemcpyAsync(dst[m], stage_aos_, sizeof(double) * N, cudaMemcpyDeviceToHost, stream_));
+      SFLOW_CU(cudaStreamSynchronize(stream_));
+    }
+    return SFLOW_OK;
+  }
+
+  // granular entry points (one Fortran call site each) ------------------------
+  int check_solve(int solve_all) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    SFLOW_CU(launch_mask(solve_all));
+    return SFLOW_OK;
+  }
+  int timestep(double* dt_out) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    SFLOW_CU(launch_flux(1));
+    RunState h;
+    SFLOW_CU(cudaMemcpyAsync(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    double dtmin;
+    unsigned long long b = h.dtmin_bits;
+    std::memcpy(&dtmin, &b, sizeof(double));
+    double dt = hs_.p.max_dt;
+    if (dtmin < dt) dt = dtmin;
+    if (dt_out) *dt_out = dt;
+    flux_ready_ = true;
+    return SFLOW_OK;
+  }
+  int imex_rk(double t, double dt) override {
+    if (!flux_ready_) { err_ = "sflow_imex_rk needs sflow_timestep on the same state first"; return SFLOW_ESTATE; }
+    RunState h;
+    SFLOW_CU(cudaMemcpyAsync(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    if (t != h.t) { err_ = "t differs from the handle's time (sflow_get_stats)"; return SFLOW_ESTATE; }
+    h.dt_old_old = h.dt_old;
+    h.dt_old = dt;
+    h.dt = dt;
+    h.t_prev = h.t;
+    h.run_step = 1;
+    int p = (int)(h.steps & 1);
+    h.last_cells = (long long)h.cells_acc[p];
+    h.cells_total += (long long)h.cells_acc[p];
+    h.cells_acc[p] = 0;
+    h.dtmin_bits = bits_of(1.0e300);
+    SFLOW_CU(cudaMemcpyAsync(st_, &h, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
+    SFLOW_CU(launch_stage2(0));
+    flux_ready_ = false;
+    pending_dt_ = dt;
+    return SFLOW_OK;
+  }
+  int erosion_deposition(double dt) override {
+    if (dt != pending_dt_) { err_ = "dt differs from the last sflow_imex_rk"; return SFLOW_ESTATE; }
+    if (hs_.p.settling_flag || hs_.p.entrainment_flag) SFLOW_CU(launch_stage2(1));
+    return SFLOW_OK;
+  }
+  int post_step(SflowStepStats* s) override {
+    SFLOW_CU(launch_stage2(2));
+    RunState h;
+    SFLOW_CU(cudaMemcpyAsync(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    h.t = h.t + h.dt;
+    h.steps += 1;
+    h.run_step = 0;
+    SFLOW_CU(cudaMemcpyAsync(st_, &h, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
+    return s ? stats(s) : SFLOW_OK;
+  }
+
+  // fused driver iteration -----------------------------------------------------
+  int step() override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    SFLOW_CU(set_limits(hs_.p.t_end, -1));
+    SFLOW_CU(launch_step());
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+
+  int advance(double t_stop, int64_t max_steps, SflowStepStats* s) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    if (max_steps <= 0) return s ? stats(s) : SFLOW_OK;
+    SFLOW_CU(cudaMemcpyAsync(&hst_, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    const double stop = t_stop < hs_.p.t_end ? t_stop : hs_.p.t_end;
+    const int64_t limit = hst_.steps + max_steps;
+    SFLOW_CU(set_limits(stop, limit));
+    if (!graph_exec_) SFLOW_CU(build_graph());
+    // replay chunks until the device reports t >= stop or the step budget
+    for (;;) {
+      const int64_t left = limit - hst_.steps;
+      const int64_t chunks = (left + kChunk - 1) / kChunk;
+      const int64_t burst = chunks < 8 ? chunks : 8;
+      for (int64_t b = 0; b < burst; ++b) {
+        SFLOW_CU(cudaGraphLaunch(graph_exec_, stream_));
+        launches_ += kChunk * 4;
+      }
+      SFLOW_CU(cudaMemcpyAsync(&hst_, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+      SFLOW_CU(cudaStreamSynchronize(stream_));
+      if (!(hst_.t < stop) || hst_.steps >= limit) break;
+    }
+    return s ? stats(s) : SFLOW_OK;
+  }
+
+  int stats(SflowStepStats* s) override {
+    SFLOW_CU(dispatch_stats());
+    double out[4];
+    SFLOW_CU(cudaMemcpyAsync(out, stat_out_, sizeof(out), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaMemcpyAsync(&hst_, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    const double a = hs_.dx * hs_.dy;
+    s->t = hst_.t;
+    s->dt = hst_.dt;
+    s->mass = a * out[0];
+    s->volume = a * out[1];
+    s->area = a * out[2];
+    s->solid_mass = a * out[3];
+    s->solve_cells = hst_.last_cells;
+    s->steps = hst_.steps;
+    s->status = hst_.status;
+    s->pad = 0;
+    return SFLOW_OK;
+  }
+  int status(uint32_t* f) override {
+    RunState h;
+    SFLOW_CU(cudaMemcpyAsync(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    *f = h.status;
+    return SFLOW_OK;
+  }
+  int clear_status() override {
+    unsigned z = 0;
+    SFLOW_CU(cudaMemcpyAsync(&st_->status, &z, sizeof(z), cudaMemcpyHostToDevice, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+  int64_t launches() const override { return launches_; }
+  int64_t device_bytes() const override { return bytes_; }
+  int newton_stats(int64_t* total, int* maxit) override {
+    RunState h;
+    SFLOW_CU(cudaMemcpyAsync(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    *total = h.newton_iters;
+    *maxit = h.newton_max;
+    return SFLOW_OK;
+  }
+  const char* error() const override { return err_.c_str(); }
+  int64_t cells_total() override {
+    RunState h;
+    if (cudaMemcpy(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return h.cells_total;
+  }
+
+ private:
+  static constexpr int kChunk = 16;   // steps per captured graph
+  HostSetup hs_;
+  int pitch_ = 0;
+  int64_t plane_ = 0;
+  int tiles_x_ = 0, tiles_y_ = 0;
+  cudaStream_t stream_ = nullptr;
+  R *q_ = nullptr, *rd_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
+  R* geo_[8];
+  uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr;
+  RunState* st_ = nullptr;
+  double *stage_aos_ = nullptr, *stat_part_ = nullptr, *stat_out_ = nullptr;
+  int nstat_blocks_ = 0;
+  std::vector<void*> allocs_;
+  int64_t bytes_ = 0, launches_ = 0;
+  KArgs<R> ka_;
+  size_t smem_flux_ = 0;
+  RunState hst_;
+  bool uploaded_ = false, flux_ready_ = false;
+  double pending_dt_ = -1.0;
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  KernelTable<R> tab_;
+
+  static unsigned long long bits_of(double x) {
+    unsigned long long b;
+    std::memcpy(&b, &x, sizeof(b));
+    return b;
+  }
+
+  cudaError_t alloc(void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) {
+      allocs_.push_back(*p);
+      bytes_ += (int64_t)bytes;
+    }
+    return e;
+  }
+
+  void release() {
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    for (void* p : allocs_) cudaFree(p);
+    allocs_.clear();
+    if (stream_) cudaStreamDestroy(stream_);
+  }
+
+  cudaError_t put_plane(R* dst, const std::vector<double>& src) {
+    std::vector<R> buf((size_t)plane_, R(0));
+    for (int k = 0; k < hs_.ny; ++k)
+      for (int j = 0; j < hs_.nx; ++j) buf[(size_t)k * pitch_ + j] = (R)src[(size_t)k * hs_.nx + j];
+    return cudaMemcpy(dst, buf.data(), sizeof(R) * plane_, cudaMemcpyHostToDevice);
+  }
+
+  static R thr(double x) {
+    if constexpr (sizeof(R) == 8) return x;
+    else return float_below(x);
+  }
+
+  template <class T>
+  void fill_phys(Phys<T>& P) {
+    const SflowParams& p = hs_.p;
+    std::memset(&P, 0, sizeof(P));
+    P.nv = hs_.nv; P.ns = hs_.ns; P.nrk = hs_.nrk;
+    P.gas = p.gas_flag; P.liquid = p.liquid_flag; P.energy = p.energy_flag; P.alpha = p.alpha_flag;
+    P.rheo = p.rheology_flag; P.rheo_model = p.rheology_model; P.slope_corr = p.slope_correction_flag;
+    P.curv = p.curvature_term_flag; P.settling = p.settling_flag; P.entrain = p.entrainment_flag;
+    P.collective = p.collective_settling_flag; P.radial_source = p.radial_source_flag;
+    P.scheme = p.solver_scheme;
+    P.eps_sing_d = hs_.eps_sing;
+    auto th = [&](double x) -> T {
+      if constexpr (sizeof(T) == 8) return x;
+      else return float_below(x);
+    };
+    P.thr_eps = th(DBL_EPSILON);
+    P.thr_eps_sing = th(hs_.eps_sing);
+    P.thr_neg1e7 = th(-1.0e-7);
+    P.thr_neg1e10 = th(-1.0e-10);
+    P.thr_1em10 = th(1.0e-10);
+    P.thr_1em7 = th(1.0e-7);
+    P.thr_1em3 = th(1.0e-3);
+    P.thr_273 = (T)273.0;
+    P.eps_sing4 = (T)hs_.eps_sing4;
+    P.sqrt2 = (T)std::sqrt(2.0);
+    P.grav = (T)p.grav; P.pres = (T)p.pres; P.inv_pres = (T)(1.0 / p.pres);
+    P.sp_heat_a = (T)p.sp_heat_a; P.sp_gas_const_a = (T)p.sp_gas_const_a; P.T_ambient = (T)p.T_ambient;
+    P.rho_a_amb = (T)hs_.rho_a_amb;
+    P.rho_l = (T)p.rho_l; P.inv_rho_l = (T)(p.rho_l != 0.0 ? 1.0 / p.rho_l : 0.0); P.sp_heat_l = (T)p.sp_heat_l;
+    for (int i = 0; i < kMaxSolid; ++i) {
+      P.rho_s[i] = (T)p.rho_s[i];
+      P.inv_rho_s[i] = (T)(p.rho_s[i] != 0.0 ? 1.0 / p.rho_s[i] : 0.0);
+      P.sp_heat_s[i] = (T)p.sp_heat_s[i];
+      P.alphas_source[i] = (T)p.alphas_source[i];
+      P.diam_s[i] = (T)p.diam_s[i];
+    }
+    P.h_source = (T)hs_.h_source; P.vel_source = (T)p.vel_source; P.T_source = (T)p.T_source;
+    P.cell_area = (T)(hs_.dx * hs_.dy);
+    P.src_rho_m = (T)hs_.src_rho_m; P.src_cp_mix = (T)hs_.src_cp_mix;
+    P.mu = (T)p.mu; P.xi = (T)p.xi; P.friction_factor = (T)p.friction_factor;
+    P.kin_visc_c = (T)hs_.kin_visc_c; P.loss_rate = (T)p.loss_rate;
+    P.alphastot_min = (T)p.alphastot_min; P.max_packing = (T)p.maximum_solid_packing;
+    P.A_drag = (T)p.A_drag; P.B_drag = (T)p.B_drag;
+    P.coeff_porosity = (T)0.0; P.rho_c_sub = (T)hs_.rho_c_sub; P.T_erodible = (T)hs_.T_erodible;
+    P.erodible_porosity = (T)0.0;
+  }
+
+  void fill_args() {
+    const SflowParams& p = hs_.p;
+    std::memset(&ka_, 0, sizeof(ka_));
+    Grid<R>& g = ka_.g;
+    g.nx = hs_.nx; g.ny = hs_.ny; g.pitch = pitch_; g.plane = plane_;
+    g.tiles_x = tiles_x_; g.tiles_y = tiles_y_;
+    g.x0 = p.x0; g.y0 = p.y0; g.dx = hs_.dx; g.dy = hs_.dy;
+    g.rdx = (R)hs_.dx; g.rdy = (R)hs_.dy;
+    g.dx2 = (R)(hs_.dx / 2.0); g.dy2 = (R)(hs_.dy / 2.0);
+    g.one_by_dx = (R)(1.0 / hs_.dx); g.one_by_dy = (R)(1.0 / hs_.dy);
+    g.rc = (R)p.reconstr_coeff; g.theta = (R)p.theta;
+    g.cfl_dx = (R)(p.cfl * hs_.dx); g.cfl_dy = (R)(p.cfl * hs_.dy);
+    for (int i = 0; i < hs_.nv; ++i) g.limiter[i] = p.limiter[i];
+    g.limiter[hs_.nv] = p.limiter[1];
+    g.limiter[hs_.nv + 1] = p.limiter[2];
+    g.cfl = p.cfl; g.max_dt = p.max_dt;
+    fill_phys(ka_.pr);
+    fill_phys(ka_.pd);
+    for (int sd = 0; sd < 4; ++sd)
+      for (int i = 0; i < kMaxVars; ++i) {
+        ka_.bc.flag[sd][i] = p.bc[sd][i].flag;
+        ka_.bc.value[sd][i] = (R)p.bc[sd][i].value;
+      }
+    ka_.q = q_; ka_.rd = rd_; ka_.rn = nullptr; ka_.qs = nullptr;
+    for (int i = 0; i < 8; ++i) ka_.geo[i] = geo_[i];
+    ka_.cflags = cflags_; ka_.arc = arc_; ka_.mask = mask_; ka_.tile_active = tile_active_;
+    ka_.hmax = hmax_; ka_.pdynmax = pdynmax_; ka_.mvmax = mvmax_; ka_.st = st_;
+    ka_.take_last = hs_.take_last;
+  }
+
+  void init_state_host() {
+    const SflowParams& p = hs_.p;
+    std::memset(&hst_, 0, sizeof(hst_));
+    hst_.t = p.t_start;
+    hst_.dt = hst_.dt_old = hst_.dt_old_old = p.dt0;
+    hst_.t_output = p.t_start + p.dt_output;
+    hst_.t_end = p.t_end;
+    hst_.t_stop = p.t_end;
+    hst_.t_prev = p.t_start;
+    hst_.dtmin_bits = bits_of(1.0e300);
+    hst_.step_limit = (long long)1 << 62;
+    for (int i = 0; i < 4; ++i) hst_.tp[i] = hs_.time_param[i];
+    hst_.pi_g = hs_.pi_g;
+  }
+
+  cudaError_t set_limits(double t_stop, int64_t step_limit) {
+    // write t_stop and step_limit into the device state without touching
+    // the rest (the device owns t, dt and the counters)
+    cudaError_t e = cudaMemcpyAsync(&st_->t_stop, &t_stop, sizeof(double), cudaMemcpyHostToDevice, stream_);
+    if (e != cudaSuccess) return e;
+    long long lim = step_limit < 0 ? ((long long)1 << 62) : (long long)step_limit;
+    static_assert(sizeof(lim) == sizeof(st_->step_limit), "step_limit size");
+    e = cudaMemcpyAsync(&st_->step_limit, &lim, sizeof(lim), cudaMemcpyHostToDevice, stream_);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(stream_);
+  }
+
+  size_t flux_smem_bytes() const {
+    const int nv = hs_.nv, np = nv + 2;
+    size_t r = (size_t)np * RX * RY + (size_t)nv * TY * (TX + 1) + (size_t)nv * (TY + 1) * TX + TY * (TX + 1) +
+               (TY + 1) * TX;
+    return r * sizeof(R) + RX * RY;
+  }
+
+  cudaError_t set_smem_attr() { return tab_.set_smem(smem_flux_); }
+
+  cudaError_t launch_mask(int solve_all) {
+    dim3 grid(tiles_x_, tiles_y_);
+    k_mask<R><<<grid, TX * TY, 0, stream_>>>(ka_, solve_all);
+    ++launches_;
+    return cudaGetLastError();
+  }
+  cudaError_t launch_flux(int want_dt) {
+    ++launches_;
+    return tab_.flux(ka_, dim3(tiles_x_, tiles_y_), smem_flux_, stream_, q_, rd_, want_dt);
+  }
+  // mode -1: full fused epilogue; 0: stage only; 1: erosion only; 2: maps only
+  cudaError_t launch_stage2(int mode) {
+    ++launches_;
+    return tab_.stage2(ka_, dim3(tiles_x_, tiles_y_), stream_, mode);
+  }
+
+  cudaError_t launch_step() {
+    cudaError_t e = launch_mask(0);
+    if (e != cudaSuccess) return e;
+    e = launch_flux(1);
+    if (e != cudaSuccess) return e;
+    k_dt<<<1, 1, 0, stream_>>>(st_, hs_.p.max_dt);
+    ++launches_;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_stage2(-1);
+  }
+
+  cudaError_t build_graph() {
+    cudaError_t e = cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const int64_t l0 = launches_;
+    for (int i = 0; i < kChunk; ++i) {
+      e = launch_step();
+      if (e != cudaSuccess) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream_, &g);
+        if (g) cudaGraphDestroy(g);
+        return e;
+      }
+    }
+    launches_ = l0;   // captured launches are counted when replayed
+    e = cudaStreamEndCapture(stream_, &graph_);
+    if (e != cudaSuccess) return e;
+    return cudaGraphInstantiate(&graph_exec_, graph_, 0);
+  }
+
+  cudaError_t dispatch_init_maps(unsigned blocks) {
+    ++launches_;
+    return tab_.init_maps(ka_, blocks, stream_);
+  }
+  cudaError_t dispatch_qp(unsigned blocks) {
+    ++launches_;
+    return tab_.qp(ka_, blocks, stream_, stage_aos_);
+  }
+  cudaError_t dispatch_stats() {
+    cudaError_t e = tab_.stats(ka_, nstat_blocks_, stream_, stat_part_);
+    if (e != cudaSuccess) return e;
+    k_stats_final<<<1, 32, 0, stream_>>>(stat_part_, nstat_blocks_, stat_out_);
+    launches_ += 2;
+    return cudaGetLastError();
+  }
+};
+
+template <class R>
+SolverBase* make_solver_impl(const HostSetup& s, std::string& err) {
+  Solver<R>* sv = new Solver<R>(s);
+  int rc = sv->init();
+  if (rc != SFLOW_OK) {
+    err = sv->err_;
+    delete sv;
+    return nullptr;
+  }
+  return sv;
+}
+
+}  // namespace sflow

@@ -1,0 +1,42 @@
+// sflow_table.h -- per-(precision, solid-class count) kernel entry points.
+// The class count is a compile-time parameter of the heavy kernels so their
+// per-variable arrays stay in registers; each (precision, count) pair is its
+// own translation unit (sflow_k_*.cu) so the build parallelises.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sflow_types.cuh"
+
+namespace sflow {
+
+template <class R>
+struct KArgs;
+
+template <class R>
+struct KernelTable {
+  cudaError_t (*flux)(const KArgs<R>&, dim3, size_t, cudaStream_t, const R*, R*, int) = nullptr;
+  cudaError_t (*stage2)(const KArgs<R>&, dim3, cudaStream_t, int) = nullptr;
+  cudaError_t (*init_maps)(const KArgs<R>&, unsigned, cudaStream_t) = nullptr;
+  cudaError_t (*qp)(const KArgs<R>&, unsigned, cudaStream_t, double*) = nullptr;
+  cudaError_t (*stats)(const KArgs<R>&, int, cudaStream_t, double*) = nullptr;
+  cudaError_t (*set_smem)(size_t) = nullptr;
+};
+
+template <class R, int NS>
+KernelTable<R> make_table();
+
+// solid-class counts with compiled kernels
+constexpr int kMinSolidBuilt = 1;
+constexpr int kMaxSolidBuilt = 3;
+
+template <class R>
+inline KernelTable<R> kernel_table(int ns) {
+  switch (ns) {
+    case 1: return make_table<R, 1>();
+    case 2: return make_table<R, 2>();
+    case 3: return make_table<R, 3>();
+  }
+  return KernelTable<R>();
+}
+
+}  // namespace sflow

@@ -1,0 +1,132 @@
+// sflow_table_impl.cuh -- launch wrappers of the class-count-templated
+// kernels; included by the sflow_k_*.cu translation units only.
+#pragma once
+#include "sflow_kernels.cuh"
+#include "sflow_table.h"
+
+namespace sflow {
+
+// qp of every cell (IMEX_SfloW2D.f90:449-505 values) in host layout
+template <class R, int NS>
+__global__ void k_qp_to_aos(KArgs<R> a, double* __restrict__ aos) {
+  constexpr int nv = 4 + NS, np = nv + 2;
+  const Grid<R>& g = a.g;
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)g.nx * g.ny) return;
+  int j = (int)(c % g.nx), k = (int)(c / g.nx);
+  int64_t d = cidx(g, j, k);
+  R q[nv], qp[np];
+  for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + d];
+  if (q[0] > R(0)) qc_to_qp<R, NS>(a.pr, q, qp);
+  else {
+    for (int i = 0; i < np; ++i) qp[i] = R(0);
+    qp[3] = a.pr.T_ambient;
+  }
+  for (int i = 0; i < np; ++i) aos[c * np + i] = (double)qp[i];
+}
+
+// initial maxima after the initial check_solve(.TRUE.) (IMEX_SfloW2D.f90:307-368)
+template <class R, int NS>
+__global__ void k_init_maps(KArgs<R> a) {
+  constexpr int nv = 4 + NS, np = nv + 2;
+  const Grid<R>& g = a.g;
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)g.nx * g.ny) return;
+  int j = (int)(c % g.nx), k = (int)(c / g.nx);
+  int64_t d = cidx(g, j, k);
+  R q[nv], qp[np];
+  for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + d];
+  R h = R(0), pd = R(0), mv = R(0);
+  if (q[0] > R(0)) {
+    R p_dyn = qc_to_qp<R, NS>(a.pr, q, qp);
+    h = qp[0];
+    if (qp[0] > a.pr.thr_1em3) {
+      pd = p_dyn;
+      mv = sqrt(sq(qp[nv]) + sq(qp[nv + 1]));
+    }
+  }
+  a.hmax[d] = h;
+  a.pdynmax[d] = pd;
+  a.mvmax[d] = mv;
+}
+
+// log-line sums over all cells (IMEX_SfloW2D.f90:535-542) in FP64 with a
+// fixed reduction order: 4 values per block, then one block over blocks.
+template <class R, int NS>
+__global__ void k_stats_partial(KArgs<R> a, double* __restrict__ part) {
+  constexpr int nv = 4 + NS, np = nv + 2;
+  const Grid<R>& g = a.g;
+  double v[4] = {0, 0, 0, 0};
+  const int64_t N = (int64_t)g.nx * g.ny;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int j = (int)(c % g.nx), k = (int)(c / g.nx);
+    int64_t d = cidx(g, j, k);
+    R q[nv];
+    for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + d];
+    v[0] += (double)q[0];
+    if (q[0] > R(0)) {
+      R qp[np];
+      qc_to_qp<R, NS>(a.pr, q, qp);
+      v[1] += (double)qp[0];
+    }
+    if ((double)q[0] > 1.0e-7) v[2] += 1.0;
+    for (int i = 0; i < NS; ++i) v[3] += (double)q[4 + i];
+  }
+  __shared__ double sh[4][256];
+  for (int m = 0; m < 4; ++m) sh[m][threadIdx.x] = v[m];
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int m = 0; m < 4; ++m) sh[m][threadIdx.x] += sh[m][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int m = 0; m < 4; ++m) part[blockIdx.x * 4 + m] = sh[m][0];
+}
+
+
+template <class R, int NS>
+static cudaError_t tab_flux(const KArgs<R>& a, dim3 grid, size_t smem, cudaStream_t s, const R* qin,
+                            R* rout, int want_dt) {
+  k_flux<R, NS><<<grid, FLUX_THREADS, smem, s>>>(a, qin, rout, want_dt);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_stage2(const KArgs<R>& a, dim3 grid, cudaStream_t s, int mode) {
+  k_stage2<R, NS><<<grid, TX * TY, 0, s>>>(a, mode);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_init_maps(const KArgs<R>& a, unsigned blocks, cudaStream_t s) {
+  k_init_maps<R, NS><<<blocks, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_qp(const KArgs<R>& a, unsigned blocks, cudaStream_t s, double* out) {
+  k_qp_to_aos<R, NS><<<blocks, 256, 0, s>>>(a, out);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_stats(const KArgs<R>& a, int blocks, cudaStream_t s, double* part) {
+  k_stats_partial<R, NS><<<blocks, 256, 0, s>>>(a, part);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_smem(size_t bytes) {
+  return cudaFuncSetAttribute(k_flux<R, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class R, int NS>
+KernelTable<R> make_table() {
+  KernelTable<R> t;
+  t.flux = &tab_flux<R, NS>;
+  t.stage2 = &tab_stage2<R, NS>;
+  t.init_maps = &tab_init_maps<R, NS>;
+  t.qp = &tab_qp<R, NS>;
+  t.stats = &tab_stats<R, NS>;
+  t.set_smem = &tab_smem<R, NS>;
+  return t;
+}
+
+}  // namespace sflow

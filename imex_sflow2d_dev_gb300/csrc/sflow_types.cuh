@@ -1,0 +1,85 @@
+// sflow_types.cuh -- parameter blocks shared by host and device code.
+#pragma once
+#include <cstdint>
+
+#include "../../include/sflow.h"
+
+namespace sflow {
+
+constexpr int kMaxSolid = SFLOW_MAX_SOLID;
+constexpr int kMaxVars = SFLOW_MAX_VARS;   // conservative variables
+constexpr int kMaxNewton = 100;            // max_nl_iter (parameters_2d.f90:362)
+
+// Physical constants and model flags, in the bulk arithmetic type R.  A
+// double copy always exists for the FP64 parts (Newton, epilogue).
+template <class R>
+struct Phys {
+  int nv, ns, nrk;
+  int gas, liquid, energy, alpha, rheo, rheo_model, slope_corr, curv;
+  int settling, entrain, collective, radial_source, scheme;
+  double eps_sing_d;          // thresholds are always tested in FP64
+  // FP64 thresholds as R: for R = float these are the largest floats not
+  // above the FP64 value, so `x > thr` on a float x gives the same answer
+  // as the FP64 test (double)x > value.
+  R thr_eps, thr_eps_sing, thr_neg1e7, thr_neg1e10, thr_1em10, thr_1em7, thr_1em3, thr_273;
+  R eps_sing4, sqrt2;
+  R grav, pres, inv_pres, sp_heat_a, sp_gas_const_a, T_ambient, rho_a_amb;
+  R rho_l, inv_rho_l, sp_heat_l;
+  R rho_s[kMaxSolid], inv_rho_s[kMaxSolid], sp_heat_s[kMaxSolid];
+  R h_source, vel_source, T_source, alphas_source[kMaxSolid], cell_area;
+  R src_rho_m, src_cp_mix;    // mixt_var of the inlet state (constant per run)
+  // FP64-only physics (semi-implicit, Newton, mass exchange)
+  R mu, xi, friction_factor, kin_visc_c, loss_rate;
+  R diam_s[kMaxSolid];
+  R alphastot_min, max_packing, A_drag, B_drag, coeff_porosity, rho_c_sub, T_erodible,
+      erodible_porosity;
+};
+
+// Topography terms of one cell.
+template <class R>
+struct Geo {
+  R Bx, By, Bxx, Bxy, Byy, gc, dgcx, dgcy;
+};
+
+// Boundary conditions per side / variable, in R.
+template <class R>
+struct BC {
+  int flag[4][kMaxVars];
+  R value[4][kMaxVars];
+};
+
+// Grid and numerics of one domain.
+template <class R>
+struct Grid {
+  int nx, ny;
+  int pitch;        // row stride of every cell plane (elements)
+  int64_t plane;    // stride between variable planes
+  int tiles_x, tiles_y;
+  double x0, y0, dx, dy;   // coordinates in FP64 (x_stag = x0 + j*dx)
+  R rdx, rdy, dx2, dy2, one_by_dx, one_by_dy;
+  R rc, theta;
+  R cfl_dx, cfl_dy;
+  int limiter[kMaxVars + 2];
+  double cfl, max_dt;
+};
+
+// Device-resident run state (one per domain).
+struct RunState {
+  double t, dt, dt_old, dt_old_old, t_output, t_end, t_stop, t_prev;
+  unsigned long long cells_acc[2];  // active-cell counts of the running step
+  unsigned long long dtmin_bits;   // atomicMin over positive doubles
+  unsigned int status;             // SFLOW_S_* bits
+  int run_step;                    // 1 when this step's dt is valid
+  long long steps;
+  long long step_limit;             // steps stop at this count
+  long long cells_total;           // sum over steps of active cells
+  long long last_cells;            // active cells of the last step
+  long long newton_iters;          // sum of Newton iterations
+  int newton_max;
+  int pad;
+  double src_t_coeff;              // ring inlet time factor at this step's t
+  double tp[4];                    // time_param
+  double pi_g;
+};
+
+}  // namespace sflow

@@ -1,0 +1,198 @@
+"""ctypes binding of libsflow_gb300.so (the C ABI of include/sflow.h).
+
+The library is built in-tree by imex_sflow2d_dev_gb300.build; there is no
+CPU fallback: if the library is missing or cannot be loaded, every entry
+point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .params import SflowParams, SflowStepStats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsflow_gb300.so")
+
+_lib = None
+
+
+class SflowError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"sflow error {code}: {msg}")
+        self.code = code
+
+
+def load(build_if_missing=True):
+    """Load libsflow_gb300.so (building it in-tree first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from .build import build
+        build()
+    if not os.path.exists(LIB_PATH):
+        raise SflowError(-3, f"{LIB_PATH} is missing; run imex_sflow2d_dev_gb300.build.build()")
+    lib = C.CDLL(LIB_PATH)
+    vp, dp, i32, i64 = C.c_void_p, C.POINTER(C.c_double), C.c_int32, C.c_int64
+    P = C.POINTER(SflowParams)
+    S = C.POINTER(SflowStepStats)
+    sigs = {
+        "sflow_last_error": (C.c_char_p, []),
+        "sflow_build_info": (C.c_char_p, []),
+        "sflow_default_params": (None, [P]),
+        "sflow_create": (C.c_int, [P, dp, C.POINTER(vp)]),
+        "sflow_destroy": (None, [vp]),
+        "sflow_upload_q": (C.c_int, [vp, dp]),
+        "sflow_download_q": (C.c_int, [vp, dp]),
+        "sflow_download_qp": (C.c_int, [vp, dp]),
+        "sflow_download_maps": (C.c_int, [vp, dp, dp, dp]),
+        "sflow_check_solve": (C.c_int, [vp, i32]),
+        "sflow_timestep": (C.c_int, [vp, dp]),
+        "sflow_imex_rk": (C.c_int, [vp, C.c_double, C.c_double]),
+        "sflow_erosion_deposition": (C.c_int, [vp, C.c_double]),
+        "sflow_post_step": (C.c_int, [vp, S]),
+        "sflow_step": (C.c_int, [vp]),
+        "sflow_advance": (C.c_int, [vp, C.c_double, i64, S]),
+        "sflow_get_stats": (C.c_int, [vp, S]),
+        "sflow_status": (C.c_int, [vp, C.POINTER(C.c_uint32)]),
+        "sflow_clear_status": (C.c_int, [vp]),
+        "sflow_launch_count": (i64, [vp]),
+        "sflow_device_bytes": (i64, [vp]),
+        "sflow_counters": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
+                                     C.POINTER(i32)]),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return ["sflow_last_error", "sflow_build_info", "sflow_default_params", "sflow_create",
+            "sflow_destroy", "sflow_upload_q", "sflow_download_q", "sflow_download_qp",
+            "sflow_download_maps", "sflow_check_solve", "sflow_timestep", "sflow_imex_rk",
+            "sflow_erosion_deposition", "sflow_post_step", "sflow_step", "sflow_advance",
+            "sflow_get_stats", "sflow_status", "sflow_clear_status", "sflow_launch_count",
+            "sflow_device_bytes", "sflow_counters"]
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _check(rc):
+    if rc < 0:
+        raise SflowError(rc, _lib.sflow_last_error().decode())
+    return rc
+
+
+class Solver:
+    """One domain on the GPU.  Method names follow the reference driver's
+    call sites (src/IMEX_SfloW2D.f90:395-505)."""
+
+    def __init__(self, params, B_cent):
+        self.lib = load()
+        self.p = params.copy()
+        self.nx, self.ny = params.comp_cells_x, params.comp_cells_y
+        self.nv = params.n_vars
+        B = np.ascontiguousarray(B_cent, dtype=np.float64).reshape(-1)
+        if B.size != self.nx * self.ny:
+            raise ValueError("B_cent must have nx*ny values")
+        h = C.c_void_p()
+        _check(self.lib.sflow_create(C.byref(self.p), _dp(B), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sflow_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # state -------------------------------------------------------------
+    def upload_q(self, q_aos):
+        q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
+        if q.size != self.nx * self.ny * self.nv:
+            raise ValueError("q must have n_vars*nx*ny values")
+        _check(self.lib.sflow_upload_q(self.h, _dp(q)))
+
+    def download_q(self, out=None):
+        if out is None:
+            out = np.empty(self.nx * self.ny * self.nv)
+        _check(self.lib.sflow_download_q(self.h, _dp(out)))
+        return out
+
+    def download_qp(self):
+        out = np.empty(self.nx * self.ny * (self.nv + 2))
+        _check(self.lib.sflow_download_qp(self.h, _dp(out)))
+        return out
+
+    def maps(self):
+        a = [np.empty(self.nx * self.ny) for _ in range(3)]
+        _check(self.lib.sflow_download_maps(self.h, *[_dp(x) for x in a]))
+        return a
+
+    # reference call sites ---------------------------------------------
+    def check_solve(self, solve_all=False):
+        return _check(self.lib.sflow_check_solve(self.h, 1 if solve_all else 0))
+
+    def timestep(self):
+        dt = C.c_double(0.0)
+        _check(self.lib.sflow_timestep(self.h, C.byref(dt)))
+        return dt.value
+
+    def imex_rk_solver(self, t, dt):
+        return _check(self.lib.sflow_imex_rk(self.h, t, dt))
+
+    def update_erosion_deposition_cell(self, dt):
+        return _check(self.lib.sflow_erosion_deposition(self.h, dt))
+
+    def post_step(self):
+        s = SflowStepStats()
+        _check(self.lib.sflow_post_step(self.h, C.byref(s)))
+        return s
+
+    # fused driver --------------------------------------------------------
+    def step(self):
+        return _check(self.lib.sflow_step(self.h))
+
+    def advance(self, t_stop=1e300, max_steps=1 << 62):
+        s = SflowStepStats()
+        _check(self.lib.sflow_advance(self.h, t_stop, max_steps, C.byref(s)))
+        return s
+
+    def stats(self):
+        s = SflowStepStats()
+        _check(self.lib.sflow_get_stats(self.h, C.byref(s)))
+        return s
+
+    def status(self):
+        f = C.c_uint32(0)
+        _check(self.lib.sflow_status(self.h, C.byref(f)))
+        return f.value
+
+    def counters(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        d = C.c_int32()
+        _check(self.lib.sflow_counters(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return {"cell_updates": a.value, "steps": b.value, "newton_iters": c.value,
+                "newton_max": d.value}
+
+    def launch_count(self):
+        return self.lib.sflow_launch_count(self.h)
+
+    def device_bytes(self):
+        return self.lib.sflow_device_bytes(self.h)

@@ -1,0 +1,229 @@
+/*
+ * sflow.h -- C ABI of the GB300 time-stepping path of IMEX_SfloW2D.
+ *
+ * The reference solver (Fortran) has no library interface: its driver
+ * (src/IMEX_SfloW2D.f90) calls argument-less module procedures that act on
+ * module globals.  Each entry point below replaces one of those call sites;
+ * the citation next to it names the reference routine it stands in for.
+ * A Fortran host binds them with ISO_C_BINDING, a C,
+ * C++ or Python host binds them directly.
+ *
+ * Conventions
+ *  - All entry points return 0 on success, a negative SFLOW_E* code on a
+ *    usage / CUDA error (message in sflow_last_error()), or, for the step
+ *    routines, a positive bit mask of SFLOW_S* solver status flags (the
+ *    reference prints and pauses on READ(*,*) in these situations).
+ *  - Host arrays are borrowed for the duration of the call only.
+ *  - Host state arrays use the reference layout: q(1:n_vars, 1:nx, 1:ny),
+ *    REAL(8), Fortran column-major, variable index fastest
+ *    (src/solver_2d.f90:277); the handle keeps a structure-of-arrays copy in
+ *    GPU memory and transposes on upload/download.
+ *  - A handle is not thread safe; all its device work runs on its own stream.
+ */
+#ifndef SFLOW_H
+#define SFLOW_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFLOW_ABI_VERSION 1
+
+#define SFLOW_MAX_SOLID 4
+/* n_vars = 4 + n_solid (src/inpout_2d.f90:2045-2046 with n_add_gas = 0,
+ * no stochastic, no pore pressure, no gas+liquid mixture). */
+#define SFLOW_MAX_VARS (4 + SFLOW_MAX_SOLID)
+
+/* ---- error codes (negative) ---------------------------------------------- */
+#define SFLOW_OK 0
+#define SFLOW_EINVAL (-1)     /* bad argument or unsupported parameter set   */
+#define SFLOW_ENOMEM (-2)     /* device or host allocation failed            */
+#define SFLOW_ECUDA (-3)      /* CUDA runtime error                          */
+#define SFLOW_ESTATE (-4)     /* call out of order (e.g. step before upload) */
+#define SFLOW_ERANGE (-5)     /* size beyond a fixed capacity                */
+
+/* ---- solver status bits (positive), sticky until sflow_clear_status ------ */
+#define SFLOW_S_NAN 0x1u          /* NaN after assembly (solver_2d.f90:1381)  */
+#define SFLOW_S_NEG_H 0x2u        /* q1 < -1e-7 (solver_2d.f90:1400-1436)     */
+#define SFLOW_S_NEG_ALPHA 0x4u    /* solid mass <= -1e-7 (solver_2d.f90:1440) */
+#define SFLOW_S_LOW_T 0x8u        /* T < 273 K (solver_2d.f90:1541)           */
+#define SFLOW_S_SOLID_GT_MASS 0x10u /* sum solids > q1 (solver_2d.f90:1562)   */
+#define SFLOW_S_NEWTON_MAXIT 0x20u  /* Newton hit max_nl_iter                 */
+#define SFLOW_S_EROSION 0x40u     /* erosion-step consistency check tripped   */
+
+/* ---- precision of the state and of the explicit (bulk) arithmetic -------- */
+#define SFLOW_PREC_FP64 0   /* plain form: everything FP64                      */
+#define SFLOW_PREC_FP32 1   /* FP32 state/fluxes; Newton, mass sums, wet/dry
+                               thresholds in FP64                              */
+
+/* ---- solver scheme (src/parameters_2d.f90 solver_scheme) ----------------- */
+#define SFLOW_SCHEME_KT 0
+#define SFLOW_SCHEME_UP 1
+
+typedef struct {
+  int32_t flag;   /* 0 Dirichlet value, 1 Neumann slope, 2 one-sided gradient */
+  int32_t pad;
+  double value;
+} SflowBC;     /* TYPE bc (src/parameters_2d.f90:393-396) */
+
+/* Boundary sides, index of SflowParams.bc */
+#define SFLOW_W 0
+#define SFLOW_E 1
+#define SFLOW_S 2
+#define SFLOW_N 3
+
+/*
+ * Parameters: the subset of the IMEX_SfloW2D.inp namelists that the time
+ * step reads.  Names follow the namelist keys (src/inpout_2d.f90:326-391,
+ * 1017-1039).  Derived constants (rho_a_amb, eps_sing, h_source from
+ * MFR_SOURCE, ...) are computed by sflow_create the way read_param does.
+ */
+typedef struct {
+  int32_t abi_version;          /* = SFLOW_ABI_VERSION */
+  int32_t precision;            /* SFLOW_PREC_* */
+
+  /* NEWRUN_PARAMETERS */
+  int32_t comp_cells_x, comp_cells_y;
+  double x0, y0, cell_size;
+  int32_t n_solid;
+  int32_t gas_flag, liquid_flag, energy_flag, alpha_flag;
+  int32_t rheology_flag;
+  int32_t slope_correction_flag, curvature_term_flag;
+  int32_t radial_source_flag;
+
+  /* NUMERIC_PARAMETERS */
+  int32_t solver_scheme;        /* SFLOW_SCHEME_* */
+  int32_t n_rk;                 /* 1..4 */
+  double dt0, max_dt, cfl, theta, reconstr_coeff;
+  int32_t limiter[SFLOW_MAX_VARS]; /* per conservative variable; u,v copy hu,hv */
+
+  /* *_BOUNDARY_CONDITIONS, per side, per variable (h, hu, hv, T, solids) */
+  SflowBC bc[4][SFLOW_MAX_VARS];
+
+  /* EXPL_TERMS_PARAMETERS */
+  double grav;
+
+  /* RHEOLOGY_PARAMETERS */
+  int32_t rheology_model;       /* 1 Voellmy-Salm, 6 quadratic friction */
+  int32_t pad0;
+  double mu, xi, friction_factor;
+
+  /* GAS_TRANSPORT_PARAMETERS */
+  double pres, sp_heat_a, sp_gas_const_a, kin_visc_a, T_ambient;
+  int32_t entrainment_flag;
+  int32_t pad1;
+
+  /* LIQUID_TRANSPORT_PARAMETERS */
+  double rho_l, sp_heat_l, kin_visc_l, loss_rate;
+
+  /* SOLID_TRANSPORT_PARAMETERS */
+  double rho_s[SFLOW_MAX_SOLID], diam_s[SFLOW_MAX_SOLID], sp_heat_s[SFLOW_MAX_SOLID];
+  int32_t settling_flag, collective_settling_flag;
+  double alphastot_min, maximum_solid_packing, A_drag, B_drag;
+  double erosion_coeff;         /* only 0 is supported */
+
+  /* RADIAL_SOURCE_PARAMETERS (lateral ring inlet) */
+  double x_source, y_source, r_source, r2_source;
+  double vel_source, T_source, h_source, mfr_source;
+  double alphas_source[SFLOW_MAX_SOLID];
+  double time_param[4];
+  double azimuth_source, arc_width_source;
+
+  /* RUN_PARAMETERS */
+  double t_start, t_end, dt_output;
+} SflowParams;
+
+/* Fill p with the defaults of init_param (src/inpout_2d.f90:408-985). */
+void sflow_default_params(SflowParams* p);
+
+/* Per-step scalars of the driver log line (src/IMEX_SfloW2D.f90:535-542),
+ * accumulated in FP64 with compensated summation. */
+typedef struct {
+  double t, dt;
+  double mass;        /* dx*dy*SUM(q(1,:,:))         */
+  double volume;      /* dx*dy*SUM(qp(1,:,:))        */
+  double area;        /* dx*dy*COUNT(q(1,:,:)>1e-7)  */
+  double solid_mass;  /* dx*dy*SUM(q(5:4+n_solid,:,:)) */
+  int64_t solve_cells;   /* active cells of this step (solver_2d.f90:788-811) */
+  int64_t steps;         /* steps taken so far */
+  uint32_t status;       /* SFLOW_S_* bits seen so far */
+  uint32_t pad;
+} SflowStepStats;
+
+typedef struct sflow_handle sflow_handle;
+
+/* Last error message of the calling thread ("" if none). */
+const char* sflow_last_error(void);
+
+/*
+ * Create a solver for one domain.  B_cent: cell-centred topography, nx*ny
+ * doubles, column-major (geometry_2d.f90 B_cent(nx,ny)); the topography
+ * derivatives (topography_reconstruction, geometry_2d.f90:555-895) and the
+ * ring-source geometry (init_source, geometry_2d.f90:907-1323) are derived
+ * from it.  Replaces init_grid + init_problem_param +
+ * allocate_solver_variables + init_source (IMEX_SfloW2D.f90:186-263).
+ */
+int sflow_create(const SflowParams* p, const double* B_cent, sflow_handle** out);
+void sflow_destroy(sflow_handle* h);
+
+/* State transfer (reference layout, see header comment).  upload also sets
+ * t = t_start, dt = dt_old = dt_old_old = dt0 (IMEX_SfloW2D.f90:300-304). */
+int sflow_upload_q(sflow_handle* h, const double* q_aos);
+int sflow_download_q(sflow_handle* h, double* q_aos);
+/* qp(1:n_vars+2,nx,ny) of the last post-step pass. */
+int sflow_download_qp(sflow_handle* h, double* qp_aos);
+/* hmax, pdynmax, mod_vel_max, each nx*ny column-major (IMEX_SfloW2D.f90:449-505) */
+int sflow_download_maps(sflow_handle* h, double* hmax, double* pdynmax, double* mod_vel_max);
+
+/* check_solve (solver_2d.f90:667-858): active-cell mask of this step. */
+int sflow_check_solve(sflow_handle* h, int32_t solve_all);
+/* timestep (solver_2d.f90:873-1006): CFL time step over the active cells. */
+int sflow_timestep(sflow_handle* h, double* dt_cfl_out);
+/* imex_RK_solver (solver_2d.f90:1022-1634) with the given t and dt. */
+int sflow_imex_rk(sflow_handle* h, double t, double dt);
+/* update_erosion_deposition_cell (solver_2d.f90:2382-2597). */
+int sflow_erosion_deposition(sflow_handle* h, double dt);
+/* Post-step qc_to_qp + maxima + log sums (IMEX_SfloW2D.f90:449-543);
+ * advances t by dt of the last imex_rk call. */
+int sflow_post_step(sflow_handle* h, SflowStepStats* stats);
+
+/*
+ * One iteration of the driver loop (IMEX_SfloW2D.f90:395-505): check_solve,
+ * timestep, the dt clamps (:417-439), imex_RK_solver, erosion/deposition,
+ * t += dt, post-step maxima.  dt is computed and clamped on the device; the
+ * call does not synchronise.  Returns status bits seen so far.
+ */
+int sflow_step(sflow_handle* h);
+/*
+ * Run driver iterations until t >= t_stop (or t_end) or max_steps are done.
+ * Steps are launched as CUDA-graph replays in chunks; the call returns after
+ * the device has finished.  stats (may be NULL) receives the last step's log
+ * scalars.
+ */
+int sflow_advance(sflow_handle* h, double t_stop, int64_t max_steps, SflowStepStats* stats);
+/* Synchronise and read the log scalars of the last completed step. */
+int sflow_get_stats(sflow_handle* h, SflowStepStats* stats);
+int sflow_status(sflow_handle* h, uint32_t* flags);
+int sflow_clear_status(sflow_handle* h);
+
+/* Number of kernel launches issued by this handle since creation (for the
+ * benchmark's launch count). */
+int64_t sflow_launch_count(const sflow_handle* h);
+
+/* Device bytes held by the handle. */
+int64_t sflow_device_bytes(const sflow_handle* h);
+
+/* Work counters since the last upload: cell updates (sum over steps of the
+ * active cells), steps, Newton iterations and the largest per-cell count. */
+int sflow_counters(sflow_handle* h, int64_t* cell_updates, int64_t* steps,
+                   int64_t* newton_iters, int32_t* newton_max);
+
+/* Build information ("fp64+fp32 sm_103a ..."). */
+const char* sflow_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SFLOW_H */
