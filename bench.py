@@ -1,0 +1,405 @@
+"""Benchmark of the IMEX_SfloW2D time step on GB300.
+
+Workload (one step = one driver iteration of the time loop): the single
+pyroclastic-style current of the benchmark configurations -- 1024x1024 cells,
+dx = 10 m, Gaussian cone (1500 m, sigma 2 km) + fBm DEM (Hurst 0.8, 20 m RMS,
+seed 1), ring inlet of radius 50 m at the summit with 1e6 kg/s at 20 m/s,
+2 particle classes (1e-4 / 1e-3 m, 2500 / 1500 kg/m^3, 1 % / 2 %), gas at
+1000 K with temperature-dependent density (total-energy equation), Voellmy
+friction (mu = 0.1, xi = 1000), slope correction, N_RK = 2, KT fluxes,
+minmod.  The state is a seeded developed current (37 % of the cells wet,
+see workloads.developed_current_state) shared by every arm.
+
+Metric: cell-updates/s = sum over steps of the active cells (solve_cells of
+the reference's check_solve) / time.  `value` is the FP32 bulk form (FP32
+state and fluxes, FP64 implicit Newton solve, FP64 mass sums, FP64-exact
+wet/dry tests) timed on the device with CUDA events on the solver's stream,
+one step per timed interval with a 512 MB write between steps to flush L2
+(the working set, ~100 MB, would otherwise stay in the 126 MB L2).  The
+plain FP64 form is timed the same way and reported beside it, with the L1
+error of h between the two forms.  `e2e` is the same metric through the C
+ABI with the state in pinned host memory copied in and out every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from imex_sflow2d_dev_gb300 import workloads as W  # noqa: E402
+from imex_sflow2d_dev_gb300.params import PREC_FP32, PREC_FP64  # noqa: E402
+
+METRIC = ("cell-updates/s (batched FP32 vs plain FP64 GPU, ≤1e-4 L1 err) ; "
+          "p50/p99 solve latency")
+UNIT = "cell-updates/s"
+WORKLOAD = "pyroclastic current 1024x1024 dx=10m, ring inlet 1e6 kg/s, 2 classes, Voellmy, N_RK=2"
+
+
+def build_workload(precision):
+    p, B, _ = W.pyroclastic(nx=1024, ny=1024, dx=10.0, settling=False, precision=precision,
+                            t_end=1.0e9)
+    q = W.developed_current_state(p, B)
+    return p, B, q
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Replica runs on N GPUs: no data exchange, only a barrier around the
+    timed region and a max over ranks of the measured time."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+            self.torch = torch
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64,
+                              device="cuda" if self.torch.cuda.is_available() else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64,
+                              device="cuda" if self.torch.cuda.is_available() else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_traffic():
+    """DRAM bytes per active cell of the dominant kernel from the committed
+    ncu summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "k_flux_pyroclastic_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                   "reasons": sorted(reasons), "samples": len(sm)}
+        return out
+
+
+def l1_rel(a, b):
+    return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+
+
+def cpu_baseline(p, B, q, max_seconds=20.0, max_steps=40):
+    """The oracle (C restatement of the reference time step, OpenMP on all
+    host cores) on a bounded sample of the same workload."""
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.Oracle(p, B)
+    o.set_q(W.to_aos(q))
+    o.step()  # first step outside the sample (page faults, thread start)
+    cells = 0
+    n = 0
+    t0 = time.perf_counter()
+    while n < max_steps:
+        o.step()
+        cells += o.stats().solve_cells
+        n += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": cells / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} steps of the 1024x1024 workload from the same initial state, "
+                      f"{cells} cell updates in {dt:.2f} s (oracle C restatement, OpenMP)",
+            "steps": n, "seconds": dt}
+
+
+def run_reference(args, d):
+    if d.rank != 0:
+        return 0
+    p, B, q = build_workload(PREC_FP64)
+    steps = max(args.steps // 10, 3)
+    cb = cpu_baseline(p, B, q, max_seconds=25.0, max_steps=steps + args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": cb["steps"], "warmup": 1,
+        "ms_per_step": 1e3 * cb["seconds"] / max(cb["steps"], 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded DEM and developed-current state)",
+        "config": {"workload": WORKLOAD, "cells": 1024 * 1024, "precision": "FP64 CPU",
+                   "implementation": "oracle/sflow_oracle.c (C restatement of the Fortran "
+                                     "reference, which has no compiler on this box)"},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def timed_form(lib, p, B, q, steps, warmup, flush=True):
+    s = lib.Solver(p, B)
+    s.upload_q(W.to_aos(q))
+    s.advance(max_steps=warmup)
+    c0 = s.counters()
+    l0 = s.launch_count()
+    ms = s.advance_timed(steps, flush_l2=flush)
+    c1 = s.counters()
+    l1 = s.launch_count()
+    cells = c1["cell_updates"] - c0["cell_updates"]
+    return s, {"ms": ms, "cells": cells, "steps": c1["steps"] - c0["steps"],
+               "launches": l1 - l0, "newton_iters": c1["newton_iters"] - c0["newton_iters"],
+               "newton_max": c1["newton_max"]}
+
+
+def run_gb300(args, d):
+    from imex_sflow2d_dev_gb300 import lib
+    lib.load()
+    p32, B, q = build_workload(PREC_FP32)
+    p64 = p32.copy()
+    p64.precision = PREC_FP64
+    nx, ny, nv = p32.comp_cells_x, p32.comp_cells_y, p32.n_vars
+
+    clocks = ClockSampler(d.local)
+    d.barrier()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    s32, r32 = timed_form(lib, p32, B, q, args.steps, args.warmup)
+    t_wall1 = time.perf_counter()
+    clk = clocks.stop()
+    d.barrier()
+    ms_max = d.max(r32["ms"])
+    cells_all = d.sum(r32["cells"])
+    value = cells_all / (ms_max / 1e3)
+
+    # plain FP64 form, same start state and step count
+    s64, r64 = timed_form(lib, p64, B, q, max(args.steps // 5, 3), args.warmup)
+    value64 = r64["cells"] / (r64["ms"] / 1e3)
+    # FP32 vs FP64 after the same number of steps from the same state
+    a32 = lib.Solver(p32, B)
+    a32.upload_q(W.to_aos(q))
+    a64 = lib.Solver(p64, B)
+    a64.upload_q(W.to_aos(q))
+    nerr = 20
+    a32.advance(max_steps=nerr)
+    a64.advance(max_steps=nerr)
+    h32 = W.from_aos(a32.download_qp(), nv + 2, nx, ny)[0]
+    h64 = W.from_aos(a64.download_qp(), nv + 2, nx, ny)[0]
+    err_h = l1_rel(h32, h64)
+    t32, t64 = a32.stats().t, a64.stats().t
+    a32.close()
+    a64.close()
+
+    # per-kernel device time (events between the kernels of each step)
+    pk = lib.Solver(p32, B)
+    pk.upload_q(W.to_aos(q))
+    pk.advance(max_steps=args.warmup)
+    c0 = pk.counters()
+    kms = pk.profile_kernels(max(args.steps // 2, 3), flush_l2=True)
+    c1 = pk.counters()
+    pk_steps = c1["steps"] - c0["steps"]
+    pk_cells = (c1["cell_updates"] - c0["cell_updates"]) / max(pk_steps, 1)
+    pk.close()
+    dom = max(("flux", "stage"), key=lambda k: kms[k])
+    s4 = 4  # FP32 bytes
+    n = nv
+    # algorithmic bytes per active cell (reads + writes a launch must do):
+    #  flux : q (n) + topography terms for the explicit sources (5) + flag and
+    #         mask bytes, write divFlux - expl (n)
+    #  stage: q (n) + divFlux - expl (n) + 3 topography terms + mask byte,
+    #         write q (n), read+write 3 maxima maps
+    alg = {"flux": (2 * n + 5) * s4 + 2, "stage": (3 * n + 3 + 6) * s4 + 1}
+    bytes_launch = alg[dom] * pk_cells
+    dur_s = kms[dom] / 1e3 / max(pk_steps, 1)
+    achieved = bytes_launch / dur_s / 1e9
+    peak, peak_kind = read_peaks()
+    tr = read_traffic()
+    traffic = None
+    if tr and tr.get("kernel") == dom and tr.get("bytes_per_active_cell"):
+        traffic = tr["bytes_per_active_cell"] * pk_cells
+
+    # end to end through the C ABI, state in pinned host memory every step
+    e2e = None
+    try:
+        import torch
+        pinned = torch.empty(nx * ny * nv, dtype=torch.float64, pin_memory=True)
+        pinned.numpy()[:] = W.to_aos(q)
+        se = lib.Solver(p32, B)
+        se.upload_q(W.to_aos(q))
+        se.advance(max_steps=args.warmup)
+        ptr = pinned.data_ptr()
+        ne = max(args.steps // 5, 3)
+        c0 = se.counters()
+        se.download_q_ptr(ptr)
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            se.put_q_ptr(ptr)
+            se.step()
+            se.download_q_ptr(ptr)
+        te = time.perf_counter() - t0
+        c1 = se.counters()
+        e2e = {"value": d.sum((c1["cell_updates"] - c0["cell_updates"])) / d.max(te),
+               "unit": UNIT, "h2d_bytes_per_step": nx * ny * nv * 8,
+               "d2h_bytes_per_step": nx * ny * nv * 8, "steps": ne,
+               "path": "sflow_put_q + sflow_step + sflow_download_q, pinned host buffers"}
+        se.close()
+    except Exception as exc:  # pragma: no cover - reported, not hidden
+        e2e = {"value": None, "unit": UNIT, "error": str(exc)}
+
+    cb = None
+    if d.rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(p64, B, q, max_seconds=args.cpu_seconds, max_steps=40)
+
+    if d.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / max(r32["steps"], 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded cone+fBm DEM, seeded developed-current state)",
+            "config": {"workload": WORKLOAD, "cells": nx * ny,
+                       "active_cells_per_step": r32["cells"] / max(r32["steps"], 1),
+                       "form": "FP32 bulk + FP64 implicit solve",
+                       "l2": "flushed between timed steps (512 MB write), one step per "
+                             "event-timed interval",
+                       "parallelism": f"replicas x{args.gpus}"},
+            "fp64_plain": {"value": value64, "ms_per_step": r64["ms"] / max(r64["steps"], 1),
+                           "steps": r64["steps"], "newton_iters_per_cell":
+                           r64["newton_iters"] / max(r64["cells"], 1)},
+            "speedup_fp32_over_fp64": value / value64 if value64 else None,
+            "error_vs_fp64": {"l1_rel_h": err_h, "steps": nerr, "t_fp32": t32, "t_fp64": t64},
+            "newton_iters_per_cell": r32["newton_iters"] / max(r32["cells"], 1),
+            "roofline": {"bound": "hbm", "kernel": "k_flux" if dom == "flux" else "k_stage2",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic, "alg_bytes_per_active_cell": alg[dom],
+                         "kernel_ms_per_step": {k: v / max(pk_steps, 1) for k, v in kms.items()}},
+            "cpu_baseline": ({k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+                             if cb else None),
+            "e2e": e2e,
+            "gpu_launches": r32["launches"],
+            "clocks": clk,
+            "wall_s_timed_region": t_wall1 - t_wall0,
+        }
+        print(json.dumps(line), flush=True)
+    for x in (s32, s64):
+        x.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    d = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, d)
+        return run_gb300(args, d)
+    finally:
+        d.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -2,6 +2,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/sflow.h"
 #include "sflow_host.h"
@@ -124,6 +125,25 @@ int sflow_upload_q(sflow_handle* h, const double* q) {
   if (!q) return fail(SFLOW_EINVAL, "q is NULL");
   FORWARD(h->solver->upload(q));
 }
+int sflow_put_q(sflow_handle* h, const double* q) {
+  CHECK_HANDLE(h);
+  if (!q) return fail(SFLOW_EINVAL, "q is NULL");
+  FORWARD(h->solver->put(q));
+}
+int sflow_set_clock(sflow_handle* h, double t, double dt_old, double dt_old_old) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->set_clock(t, dt_old, dt_old_old));
+}
+int sflow_advance_timed(sflow_handle* h, int64_t steps, int32_t flush_l2, double* ms) {
+  CHECK_HANDLE(h);
+  if (!ms || steps < 0) return fail(SFLOW_EINVAL, "bad arguments");
+  FORWARD(h->solver->advance_timed(steps, flush_l2, ms));
+}
+int sflow_profile_kernels(sflow_handle* h, int64_t steps, int32_t flush_l2, double* ms4) {
+  CHECK_HANDLE(h);
+  if (!ms4 || steps < 0) return fail(SFLOW_EINVAL, "bad arguments");
+  FORWARD(h->solver->profile_kernels(steps, flush_l2, ms4));
+}
 int sflow_download_q(sflow_handle* h, double* q) {
   CHECK_HANDLE(h);
   if (!q) return fail(SFLOW_EINVAL, "q is NULL");
@@ -197,6 +217,43 @@ int64_t sflow_launch_count(const sflow_handle* h) {
 int64_t sflow_device_bytes(const sflow_handle* h) {
   return (h && h->solver) ? h->solver->device_bytes() : -1;
 }
+int sflow_host_geometry(const SflowParams* p, const double* B_cent, int32_t which, double* out) {
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  HostSetup s;
+  std::string err;
+  int rc = sflow::host_setup(p, B_cent, s, err);
+  if (rc != SFLOW_OK) return fail(rc, err);
+  const std::vector<double>* f[11] = {&s.Bx, &s.By, &s.Bxx, &s.Bxy, &s.Byy, &s.gc, &s.dgcx, &s.dgcy,
+                                      &s.arc_perim, &s.arc_nx, &s.arc_ny};
+  const size_t N = (size_t)s.nx * s.ny;
+  if (which >= 0 && which <= 10) {
+    for (size_t i = 0; i < N; ++i) out[i] = (*f[which])[i];
+  } else if (which == 11) {
+    for (size_t i = 0; i < N; ++i) out[i] = (double)(s.cflags[i] & 0x3);
+  } else if (which == 12) {
+    for (size_t i = 0; i < N; ++i) {
+      uint8_t c = s.cflags[i];
+      out[i] = (double)(((c >> 2) & 1) | (((c >> 3) & 1) << 1) | (((c >> 4) & 1) << 2) | (((c >> 5) & 1) << 3));
+    }
+  } else {
+    return fail(SFLOW_EINVAL, "which must be in 0..12");
+  }
+  return SFLOW_OK;
+}
+
+int sflow_host_scalars(const SflowParams* p, const double* B_cent, double* out4) {
+  if (!out4) return fail(SFLOW_EINVAL, "out is NULL");
+  HostSetup s;
+  std::string err;
+  int rc = sflow::host_setup(p, B_cent, s, err);
+  if (rc != SFLOW_OK) return fail(rc, err);
+  out4[0] = s.h_source;
+  out4[1] = s.src_rho_m;
+  out4[2] = s.src_cp_mix;
+  out4[3] = s.eps_sing;
+  return SFLOW_OK;
+}
+
 int sflow_counters(sflow_handle* h, int64_t* cell_updates, int64_t* steps, int64_t* newton_iters,
                    int32_t* newton_max) {
   CHECK_HANDLE(h);

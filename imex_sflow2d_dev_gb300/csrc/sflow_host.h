@@ -44,6 +44,10 @@ class SolverBase {
  public:
   virtual ~SolverBase() {}
   virtual int upload(const double* q_aos) = 0;
+  virtual int put(const double* q_aos) = 0;
+  virtual int set_clock(double t, double dt_old, double dt_old_old) = 0;
+  virtual int advance_timed(int64_t steps, int flush, double* ms) = 0;
+  virtual int profile_kernels(int64_t steps, int flush, double* ms4) = 0;
   virtual int download(double* q_aos) = 0;
   virtual int download_qp(double* qp_aos) = 0;
   virtual int download_maps(double* h, double* p, double* v) = 0;

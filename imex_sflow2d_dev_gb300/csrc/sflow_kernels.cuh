@@ -79,22 +79,22 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
 template <class R>
 __device__ __forceinline__ R xstag(const Grid<R>& g, int j) {
   if constexpr (sizeof(R) == 8) return g.x0 + (double)j * g.dx;
-  else return (R)g.x0 + (R)j * g.rdx;
+  else return g.x0r + (R)j * g.rdx;
 }
 template <class R>
 __device__ __forceinline__ R xcomp(const Grid<R>& g, int j) {
   if constexpr (sizeof(R) == 8) return 0.5 * ((g.x0 + (double)j * g.dx) + (g.x0 + (double)(j + 1) * g.dx));
-  else return (R)g.x0 + ((R)j + 0.5f) * g.rdx;
+  else return g.x0r + ((R)j + 0.5f) * g.rdx;
 }
 template <class R>
 __device__ __forceinline__ R ystag(const Grid<R>& g, int k) {
   if constexpr (sizeof(R) == 8) return g.y0 + (double)k * g.dy;
-  else return (R)g.y0 + (R)k * g.rdy;
+  else return g.y0r + (R)k * g.rdy;
 }
 template <class R>
 __device__ __forceinline__ R ycomp(const Grid<R>& g, int k) {
   if constexpr (sizeof(R) == 8) return 0.5 * ((g.y0 + (double)k * g.dy) + (g.y0 + (double)(k + 1) * g.dy));
-  else return (R)g.y0 + ((R)k + 0.5f) * g.rdy;
+  else return g.y0r + ((R)k + 0.5f) * g.rdy;
 }
 
 template <class R>
@@ -157,206 +157,190 @@ __global__ void __launch_bounds__(TX* TY) k_mask(KArgs<R> a, int solve_all) {
   }
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
     st->src_t_coeff = source_time_coeff(st->tp, st->pi_g, t);
+    st->src_t_coeff_f = (float)st->src_t_coeff;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Limited slopes (geometry_2d.f90:1776-1897).  The plain FP64 form divides by
+// the stencil spacings exactly as the reference; the FP32 form multiplies by
+// reciprocals (1/dx for the uniform interior stencil) and takes signs with
+// copysign instead of a/|a|.
+// ---------------------------------------------------------------------------
+template <class R>
+struct Spacing {
+  R z0, z1, z2;
+  R r01, r12, r02;   // FP32 form only
+};
+
+template <class R>
+__device__ __forceinline__ Spacing<R> spacing(R z0, R z1, R z2, bool uniform, R inv_d) {
+  Spacing<R> s;
+  s.z0 = z0; s.z1 = z1; s.z2 = z2;
+  if constexpr (sizeof(R) == 4) {
+    if (uniform) { s.r01 = inv_d; s.r12 = inv_d; s.r02 = 0.5f * inv_d; }
+    else { s.r01 = 1.0f / (z1 - z0); s.r12 = 1.0f / (z2 - z1); s.r02 = 1.0f / (z2 - z0); }
+  } else {
+    s.r01 = s.r12 = s.r02 = R(0);
+  }
+  return s;
+}
+
+__device__ __forceinline__ float minmod_f(float a, float b) {
+  float m = fminf(fabsf(a), fabsf(b));
+  if (m <= 0.0f) return 0.0f;
+  return 0.5f * (copysignf(1.0f, a) + copysignf(1.0f, b)) * m;
+}
+__device__ __forceinline__ float maxmod_f(float a, float b) {
+  if (fabsf(a * b) <= 0.0f) return 0.0f;
+  return 0.5f * (copysignf(1.0f, a) + copysignf(1.0f, b)) * fmaxf(fabsf(a), fabsf(b));
+}
+
+template <class R>
+__device__ __forceinline__ R slope(R v0, R v1, R v2, const Spacing<R>& s, int lim, R theta) {
+  if constexpr (sizeof(R) == 8) {
+    return limit(v0, v1, v2, s.z0, s.z1, s.z2, lim, theta);
+  } else {
+    const float a = (v2 - v1) * s.r12, b = (v1 - v0) * s.r01;
+    switch (lim) {
+      case 0: return 0.0f;
+      case 1: return minmod_f(a, b);
+      case 2: return maxmod_f(minmod_f(a, 2.0f * b), minmod_f(2.0f * a, b));
+      case 3: return minmod_f((v2 - v0) * s.r02, theta * minmod_f(a, b));
+      case 4: return minmod_f((v2 - v0) * s.r02, 2.0f * minmod_f(a, b));
+      case 5: return (v2 - v0) * s.r02;
+      case 6: return a;
+      case 7: return b;
+    }
+    return 0.0f;
   }
 }
 
 // ---------------------------------------------------------------------------
 // Reconstruction of one side of one face (solver_2d.f90:3095-3924).
 // The cell is at region coordinates (rx, ry) of the shared tile, global
-// (j, k).  dir 1: x faces, plus = 1 east side, 0 west side; dir 2: y faces,
+// (j, k).  DIR 1: x faces, plus = 1 east side, 0 west side; DIR 2: y faces,
 // plus = 1 north side, 0 south side.  Writes the physical face state qp
-// (n_vars+2).  Only the stencil along `dir` enters, apart from the
-// reference's use of y_stag in the x slope of v at some ring cells
-// (solver_2d.f90:3605, kept as is).
+// (n_vars+2).  Only the stencil along DIR enters, apart from the
+// reference's use of y_stag in the x slope of v at ring cells with a ring
+// face to the north only (solver_2d.f90:3605, kept as is).
 // ---------------------------------------------------------------------------
-template <class R, int NS>
+template <class R, int NS, int DIR>
 __device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, const uint8_t* sfl,
-                                           int rx, int ry, int j, int k, int dir, int plus, R* out) {
+                                           int rx, int ry, int j, int k, int plus, R* out) {
   constexpr int nv = 4 + NS, np = nv + 2;
   const Grid<R>& g = a.g;
-  const Phys<R>& P = a.pr;
-  const int plane = RX * RY;
-  auto QP = [&](int i, int ox, int oy) -> R { return sqp[i * plane + (ry + oy) * RX + (rx + ox)]; };
+  constexpr int plane = RX * RY;
+  constexpr int side_lo = (DIR == 1) ? SFLOW_W : SFLOW_S;
+  constexpr int side_hi = (DIR == 1) ? SFLOW_E : SFLOW_N;
+  constexpr int mom = DIR;   // hu (x) or hv (y) in the conservative/physical index
+  auto QP = [&](int i, int o) -> R {
+    return (DIR == 1) ? sqp[i * plane + ry * RX + (rx + o)] : sqp[i * plane + (ry + o) * RX + rx];
+  };
   const uint8_t fl = sfl[ry * RX + rx];
   const int sc = fl & F_SC_MASK;
-  const bool radial = P.radial_source;
-  const bool src2 = radial && sc == 2;
+  const bool src2 = a.pr.radial_source && sc == 2;
+  const int n = (DIR == 1) ? g.nx : g.ny;
+  const int c = (DIR == 1) ? j : k;
+  const bool b0 = (c == 0), b1 = (c == n - 1);
+  const bool interior = !b0 && !b1;
+  // ring faces of the cell along DIR: "hi" = E or N, "lo" = W or S
+  const bool s_hi = (DIR == 1) ? (fl & F_E) : (fl & F_N);
+  const bool s_lo = (DIR == 1) ? (fl & F_W) : (fl & F_S);
+  // x: IF sourceE ... ELSEIF sourceW;  y: IF sourceS ... ELSEIF sourceN
+  const bool use_hi = (DIR == 1) ? s_hi : (s_hi && !s_lo);
+  const bool use_lo = (DIR == 1) ? (s_lo && !s_hi) : s_lo;
+  auto stag = [&](int m) -> R { return (DIR == 1) ? xstag(g, m) : ystag(g, m); };
+  auto comp = [&](int m) -> R { return (DIR == 1) ? xcomp(g, m) : ycomp(g, m); };
+  const R inv_d = (DIR == 1) ? g.one_by_dx : g.one_by_dy;
+  const R d2 = (DIR == 1) ? g.dx2 : g.dy2;
   R cell[np];
 #pragma unroll
-  for (int i = 0; i < np; ++i) cell[i] = QP(i, 0, 0);
-  R qm[np];   // the reconstructed side (W/S for plus=0, E/N for plus=1)
-  if (dir == 1) {
-    const int nx = g.nx;
-    const bool jb0 = (j == 0), jb1 = (j == nx - 1);
-    const bool interior = !jb0 && !jb1;
-    const bool sE = fl & F_E, sW = fl & F_W;
-    R z0, z1 = xcomp(g, j), z2;
-    if (jb0) { z0 = xstag(g, 0); z2 = xcomp(g, 1); }
-    else if (jb1) { z0 = xcomp(g, nx - 2); z2 = xstag(g, nx); }
-    else {
-      z0 = xcomp(g, j - 1); z2 = xcomp(g, j + 1);
-      if (src2) { if (sE) z2 = xstag(g, j + 1); else if (sW) z0 = xstag(g, j); }
+  for (int i = 0; i < np; ++i) cell[i] = QP(i, 0);
+  R z0, z1 = comp(c), z2;
+  bool uniform = false;
+  if (b0) { z0 = stag(0); z2 = comp(1); }
+  else if (b1) { z0 = comp(n - 2); z2 = stag(n); }
+  else {
+    z0 = comp(c - 1); z2 = comp(c + 1);
+    uniform = true;
+    if (src2) {
+      if (use_hi) { z2 = stag(c + 1); uniform = false; }
+      else if (use_lo) { z0 = stag(c); uniform = false; }
     }
-    // conservative-index variables (vars_loop)
-    R wv[nv], ev[nv];
+  }
+  const Spacing<R> sp = spacing<R>(z0, z1, z2, uniform, inv_d);
+  R qm[np];
+  R lo[nv], hi[nv];
+  // conservative-index variables (vars_loop)
 #pragma unroll
-    for (int i = 0; i < nv; ++i) {
-      R slope;
-      const R v1 = cell[i];
-      if (jb0) {
-        if (sc == 2) slope = limit(cell[i], v1, QP(i, 1, 0), z0, z1, z2, g.limiter[i], g.theta);
-        else if (a.bc.flag[SFLOW_W][i] == 0) slope = limit(a.bc.value[SFLOW_W][i], v1, QP(i, 1, 0), z0, z1, z2, g.limiter[i], g.theta);
-        else if (a.bc.flag[SFLOW_W][i] == 1) slope = a.bc.value[SFLOW_W][i];
-        else slope = (QP(i, 1, 0) - QP(i, 0, 0)) * g.one_by_dx;
-      } else if (jb1) {
-        if (sc == 2) slope = limit(QP(i, -1, 0), v1, cell[i], z0, z1, z2, g.limiter[i], g.theta);
-        else if (a.bc.flag[SFLOW_E][i] == 0) slope = limit(QP(i, -1, 0), v1, a.bc.value[SFLOW_E][i], z0, z1, z2, g.limiter[i], g.theta);
-        else if (a.bc.flag[SFLOW_E][i] == 1) slope = a.bc.value[SFLOW_E][i];
-        else slope = (QP(i, 0, 0) - QP(i, -1, 0)) * g.one_by_dx;
-      } else {
-        R v0 = QP(i, -1, 0), v2 = QP(i, 1, 0);
-        if (src2) { if (sE) v2 = cell[i]; else if (sW) v0 = cell[i]; }
-        slope = limit(v0, v1, v2, z0, z1, z2, g.limiter[i], g.theta);
-      }
-      const R dq = g.rc * g.dx2 * slope;
-      R w = v1 - dq, e = v1 + dq;
-      if (jb0) {
-        if (sc == 2) w = cell[i];
-        else if (a.bc.flag[SFLOW_W][i] == 0) w = a.bc.value[SFLOW_W][i];
-        else if (i == 1) w = rmin(w, R(0));
-      }
-      if (jb1) {
-        if (sc == 2) e = cell[i];
-        else if (a.bc.flag[SFLOW_E][i] == 0) e = a.bc.value[SFLOW_E][i];
-        else if (i == 1) e = rmax(e, R(0));
-      }
-      wv[i] = w;
-      ev[i] = e;
-      qm[i] = plus ? e : w;
+  for (int i = 0; i < nv; ++i) {
+    const R v1 = cell[i];
+    const int bl = a.bc.flag[side_lo][i], bh = a.bc.flag[side_hi][i];
+    R sl;
+    if (b0) {
+      if (DIR == 1 && sc == 2) sl = slope(cell[i], v1, QP(i, 1), sp, g.limiter[i], g.theta);
+      else if (bl == 0) sl = slope(a.bc.value[side_lo][i], v1, QP(i, 1), sp, g.limiter[i], g.theta);
+      else if (bl == 1) sl = a.bc.value[side_lo][i];
+      else sl = (QP(i, 1) - QP(i, 0)) * inv_d;
+    } else if (b1) {
+      if (DIR == 1 && sc == 2) sl = slope(QP(i, -1), v1, cell[i], sp, g.limiter[i], g.theta);
+      else if (bh == 0) sl = slope(QP(i, -1), v1, a.bc.value[side_hi][i], sp, g.limiter[i], g.theta);
+      else if (bh == 1) sl = a.bc.value[side_hi][i];
+      else sl = (QP(i, 0) - QP(i, -1)) * inv_d;
+    } else {
+      R v0 = QP(i, -1), v2 = QP(i, 1);
+      if (src2) { if (use_hi) v2 = cell[i]; else if (use_lo) v0 = cell[i]; }
+      sl = slope(v0, v1, v2, sp, g.limiter[i], g.theta);
     }
-    // velocities (add_vars_loop); qp_to_qp2 (constitutive_2d.f90:2164-2188)
-    // gives u = hu/h, v = hv/h of the west/east state at the domain edges
+    const R dq = g.rc * d2 * sl;
+    R l_ = v1 - dq, h_ = v1 + dq;
+    if (b0) {
+      if (DIR == 1 && sc == 2) l_ = cell[i];
+      else if (bl == 0) l_ = a.bc.value[side_lo][i];
+      else if (i == mom) l_ = rmin(l_, R(0));
+    }
+    if (b1) {
+      if (DIR == 1 && sc == 2) h_ = cell[i];
+      else if (bh == 0) h_ = a.bc.value[side_hi][i];
+      else if (i == mom) h_ = rmax(h_, R(0));
+    }
+    lo[i] = l_;
+    hi[i] = h_;
+    qm[i] = plus ? h_ : l_;
+  }
+  // velocities u, v (add_vars_loop); qp_to_qp2 (constitutive_2d.f90:2164-2188)
+  // gives u = hu/h, v = hv/h of the low / high state at the domain edges
+  Spacing<R> spv = sp;
+  if (DIR == 1 && interior && src2 && !s_hi) {
     const bool kint = (k > 0 && k < g.ny - 1);
     const bool sN = fl & F_N, sS = fl & F_S;
+    if (kint && sN && !sS) spv = spacing<R>(sp.z0, sp.z1, ystag(g, k + 1), false, inv_d);
+  }
 #pragma unroll
-    for (int m = 0; m < 2; ++m) {
-      const int i = nv + m;
-      const R v1 = cell[i];
-      const R uw = (wv[0] <= R(0)) ? R(0) : wv[1 + m] / wv[0];
-      const R ue = (ev[0] <= R(0)) ? R(0) : ev[1 + m] / ev[0];
-      R v0, v2, zz0 = z0, zz2 = z2;
-      if (jb0) {
-        v0 = uw;
-        v2 = QP(i, 1, 0);
-      } else if (jb1) {
-        v0 = QP(i, -1, 0);
-        v2 = ue;
-      } else {
-        v0 = QP(i, -1, 0);
-        v2 = QP(i, 1, 0);
-        if (m == 1 && src2 && kint && !sS && sN) zz2 = ystag(g, k + 1);
-        if (src2) {
-          if (sE) { zz2 = xstag(g, j + 1); v2 = cell[i]; }
-          else if (sW) { zz0 = xstag(g, j); v0 = cell[i]; }
-        }
-      }
-      const R slope = limit(v0, v1, v2, zz0, z1, zz2, g.limiter[i], g.theta);
-      const R dq = g.rc * g.dx2 * slope;
-      R val = plus ? v1 + dq : v1 - dq;
-      if (jb0 && !plus) val = uw;
-      if (jb1 && plus) val = ue;
-      qm[i] = val;
-    }
-    if (interior && src2) {
-      if (plus && sE) {
-#pragma unroll
-        for (int i = 0; i < np; ++i) qm[i] = cell[i];
-      } else if (!plus && sW && !sE) {
-#pragma unroll
-        for (int i = 0; i < np; ++i) qm[i] = cell[i];
-      }
-    }
-  } else {
-    const int ny = g.ny;
-    const bool kb0 = (k == 0), kb1 = (k == ny - 1);
-    const bool interior = !kb0 && !kb1;
-    const bool sN = fl & F_N, sS = fl & F_S;
-    R z0, z1 = ycomp(g, k), z2;
-    if (kb0) { z0 = ystag(g, 0); z2 = ycomp(g, 1); }
-    else if (kb1) { z0 = ycomp(g, ny - 2); z2 = ystag(g, ny); }
+  for (int m = 0; m < 2; ++m) {
+    const int i = nv + m;
+    const R v1 = cell[i];
+    const R ul = (lo[0] <= R(0)) ? R(0) : lo[1 + m] / lo[0];
+    const R uh = (hi[0] <= R(0)) ? R(0) : hi[1 + m] / hi[0];
+    R v0, v2;
+    if (b0) { v0 = ul; v2 = QP(i, 1); }
+    else if (b1) { v0 = QP(i, -1); v2 = uh; }
     else {
-      z0 = ycomp(g, k - 1); z2 = ycomp(g, k + 1);
-      if (src2) { if (sS) z0 = ystag(g, k); else if (sN) z2 = ystag(g, k + 1); }
+      v0 = QP(i, -1);
+      v2 = QP(i, 1);
+      if (src2) { if (use_hi) v2 = cell[i]; else if (use_lo) v0 = cell[i]; }
     }
-    R sv[nv], nvv[nv];
+    const R sl = slope(v0, v1, v2, (m == 1) ? spv : sp, g.limiter[i], g.theta);
+    const R dq = g.rc * d2 * sl;
+    R val = plus ? v1 + dq : v1 - dq;
+    if (b0 && !plus) val = ul;
+    if (b1 && plus) val = uh;
+    qm[i] = val;
+  }
+  if (interior && src2 && ((plus && use_hi) || (!plus && use_lo))) {
 #pragma unroll
-    for (int i = 0; i < nv; ++i) {
-      R slope;
-      const R v1 = cell[i];
-      if (kb0) {
-        if (a.bc.flag[SFLOW_S][i] == 0) slope = limit(a.bc.value[SFLOW_S][i], v1, QP(i, 0, 1), z0, z1, z2, g.limiter[i], g.theta);
-        else if (a.bc.flag[SFLOW_S][i] == 1) slope = a.bc.value[SFLOW_S][i];
-        else slope = (QP(i, 0, 1) - QP(i, 0, 0)) * g.one_by_dy;
-      } else if (kb1) {
-        if (a.bc.flag[SFLOW_N][i] == 0) slope = limit(QP(i, 0, -1), v1, a.bc.value[SFLOW_N][i], z0, z1, z2, g.limiter[i], g.theta);
-        else if (a.bc.flag[SFLOW_N][i] == 1) slope = a.bc.value[SFLOW_N][i];
-        else slope = (QP(i, 0, 0) - QP(i, 0, -1)) * g.one_by_dy;
-      } else {
-        R v0 = QP(i, 0, -1), v2 = QP(i, 0, 1);
-        if (src2) { if (sS) v0 = cell[i]; else if (sN) v2 = cell[i]; }
-        slope = limit(v0, v1, v2, z0, z1, z2, g.limiter[i], g.theta);
-      }
-      const R dq = g.rc * g.dy2 * slope;
-      R s_ = v1 - dq, n_ = v1 + dq;
-      if (kb0) {
-        if (a.bc.flag[SFLOW_S][i] == 0) s_ = a.bc.value[SFLOW_S][i];
-        else if (i == 2) s_ = rmin(s_, R(0));
-      }
-      if (kb1) {
-        if (a.bc.flag[SFLOW_N][i] == 0) n_ = a.bc.value[SFLOW_N][i];
-        else if (i == 2) n_ = rmax(n_, R(0));
-      }
-      sv[i] = s_;
-      nvv[i] = n_;
-      qm[i] = plus ? n_ : s_;
-    }
-#pragma unroll
-    for (int m = 0; m < 2; ++m) {
-      const int i = nv + m;
-      const R v1 = cell[i];
-      const R us = (sv[0] <= R(0)) ? R(0) : sv[1 + m] / sv[0];
-      const R un = (nvv[0] <= R(0)) ? R(0) : nvv[1 + m] / nvv[0];
-      R v0, v2, zz0 = z0;
-      if (kb0) {
-        v0 = us;
-        v2 = QP(i, 0, 1);
-      } else if (kb1) {
-        v0 = QP(i, 0, -1);
-        v2 = un;
-      } else {
-        v0 = QP(i, 0, -1);
-        v2 = QP(i, 0, 1);
-        if (src2) {
-          if (sS) { zz0 = ystag(g, k); v0 = cell[i]; }
-          else if (sN) { v2 = cell[i]; }
-        }
-      }
-      const R slope = limit(v0, v1, v2, zz0, z1, z2, g.limiter[i], g.theta);
-      const R dq = g.rc * g.dy2 * slope;
-      R val = plus ? v1 + dq : v1 - dq;
-      if (kb0 && !plus) val = us;
-      if (kb1 && plus) val = un;
-      qm[i] = val;
-    }
-    if (interior && src2) {
-      if (!plus && sS) {
-#pragma unroll
-        for (int i = 0; i < np; ++i) qm[i] = cell[i];
-      } else if (plus && sN && !sS) {
-#pragma unroll
-        for (int i = 0; i < np; ++i) qm[i] = cell[i];
-      }
-    }
+    for (int i = 0; i < np; ++i) qm[i] = cell[i];
   }
 #pragma unroll
   for (int i = 0; i < np; ++i) out[i] = qm[i];
@@ -371,15 +355,15 @@ struct Side {
   R hu_p;   // qp(2): x zero-velocity test
 };
 
-template <class R, int NS>
-__device__ __forceinline__ void side_from_qp(const KArgs<R>& a, const R* qp, R gcs, int dir,
-                                             Side<R, NS>& s, int negate = -1) {
+template <class R, int NS, int DIR>
+__device__ __forceinline__ void side_from_qp(const KArgs<R>& a, const R* qp, R gcs, Side<R, NS>& s,
+                                             bool mirrored) {
   const Phys<R>& P = a.pr;
   qp_to_qc<R, NS>(P, qp, s.q);
-  if (negate >= 0) s.q[negate] = -s.q[negate];
+  if (mirrored) s.q[DIR] = -s.q[DIR];   // hu (x) / hv (y) of the wall mirror
   Mixt<R> m = mixt_var<R, NS>(P, qp, false);
-  local_speeds<R, NS>(P, qp, m.red_grav, gcs, dir, s.vmin, s.vmax);
-  eval_fluxes<R, NS>(P, s.q, qp, m, gcs, dir, s.f);
+  local_speeds<R, NS>(P, qp, m.red_grav, gcs, DIR, s.vmin, s.vmax);
+  eval_fluxes<R, NS>(P, s.q, qp, m, gcs, DIR, s.f);
   s.hu_p = qp[1];
 }
 
@@ -391,8 +375,8 @@ __device__ __forceinline__ void side_zero(Side<R, NS>& s) {
 }
 
 // KT flux across one face (solver_2d.f90:2834-3049).  H has n_vars entries.
-template <class R, int NS>
-__device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt, int dir, R* H) {
+template <class R, int NS, int DIR>
+__device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt, R* H) {
   constexpr int nv = 4 + NS, ns = NS;
   R a1 = rmin(rmin(L.vmin, Rt.vmin), R(0));
   R a2 = rmax(rmax(L.vmax, Rt.vmax), R(0));
@@ -404,12 +388,14 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
     const R fac = (a2 * a1) / den;
 #pragma unroll
     for (int i = 0; i < nv; ++i) {
-      R avg = (a2 * L.f[i] - a1 * Rt.f[i]) / den;
+      R avg;
+      if constexpr (sizeof(R) == 8) avg = (a2 * L.f[i] - a1 * Rt.f[i]) / den;
+      else avg = (a2 * L.f[i] - a1 * Rt.f[i]) * (1.0f / den);
       H[i] = avg + fac * (Rt.q[i] - L.q[i]);
     }
   }
   if (ns > 0) {
-    if (dir == 1) {
+    if (DIR == 1) {
       R s = R(0), s2 = R(0);
 #pragma unroll
       for (int i = 0; i < ns; ++i) { s += H[4 + i] / H[0]; s2 += H[4 + i]; }
@@ -428,7 +414,7 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
       }
     }
   }
-  const bool zero_vel = (dir == 1) ? (L.hu_p == R(0) && Rt.hu_p == R(0))
+  const bool zero_vel = (DIR == 1) ? (L.hu_p == R(0) && Rt.hu_p == R(0))
                                    : (L.q[2] == R(0) && Rt.q[2] == R(0));
   if (zero_vel) {
     H[0] = R(0);
@@ -436,6 +422,60 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
     for (int i = 3; i < nv; ++i) H[i] = R(0);
   }
   return rmax(a2, -a1);
+}
+
+// One face along DIR between the low cell (f-1) and the high cell (f):
+// reconstruction of both sides, the domain-edge copies and the wall mirror
+// at ring-inlet faces (solver_2d.f90:3716-3920), KT flux.  Returns the
+// largest |speed| at the face (a_interface_*_max).
+template <class R, int NS, int DIR>
+__device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const uint8_t* sfl, int f,
+                                       int o, int rxl, int ryl, int rxh, int ryh, R gcs, R* H) {
+  constexpr int nv = 4 + NS, np = nv + 2;
+  constexpr int vel = (DIR == 1) ? nv : nv + 1;
+  const int n = (DIR == 1) ? a.g.nx : a.g.ny;
+  const uint8_t fll = (f > 0) ? sfl[ryl * RX + rxl] : 0;
+  const uint8_t flh = (f < n) ? sfl[ryh * RX + rxh] : 0;
+  const bool actl = fll & F_ACTIVE, acth = flh & F_ACTIVE;
+  const bool radial = a.pr.radial_source;
+  const bool ring_l = radial && (fll & F_SC_MASK) == 2 && f - 1 > 0 && f - 1 < n - 1;
+  const bool ring_h = radial && (flh & F_SC_MASK) == 2 && f > 0 && f < n - 1;
+  const bool mirror_h = actl && ring_l && ((DIR == 1) ? (fll & F_E) : ((fll & F_N) && !(fll & F_S)));
+  const bool mirror_l = !mirror_h && acth && ring_h && ((DIR == 1) ? ((flh & F_W) && !(flh & F_E)) : (flh & F_S));
+  R qpl[np], qph[np];
+  bool hl = false, hh = false;
+  const int jl = (DIR == 1) ? f - 1 : o, kl = (DIR == 1) ? o : f - 1;
+  const int jh = (DIR == 1) ? f : o, kh = (DIR == 1) ? o : f;
+  if (f > 0 && actl) { recon_side<R, NS, DIR>(a, sqp, sfl, rxl, ryl, jl, kl, 1, qpl); hl = true; }
+  if (f < n && acth && !mirror_h) { recon_side<R, NS, DIR>(a, sqp, sfl, rxh, ryh, jh, kh, 0, qph); hh = true; }
+  if (f == 0) {
+#pragma unroll
+    for (int i = 0; i < np; ++i) qpl[i] = qph[i];
+    hl = hh;
+  }
+  if (f == n) {
+#pragma unroll
+    for (int i = 0; i < np; ++i) qph[i] = qpl[i];
+    hh = hl;
+  }
+  if (mirror_h) {
+#pragma unroll
+    for (int i = 0; i < np; ++i) qph[i] = qpl[i];
+    qph[vel] = -qph[vel];
+    hh = true;
+  }
+  if (mirror_l) {
+#pragma unroll
+    for (int i = 0; i < np; ++i) qpl[i] = qph[i];
+    qpl[vel] = -qpl[vel];
+    hl = true;
+  }
+  Side<R, NS> L, Hs;
+  if (hl) side_from_qp<R, NS, DIR>(a, qpl, gcs, L, mirror_l);
+  else side_zero(L);
+  if (hh) side_from_qp<R, NS, DIR>(a, qph, gcs, Hs, mirror_h);
+  else side_zero(Hs);
+  return kt_flux<R, NS, DIR>(L, Hs, H);
 }
 
 // ---------------------------------------------------------------------------
@@ -500,63 +540,17 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
     const int f = j0 + fx, k = k0 + fy;
     R H[nv];
     R amax = R(0);
-    bool done = false;
-    if (k < g.ny && f <= g.nx) {
-      const int rxl = fx - 1 + HALO, rxr = fx + HALO, ry = fy + HALO;
-      const bool actl = (f - 1 >= 0) && (sfl[ry * RX + rxl] & F_ACTIVE);
-      const bool actr = (f < g.nx) && (sfl[ry * RX + rxr] & F_ACTIVE);
-      if (actl || actr) {
-        const int64_t cl = cidx(g, f > 0 ? f - 1 : 0, k), cr = cidx(g, f < g.nx ? f : g.nx - 1, k);
-        R gcs;
-        if (f == 0) gcs = __ldg(a.geo[5] + cr);
-        else if (f == g.nx) gcs = __ldg(a.geo[5] + cl);
-        else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cl) + __ldg(a.geo[5] + cr));
-        Side<R, NS> L, Rt;
-        R qp[np];
-        if (f == 0) {
-          recon_side<R, NS>(a, sqp, sfl, rxr, ry, f, k, 1, 0, qp);
-          side_from_qp<R, NS>(a, qp, gcs, 1, Rt);
-          L = Rt;
-        } else if (f == g.nx) {
-          recon_side<R, NS>(a, sqp, sfl, rxl, ry, f - 1, k, 1, 1, qp);
-          side_from_qp<R, NS>(a, qp, gcs, 1, L);
-          Rt = L;
-        } else {
-          const uint8_t fll = sfl[ry * RX + rxl], flr = sfl[ry * RX + rxr];
-          const bool mirror_r = actl && P.radial_source && (fll & F_SC_MASK) == 2 && (fll & F_E) &&
-                                f - 1 > 0 && f - 1 < g.nx - 1;
-          const bool mirror_l = !mirror_r && actr && P.radial_source && (flr & F_SC_MASK) == 2 &&
-                                (flr & F_W) && !(flr & F_E) && f > 0 && f < g.nx - 1;
-          if (actl) {
-            recon_side<R, NS>(a, sqp, sfl, rxl, ry, f - 1, k, 1, 1, qp);
-            side_from_qp<R, NS>(a, qp, gcs, 1, L);
-            if (mirror_r) {
-              // wall mirror: only hu (q) and u (qp) change sign
-              // (solver_2d.f90:3735-3738); qp(2) keeps its sign
-              qp[nv] = -qp[nv];
-              side_from_qp<R, NS>(a, qp, gcs, 1, Rt, 1);
-            }
-          } else {
-            side_zero(L);
-          }
-          if (!mirror_r) {
-            if (actr) {
-              recon_side<R, NS>(a, sqp, sfl, rxr, ry, f, k, 1, 0, qp);
-              side_from_qp<R, NS>(a, qp, gcs, 1, Rt);
-              if (mirror_l) {
-                qp[nv] = -qp[nv];
-                side_from_qp<R, NS>(a, qp, gcs, 1, L, 1);
-              }
-            } else {
-              side_zero(Rt);
-            }
-          }
-        }
-        amax = kt_flux<R, NS>(L, Rt, 1, H);
-        done = true;
-      }
-    }
-    if (!done) {
+    const int ry = fy + HALO, rxl = fx - 1 + HALO, rxh = fx + HALO;
+    const bool any = (k < g.ny && f <= g.nx) &&
+                     (((f > 0) && (sfl[ry * RX + rxl] & F_ACTIVE)) || ((f < g.nx) && (sfl[ry * RX + rxh] & F_ACTIVE)));
+    if (any) {
+      const int64_t cl = cidx(g, f > 0 ? f - 1 : 0, k), ch = cidx(g, f < g.nx ? f : g.nx - 1, k);
+      R gcs;
+      if (f == 0) gcs = __ldg(a.geo[5] + ch);
+      else if (f == g.nx) gcs = __ldg(a.geo[5] + cl);
+      else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cl) + __ldg(a.geo[5] + ch));
+      amax = face_flux<R, NS, 1>(a, sqp, sfl, f, k, rxl, ry, rxh, ry, gcs, H);
+    } else {
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = R(0);
     }
@@ -571,62 +565,17 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
     const int j = j0 + fx, f = k0 + fy;
     R H[nv];
     R amax = R(0);
-    bool done = false;
-    if (j < g.nx && f <= g.ny) {
-      const int rx = fx + HALO, ryb = fy - 1 + HALO, ryt = fy + HALO;
-      const bool actb = (f - 1 >= 0) && (sfl[ryb * RX + rx] & F_ACTIVE);
-      const bool actt = (f < g.ny) && (sfl[ryt * RX + rx] & F_ACTIVE);
-      if (actb || actt) {
-        const int64_t cb = cidx(g, j, f > 0 ? f - 1 : 0), ct = cidx(g, j, f < g.ny ? f : g.ny - 1);
-        R gcs;
-        if (f == 0) gcs = __ldg(a.geo[5] + ct);
-        else if (f == g.ny) gcs = __ldg(a.geo[5] + cb);
-        else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cb) + __ldg(a.geo[5] + ct));
-        Side<R, NS> B, T;
-        R qp[np];
-        if (f == 0) {
-          recon_side<R, NS>(a, sqp, sfl, rx, ryt, j, f, 2, 0, qp);
-          side_from_qp<R, NS>(a, qp, gcs, 2, T);
-          B = T;
-        } else if (f == g.ny) {
-          recon_side<R, NS>(a, sqp, sfl, rx, ryb, j, f - 1, 2, 1, qp);
-          side_from_qp<R, NS>(a, qp, gcs, 2, B);
-          T = B;
-        } else {
-          const uint8_t flb = sfl[ryb * RX + rx], flt = sfl[ryt * RX + rx];
-          // cell below with ring to its north mirrors onto the top side
-          const bool mirror_t = actb && P.radial_source && (flb & F_SC_MASK) == 2 && (flb & F_N) &&
-                                !(flb & F_S) && f - 1 > 0 && f - 1 < g.ny - 1;
-          const bool mirror_b = !mirror_t && actt && P.radial_source && (flt & F_SC_MASK) == 2 &&
-                                (flt & F_S) && f > 0 && f < g.ny - 1;
-          if (actb) {
-            recon_side<R, NS>(a, sqp, sfl, rx, ryb, j, f - 1, 2, 1, qp);
-            side_from_qp<R, NS>(a, qp, gcs, 2, B);
-            if (mirror_t) {
-              qp[nv + 1] = -qp[nv + 1];
-              side_from_qp<R, NS>(a, qp, gcs, 2, T, 2);
-            }
-          } else {
-            side_zero(B);
-          }
-          if (!mirror_t) {
-            if (actt) {
-              recon_side<R, NS>(a, sqp, sfl, rx, ryt, j, f, 2, 0, qp);
-              side_from_qp<R, NS>(a, qp, gcs, 2, T);
-              if (mirror_b) {
-                qp[nv + 1] = -qp[nv + 1];
-                side_from_qp<R, NS>(a, qp, gcs, 2, B, 2);
-              }
-            } else {
-              side_zero(T);
-            }
-          }
-        }
-        amax = kt_flux<R, NS>(B, T, 2, H);
-        done = true;
-      }
-    }
-    if (!done) {
+    const int rx = fx + HALO, ryl = fy - 1 + HALO, ryh = fy + HALO;
+    const bool any = (j < g.nx && f <= g.ny) &&
+                     (((f > 0) && (sfl[ryl * RX + rx] & F_ACTIVE)) || ((f < g.ny) && (sfl[ryh * RX + rx] & F_ACTIVE)));
+    if (any) {
+      const int64_t cl = cidx(g, j, f > 0 ? f - 1 : 0), ch = cidx(g, j, f < g.ny ? f : g.ny - 1);
+      R gcs;
+      if (f == 0) gcs = __ldg(a.geo[5] + ch);
+      else if (f == g.ny) gcs = __ldg(a.geo[5] + cl);
+      else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cl) + __ldg(a.geo[5] + ch));
+      amax = face_flux<R, NS, 2>(a, sqp, sfl, f, j, rx, ryl, rx, ryh, gcs, H);
+    } else {
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = R(0);
     }
@@ -637,7 +586,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
   __syncthreads();
 
   // 4. cells: divergence, explicit terms, CFL step
-  double dtloc = 1.0e300;
+  R dtloc = R(3.0e38);
   if (tid < TX * TY) {
     const int cx = tid % TX, cy = tid / TX;
     const int j = j0 + cx, k = k0 + cy;
@@ -656,7 +605,10 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
         anx = __ldg(a.arc + g.plane + c);
         any_ = __ldg(a.arc + 2 * g.plane + c);
       }
-      expl_terms<R, NS>(P, geo, qp, (R)st->src_t_coeff, ap, anx, any_, e);
+      R tcoef;
+      if constexpr (sizeof(R) == 8) tcoef = st->src_t_coeff;
+      else tcoef = st->src_t_coeff_f;
+      expl_terms<R, NS>(P, geo, qp, tcoef, ap, anx, any_, e);
 #pragma unroll
       for (int i = 0; i < nv; ++i) {
         R d = R(0);
@@ -672,29 +624,25 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
           double dty = (ay > 0.0) ? g.cfl * g.dy / ay : 1.0e300;
           dtloc = rmin(dtx, dty);
         } else {
-          // FP32 form: the CFL bound in float, widened once per block
           float dtx = (ax > 0.0f) ? g.cfl_dx / ax : 3.0e38f;
           float dty = (ay > 0.0f) ? g.cfl_dy / ay : 3.0e38f;
-          float m = fminf(dtx, dty);
-          dtloc = (m < 3.0e38f) ? (double)m : 1.0e300;
+          dtloc = fminf(dtx, dty);
         }
       }
     }
   }
   if (want_dt) {
-    // block minimum: warp shuffle then shared memory
-    unsigned long long b = dbits(dtloc);
-    for (int o = 16; o > 0; o >>= 1) {
-      unsigned long long ob = __shfl_xor_sync(0xffffffffu, b, o);
-      b = ob < b ? ob : b;
-    }
-    __shared__ unsigned long long wmin[FLUX_THREADS / 32];
-    if ((tid & 31) == 0) wmin[tid >> 5] = b;
+    // block minimum (warp shuffle, then shared memory), one atomic per block
+    R m = dtloc;
+    for (int o = 16; o > 0; o >>= 1) m = rmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ R wmin[FLUX_THREADS / 32];
+    if ((tid & 31) == 0) wmin[tid >> 5] = m;
     __syncthreads();
     if (tid == 0) {
-      unsigned long long m = wmin[0];
-      for (int w = 1; w < FLUX_THREADS / 32; ++w) m = wmin[w] < m ? wmin[w] : m;
-      if (m < dbits(1.0e300)) atomicMin(&a.st->dtmin_bits, m);
+      R b = wmin[0];
+      for (int w = 1; w < FLUX_THREADS / 32; ++w) b = rmin(b, wmin[w]);
+      const double bd = (double)b;
+      if (bd < (sizeof(R) == 8 ? 1.0e300 : 3.0e38)) atomicMin(&a.st->dtmin_bits, dbits(bd));
     }
   }
 }
@@ -961,15 +909,12 @@ __global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
             qsi[1] = m1 * qfv[1] / m0;
             qsi[2] = m1 * qfv[2] / m0;
           }
-          double qd[nv];
-#pragma unroll
-          for (int i = 0; i < nv; ++i) qd[i] = (double)qsi[i];
-          double e1, e2;
-          double s = reduced_friction_solve<NS>(a.pd, (double)geo.Bx, (double)geo.By, qd, dt, e1, e2, nit);
+          float e1, e2;
+          const float sv = reduced_friction_solve<NS>(P, geo.Bx, geo.By, qsi, dt, e1, e2, nit);
 #pragma unroll
           for (int i = 0; i < nv; ++i) q[i] = qsi[i];
-          q[1] = (R)(s * e1);
-          q[2] = (R)(s * e2);
+          q[1] = sv * e1;
+          q[2] = sv * e2;
           if (g.ny == 1) q[2] = R(0);
         } else {
 #pragma unroll

@@ -118,10 +118,19 @@ __device__ __forceinline__ R qc_to_qp(const Phys<R>& P, const R* q, R* qp) {
     u = q[1] * inv_qj1;
     v = q[2] * inv_qj1;
   } else {
-    R q12 = q[0] * q[0];
-    R den = sqrt(q12 * q12 + P.eps_sing4);
-    u = P.sqrt2 * q[0] * q[1] / den;
-    v = P.sqrt2 * q[0] * q[2] / den;
+    if constexpr (sizeof(R) == 8) {
+      R q12 = q[0] * q[0];
+      R den = sqrt(q12 * q12 + P.eps_sing4);
+      u = P.sqrt2 * q[0] * q[1] / den;
+      v = P.sqrt2 * q[0] * q[2] / den;
+    } else {
+      // same expression scaled by eps_sing: q1^4 and eps_sing^4 (1e-40)
+      // are below the float range, (q1/eps)^4 is not
+      R s = q[0] * P.inv_eps_sing;
+      R f = P.sqrt2 * s * P.inv_eps_sing / sqrt(R(1) + (s * s) * (s * s));
+      u = f * q[1];
+      v = f * q[2];
+    }
   }
   qp[0] = h;
   qp[1] = h * u;
@@ -533,6 +542,7 @@ __device__ int solve_rk_step(const NewtonCtx& c, double* qj) {
     double mf = 0.0;
     for (int i = 0; i < nv; ++i) mf = rmax(mf, fabs(f[i]));
     if (mf < TOLF) return it;
+    if (!isfinite(scal_f)) return kMaxNewton + 1;   // NaN/Inf state: give up at once
     double s11, s12, s21, s22;
     newton_jacobian<NS>(c, qj, qj_org, s11, s12, s21, s22);
     // explicit rows: diagonal qj_org (mask11); coupling mask21 is zero
@@ -726,86 +736,109 @@ __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R 
 // ---------------------------------------------------------------------------
 // FP32 form: the implicit friction step solved as a scalar FP64 Newton.
 // With the non-momentum components fixed, q_h = q_si_h + dt*a*NH_h(q) and
-// NH_h is antiparallel to q_h (both rheologies 1 and 6), so the solution is
-// s*e with e = q_si_h/|q_si_h| and s >= 0 the root of
+// NH_h is antiparallel to q_h (rheologies 1 and 6), so the solution is s*e
+// with e = q_si_h/|q_si_h| and s >= 0 the root of
 //     g(s) = s + dt*a*K(s)*s^2 - S,   S = |q_si_h|,
-// K = rho_m g' kappa phi^2 / xi (Voellmy) or rho_m ff kappa^2 phi^2 (6),
-// kappa = sqrt(1+(e.grad B)^2) with slope correction, phi = u/hu.  K depends
-// on s only through T (energy equation: kinetic energy is subtracted) and
-// the gas density.  This is the same fixed point the reference's 2x2
-// Newton (solver_2d.f90:1662-1996) converges to, computed in FP64 with an
-// analytic derivative.  Returns s; writes e.
+// K = (rho_m - rho_a) g kappa phi^2 / xi (Voellmy) or rho_m ff kappa^2
+// phi^2 (rheology 6), kappa = sqrt(1 + (e.grad B)^2) with slope correction,
+// phi = u/hu.  K depends on s only through T (the energy equation subtracts
+// the kinetic energy) and through the gas density.  This is the fixed point
+// of the reference's 2x2 Newton (solver_2d.f90:1662-1996).  The
+// coefficients come from the FP32 state; an FP32 Newton gives the start,
+// FP64 Newton steps with an analytic derivative converge it to
+// |ds| <= 1e-15 s (one or two steps).
 // ---------------------------------------------------------------------------
+
+// 1/x to ~1 ulp: float estimate + two Newton-Raphson refinements in FP64
+__device__ __forceinline__ double rcp64(double x) {
+  double r = (double)__frcp_rn((float)x);
+  r = r * (2.0 - x * r);
+  r = r * (2.0 - x * r);
+  return r;
+}
+
 template <int NS>
-__device__ __forceinline__ double reduced_friction_solve(const Phys<double>& P, double Bx,
-                                                         double By, const double* q, double dta,
-                                                         double& e1, double& e2, int& iters) {
+__device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, float Bx, float By,
+                                                        const float* q, double dta, float& e1,
+                                                        float& e2, int& iters) {
   constexpr int ns = NS;
   iters = 0;
-  double S = sqrt(q[1] * q[1] + q[2] * q[2]);
-  if (S == 0.0) { e1 = 0.0; e2 = 0.0; return 0.0; }
-  e1 = q[1] / S;
-  e2 = q[2] / S;
-  if (!P.rheo || !(q[0] > kEps)) return S;
-  const double q1 = q[0];
-  const double inv_q1 = 1.0 / q1;
-  double xs_tot = 0.0, dcp = 0.0, dinv = 0.0;
+  const float S = sqrtf(q[1] * q[1] + q[2] * q[2]);
+  if (S == 0.0f) { e1 = 0.0f; e2 = 0.0f; return 0.0f; }
+  const float iS = 1.0f / S;
+  e1 = q[1] * iS;
+  e2 = q[2] * iS;
+  if (!P.rheo || !(q[0] > P.thr_eps)) return S;
+  const float q1 = q[0], inv_q1 = 1.0f / q1;
+  float xs_tot = 0.0f, dcp = 0.0f, dinv = 0.0f;
+#pragma unroll
   for (int i = 0; i < ns; ++i) {
-    double xs = q[4 + i] * inv_q1;
+    const float xs = q[4 + i] * inv_q1;
     xs_tot += xs;
     dcp += xs * P.sp_heat_s[i];
     dinv += xs * P.inv_rho_s[i];
   }
-  const double xc = 1.0 - xs_tot;
-  const double cp_c = P.gas ? P.sp_heat_a : P.sp_heat_l;
-  const double cmix = dcp + xc * cp_c;
-  const double phi = (q1 > P.eps_sing_d) ? inv_q1 : P.sqrt2 * q1 / sqrt(q1 * q1 * q1 * q1 + P.eps_sing4);
-  double kappa2 = 1.0;
-  if (P.slope_corr) { double w = e1 * Bx + e2 * By; kappa2 = 1.0 + w * w; }
-  const double kappa = sqrt(kappa2);
-  const double cgeo = (P.rheo_model == 1) ? P.grav * kappa * phi * phi / P.xi
-                                          : P.friction_factor * kappa2 * phi * phi;
-  // rho_m(s) through T(s); for rheology 1 K uses (rho_m - rho_a) g, for 6 rho_m
-  const bool varT = P.gas && P.energy && (q1 > P.eps_sing_d);
-  const double a_T = q[3] / (q1 * cmix), b_T = 0.5 * inv_q1 / (q1 * cmix);
-  const double c_inv = xc * P.sp_gas_const_a * P.inv_pres;
-  auto K_of = [&](double s, double& dK) -> double {
-    double T, dT;
-    if (P.gas) {
-      if (varT) { T = a_T - b_T * s * s; dT = -2.0 * b_T * s; }
-      else if (q1 > P.eps_sing_d) { T = P.energy ? a_T : q[3] / (q1 * cmix); dT = 0.0; }
-      else { T = P.T_ambient; dT = 0.0; }
-      if (T <= 0.0) { T = P.T_ambient; dT = 0.0; }
-      double inv_rhom = dinv + c_inv * T;
-      double rho_m = 1.0 / inv_rhom;
-      double drho = -rho_m * rho_m * c_inv * dT;
-      double base = (P.rheo_model == 1) ? (rho_m - P.rho_a_amb) : rho_m;
-      dK = cgeo * drho;
-      return cgeo * base;
-    } else {
-      double rho_m = 1.0 / (dinv + xc * P.inv_rho_l);
-      dK = 0.0;
-      return cgeo * ((P.rheo_model == 1) ? (rho_m - P.rho_a_amb) : rho_m);
-    }
-  };
-  double dK;
-  double K = K_of(S, dK);
-  double disc = 1.0 + 4.0 * dta * K * S;
-  double s = (disc >= 0.0) ? 2.0 * S / (1.0 + sqrt(disc)) : S;
-  if (varT) {
-    for (int it = 0; it < 20; ++it) {
-      K = K_of(s, dK);
-      double gv = s + dta * K * s * s - S;
-      double gd = 1.0 + dta * (dK * s * s + 2.0 * K * s);
-      double ds = gv / gd;
-      s = s - ds;
-      ++iters;
-      if (!(fabs(ds) > 1.0e-15 * s)) break;
-    }
-  } else {
-    iters = 1;
+  const float xc = 1.0f - xs_tot;
+  const float cmix = dcp + xc * (P.gas ? P.sp_heat_a : P.sp_heat_l);
+  float phi;
+  if (q1 > P.thr_eps_sing) phi = inv_q1;
+  else {
+    const float sc = q1 * P.inv_eps_sing;
+    phi = P.sqrt2 * sc * P.inv_eps_sing / sqrtf(1.0f + (sc * sc) * (sc * sc));
   }
-  return s > 0.0 ? s : 0.0;
+  float kappa2 = 1.0f;
+  if (P.slope_corr) { const float w = e1 * Bx + e2 * By; kappa2 = 1.0f + w * w; }
+  const float cgeo = (P.rheo_model == 1) ? P.grav * sqrtf(kappa2) * phi * phi / P.xi
+                                         : P.friction_factor * kappa2 * phi * phi;
+  const bool gas = P.gas;
+  const bool varT = gas && P.energy && (q1 > P.thr_eps_sing);
+  const float icm = 1.0f / (q1 * cmix);
+  const float a_T = (q1 > P.thr_eps_sing) ? q[3] * icm : P.T_ambient;
+  const float b_T = varT ? 0.5f * inv_q1 * icm : 0.0f;
+  const float c_inv = gas ? xc * P.sp_gas_const_a * P.inv_pres : 0.0f;
+  const float base_inv = gas ? dinv : dinv + xc * P.inv_rho_l;
+  const float rho_a = (P.rheo_model == 1) ? P.rho_a_amb : 0.0f;
+  // K(s) and dK/ds in float
+  auto Kf = [&](float sv, float& dK) -> float {
+    float T = a_T - b_T * sv * sv, dT = -2.0f * b_T * sv;
+    if (T <= 0.0f) { T = P.T_ambient; dT = 0.0f; }
+    const float inv_rhom = base_inv + c_inv * T;
+    const float rho_m = 1.0f / inv_rhom;
+    dK = cgeo * (-rho_m * rho_m * c_inv * dT);
+    return cgeo * (rho_m - rho_a);
+  };
+  const float dtaf = (float)dta;
+  float dKf;
+  float K = Kf(S, dKf);
+  float s = 2.0f * S / (1.0f + sqrtf(fmaxf(1.0f + 4.0f * dtaf * K * S, 0.0f)));
+  if (varT) {
+    for (int it = 0; it < 8; ++it) {
+      K = Kf(s, dKf);
+      const float gv = s + dtaf * K * s * s - S;
+      const float gd = 1.0f + dtaf * (dKf * s * s + 2.0f * K * s);
+      const float ds = gv / gd;
+      s -= ds;
+      if (!(fabsf(ds) > 1.0e-7f * s)) break;
+    }
+  }
+  // FP64 Newton steps from the FP32 root
+  const double Sd = S, cg = cgeo, aT = a_T, bT = b_T, ci = c_inv, bi = base_inv, ra = rho_a;
+  const double Tamb = P.T_ambient;
+  double sd = s;
+  for (int it = 0; it < 4; ++it) {
+    double T = aT - bT * sd * sd, dT = -2.0 * bT * sd;
+    if (T <= 0.0) { T = Tamb; dT = 0.0; }
+    const double rho_m = rcp64(bi + ci * T);
+    const double Kd = cg * (rho_m - ra);
+    const double dKd = cg * (-rho_m * rho_m * ci * dT);
+    const double gv = sd + dta * Kd * sd * sd - Sd;
+    const double gd = 1.0 + dta * (dKd * sd * sd + 2.0 * Kd * sd);
+    const double ds = gv * rcp64(gd);
+    sd -= ds;
+    ++iters;
+    if (!(fabs(ds) > 1.0e-15 * sd)) break;
+  }
+  return sd > 0.0 ? (float)sd : 0.0f;
 }
 
 }  // namespace sflow

@@ -293,6 +293,13 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   if (p.radial_source_flag) {
     if (!(p.r_source > 0.0)) { err = "r_source must be > 0"; return SFLOW_EINVAL; }
     if (p.r2_source <= 0.0) p.r2_source = p.r_source;
+    // inpout_2d.f90:4140-4175: the ring must stay a cell away from the edges
+    const double rmax_ = std::fmax(p.r_source, p.r2_source);
+    if (p.x_source - rmax_ <= p.x0 + p.cell_size || p.x_source + rmax_ >= p.x0 + (p.comp_cells_x - 1) * p.cell_size ||
+        p.y_source - rmax_ <= p.y0 + p.cell_size || p.y_source + rmax_ >= p.y0 + (p.comp_cells_y - 1) * p.cell_size) {
+      err = "radial source too close to the domain boundary";
+      return SFLOW_EINVAL;
+    }
     if (s.time_param[0] < 0.0 || s.time_param[1] < 0.0 || s.time_param[2] < 0.0 || s.time_param[3] < 0.0) {
       s.time_param[0] = p.t_end; s.time_param[1] = p.t_end; s.time_param[2] = 0.0; s.time_param[3] = p.t_end;
     }

@@ -47,18 +47,25 @@ __global__ void k_map_to_host(const R* __restrict__ m, double* __restrict__ out,
 }
 
 static __global__ void k_stats_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
-  // Neumaier-compensated sum over the block partials, in block order
-  if (threadIdx.x >= 4) return;
-  int m = threadIdx.x;
+  // block m reduces value m: Neumaier-compensated strided sums per thread,
+  // then a fixed-order tree (deterministic)
+  const int m = blockIdx.x;
   double s = 0.0, cmp = 0.0;
-  for (int b = 0; b < nblk; ++b) {
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
     double x = part[b * 4 + m];
     double t = s + x;
     if (fabs(s) >= fabs(x)) cmp += (s - t) + x;
     else cmp += (x - t) + s;
     s = t;
   }
-  out[m] = s + cmp;
+  __shared__ double sh[256];
+  sh[threadIdx.x] = s + cmp;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[m] = sh[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -145,6 +152,81 @@ class Solver : public SolverBase {
     SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
     SFLOW_CU(cudaStreamSynchronize(stream_));
     uploaded_ = true;
+    return SFLOW_OK;
+  }
+
+  int put(const double* q_aos) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
+    const size_t N = (size_t)nx * ny;
+    SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
+    k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
+    ++launches_;
+    SFLOW_CU(cudaGetLastError());
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+
+  int set_clock(double t, double dt_old, double dt_old_old) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    SFLOW_CU(cudaMemcpyAsync(&hst_, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    hst_.t = t;
+    hst_.t_prev = t;
+    hst_.dt_old = dt_old;
+    hst_.dt_old_old = dt_old_old;
+    SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+
+  int advance_timed(int64_t steps, int flush, double* ms) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    SFLOW_CU(prepare_timing(flush));
+    SFLOW_CU(set_limits(hs_.p.t_end, -1));
+    if (!graph1_exec_) SFLOW_CU(build_graph1());
+    double total = 0.0;
+    for (int64_t i = 0; i < steps; ++i) {
+      if (flush) SFLOW_CU(flush_l2());
+      SFLOW_CU(cudaEventRecord(ev_[0], stream_));
+      SFLOW_CU(cudaGraphLaunch(graph1_exec_, stream_));
+      launches_ += 4;
+      SFLOW_CU(cudaEventRecord(ev_[1], stream_));
+      SFLOW_CU(cudaEventSynchronize(ev_[1]));
+      float m = 0.0f;
+      SFLOW_CU(cudaEventElapsedTime(&m, ev_[0], ev_[1]));
+      total += m;
+    }
+    *ms = total;
+    return SFLOW_OK;
+  }
+
+  int profile_kernels(int64_t steps, int flush, double* ms4) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    SFLOW_CU(prepare_timing(flush));
+    SFLOW_CU(set_limits(hs_.p.t_end, -1));
+    double tot[4] = {0, 0, 0, 0};
+    for (int64_t i = 0; i < steps; ++i) {
+      if (flush) SFLOW_CU(flush_l2());
+      SFLOW_CU(cudaEventRecord(ev_[0], stream_));
+      SFLOW_CU(launch_mask(0));
+      SFLOW_CU(cudaEventRecord(ev_[1], stream_));
+      SFLOW_CU(launch_flux(1));
+      SFLOW_CU(cudaEventRecord(ev_[2], stream_));
+      k_dt<<<1, 1, 0, stream_>>>(st_, hs_.p.max_dt);
+      ++launches_;
+      SFLOW_CU(cudaGetLastError());
+      SFLOW_CU(cudaEventRecord(ev_[3], stream_));
+      SFLOW_CU(launch_stage2(-1));
+      SFLOW_CU(cudaEventRecord(ev_[4], stream_));
+      SFLOW_CU(cudaEventSynchronize(ev_[4]));
+      for (int k = 0; k < 4; ++k) {
+        float m = 0.0f;
+        SFLOW_CU(cudaEventElapsedTime(&m, ev_[k], ev_[k + 1]));
+        tot[k] += m;
+      }
+    }
+    for (int k = 0; k < 4; ++k) ms4[k] = tot[k];
     return SFLOW_OK;
   }
 
@@ -348,7 +430,43 @@ class Solver : public SolverBase {
   double pending_dt_ = -1.0;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
+  cudaGraph_t graph1_ = nullptr;
+  cudaGraphExec_t graph1_exec_ = nullptr;
+  cudaEvent_t ev_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  void* flush_buf_ = nullptr;
+  size_t flush_bytes_ = 0;
   KernelTable<R> tab_;
+
+  cudaError_t prepare_timing(int flush) {
+    if (!ev_[0])
+      for (int k = 0; k < 5; ++k) {
+        cudaError_t e = cudaEventCreate(&ev_[k]);
+        if (e != cudaSuccess) return e;
+      }
+    if (flush && !flush_buf_) {
+      flush_bytes_ = (size_t)512 << 20;   // 4x the 126 MB L2
+      cudaError_t e = cudaMalloc(&flush_buf_, flush_bytes_);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  cudaError_t flush_l2() {
+    static int salt = 0;
+    return cudaMemsetAsync(flush_buf_, (++salt) & 0xff, flush_bytes_, stream_);
+  }
+  cudaError_t build_graph1() {
+    cudaError_t e = cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const int64_t l0 = launches_;
+    e = launch_step();
+    launches_ = l0;
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
+    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return e; }
+    if (e2 != cudaSuccess) return e2;
+    graph1_ = g;
+    return cudaGraphInstantiate(&graph1_exec_, graph1_, 0);
+  }
 
   static unsigned long long bits_of(double x) {
     unsigned long long b;
@@ -368,6 +486,11 @@ class Solver : public SolverBase {
   void release() {
     if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
     if (graph_) cudaGraphDestroy(graph_);
+    if (graph1_exec_) cudaGraphExecDestroy(graph1_exec_);
+    if (graph1_) cudaGraphDestroy(graph1_);
+    for (int k = 0; k < 5; ++k)
+      if (ev_[k]) cudaEventDestroy(ev_[k]);
+    if (flush_buf_) cudaFree(flush_buf_);
     for (void* p : allocs_) cudaFree(p);
     allocs_.clear();
     if (stream_) cudaStreamDestroy(stream_);
@@ -409,6 +532,7 @@ class Solver : public SolverBase {
     P.thr_1em3 = th(1.0e-3);
     P.thr_273 = (T)273.0;
     P.eps_sing4 = (T)hs_.eps_sing4;
+    P.inv_eps_sing = (T)(1.0 / hs_.eps_sing);
     P.sqrt2 = (T)std::sqrt(2.0);
     P.grav = (T)p.grav; P.pres = (T)p.pres; P.inv_pres = (T)(1.0 / p.pres);
     P.sp_heat_a = (T)p.sp_heat_a; P.sp_gas_const_a = (T)p.sp_gas_const_a; P.T_ambient = (T)p.T_ambient;
@@ -440,6 +564,7 @@ class Solver : public SolverBase {
     g.tiles_x = tiles_x_; g.tiles_y = tiles_y_;
     g.x0 = p.x0; g.y0 = p.y0; g.dx = hs_.dx; g.dy = hs_.dy;
     g.rdx = (R)hs_.dx; g.rdy = (R)hs_.dy;
+    g.x0r = (R)p.x0; g.y0r = (R)p.y0;
     g.dx2 = (R)(hs_.dx / 2.0); g.dy2 = (R)(hs_.dy / 2.0);
     g.one_by_dx = (R)(1.0 / hs_.dx); g.one_by_dy = (R)(1.0 / hs_.dy);
     g.rc = (R)p.reconstr_coeff; g.theta = (R)p.theta;
@@ -556,7 +681,7 @@ class Solver : public SolverBase {
   cudaError_t dispatch_stats() {
     cudaError_t e = tab_.stats(ka_, nstat_blocks_, stream_, stat_part_);
     if (e != cudaSuccess) return e;
-    k_stats_final<<<1, 32, 0, stream_>>>(stat_part_, nstat_blocks_, stat_out_);
+    k_stats_final<<<4, 256, 0, stream_>>>(stat_part_, nstat_blocks_, stat_out_);
     launches_ += 2;
     return cudaGetLastError();
   }

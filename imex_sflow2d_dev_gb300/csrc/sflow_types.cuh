@@ -22,7 +22,7 @@ struct Phys {
   // above the FP64 value, so `x > thr` on a float x gives the same answer
   // as the FP64 test (double)x > value.
   R thr_eps, thr_eps_sing, thr_neg1e7, thr_neg1e10, thr_1em10, thr_1em7, thr_1em3, thr_273;
-  R eps_sing4, sqrt2;
+  R eps_sing4, inv_eps_sing, sqrt2;
   R grav, pres, inv_pres, sp_heat_a, sp_gas_const_a, T_ambient, rho_a_amb;
   R rho_l, inv_rho_l, sp_heat_l;
   R rho_s[kMaxSolid], inv_rho_s[kMaxSolid], sp_heat_s[kMaxSolid];
@@ -56,7 +56,7 @@ struct Grid {
   int64_t plane;    // stride between variable planes
   int tiles_x, tiles_y;
   double x0, y0, dx, dy;   // coordinates in FP64 (x_stag = x0 + j*dx)
-  R rdx, rdy, dx2, dy2, one_by_dx, one_by_dy;
+  R x0r, y0r, rdx, rdy, dx2, dy2, one_by_dx, one_by_dy;
   R rc, theta;
   R cfl_dx, cfl_dy;
   int limiter[kMaxVars + 2];
@@ -78,6 +78,8 @@ struct RunState {
   int newton_max;
   int pad;
   double src_t_coeff;              // ring inlet time factor at this step's t
+  float src_t_coeff_f;
+  int pad2;
   double tp[4];                    // time_param
   double pi_g;
 };

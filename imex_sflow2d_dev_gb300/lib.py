@@ -61,6 +61,12 @@ def load(build_if_missing=True):
         "sflow_device_bytes": (i64, [vp]),
         "sflow_counters": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
                                      C.POINTER(i32)]),
+        "sflow_put_q": (C.c_int, [vp, dp]),
+        "sflow_set_clock": (C.c_int, [vp, C.c_double, C.c_double, C.c_double]),
+        "sflow_advance_timed": (C.c_int, [vp, i64, i32, dp]),
+        "sflow_profile_kernels": (C.c_int, [vp, i64, i32, dp]),
+        "sflow_host_geometry": (C.c_int, [P, dp, i32, dp]),
+        "sflow_host_scalars": (C.c_int, [P, dp, dp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -76,7 +82,27 @@ def exported_symbols():
             "sflow_download_maps", "sflow_check_solve", "sflow_timestep", "sflow_imex_rk",
             "sflow_erosion_deposition", "sflow_post_step", "sflow_step", "sflow_advance",
             "sflow_get_stats", "sflow_status", "sflow_clear_status", "sflow_launch_count",
-            "sflow_device_bytes", "sflow_counters"]
+            "sflow_device_bytes", "sflow_counters", "sflow_host_geometry", "sflow_host_scalars",
+            "sflow_put_q", "sflow_set_clock", "sflow_advance_timed", "sflow_profile_kernels"]
+
+
+def host_geometry(params, B_cent, which):
+    """Derived per-cell field of the host set-up (no GPU needed)."""
+    lib = load()
+    p = params.copy()
+    B = np.ascontiguousarray(B_cent, dtype=np.float64).reshape(-1)
+    out = np.empty(params.comp_cells_x * params.comp_cells_y)
+    _check(lib.sflow_host_geometry(C.byref(p), _dp(B), which, _dp(out)))
+    return out
+
+
+def host_scalars(params, B_cent):
+    lib = load()
+    p = params.copy()
+    B = np.ascontiguousarray(B_cent, dtype=np.float64).reshape(-1)
+    out = np.empty(4)
+    _check(lib.sflow_host_scalars(C.byref(p), _dp(B), _dp(out)))
+    return {"h_source": out[0], "src_rho_m": out[1], "src_cp_mix": out[2], "eps_sing": out[3]}
 
 
 def _dp(a):
@@ -128,6 +154,33 @@ class Solver:
         if q.size != self.nx * self.ny * self.nv:
             raise ValueError("q must have n_vars*nx*ny values")
         _check(self.lib.sflow_upload_q(self.h, _dp(q)))
+
+    def put_q(self, q_aos):
+        """Replace the state, keeping time, dt history, maxima and counters."""
+        q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
+        if q.size != self.nx * self.ny * self.nv:
+            raise ValueError("q must have n_vars*nx*ny values")
+        _check(self.lib.sflow_put_q(self.h, _dp(q)))
+
+    def put_q_ptr(self, addr):
+        """put_q from a raw host address (e.g. pinned memory)."""
+        _check(self.lib.sflow_put_q(self.h, C.cast(addr, C.POINTER(C.c_double))))
+
+    def download_q_ptr(self, addr):
+        _check(self.lib.sflow_download_q(self.h, C.cast(addr, C.POINTER(C.c_double))))
+
+    def set_clock(self, t, dt_old, dt_old_old):
+        _check(self.lib.sflow_set_clock(self.h, t, dt_old, dt_old_old))
+
+    def advance_timed(self, steps, flush_l2=True):
+        ms = C.c_double(0.0)
+        _check(self.lib.sflow_advance_timed(self.h, steps, 1 if flush_l2 else 0, C.byref(ms)))
+        return ms.value
+
+    def profile_kernels(self, steps, flush_l2=True):
+        out = np.zeros(4)
+        _check(self.lib.sflow_profile_kernels(self.h, steps, 1 if flush_l2 else 0, _dp(out)))
+        return dict(zip(("mask", "flux", "dt", "stage"), out.tolist()))
 
     def download_q(self, out=None):
         if out is None:

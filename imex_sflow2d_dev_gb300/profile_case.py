@@ -1,0 +1,40 @@
+"""A short run of the pyroclastic workload for profilers (ncu).
+
+    python -m imex_sflow2d_dev_gb300.profile_case --n 2048 --steps 6 --precision fp32
+
+Builds the n x n version of the benchmark workload (cone + fBm DEM with
+dx = 10240/n m, seeded developed-current state), uploads it and runs
+`steps` driver iterations one at a time (no graph, so every kernel is a
+separate launch).  With n = 2048 the FP32 working set (~400 MB) exceeds the
+126 MB L2, so DRAM counters of a single launch are meaningful.
+"""
+import argparse
+
+from . import lib
+from . import workloads as W
+from .params import PREC_FP32, PREC_FP64
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=2048)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    a = ap.parse_args()
+    prec = PREC_FP32 if a.precision == "fp32" else PREC_FP64
+    p, B, _ = W.pyroclastic(nx=a.n, ny=a.n, dx=10240.0 / a.n, settling=False, precision=prec,
+                            t_end=1.0e9)
+    q = W.developed_current_state(p, B)
+    s = lib.Solver(p, B)
+    s.upload_q(W.to_aos(q))
+    for _ in range(a.steps):
+        s.step()
+    st = s.stats()
+    c = s.counters()
+    print(f"n={a.n} precision={a.precision} steps={st.steps} t={st.t:.4f} "
+          f"active/step={c['cell_updates'] / max(c['steps'], 1):.0f} status={st.status}")
+    s.close()
+
+
+if __name__ == "__main__":
+    main()

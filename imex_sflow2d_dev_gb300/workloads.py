@@ -255,6 +255,36 @@ def pyroclastic(nx=1024, ny=1024, dx=10.0, precision=PREC_FP64, t_end=600.0, see
     return p, B, q
 
 
+def developed_current_state(p, B, radius=3500.0, h_max=3.0, u_max=15.0, T=950.0, seed=11):
+    """A spread gas-particle current over the cone, as a seeded stand-in for
+    the state of the pyroclastic run a few minutes after the inlet opened:
+    thickness 1 - (r/R)^2 profile (max h_max), radial velocity growing as
+    sqrt(r/R) up to u_max, uniform temperature T, the inlet's particle volume
+    fractions, and a 5 % seeded perturbation of h.  Returns q (n_vars, ny, nx)."""
+    nx, ny, dx = p.comp_cells_x, p.comp_cells_y, p.cell_size
+    x = p.x0 + (np.arange(nx) + 0.5) * dx
+    y = p.y0 + (np.arange(ny) + 0.5) * dx
+    X, Y = np.meshgrid(x, y)
+    dxs, dys = X - p.x_source, Y - p.y_source
+    r = np.sqrt(dxs * dxs + dys * dys)
+    rr = np.minimum(r / radius, 1.0)
+    pert = 1.0 + 0.05 * (uniform01(seed, nx * ny).reshape(ny, nx) - 0.5)
+    # the ring interior stays dry: the reference never updates those cells
+    h = np.where((r < radius) & (r > p.r_source), h_max * (1.0 - rr * rr) * pert, 0.0)
+    ur = u_max * np.sqrt(rr)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ex = np.where(r > 0, dxs / r, 0.0)
+        ey = np.where(r > 0, dys / r, 0.0)
+    alphas = [p.alphas_source[i] for i in range(p.n_solid)]
+    q = rest_state_q(p, h, T, alphas)
+    # add momentum and, with the energy equation, its kinetic energy
+    q[1] = q[0] * ur * ex
+    q[2] = q[0] * ur * ey
+    if p.energy_flag:
+        q[3] = q[3] + 0.5 * q[0] * ur * ur
+    return q
+
+
 def ensemble_params(index, precision=PREC_FP32, steps=2000):
     """Member `index` of the 256-run ensemble; its draws use seed = index."""
     u = uniform01(0x5EED0000 + index, 8)

@@ -172,6 +172,11 @@ void sflow_destroy(sflow_handle* h);
  * t = t_start, dt = dt_old = dt_old_old = dt0 (IMEX_SfloW2D.f90:300-304). */
 int sflow_upload_q(sflow_handle* h, const double* q_aos);
 int sflow_download_q(sflow_handle* h, double* q_aos);
+/* Replace the state only (time, dt history, maxima and counters kept): for
+ * a host that owns q between steps and hands it over at every call. */
+int sflow_put_q(sflow_handle* h, const double* q_aos);
+/* Set the driver clock: t, dt_old, dt_old_old (IMEX_SfloW2D.f90:417-439). */
+int sflow_set_clock(sflow_handle* h, double t, double dt_old, double dt_old_old);
 /* qp(1:n_vars+2,nx,ny) of the last post-step pass. */
 int sflow_download_qp(sflow_handle* h, double* qp_aos);
 /* hmax, pdynmax, mod_vel_max, each nx*ny column-major (IMEX_SfloW2D.f90:449-505) */
@@ -208,6 +213,17 @@ int sflow_get_stats(sflow_handle* h, SflowStepStats* stats);
 int sflow_status(sflow_handle* h, uint32_t* flags);
 int sflow_clear_status(sflow_handle* h);
 
+/*
+ * Timing support.  sflow_advance_timed runs `steps` driver iterations one
+ * at a time, each bracketed by CUDA events on the handle's stream, and
+ * returns the summed device time in ms; with flush_l2 != 0 a buffer larger
+ * than L2 is written between steps, outside the timed intervals.
+ * sflow_profile_kernels does the same with events between the four kernels
+ * of a step and returns the summed ms of each (mask, flux, dt, stage).
+ */
+int sflow_advance_timed(sflow_handle* h, int64_t steps, int32_t flush_l2, double* device_ms);
+int sflow_profile_kernels(sflow_handle* h, int64_t steps, int32_t flush_l2, double* ms4);
+
 /* Number of kernel launches issued by this handle since creation (for the
  * benchmark's launch count). */
 int64_t sflow_launch_count(const sflow_handle* h);
@@ -219,6 +235,20 @@ int64_t sflow_device_bytes(const sflow_handle* h);
  * active cells), steps, Newton iterations and the largest per-cell count. */
 int sflow_counters(sflow_handle* h, int64_t* cell_updates, int64_t* steps,
                    int64_t* newton_iters, int32_t* newton_max);
+
+/*
+ * Host-side set-up of a domain without touching the GPU (for tests and
+ * tools).  Fills out (nx*ny doubles, column-major) with one derived field:
+ * 0 B'_x  1 B'_y  2 B''_xx  3 B''_xy  4 B''_yy (topography_reconstruction,
+ * geometry_2d.f90:555-895), 5 grav_coeff  6 d grav_coeff/dx
+ * 7 d grav_coeff/dy, 8 ring inlet perimeter  9 its normal x  10 normal y
+ * (init_source, geometry_2d.f90:907-1323), 11 source_cell (0, 1, 2),
+ * 12 ring face flags (E | W<<1 | N<<2 | S<<3).
+ */
+int sflow_host_geometry(const SflowParams* p, const double* B_cent, int32_t which, double* out);
+/* out[0] = h_source (inpout_2d.f90:4745), out[1] = rho_m and out[2] = c_p of
+ * the inlet state, out[3] = eps_sing (geometry_2d.f90:300-310). */
+int sflow_host_scalars(const SflowParams* p, const double* B_cent, double* out4);
 
 /* Build information ("fp64+fp32 sm_103a ..."). */
 const char* sflow_build_info(void);

@@ -33,6 +33,8 @@
  *      leaves it unset (geometry_2d.f90:884-886 assigns dx twice).
  *  D3  The reference pauses on READ(*,*) on a NaN / negative thickness /
  *      T < 273 K; here a status bit is raised and the step continues.
+ *  D4  A non-finite Newton residual ends the Newton solve at once (the
+ *      reference iterates to its iteration limits on such a cell).
  *  Scope: n_add_gas = 0, no stochastic / pore-pressure / vertical-profile
  *  terms, no bottom radial source, no erosion (EROSION_COEFF = 0),
  *  rheology models 1 (Voellmy-Salm) and 6, SOLVER_SCHEME KT or UP.
@@ -449,7 +451,7 @@ static void c_implicit_terms(const phys_t* P, double Bx, double By, const cplx* 
 /* real call of eval_implicit_terms (r_qj path): complex with zero imag */
 static void r_implicit_terms(const phys_t* P, double Bx, double By, const double* q, double* nh) {
   cplx cq[SFLOW_MAX_VARS], cn[SFLOW_MAX_VARS];
-  for (int i = 0; i < P->nv; ++i) cq[i] = q[i];
+  for (int i = 0; i < SFLOW_MAX_VARS; ++i) cq[i] = (i < P->nv) ? q[i] : 0.0;
   c_implicit_terms(P, Bx, By, cq, cn);
   for (int i = 0; i < P->nv; ++i) nh[i] = creal(cn[i]);
 }
@@ -608,6 +610,7 @@ static int solve_rk_step(const newton_ctx* c, double* qj) {
     double mf = 0.0;
     for (int i = 0; i < nv; ++i) mf = dmax(mf, fabs(right_term[i]));
     if (mf < TOLF) return nl_iter;
+    if (!isfinite(scal_f)) return max_nl_iter + 1; /* D4: NaN/Inf state */
     eval_jacobian(c, qj_rel, qj_org, L);
     /* explicit block: diagonal (mask11), coupling mask21 is identically 0
      * for a Jacobian with only implicit columns filled */
