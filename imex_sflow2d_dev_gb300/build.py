@@ -27,6 +27,7 @@ UNITS = [
     ("sflow_k_fp32_ns3.cu", FP32),
     ("sflow_k_fp64_ns1.cu", FP64),
     ("sflow_k_fp32_ns1.cu", FP32),
+    ("sflow_noalloc.cu", FP64),
     ("sflow_fp64.cu", FP64),
     ("sflow_fp32.cu", FP32),
     ("sflow_setup.cpp", []),

@@ -65,6 +65,8 @@ def load(build_if_missing=True):
         "sflow_set_clock": (C.c_int, [vp, C.c_double, C.c_double, C.c_double]),
         "sflow_advance_timed": (C.c_int, [vp, i64, i32, dp]),
         "sflow_profile_kernels": (C.c_int, [vp, i64, i32, dp]),
+        "sflow_log_sums_noalloc": (C.c_int, [P, vp, vp, vp]),
+        "sflow_log_sums_noalloc_error": (C.c_char_p, []),
         "sflow_host_geometry": (C.c_int, [P, dp, i32, dp]),
         "sflow_host_scalars": (C.c_int, [P, dp, dp]),
     }
@@ -83,7 +85,21 @@ def exported_symbols():
             "sflow_erosion_deposition", "sflow_post_step", "sflow_step", "sflow_advance",
             "sflow_get_stats", "sflow_status", "sflow_clear_status", "sflow_launch_count",
             "sflow_device_bytes", "sflow_counters", "sflow_host_geometry", "sflow_host_scalars",
-            "sflow_put_q", "sflow_set_clock", "sflow_advance_timed", "sflow_profile_kernels"]
+            "sflow_put_q", "sflow_set_clock", "sflow_advance_timed", "sflow_profile_kernels",
+            "sflow_log_sums_noalloc", "sflow_log_sums_noalloc_error"]
+
+
+def log_sums_noalloc(params, q_dev_ptr, sums_dev_ptr, stream_ptr=0):
+    """Mass, volume, wet area and solid mass of a device-resident state
+    (reference layout) into 4 device doubles, without any device allocation
+    (see include/sflow.h).  Pointers are integers (device addresses)."""
+    lib = load()
+    p = params.copy()
+    rc = lib.sflow_log_sums_noalloc(C.byref(p), C.c_void_p(q_dev_ptr), C.c_void_p(sums_dev_ptr),
+                                    C.c_void_p(stream_ptr))
+    if rc < 0:
+        raise SflowError(rc, lib.sflow_log_sums_noalloc_error().decode())
+    return rc
 
 
 def host_geometry(params, B_cent, which):

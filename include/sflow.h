@@ -250,6 +250,31 @@ int sflow_host_geometry(const SflowParams* p, const double* B_cent, int32_t whic
  * the inlet state, out[3] = eps_sing (geometry_2d.f90:300-310). */
 int sflow_host_scalars(const SflowParams* p, const double* B_cent, double* out4);
 
+/*
+ * Log-line sums (mass, volume, wet area, solid mass -- the four values of
+ * SflowStepStats, IMEX_SfloW2D.f90:535-542) of a state that the caller
+ * already holds in device memory, computed without allocating anything.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc when they need the sums (inside a CUDA graph capture, in a
+ * stream callback or host node, or under a host framework that owns all
+ * device memory).
+ *   p        parameters of the domain (only grid size, n_solid and the
+ *            carrier/energy constants are read)
+ *   q_dev    device pointer, q(1:n_vars,1:nx,1:ny) doubles, reference layout
+ *   sums_dev device pointer to 4 doubles, written asynchronously
+ *   stream   cudaStream_t to launch on (NULL = default stream)
+ * Scratch: one fixed 128 KiB device array inside the library, held by every
+ * GPU that loads the library until the process exits.  Domains above
+ * 67,108,864 cells (8192 x 8192) are rejected with SFLOW_ERANGE.  The first
+ * call on a device looks up the array's address; make that first call
+ * before any stream capture.  All calls share the array: calls whose kernels
+ * may overlap on the GPU (different streams without ordering) race and can
+ * return wrong sums; calls on one stream are safe.  Errors:
+ * sflow_log_sums_noalloc_error().
+ */
+int sflow_log_sums_noalloc(const SflowParams* p, const double* q_dev, double* sums_dev, void* stream);
+const char* sflow_log_sums_noalloc_error(void);
+
 /* Build information ("fp64+fp32 sm_103a ..."). */
 const char* sflow_build_info(void);
 

@@ -60,3 +60,11 @@ def test_host_geometry_matches_oracle(case):
         np.testing.assert_array_equal(g, want, err_msg=f"field {which}")
     sc = L.host_scalars(p, B)
     assert sc["h_source"] == o.h_source
+
+
+def test_log_sums_noalloc_rejects_domains_beyond_its_scratch():
+    p, B, q = W.dam_break(nx=16, ny=16)
+    p.comp_cells_x = p.comp_cells_y = 8193
+    with pytest.raises(L.SflowError) as e:
+        L.log_sums_noalloc(p, 1, 1)
+    assert e.value.code == -5 and "67,108,864" in str(e.value)
