@@ -491,7 +491,9 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
                                                        R* __restrict__ rout, int want_dt) {
   constexpr int nv = 4 + NS, np = nv + 2;
   const RunState* st = a.st;
-  if (!running(st)) return;
+  // the timestep pass runs before k_dt advances the clock; the later stage
+  // fluxes of a step run after it and follow its run_step decision
+  if (want_dt ? !running(st) : !st->run_step) return;
   if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
   const Grid<R>& g = a.g;
   const Phys<R>& P = a.pr;
@@ -614,7 +616,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
         R d = R(0);
         d = d + (sHx[i * TY * (TX + 1) + cy * (TX + 1) + cx + 1] - sHx[i * TY * (TX + 1) + cy * (TX + 1) + cx]) * g.one_by_dx;
         d = d + (sHy[i * (TY + 1) * TX + (cy + 1) * TX + cx] - sHy[i * (TY + 1) * TX + cy * TX + cx]) * g.one_by_dy;
-        rout[i * g.plane + c] = d - e[i];
+        if (rout) rout[i * g.plane + c] = d - e[i];
       }
       if (want_dt) {
         R ax = rmax(sAx[cy * (TX + 1) + cx], sAx[cy * (TX + 1) + cx + 1]);
@@ -805,13 +807,139 @@ __device__ __forceinline__ void post_step_maps(const KArgs<R>& a, int64_t c, con
 }
 
 // ---------------------------------------------------------------------------
-// k_stage2: the pointwise part of an N_RK = 2 step after the flux stage:
-// imex_RK_solver stage 2 (solver_2d.f90:1103-1328), assemble_sol
-// (1342-1630), update_erosion_deposition_cell, post-step maxima.
+// One stage of imex_RK_solver for one cell (solver_2d.f90:1103-1281):
+//   q_fv = q0 - dt*(s1 - s2),  s1 = sum a_tilde*(divFlux - expl),
+//                              s2 = sum a_dirk*(NH + SI) over earlier stages,
+// then for an implicit stage (a_diag /= 0) and q_fv(1) > 0 the semi-implicit
+// Coulomb term with its velocity fixes, the implicit Newton, the fixes after
+// it, and NH = (q_guess - q_si)/(dt a_diag).  Writes q_guess (the stage
+// state q_rk) and NH + SI of the stage.
 // ---------------------------------------------------------------------------
+template <class R, int NS>
+__device__ __forceinline__ unsigned stage_cell(const KArgs<R>& a, const Geo<R>& geo, const R* q0,
+                                               const R* s1, const R* s2, double dt, double a_diag,
+                                               R* qg_out, R* rn_out, int& nit) {
+  constexpr int nv = 4 + NS;
+  unsigned status = 0;
+  nit = 0;
+  if constexpr (sizeof(R) == 8) {
+    // ---- plain FP64 form: the reference's Newton, step by step ----
+    const Phys<double>& P = a.pd;
+    double qfv[nv], qp[nv + 2], si[nv], qsi[nv], qg[nv], Rj[nv];
+#pragma unroll
+    for (int i = 0; i < nv; ++i) qfv[i] = q0[i] - dt * (s1[i] - s2[i]);
+#pragma unroll
+    for (int i = 0; i < nv; ++i) { si[i] = 0.0; qsi[i] = qfv[i]; qg[i] = qfv[i]; }
+    if (a_diag != 0.0) {
+      if (qfv[0] > 0.0) {
+        qc_to_qp<double, NS>(P, qfv, qp);
+        semi_impl_terms<double, NS>(P, geo, qp, si);
+#pragma unroll
+        for (int i = 0; i < nv; ++i) qsi[i] = qfv[i] + dt * a_diag * si[i];
+        if (sq(qfv[1]) + sq(qfv[2]) == 0.0) {
+          qsi[1] = 0.0; qsi[2] = 0.0;
+        } else if (qsi[1] * qfv[1] < 0.0 || qsi[2] * qfv[2] < 0.0) {
+          qsi[1] = 0.0; qsi[2] = 0.0;
+        } else {
+          double m1 = sqrt(sq(qsi[1]) + sq(qsi[2])), m0 = sqrt(sq(qfv[1]) + sq(qfv[2]));
+          qsi[1] = m1 * qfv[1] / m0;
+          qsi[2] = m1 * qfv[2] / m0;
+        }
+#pragma unroll
+        for (int i = 0; i < nv; ++i) { si[i] = (qsi[i] - qfv[i]) / (dt * a_diag); qg[i] = qsi[i]; }
+#pragma unroll
+        for (int i = 0; i < nv; ++i) Rj[i] = (s1[i] - s2[i]) - a_diag * si[i];
+        NewtonCtx nc{&P, dt, a_diag, geo.Bx, geo.By, q0, Rj};
+        nit = solve_rk_step<NS>(nc, qg);
+        if (nit > kMaxNewton) status |= SFLOW_S_NEWTON_MAXIT;
+        if (a.g.ny == 1) qg[2] = 0.0;
+        if (sq(qsi[1]) + sq(qsi[2]) == 0.0) {
+          qg[1] = 0.0; qg[2] = 0.0;
+        } else if (qg[1] * qsi[1] <= 0.0 && qg[2] * qsi[2] <= 0.0) {
+          qg[1] = 0.0; qg[2] = 0.0;
+        } else {
+          double m1 = sqrt(sq(qg[1]) + sq(qg[2])), m0 = sqrt(sq(qsi[1]) + sq(qsi[2]));
+          qg[1] = m1 * qsi[1] / m0;
+          qg[2] = m1 * qsi[2] / m0;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < nv; ++i) rn_out[i] = (qg[i] - qsi[i]) / (dt * a_diag) + si[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < nv; ++i) rn_out[i] = 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < nv; ++i) qg_out[i] = qg[i];
+  } else {
+    // ---- FP32 bulk form: FP32 explicit part, FP64 scalar Newton ----
+    const Phys<R>& P = a.pr;
+    const R dtr = (R)dt;
+    const R dta = (R)(dt * a_diag);
+    R qfv[nv], qp[nv + 2], si[nv], qsi[nv], qg[nv];
+#pragma unroll
+    for (int i = 0; i < nv; ++i) qfv[i] = q0[i] - dtr * (s1[i] - s2[i]);
+#pragma unroll
+    for (int i = 0; i < nv; ++i) { si[i] = R(0); qsi[i] = qfv[i]; qg[i] = qfv[i]; }
+    if (a_diag != 0.0) {
+      if (qfv[0] > R(0)) {
+        qc_to_qp<R, NS>(P, qfv, qp);
+        semi_impl_terms<R, NS>(P, geo, qp, si);
+#pragma unroll
+        for (int i = 0; i < nv; ++i) qsi[i] = qfv[i] + dta * si[i];
+        if (sq(qfv[1]) + sq(qfv[2]) == R(0)) {
+          qsi[1] = R(0); qsi[2] = R(0);
+        } else if (qsi[1] * qfv[1] < R(0) || qsi[2] * qfv[2] < R(0)) {
+          qsi[1] = R(0); qsi[2] = R(0);
+        } else {
+          R m1 = sqrt(sq(qsi[1]) + sq(qsi[2])), m0 = sqrt(sq(qfv[1]) + sq(qfv[2]));
+          qsi[1] = m1 * qfv[1] / m0;
+          qsi[2] = m1 * qfv[2] / m0;
+        }
+        const R idta = R(1) / dta;
+#pragma unroll
+        for (int i = 0; i < nv; ++i) { si[i] = (qsi[i] - qfv[i]) * idta; qg[i] = qsi[i]; }
+        float e1, e2;
+        const float sv = reduced_friction_solve<NS>(P, geo.Bx, geo.By, qsi, dt * a_diag, e1, e2, nit);
+        qg[1] = sv * e1;
+        qg[2] = sv * e2;
+        if (a.g.ny == 1) qg[2] = R(0);
+      }
+      const R idta = R(1) / dta;
+#pragma unroll
+      for (int i = 0; i < nv; ++i) rn_out[i] = (qg[i] - qsi[i]) * idta + si[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < nv; ++i) rn_out[i] = R(0);
+    }
+#pragma unroll
+    for (int i = 0; i < nv; ++i) qg_out[i] = qg[i];
+  }
+  return status;
+}
+
+template <class R>
+__device__ __forceinline__ void newton_stats(RunState* st, unsigned status, int nit) {
+  if (status) atomicOr(&st->status, status);
+  int wsum = nit;
+  for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+  int wmax = nit;
+  for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+  if ((threadIdx.x & 31) == 0 && wsum > 0) {
+    atomicAdd((unsigned long long*)&st->newton_iters, (unsigned long long)wsum);
+    atomicMax(&st->newton_max, wmax);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_stage2: the pointwise part of an N_RK = 2 step after the flux stage:
+// imex_RK_solver stage 2 (a_tilde(2,1) = 1, a_dirk(2,2) = 1), assemble_sol
+// (1342-1630; the last tableau row equals omega, so q = q_rk(2)),
+// update_erosion_deposition_cell, post-step maxima.
 // mode -1: stage + assembly + erosion/deposition + maxima (fused step);
 // 0: stage + assembly (imex_RK_solver); 1: erosion/deposition only;
 // 2: maxima only.
+// ---------------------------------------------------------------------------
 template <class R, int NS>
 __global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
   constexpr int nv = 4 + NS;
@@ -825,120 +953,138 @@ __global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
   int nit = 0;
   if (j < g.nx && k < g.ny) {
     const int64_t c = cidx(g, j, k);
-    if (a.mask[c] && mode > 0) {
+    if (a.mask[c]) {
       const double dt = st->dt;
       R q[nv];
 #pragma unroll
       for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + c];
-      if (mode == 1) {
+      if (mode > 0) {
+        if (mode == 1) {
+          const Geo<R> geo = load_geo(a, c);
+          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q);
+#pragma unroll
+          for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
+        } else {
+          post_step_maps<R, NS>(a, c, q);
+        }
+      } else {
         const Geo<R> geo = load_geo(a, c);
-        status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q);
+        R s1[nv], s2[nv], rn[nv];
+#pragma unroll
+        for (int i = 0; i < nv; ++i) {
+          s1[i] = R(0) + a.rd[i * g.plane + c] * R(1);
+          s2[i] = R(0);
+        }
+        status |= stage_cell<R, NS>(a, geo, q, s1, s2, dt, 1.0, q, rn, nit);
+        status |= assemble_fixes<R, NS>(a.pr, q);
+        if (mode < 0 && (a.pd.settling || a.pd.entrain))
+          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q);
 #pragma unroll
         for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
-      } else {
-        post_step_maps<R, NS>(a, c, q);
+        if (mode < 0) post_step_maps<R, NS>(a, c, q);
       }
-    } else if (a.mask[c]) {
+    }
+  }
+  newton_stats<R>(st, status, nit);
+}
+
+// ---------------------------------------------------------------------------
+// General tableaux (N_RK = 1, 3, 4; solver_2d.f90:429-487): one kernel per
+// stage, the flux kernel for stages with omega_tilde > 0, one assembly.
+// rd holds divFlux - expl and rn holds NH + SI of every stage (n_vars planes
+// per stage); qs holds the state of the running stage.
+// ---------------------------------------------------------------------------
+template <class R, int NS>
+__global__ void __launch_bounds__(TX* TY) k_stage(KArgs<R> a, int irk) {
+  constexpr int nv = 4 + NS;
+  RunState* st = a.st;
+  if (!st->run_step) return;
+  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  const Grid<R>& g = a.g;
+  const int j = blockIdx.x * TX + threadIdx.x % TX;
+  const int k = blockIdx.y * TY + threadIdx.x / TX;
+  unsigned status = 0;
+  int nit = 0;
+  if (j < g.nx && k < g.ny) {
+    const int64_t c = cidx(g, j, k);
+    if (a.mask[c]) {
       const double dt = st->dt;
       const Geo<R> geo = load_geo(a, c);
-      R q[nv];
-      if constexpr (sizeof(R) == 8) {
-        // ---- plain FP64 form: the reference's Newton, step by step ----
-        const Phys<double>& P = a.pd;
-        double q0[nv], r1[nv], qfv[nv], qp[nv + 2], si[nv], qsi[nv], qg[nv], Rj[nv];
+      const int64_t sv = (int64_t)nv * g.plane;
+      R q0[nv], s1[nv], s2[nv], qg[nv], rn[nv];
 #pragma unroll
-        for (int i = 0; i < nv; ++i) { q0[i] = a.q[i * g.plane + c]; r1[i] = a.rd[i * g.plane + c]; }
+      for (int i = 0; i < nv; ++i) {
+        q0[i] = a.q[i * g.plane + c];
+        s1[i] = R(0);
+        s2[i] = R(0);
+      }
+      for (int r = 0; r < irk; ++r) {
+        const R at = (R)a.tableau_at[irk * 4 + r], ad = (R)a.tableau_ad[irk * 4 + r];
 #pragma unroll
-        for (int i = 0; i < nv; ++i) qfv[i] = q0[i] - dt * (r1[i] * 1.0 - 0.0);
-        qc_to_qp<double, NS>(P, qfv, qp);
-        const double a_diag = 1.0;
-        if (qfv[0] > 0.0) {
-          semi_impl_terms<double, NS>(P, geo, qp, si);
-#pragma unroll
-          for (int i = 0; i < nv; ++i) qsi[i] = qfv[i] + dt * a_diag * si[i];
-          if (sq(qfv[1]) + sq(qfv[2]) == 0.0) {
-            qsi[1] = 0.0; qsi[2] = 0.0;
-          } else if (qsi[1] * qfv[1] < 0.0 || qsi[2] * qfv[2] < 0.0) {
-            qsi[1] = 0.0; qsi[2] = 0.0;
-          } else {
-            double m1 = sqrt(sq(qsi[1]) + sq(qsi[2])), m0 = sqrt(sq(qfv[1]) + sq(qfv[2]));
-            qsi[1] = m1 * qfv[1] / m0;
-            qsi[2] = m1 * qfv[2] / m0;
-          }
-#pragma unroll
-          for (int i = 0; i < nv; ++i) { si[i] = (qsi[i] - qfv[i]) / (dt * a_diag); qg[i] = qsi[i]; }
-#pragma unroll
-          for (int i = 0; i < nv; ++i) Rj[i] = (r1[i] * 1.0 - 0.0) - a_diag * si[i];
-          NewtonCtx nc{&P, dt, a_diag, geo.Bx, geo.By, q0, Rj};
-          nit = solve_rk_step<NS>(nc, qg);
-          if (nit > kMaxNewton) status |= SFLOW_S_NEWTON_MAXIT;
-          if (g.ny == 1) qg[2] = 0.0;
-          if (sq(qsi[1]) + sq(qsi[2]) == 0.0) {
-            qg[1] = 0.0; qg[2] = 0.0;
-          } else if (qg[1] * qsi[1] <= 0.0 && qg[2] * qsi[2] <= 0.0) {
-            qg[1] = 0.0; qg[2] = 0.0;
-          } else {
-            double m1 = sqrt(sq(qg[1]) + sq(qg[2])), m0 = sqrt(sq(qsi[1]) + sq(qsi[2]));
-            qg[1] = m1 * qsi[1] / m0;
-            qg[2] = m1 * qsi[2] / m0;
-          }
-        } else {
-#pragma unroll
-          for (int i = 0; i < nv; ++i) qg[i] = qfv[i];
-        }
-#pragma unroll
-        for (int i = 0; i < nv; ++i) q[i] = qg[i];
-      } else {
-        // ---- FP32 bulk form: FP32 explicit part, FP64 scalar Newton ----
-        const Phys<R>& P = a.pr;
-        const R dtr = (R)dt;
-        R qfv[nv], qp[nv + 2], si[nv], qsi[nv];
-#pragma unroll
-        for (int i = 0; i < nv; ++i) qfv[i] = a.q[i * g.plane + c] - dtr * a.rd[i * g.plane + c];
-        qc_to_qp<R, NS>(P, qfv, qp);
-        if (qfv[0] > R(0)) {
-          semi_impl_terms<R, NS>(P, geo, qp, si);
-#pragma unroll
-          for (int i = 0; i < nv; ++i) qsi[i] = qfv[i] + dtr * si[i];
-          if (sq(qfv[1]) + sq(qfv[2]) == R(0)) {
-            qsi[1] = R(0); qsi[2] = R(0);
-          } else if (qsi[1] * qfv[1] < R(0) || qsi[2] * qfv[2] < R(0)) {
-            qsi[1] = R(0); qsi[2] = R(0);
-          } else {
-            R m1 = sqrt(sq(qsi[1]) + sq(qsi[2])), m0 = sqrt(sq(qfv[1]) + sq(qfv[2]));
-            qsi[1] = m1 * qfv[1] / m0;
-            qsi[2] = m1 * qfv[2] / m0;
-          }
-          float e1, e2;
-          const float sv = reduced_friction_solve<NS>(P, geo.Bx, geo.By, qsi, dt, e1, e2, nit);
-#pragma unroll
-          for (int i = 0; i < nv; ++i) q[i] = qsi[i];
-          q[1] = sv * e1;
-          q[2] = sv * e2;
-          if (g.ny == 1) q[2] = R(0);
-        } else {
-#pragma unroll
-          for (int i = 0; i < nv; ++i) q[i] = qfv[i];
+        for (int i = 0; i < nv; ++i) {
+          s1[i] = s1[i] + a.rd[r * sv + i * g.plane + c] * at;
+          s2[i] = s2[i] + a.rn[r * sv + i * g.plane + c] * ad;
         }
       }
+      status |= stage_cell<R, NS>(a, geo, q0, s1, s2, dt, a.tableau_ad[irk * 4 + irk], qg, rn, nit);
+#pragma unroll
+      for (int i = 0; i < nv; ++i) {
+        a.qs[i * g.plane + c] = qg[i];
+        a.rn[irk * sv + i * g.plane + c] = rn[i];
+      }
+    }
+  }
+  newton_stats<R>(st, status, nit);
+}
+
+// assemble_sol (solver_2d.f90:1342-1630) + erosion/deposition + maxima
+template <class R, int NS>
+__global__ void __launch_bounds__(TX* TY) k_assemble(KArgs<R> a) {
+  constexpr int nv = 4 + NS;
+  RunState* st = a.st;
+  if (!st->run_step) return;
+  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  const Grid<R>& g = a.g;
+  const int j = blockIdx.x * TX + threadIdx.x % TX;
+  const int k = blockIdx.y * TY + threadIdx.x / TX;
+  unsigned status = 0;
+  if (j < g.nx && k < g.ny) {
+    const int64_t c = cidx(g, j, k);
+    if (a.mask[c]) {
+      const double dt = st->dt;
+      const int64_t sv = (int64_t)nv * g.plane;
+      const int nrk = a.pd.nrk;
+      R q[nv];
+      if (a.take_last) {
+#pragma unroll
+        for (int i = 0; i < nv; ++i) q[i] = a.qs[i * g.plane + c];
+      } else {
+        R s1[nv], s2[nv];
+#pragma unroll
+        for (int i = 0; i < nv; ++i) { s1[i] = R(0); s2[i] = R(0); }
+        for (int r = 0; r < nrk; ++r) {
+          const R ot = (R)a.omega_t[r], om = (R)a.omega[r];
+#pragma unroll
+          for (int i = 0; i < nv; ++i) {
+            s1[i] = s1[i] + a.rd[r * sv + i * g.plane + c] * ot;
+            s2[i] = s2[i] + a.rn[r * sv + i * g.plane + c] * om;
+          }
+        }
+        const R dtr = (R)dt;
+#pragma unroll
+        for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + c] - dtr * (s1[i] - s2[i]);
+      }
       status |= assemble_fixes<R, NS>(a.pr, q);
-      if (mode < 0 && (a.pd.settling || a.pd.entrain))
+      if (a.pd.settling || a.pd.entrain) {
+        const Geo<R> geo = load_geo(a, c);
         status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q);
+      }
 #pragma unroll
       for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
-      if (mode < 0) post_step_maps<R, NS>(a, c, q);
+      post_step_maps<R, NS>(a, c, q);
     }
   }
   if (status) atomicOr(&st->status, status);
-  // Newton iteration statistics (one atomic per warp)
-  int wsum = nit;
-  for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
-  int wmax = nit;
-  for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
-  if ((threadIdx.x & 31) == 0 && wsum > 0) {
-    atomicAdd((unsigned long long*)&st->newton_iters, (unsigned long long)wsum);
-    atomicMax(&st->newton_max, wmax);
-  }
 }
 
 }  // namespace sflow

@@ -744,9 +744,8 @@ __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R 
 // phi = u/hu.  K depends on s only through T (the energy equation subtracts
 // the kinetic energy) and through the gas density.  This is the fixed point
 // of the reference's 2x2 Newton (solver_2d.f90:1662-1996).  The
-// coefficients come from the FP32 state; an FP32 Newton gives the start,
-// FP64 Newton steps with an analytic derivative converge it to
-// |ds| <= 1e-15 s (one or two steps).
+// coefficients come from the FP32 state; an FP32 Newton gives the start and
+// one FP64 Newton step with the analytic derivative finishes it.
 // ---------------------------------------------------------------------------
 
 // 1/x to ~1 ulp: float estimate + two Newton-Raphson refinements in FP64
@@ -821,22 +820,27 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, fl
       if (!(fabsf(ds) > 1.0e-7f * s)) break;
     }
   }
-  // FP64 Newton steps from the FP32 root
-  const double Sd = S, cg = cgeo, aT = a_T, bT = b_T, ci = c_inv, bi = base_inv, ra = rho_a;
-  const double Tamb = P.T_ambient;
+  // One FP64 Newton step from the FP32 root.  The FP32 root is within
+  // ~1e-7 relative of the solution, so the step leaves an error of order
+  // 1e-14, far below the float the result is stored in; residual and
+  // derivative are evaluated in FP64 (rho_m to ~1e-14 by one refinement of
+  // the float reciprocal; the step itself needs only ~1e-7 relative).
+  const double Sd = S, cg = cgeo, bi = base_inv, ra = rho_a;
   double sd = s;
-  for (int it = 0; it < 4; ++it) {
-    double T = aT - bT * sd * sd, dT = -2.0 * bT * sd;
-    if (T <= 0.0) { T = Tamb; dT = 0.0; }
-    const double rho_m = rcp64(bi + ci * T);
+  {
+    double T = (double)a_T - (double)b_T * sd * sd;
+    double dT = -2.0 * (double)b_T * sd;
+    if (T <= 0.0) { T = (double)P.T_ambient; dT = 0.0; }
+    const double ci = c_inv;
+    const double x = bi + ci * T;
+    double rho_m = (double)__frcp_rn((float)x);
+    rho_m = rho_m * (2.0 - x * rho_m);
     const double Kd = cg * (rho_m - ra);
     const double dKd = cg * (-rho_m * rho_m * ci * dT);
     const double gv = sd + dta * Kd * sd * sd - Sd;
     const double gd = 1.0 + dta * (dKd * sd * sd + 2.0 * Kd * sd);
-    const double ds = gv * rcp64(gd);
-    sd -= ds;
-    ++iters;
-    if (!(fabs(ds) > 1.0e-15 * sd)) break;
+    sd -= gv * (double)__frcp_rn((float)gd);
+    iters = 1;
   }
   return sd > 0.0 ? (float)sd : 0.0f;
 }

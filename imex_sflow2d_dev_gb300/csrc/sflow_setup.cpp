@@ -240,7 +240,7 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   if (p.comp_cells_x < 5 || p.comp_cells_y < 5) { err = "comp_cells_x and comp_cells_y must be >= 5"; return SFLOW_EINVAL; }
   if ((int64_t)p.comp_cells_x * p.comp_cells_y > (int64_t)1 << 31) { err = "domain larger than 2^31 cells"; return SFLOW_ERANGE; }
   if (p.n_solid < 1 || p.n_solid > 3) { err = "the GPU kernels are built for n_solid = 1, 2 or 3"; return SFLOW_EINVAL; }
-  if (p.n_rk != 2) { err = "only N_RK = 2 (the reference default tableau) is implemented on the GPU"; return SFLOW_EINVAL; }
+  if (p.n_rk < 1 || p.n_rk > 4) { err = "N_RK must be 1, 2, 3 or 4"; return SFLOW_EINVAL; }
   if (p.gas_flag && p.liquid_flag) { err = "gas carrier with a liquid phase is not supported"; return SFLOW_EINVAL; }
   if (!p.gas_flag && !p.liquid_flag) { err = "one of gas_flag / liquid_flag must be set"; return SFLOW_EINVAL; }
   if (p.rheology_flag && p.rheology_model != 1 && p.rheology_model != 6) { err = "rheology_model must be 1 or 6"; return SFLOW_EINVAL; }
@@ -277,12 +277,38 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   s.T_erodible = 300.0;
   s.rho_c_sub = p.gas_flag ? p.pres / (p.sp_gas_const_a * s.T_erodible) : p.rho_l;
 
-  // tableau (solver_2d.f90:429-439 for N_RK = 2)
-  s.a_tilde[1 * 4 + 0] = 1.0;
-  s.omega_tilde[0] = 1.0;
-  s.a_dirk[1 * 4 + 1] = 1.0;
-  s.omega[1] = 1.0;
-  s.take_last = 1;
+  // IMEX tableaux (solver_2d.f90:421-487)
+  {
+    auto AT = [&](int i, int j) -> double& { return s.a_tilde[(i - 1) * 4 + (j - 1)]; };
+    auto AD = [&](int i, int j) -> double& { return s.a_dirk[(i - 1) * 4 + (j - 1)]; };
+    switch (p.n_rk) {
+      case 1:
+        AT(1, 1) = 1.0; s.omega_tilde[0] = 1.0;
+        break;
+      case 2:
+        AT(2, 1) = 1.0; s.omega_tilde[0] = 1.0; AD(2, 2) = 1.0; s.omega[1] = 1.0;
+        break;
+      case 3:
+        AT(2, 1) = 0.5; AT(3, 1) = 0.5; AT(3, 2) = 0.5;
+        s.omega_tilde[0] = s.omega_tilde[1] = s.omega_tilde[2] = 1.0 / 3.0;
+        AD(1, 1) = 0.25; AD(2, 2) = 0.25; AD(3, 1) = 1.0 / 3.0; AD(3, 2) = 1.0 / 3.0; AD(3, 3) = 1.0 / 3.0;
+        s.omega[0] = s.omega[1] = s.omega[2] = 1.0 / 3.0;
+        break;
+      case 4:
+        AT(2, 1) = 0.5; AT(3, 1) = 1.0 / 3.0; AT(4, 2) = 1.0;
+        s.omega_tilde[1] = 1.0;
+        AD(2, 2) = 0.5; AD(3, 3) = 1.0 / 3.0; AD(4, 3) = 0.75; AD(4, 4) = 0.25;
+        s.omega[2] = 0.75; s.omega[3] = 0.25;
+        break;
+    }
+    // q = q_rk(n_RK) when the last row equals the weights (solver_2d.f90:1362-1372)
+    double d1 = 0.0, d2 = 0.0;
+    for (int r = 0; r < p.n_rk; ++r) {
+      d1 += std::fabs(s.omega_tilde[r] - s.a_tilde[(p.n_rk - 1) * 4 + r]);
+      d2 += std::fabs(s.omega[r] - s.a_dirk[(p.n_rk - 1) * 4 + r]);
+    }
+    s.take_last = (d1 == 0.0 && d2 == 0.0) ? 1 : 0;
+  }
 
   if (!B) { err = "B_cent is NULL"; return SFLOW_EINVAL; }
   topography(s, B);

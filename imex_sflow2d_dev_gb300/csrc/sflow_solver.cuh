@@ -97,7 +97,15 @@ class Solver : public SolverBase {
     tiles_y_ = (ny + TY - 1) / TY;
     SFLOW_CU(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     SFLOW_CU(alloc((void**)&q_, sizeof(R) * plane_ * nv));
-    SFLOW_CU(alloc((void**)&rd_, sizeof(R) * plane_ * nv));
+    const int nstage = (hs_.nrk == 2) ? 1 : hs_.nrk;
+    SFLOW_CU(alloc((void**)&rd_, sizeof(R) * plane_ * nv * nstage));
+    SFLOW_CU(cudaMemset(rd_, 0, sizeof(R) * plane_ * nv * nstage));
+    if (hs_.nrk != 2) {
+      SFLOW_CU(alloc((void**)&rn_, sizeof(R) * plane_ * nv * nstage));
+      SFLOW_CU(cudaMemset(rn_, 0, sizeof(R) * plane_ * nv * nstage));
+      SFLOW_CU(alloc((void**)&qs_, sizeof(R) * plane_ * nv));
+      SFLOW_CU(cudaMemset(qs_, 0, sizeof(R) * plane_ * nv));
+    }
     for (int i = 0; i < 8; ++i) geo_[i] = nullptr;
     const std::vector<double>* gsrc[8] = {&hs_.Bx, &hs_.By, &hs_.Bxx, &hs_.Bxy, &hs_.Byy, &hs_.gc, &hs_.dgcx, &hs_.dgcy};
     for (int i = 0; i < 8; ++i) {
@@ -128,7 +136,6 @@ class Solver : public SolverBase {
     SFLOW_CU(alloc((void**)&stat_part_, sizeof(double) * 4 * nstat_blocks_));
     SFLOW_CU(alloc((void**)&stat_out_, sizeof(double) * 4));
     SFLOW_CU(cudaMemset(q_, 0, sizeof(R) * plane_ * nv));
-    SFLOW_CU(cudaMemset(rd_, 0, sizeof(R) * plane_ * nv));
     fill_args();
     // shared memory of the flux kernel
     smem_flux_ = flux_smem_bytes();
@@ -190,7 +197,7 @@ class Solver : public SolverBase {
       if (flush) SFLOW_CU(flush_l2());
       SFLOW_CU(cudaEventRecord(ev_[0], stream_));
       SFLOW_CU(cudaGraphLaunch(graph1_exec_, stream_));
-      launches_ += 4;
+      launches_ += steps_launches();
       SFLOW_CU(cudaEventRecord(ev_[1], stream_));
       SFLOW_CU(cudaEventSynchronize(ev_[1]));
       float m = 0.0f;
@@ -203,6 +210,7 @@ class Solver : public SolverBase {
 
   int profile_kernels(int64_t steps, int flush, double* ms4) override {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    if (hs_.nrk != 2) { err_ = "kernel profile is for N_RK = 2"; return SFLOW_EINVAL; }
     SFLOW_CU(prepare_timing(flush));
     SFLOW_CU(set_limits(hs_.p.t_end, -1));
     double tot[4] = {0, 0, 0, 0};
@@ -273,6 +281,7 @@ class Solver : public SolverBase {
   }
   int timestep(double* dt_out) override {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    if (hs_.nrk != 2) { err_ = "the per-call-site entry points need N_RK = 2; use sflow_step / sflow_advance"; return SFLOW_EINVAL; }
     SFLOW_CU(launch_flux(1));
     RunState h;
     SFLOW_CU(cudaMemcpyAsync(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
@@ -350,7 +359,7 @@ class Solver : public SolverBase {
       const int64_t burst = chunks < 8 ? chunks : 8;
       for (int64_t b = 0; b < burst; ++b) {
         SFLOW_CU(cudaGraphLaunch(graph_exec_, stream_));
-        launches_ += kChunk * 4;
+        launches_ += kChunk * steps_launches();
       }
       SFLOW_CU(cudaMemcpyAsync(&hst_, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
       SFLOW_CU(cudaStreamSynchronize(stream_));
@@ -415,7 +424,7 @@ class Solver : public SolverBase {
   int64_t plane_ = 0;
   int tiles_x_ = 0, tiles_y_ = 0;
   cudaStream_t stream_ = nullptr;
-  R *q_ = nullptr, *rd_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
+  R *q_ = nullptr, *rd_ = nullptr, *rn_ = nullptr, *qs_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
   R* geo_[8];
   uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr;
   RunState* st_ = nullptr;
@@ -466,6 +475,15 @@ class Solver : public SolverBase {
     if (e2 != cudaSuccess) return e2;
     graph1_ = g;
     return cudaGraphInstantiate(&graph1_exec_, graph1_, 0);
+  }
+
+  int steps_launches() const {
+    if (hs_.nrk == 2) return 4;
+    int n = 3 + hs_.nrk + 1;
+    const bool fused0 = hs_.a_dirk[0] == 0.0 && hs_.omega_tilde[0] > 0.0;
+    for (int i = 0; i < hs_.nrk; ++i)
+      if (hs_.omega_tilde[i] > 0.0 && !(i == 0 && fused0)) ++n;
+    return n;
   }
 
   static unsigned long long bits_of(double x) {
@@ -580,7 +598,9 @@ class Solver : public SolverBase {
         ka_.bc.flag[sd][i] = p.bc[sd][i].flag;
         ka_.bc.value[sd][i] = (R)p.bc[sd][i].value;
       }
-    ka_.q = q_; ka_.rd = rd_; ka_.rn = nullptr; ka_.qs = nullptr;
+    ka_.q = q_; ka_.rd = rd_; ka_.rn = rn_; ka_.qs = qs_;
+    for (int i = 0; i < 16; ++i) { ka_.tableau_at[i] = hs_.a_tilde[i]; ka_.tableau_ad[i] = hs_.a_dirk[i]; }
+    for (int i = 0; i < 4; ++i) { ka_.omega_t[i] = hs_.omega_tilde[i]; ka_.omega[i] = hs_.omega[i]; }
     for (int i = 0; i < 8; ++i) ka_.geo[i] = geo_[i];
     ka_.cflags = cflags_; ka_.arc = arc_; ka_.mask = mask_; ka_.tile_active = tile_active_;
     ka_.hmax = hmax_; ka_.pdynmax = pdynmax_; ka_.mvmax = mvmax_; ka_.st = st_;
@@ -640,15 +660,49 @@ class Solver : public SolverBase {
   }
 
   cudaError_t launch_step() {
+    if (hs_.nrk == 2) {
+      cudaError_t e = launch_mask(0);
+      if (e != cudaSuccess) return e;
+      e = launch_flux(1);
+      if (e != cudaSuccess) return e;
+      k_dt<<<1, 1, 0, stream_>>>(st_, hs_.p.max_dt);
+      ++launches_;
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      return launch_stage2(-1);
+    }
+    return launch_step_general();
+  }
+
+  // N_RK = 1, 3, 4: the timestep pass at q0 (fused with the stage-1 flux
+  // when stage 1 is explicit and has a flux), then per stage the pointwise
+  // stage kernel and, when omega_tilde > 0, the flux at the stage state.
+  cudaError_t launch_step_general() {
+    const int nv = hs_.nv;
+    const int64_t sv = (int64_t)nv * plane_;
+    const dim3 grid(tiles_x_, tiles_y_);
+    const bool fused0 = hs_.a_dirk[0] == 0.0 && hs_.omega_tilde[0] > 0.0;
     cudaError_t e = launch_mask(0);
     if (e != cudaSuccess) return e;
-    e = launch_flux(1);
+    ++launches_;
+    e = tab_.flux(ka_, grid, smem_flux_, stream_, q_, fused0 ? rd_ : nullptr, 1);
     if (e != cudaSuccess) return e;
     k_dt<<<1, 1, 0, stream_>>>(st_, hs_.p.max_dt);
     ++launches_;
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return launch_stage2(-1);
+    for (int i = 0; i < hs_.nrk; ++i) {
+      ++launches_;
+      e = tab_.stage(ka_, grid, stream_, i);
+      if (e != cudaSuccess) return e;
+      if (hs_.omega_tilde[i] > 0.0 && !(i == 0 && fused0)) {
+        ++launches_;
+        e = tab_.flux(ka_, grid, smem_flux_, stream_, qs_, rd_ + i * sv, 0);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    ++launches_;
+    return tab_.assemble(ka_, grid, stream_);
   }
 
   cudaError_t build_graph() {

@@ -16,6 +16,8 @@ template <class R>
 struct KernelTable {
   cudaError_t (*flux)(const KArgs<R>&, dim3, size_t, cudaStream_t, const R*, R*, int) = nullptr;
   cudaError_t (*stage2)(const KArgs<R>&, dim3, cudaStream_t, int) = nullptr;
+  cudaError_t (*stage)(const KArgs<R>&, dim3, cudaStream_t, int) = nullptr;
+  cudaError_t (*assemble)(const KArgs<R>&, dim3, cudaStream_t) = nullptr;
   cudaError_t (*init_maps)(const KArgs<R>&, unsigned, cudaStream_t) = nullptr;
   cudaError_t (*qp)(const KArgs<R>&, unsigned, cudaStream_t, double*) = nullptr;
   cudaError_t (*stats)(const KArgs<R>&, int, cudaStream_t, double*) = nullptr;

@@ -98,6 +98,16 @@ static cudaError_t tab_stage2(const KArgs<R>& a, dim3 grid, cudaStream_t s, int 
   return cudaGetLastError();
 }
 template <class R, int NS>
+static cudaError_t tab_stage(const KArgs<R>& a, dim3 grid, cudaStream_t s, int irk) {
+  k_stage<R, NS><<<grid, TX * TY, 0, s>>>(a, irk);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_assemble(const KArgs<R>& a, dim3 grid, cudaStream_t s) {
+  k_assemble<R, NS><<<grid, TX * TY, 0, s>>>(a);
+  return cudaGetLastError();
+}
+template <class R, int NS>
 static cudaError_t tab_init_maps(const KArgs<R>& a, unsigned blocks, cudaStream_t s) {
   k_init_maps<R, NS><<<blocks, 256, 0, s>>>(a);
   return cudaGetLastError();
@@ -122,6 +132,8 @@ KernelTable<R> make_table() {
   KernelTable<R> t;
   t.flux = &tab_flux<R, NS>;
   t.stage2 = &tab_stage2<R, NS>;
+  t.stage = &tab_stage<R, NS>;
+  t.assemble = &tab_assemble<R, NS>;
   t.init_maps = &tab_init_maps<R, NS>;
   t.qp = &tab_qp<R, NS>;
   t.stats = &tab_stats<R, NS>;

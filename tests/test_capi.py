@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_create_rejects_unsupported_parameters():
     p, B, q = W.dam_break(nx=16, ny=16)
-    p.n_rk = 3
+    p.n_rk = 5
     with pytest.raises(L.SflowError) as e:
         L.Solver(p, B)
     assert e.value.code == -1 and "N_RK" in str(e.value)

@@ -253,3 +253,64 @@ def test_full_size_fp32_against_fp64_gpu():
     sa, sb = a.stats(), b.stats()
     assert abs(sa.t - sb.t) / sa.t < 1e-3
     assert abs(sa.mass / sa.t - sb.mass / sb.t) / (sa.mass / sa.t) < 1e-4
+
+
+# ---------------------------------------------------------------------------
+# The other IMEX tableaux of solver_2d.f90:419-487 (N_RK = 1, 3, 4): one
+# kernel per stage, the flux kernel for the stages with omega_tilde > 0 and
+# one assembly kernel.
+# ---------------------------------------------------------------------------
+def _tableau_case(case, n_rk):
+    if case == "dam_break":
+        p, B, q = W.dam_break(nx=64, ny=48, t_end=100.0, n_rk=n_rk)
+        return p, B, q, 30
+    p, B, q = _pyro(settling=True, entrainment=True, n_rk=n_rk)
+    return p, B, q, 40
+
+
+@pytest.mark.parametrize("n_rk", [1, 3, 4])
+@pytest.mark.parametrize("case", ["dam_break", "pyroclastic_settling_entrainment"])
+def test_fp64_other_tableaux_match_oracle(case, n_rk):
+    p, B, q, steps = _tableau_case(case, n_rk)
+    o, s = run_pair(p, B, q, steps)
+    so, sg = o.stats(), s.stats()
+    assert sg.status == so.status == 0
+    assert sg.steps == so.steps == steps
+    assert abs(sg.t - so.t) <= 1e-12 * max(so.t, 1.0)
+    assert sg.solve_cells == so.solve_cells
+    err = rel_err(s.download_q(), o.q(), p.n_vars, p.comp_cells_x, p.comp_cells_y)
+    assert max(err) <= FP64_TOL, err
+    for a, b in zip(s.maps(), o.maps()):
+        assert np.abs(a - b).max() <= FP64_TOL * max(np.abs(b).max(), 1e-30)
+
+
+@pytest.mark.parametrize("n_rk", [1, 3, 4])
+def test_fp32_other_tableaux_error_against_fp64(n_rk):
+    p, B, q, steps = _tableau_case("pyroclastic_settling_entrainment", n_rk)
+    o, s = run_pair(p, B, q, steps, precision=PREC_FP32)
+    assert s.stats().status == 0
+    nv, nx, ny = p.n_vars, p.comp_cells_x, p.comp_cells_y
+    assert l1_err(s.download_q(), o.q(), nv, nx, ny, 0) <= FP32_L1_TOL
+
+
+@pytest.mark.parametrize("n_rk", [3, 4])
+def test_other_tableaux_graph_advance_equals_single_steps(n_rk):
+    p, B, q, _ = _tableau_case("pyroclastic_settling_entrainment", n_rk)
+    s1 = L.Solver(p, B)
+    s1.upload_q(W.to_aos(q))
+    for _ in range(21):
+        s1.step()
+    s2 = L.Solver(p, B)
+    s2.upload_q(W.to_aos(q))
+    st = s2.advance(max_steps=21)
+    assert st.steps == 21
+    np.testing.assert_array_equal(s1.download_q(), s2.download_q())
+
+
+def test_other_tableaux_refuse_per_call_site_entry_points():
+    p, B, q, _ = _tableau_case("dam_break", 3)
+    s = L.Solver(p, B)
+    s.upload_q(W.to_aos(q))
+    with pytest.raises(Exception):
+        s.timestep()
+    assert s.step() == 0

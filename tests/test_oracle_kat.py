@@ -175,3 +175,33 @@ def test_dam_break_mass_is_conserved():
     m0 = o.stats().mass
     o.run(max_steps=40)
     assert abs(o.stats().mass - m0) / m0 < 1e-13
+
+
+def test_single_stage_tableau_keeps_the_state():
+    """N_RK = 1 (solver_2d.f90:419-427): a_tilde_ij(1,1) = omega_tilde(1) = 1
+    and a_dirk_ij(1,1) = omega(1) = 0, so the last tableau row equals the
+    weights and assemble_sol takes q = q_rk(1) = q0 (solver_2d.f90:1369-1372):
+    the clock advances, the state does not."""
+    p, B, q = W.dam_break(nx=40, ny=24, t_end=100.0, n_rk=1)
+    o = oracle.Oracle(p, B)
+    o.set_q(W.to_aos(q))
+    for _ in range(5):
+        assert o.step() == 0
+    assert o.t > 0.0
+    np.testing.assert_array_equal(o.q(), W.to_aos(q))
+
+
+@pytest.mark.parametrize("n_rk", [3, 4])
+def test_multi_stage_tableaux_stoker_and_mass(n_rk):
+    s = GOLD["stoker"]
+    p, B, q = _dambreak_1d(n_rk)
+    o = oracle.Oracle(p, B)
+    o.set_q(W.to_aos(q))
+    m0 = o.stats().mass
+    o.run(t_stop=s["t"])
+    assert o.stats().status == 0
+    assert abs(o.stats().mass - m0) <= 1e-12 * m0
+    qp = W.from_aos(o.qp(), p.n_vars + 2, p.comp_cells_x, p.comp_cells_y)
+    h = qp[0][4]
+    ref = np.array(s["h"])
+    assert np.abs(h - ref).sum() / np.abs(ref).sum() < 0.03
