@@ -246,6 +246,109 @@ def timed_form(lib, p, B, q, steps, warmup, flush=True):
                "newton_max": c1["newton_max"]}
 
 
+def ensemble_leg(lib, n_runs, steps):
+    """Batched ensemble: n_runs independent ring-inlet runs (side log-uniform
+    in [128, 1024], dx U[5, 20] m, own DEM seed, mu, xi, source radius and
+    temperature, particle fractions; workloads.ensemble_params) resident
+    together and advanced `steps` steps each by the batched engine (FP32
+    bulk form, FP64 Newton).  Inputs are uploaded before the timed region;
+    the timed region is the batch advance until every run has stopped."""
+    members = [W.ensemble_params(i, PREC_FP32, steps) for i in range(n_runs)]
+    cells = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members)
+    b = lib.Batch(PREC_FP32, max_runs=n_runs, max_cells=int(cells * 1.2) + 4096)
+    ids = []
+    for p, B, q, st in members:
+        rid = b.submit(p, B, W.to_aos(q), max_steps=st)
+        if rid is None:
+            raise RuntimeError("ensemble member not admitted")
+        ids.append(rid)
+    l0 = b.launch_count()
+    t0 = time.perf_counter()
+    while True:
+        fin = b.advance(64)
+        if fin == len(ids):
+            break
+    dt = time.perf_counter() - t0
+    launches = b.launch_count() - l0
+    cu = sum(b.counters(i)["cell_updates"] for i in ids)
+    dense = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members) * steps
+    b.close()
+    return {"runs": n_runs, "steps_per_run": steps, "cells_total": cells,
+            "cell_updates": cu, "dense_cell_steps": dense, "seconds": dt,
+            "value": cu / dt, "unit": UNIT, "gpu_launches": launches,
+            "timing": "host clock around the batch advance calls (each ends synchronised)"}
+
+
+def form_errors(lib, p, B, q, steps):
+    """L1 and Linf relative errors of h, hu, hv, alpha_s and T of the FP32
+    bulk form against the plain FP64 form after `steps` steps from the same
+    state (the FP64 form matches the CPU oracle to 1e-10 in the parity
+    tests, so it stands in for the oracle at sizes the oracle cannot run in
+    seconds)."""
+    nx, ny, nv = p.comp_cells_x, p.comp_cells_y, p.n_vars
+    out = {}
+    res = {}
+    for prec in (PREC_FP32, PREC_FP64):
+        pp = p.copy()
+        pp.precision = prec
+        s = lib.Solver(pp, B)
+        s.upload_q(W.to_aos(q))
+        s.advance(max_steps=steps)
+        res[prec] = (W.from_aos(s.download_q(), nv, nx, ny), W.from_aos(s.download_qp(), nv + 2, nx, ny))
+        s.close()
+    (q32, qp32), (q64, qp64) = res[PREC_FP32], res[PREC_FP64]
+    fields = {"h": (qp32[0], qp64[0]), "hu": (q32[1], q64[1]), "hv": (q32[2], q64[2]),
+              "T": (qp32[3], qp64[3])}
+    for i in range(p.n_solid):
+        fields[f"alpha_s{i + 1}"] = (qp32[4 + i], qp64[4 + i])
+    for n, (a, r) in fields.items():
+        if n == "T":   # temperature of wet cells only (dry cells carry T_ambient)
+            wet = qp64[0] > 0
+            a, r = a[wet], r[wet]
+        out[n] = {"l1_rel": float(np.abs(a - r).sum() / max(np.abs(r).sum(), 1e-300)),
+                  "linf_rel": float(np.abs(a - r).max() / max(np.abs(r).max(), 1e-300)) if r.size else 0.0}
+    return out
+
+
+def served_leg(lib, n_requests, rate):
+    """Served solves: Poisson arrivals (mean `rate` per s) of dam-break and
+    ring-inlet jobs (side log-uniform in [64, 2048], 1-3 classes, 500-5000
+    steps; workloads.served_job) through the request loop (continuous
+    batching).  Job inputs are prepared before the clock starts; time to
+    solution = finish - arrival."""
+    from imex_sflow2d_dev_gb300 import serve as S
+    jobs = [W.served_job(i, PREC_FP32) for i in range(n_requests)]
+    arr = W.poisson_arrivals(n_requests, rate)
+    reqs = [S.Request(i, arr[i], p, B, q, st, kind) for i, (p, B, q, st, kind) in enumerate(jobs)]
+    cells = sum(p.comp_cells_x * p.comp_cells_y for p, *_ in jobs)
+    loop = S.RequestLoop(PREC_FP32, max_runs=64, max_cells=int(cells * 1.2) + 4096, chunk=16)
+    recs = loop.run(reqs)
+    launches = loop.batch.launch_count()
+    loop.close()
+    out = S.summarize(recs)
+    out.update({"rate_per_s": rate, "gpu_launches": launches,
+                "jobs": [{k: r[k] for k in ("kind", "cells", "n_solid", "steps", "tts_s")} for r in recs]})
+    return out, recs
+
+
+def fp64_one_at_a_time(recs, fp64_rate):
+    """Time to solution of the same request stream served one job at a time
+    by the plain FP64 form, modelled from the measured FP64 cell-update rate
+    (each job's service time = its cell updates / rate; first come, first
+    served)."""
+    order = sorted(recs, key=lambda r: r["arrival_s"])
+    t = 0.0
+    tts = []
+    for r in order:
+        t = max(t, r["arrival_s"]) + r["cell_updates"] / fp64_rate
+        tts.append(t - r["arrival_s"])
+    tts = np.array(tts)
+    total = sum(r["cell_updates"] for r in order)
+    return {"p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
+            "cell_updates_per_s": total / (t - order[0]["arrival_s"]),
+            "basis": "modelled from the measured plain-FP64 cell-update rate of the main workload"}
+
+
 def run_gb300(args, d):
     from imex_sflow2d_dev_gb300 import lib
     lib.load()
@@ -270,19 +373,8 @@ def run_gb300(args, d):
     s64, r64 = timed_form(lib, p64, B, q, max(args.steps // 5, 3), args.warmup)
     value64 = r64["cells"] / (r64["ms"] / 1e3)
     # FP32 vs FP64 after the same number of steps from the same state
-    a32 = lib.Solver(p32, B)
-    a32.upload_q(W.to_aos(q))
-    a64 = lib.Solver(p64, B)
-    a64.upload_q(W.to_aos(q))
     nerr = 20
-    a32.advance(max_steps=nerr)
-    a64.advance(max_steps=nerr)
-    h32 = W.from_aos(a32.download_qp(), nv + 2, nx, ny)[0]
-    h64 = W.from_aos(a64.download_qp(), nv + 2, nx, ny)[0]
-    err_h = l1_rel(h32, h64)
-    t32, t64 = a32.stats().t, a64.stats().t
-    a32.close()
-    a64.close()
+    errs = form_errors(lib, p32, B, q, nerr)
 
     # per-kernel device time (events between the kernels of each step)
     pk = lib.Solver(p32, B)
@@ -344,6 +436,18 @@ def run_gb300(args, d):
     if d.rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(p64, B, q, max_seconds=args.cpu_seconds, max_steps=40)
 
+    ens = None
+    if d.rank == 0 and args.ensemble_runs > 0:
+        ens = ensemble_leg(lib, args.ensemble_runs, args.ensemble_steps)
+        ens["speedup_vs_fp64_plain"] = ens["value"] / value64 if value64 else None
+        pe, Be, qe, _ = W.ensemble_params(0, PREC_FP32, 300)
+        ens["error_vs_fp64"] = {"member": 0, "side": pe.comp_cells_x, "steps": 300,
+                                **form_errors(lib, pe, Be, qe, 300)}
+    srv = None
+    if d.rank == 0 and args.served_requests > 0:
+        srv, recs = served_leg(lib, args.served_requests, args.served_rate)
+        srv["fp64_one_at_a_time"] = fp64_one_at_a_time(recs, value64)
+
     if d.rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
@@ -361,7 +465,7 @@ def run_gb300(args, d):
                            "steps": r64["steps"], "newton_iters_per_cell":
                            r64["newton_iters"] / max(r64["cells"], 1)},
             "speedup_fp32_over_fp64": value / value64 if value64 else None,
-            "error_vs_fp64": {"l1_rel_h": err_h, "steps": nerr, "t_fp32": t32, "t_fp64": t64},
+            "error_vs_fp64": {"l1_rel_h": errs["h"]["l1_rel"], "steps": nerr, **errs},
             "newton_iters_per_cell": r32["newton_iters"] / max(r32["cells"], 1),
             "roofline": {"bound": "hbm", "kernel": "k_flux" if dom == "flux" else "k_stage2",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -372,6 +476,8 @@ def run_gb300(args, d):
                              if cb else None),
             "e2e": e2e,
             "gpu_launches": r32["launches"],
+            "ensemble": ens,
+            "served": srv,
             "clocks": clk,
             "wall_s_timed_region": t_wall1 - t_wall0,
         }
@@ -389,6 +495,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ensemble-runs", type=int, default=256)
+    ap.add_argument("--ensemble-steps", type=int, default=2000)
+    ap.add_argument("--served-requests", type=int, default=24)
+    ap.add_argument("--served-rate", type=float, default=20.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

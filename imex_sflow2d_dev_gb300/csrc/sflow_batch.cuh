@@ -1,0 +1,367 @@
+// sflow_batch.cuh -- host side of the batched engine: many independent runs
+// (uneven grid sizes and parameters) resident on one GPU and advanced
+// together by the persistent kernels of sflow_batch_kernels.cuh.
+//
+// Runs are grouped by solid-class count (a template parameter of the heavy
+// kernels); each group has its own stream, tile lists and CUDA graph of
+// kChunk batch steps.  The graph's kernel arguments point at device tables
+// (run arguments, run slots, lists, counters), so the same graph serves any
+// membership: runs are admitted and collected between graph launches
+// without re-capturing.  Admission checks a free slot, the tile-list
+// capacity and the free device memory (cudaMemGetInfo) against the run's
+// footprint.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "sflow_batch_kernels.cuh"
+#include "sflow_solver.cuh"
+
+namespace sflow {
+
+template <class R>
+class Batch : public BatchBase {
+ public:
+  static constexpr int kChunk = 16;
+
+  Batch(int max_runs, int64_t max_tiles) : max_runs_(max_runs), max_tiles_(max_tiles) {}
+  ~Batch() override {
+    for (auto& g : groups_)
+      if (g) g->release();
+  }
+  std::string err_;
+
+  int submit(const HostSetup& hs, const double* q_aos, int64_t max_steps, int* id) override {
+    if (hs.nrk != 2) { err_ = "batched runs use the N_RK = 2 tableau"; return SFLOW_EINVAL; }
+    if (hs.ns < kMinSolidBuilt || hs.ns > kMaxSolidBuilt) { err_ = "n_solid out of range"; return SFLOW_EINVAL; }
+    Group* g = group(hs.ns);
+    if (!g) return SFLOW_ECUDA;
+    int slot = -1;
+    for (int i = 0; i < max_runs_; ++i)
+      if (!g->slots[i].solver) { slot = i; break; }
+    if (slot < 0) { err_ = "no free run slot"; return SFLOW_EBUSY; }
+    const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + TY - 1) / TY);
+    if (g->tiles_live + g->tiles_draining + tiles > max_tiles_) {
+      err_ = "tile-list capacity of the batch is in use";
+      return SFLOW_EBUSY;
+    }
+    const int64_t need = Solver<R>::batch_bytes(hs) +
+                         (int64_t)sizeof(double) * hs.nx * hs.ny * (hs.nv + 2);   // staging, freed after upload
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
+    if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
+
+    std::unique_ptr<Solver<R>> sv(new Solver<R>(hs));
+    int rc = sv->init();
+    if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
+    rc = sv->upload(q_aos);
+    if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
+    rc = sv->limits(hs.p.t_end, max_steps > 0 ? max_steps : -1);
+    if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
+    sv->trim_stage();
+    uint32_t* cand = nullptr;
+    if (cudaMalloc((void**)&cand, sizeof(uint32_t) * tiles) != cudaSuccess) { err_ = "cudaMalloc failed"; return SFLOW_ENOMEM; }
+    if (cudaMemset(cand, 0, sizeof(uint32_t) * tiles) != cudaSuccess) {
+      cudaFree(cand);
+      err_ = "cudaMemset failed";
+      return SFLOW_ECUDA;
+    }
+    Slot& s = g->slots[slot];
+    s.gen = (s.gen + 1u) & 0xffffu;
+    s.cand = cand;
+    s.tiles = tiles;
+    BatchRun br;
+    br.st = sv->state_dev();
+    br.cand = cand;
+    br.tiles_x = sv->tiles_x();
+    br.tiles_y = sv->tiles_y();
+    br.gen = s.gen;
+    br.live = 1;
+    br.max_dt = hs.p.max_dt;
+    const KArgs<R> ka = sv->kargs();
+    if (g->smem_flux < sv->smem_flux()) { err_ = "flux shared memory mismatch"; cudaFree(cand); return SFLOW_EINVAL; }
+    // the batch stream is idle here (every advance ends synchronised)
+    if (cudaMemcpy(g->d_args + slot, &ka, sizeof(ka), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->d_runs + slot, &br, sizeof(br), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaFree(cand);
+      err_ = "cudaMemcpy failed";
+      return SFLOW_ECUDA;
+    }
+    cudaError_t e = g->tab.b_admit(g->args, g->stream, slot, s.gen, (unsigned)tiles);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+    ++g->launches;
+    s.solver = std::move(sv);
+    s.done = false;
+    g->tiles_live += tiles;
+    g->live += 1;
+    const int rid = (int)recs_.size();
+    recs_.push_back(Rec{hs.ns, slot, true});
+    s.rec = rid;
+    *id = rid;
+    return SFLOW_OK;
+  }
+
+  int advance(int64_t steps, int* finished) override {
+    int nfin = 0;
+    for (auto& gp : groups_) {
+      Group* g = gp.get();
+      if (!g || g->live == 0) continue;
+      int64_t left = steps;
+      while (left >= kChunk) {
+        if (!g->graph_exec) {
+          cudaError_t e = g->capture();
+          if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+        }
+        cudaError_t e = cudaGraphLaunch(g->graph_exec, g->stream);
+        if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+        g->launches += 5 * kChunk;
+        left -= kChunk;
+      }
+      for (; left > 0; --left) {
+        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux);
+        if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+        g->launches += 5;
+      }
+    }
+    // groups run concurrently on their streams; wait for all, then read the
+    // per-slot summaries
+    for (auto& gp : groups_) {
+      Group* g = gp.get();
+      if (!g || g->live == 0) continue;
+      cudaError_t e = g->tab.b_summary(g->args, g->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g->h_summary, g->d_summary, sizeof(BatchSummary) * max_runs_,
+                            cudaMemcpyDeviceToHost, g->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+      if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+      ++g->launches;
+      g->tiles_draining = 0;   // entries of collected runs left the lists
+      for (int i = 0; i < max_runs_; ++i) {
+        Slot& s = g->slots[i];
+        if (!s.solver) continue;
+        if (!g->h_summary[i].running) s.done = true;
+        if (s.done) ++nfin;
+      }
+    }
+    if (finished) *finished = nfin;
+    return SFLOW_OK;
+  }
+
+  int poll(int id, SflowStepStats* st, int* done) override {
+    Slot* s = lookup(id);
+    if (!s) return SFLOW_EINVAL;
+    if (st) {
+      int rc = s->solver->stats(st);
+      if (rc != SFLOW_OK) { err_ = s->solver->error(); return rc; }
+    }
+    if (done) *done = s->done ? 1 : 0;
+    return SFLOW_OK;
+  }
+
+  int counters(int id, int64_t* cells, int64_t* steps) override {
+    Slot* s = lookup(id);
+    if (!s) return SFLOW_EINVAL;
+    SflowStepStats st;
+    int rc = s->solver->stats(&st);
+    if (rc != SFLOW_OK) { err_ = s->solver->error(); return rc; }
+    if (cells) *cells = s->solver->cells_total();
+    if (steps) *steps = st.steps;
+    return SFLOW_OK;
+  }
+
+  int collect(int id, double* q_aos) override {
+    Slot* s = lookup(id);
+    if (!s) return SFLOW_EINVAL;
+    Group* g = group(recs_[id].ns);
+    if (q_aos) {
+      int rc = s->solver->download(q_aos);
+      if (rc != SFLOW_OK) { err_ = s->solver->error(); return rc; }
+    }
+    BatchRun br;
+    std::memset(&br, 0, sizeof(br));
+    br.live = 0;
+    br.gen = s->gen;
+    if (cudaMemcpy(g->d_runs + recs_[id].slot, &br, sizeof(br), cudaMemcpyHostToDevice) != cudaSuccess) {
+      err_ = "cudaMemcpy failed";
+      return SFLOW_ECUDA;
+    }
+    s->solver.reset();
+    cudaFree(s->cand);
+    s->cand = nullptr;
+    g->tiles_live -= s->tiles;
+    g->tiles_draining += s->tiles;
+    g->live -= 1;
+    s->done = false;
+    recs_[id].alive = false;
+    if (g->live == 0) {
+      // no run left: start the group's lists afresh (drops stale entries)
+      if (cudaMemset(g->d_ctl, 0, sizeof(BatchCtl)) != cudaSuccess) {
+        err_ = "cudaMemset failed";
+        return SFLOW_ECUDA;
+      }
+      g->tiles_draining = 0;
+    }
+    return SFLOW_OK;
+  }
+
+  int download(int id, double* q_aos) override {
+    Slot* s = lookup(id);
+    if (!s) return SFLOW_EINVAL;
+    int rc = s->solver->download(q_aos);
+    if (rc != SFLOW_OK) { err_ = s->solver->error(); return rc; }
+    s->solver->trim_stage();
+    return SFLOW_OK;
+  }
+
+  int live() const override {
+    int n = 0;
+    for (auto& g : groups_)
+      if (g) n += g->live;
+    return n;
+  }
+  int64_t launches() const override {
+    int64_t n = 0;
+    for (auto& g : groups_)
+      if (g) n += g->launches;
+    return n;
+  }
+  const char* error() const override { return err_.c_str(); }
+
+ private:
+  static constexpr int64_t kReserve = (int64_t)1 << 30;   // device memory kept free
+
+  struct Slot {
+    std::unique_ptr<Solver<R>> solver;
+    uint32_t* cand = nullptr;
+    int64_t tiles = 0;
+    unsigned gen = 0;
+    bool done = false;
+    int rec = -1;
+  };
+  struct Rec {
+    int ns, slot;
+    bool alive;
+  };
+  struct Group {
+    KernelTable<R> tab;
+    cudaStream_t stream = nullptr;
+    KArgs<R>* d_args = nullptr;
+    BatchRun* d_runs = nullptr;
+    BatchCtl* d_ctl = nullptr;
+    unsigned long long *d_list0 = nullptr, *d_list1 = nullptr, *d_cand = nullptr;
+    BatchSummary* d_summary = nullptr;
+    BatchSummary* h_summary = nullptr;
+    BatchArgs<R> args;
+    int grids[4] = {0, 0, 0, 0};
+    size_t smem_flux = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<Slot> slots;
+    int64_t tiles_live = 0, tiles_draining = 0, launches = 0;
+    int live = 0;
+
+    cudaError_t capture() {
+      cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return e;
+      for (int i = 0; i < kChunk; ++i) {
+        e = tab.b_step(args, stream, grids, smem_flux);
+        if (e != cudaSuccess) {
+          cudaGraph_t g0 = nullptr;
+          cudaStreamEndCapture(stream, &g0);
+          if (g0) cudaGraphDestroy(g0);
+          return e;
+        }
+      }
+      e = cudaStreamEndCapture(stream, &graph);
+      if (e != cudaSuccess) return e;
+      return cudaGraphInstantiate(&graph_exec, graph, 0);
+    }
+    void release() {
+      if (stream) cudaStreamSynchronize(stream);
+      for (auto& s : slots) {
+        s.solver.reset();
+        if (s.cand) cudaFree(s.cand);
+        s.cand = nullptr;
+      }
+      if (graph_exec) cudaGraphExecDestroy(graph_exec);
+      if (graph) cudaGraphDestroy(graph);
+      void* bufs[7] = {d_args, d_runs, d_ctl, d_list0, d_list1, d_cand, d_summary};
+      for (void* p : bufs)
+        if (p) cudaFree(p);
+      if (h_summary) cudaFreeHost(h_summary);
+      if (stream) cudaStreamDestroy(stream);
+      stream = nullptr;
+    }
+  };
+
+  Slot* lookup(int id) {
+    if (id < 0 || id >= (int)recs_.size() || !recs_[id].alive) {
+      err_ = "unknown or collected run id";
+      return nullptr;
+    }
+    Group* g = groups_[recs_[id].ns].get();
+    return &g->slots[recs_[id].slot];
+  }
+
+  Group* group(int ns) {
+    if (groups_[ns]) return groups_[ns].get();
+    std::unique_ptr<Group> g(new Group());
+    g->tab = kernel_table<R>(ns);
+    if (!g->tab.b_step) { err_ = "no batch kernels for this class count"; return nullptr; }
+    g->slots.resize(max_runs_);
+    // shared memory of the flux kernel for this class count (the largest
+    // any run of the group needs: it depends on n_vars only)
+    const int nv = 4 + ns, np = nv + 2;
+    g->smem_flux = sizeof(R) * ((size_t)np * RX * RY + (size_t)nv * TY * (TX + 1) + (size_t)nv * (TY + 1) * TX +
+                                (size_t)TY * (TX + 1) + (size_t)(TY + 1) * TX) +
+                   (size_t)RX * RY;
+    g->smem_flux = (g->smem_flux + 15) / 16 * 16;
+    auto fail = [&](cudaError_t e) -> Group* {
+      err_ = cudaGetErrorString(e);
+      g->release();
+      return nullptr;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(e);
+    if ((e = g->tab.b_setup(g->smem_flux, g->grids)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_args, sizeof(KArgs<R>) * max_runs_)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_runs, sizeof(BatchRun) * max_runs_)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemset(g->d_runs, 0, sizeof(BatchRun) * max_runs_)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_ctl, sizeof(BatchCtl))) != cudaSuccess) return fail(e);
+    if ((e = cudaMemset(g->d_ctl, 0, sizeof(BatchCtl))) != cudaSuccess) return fail(e);
+    const size_t lb = sizeof(unsigned long long) * (size_t)max_tiles_;
+    if ((e = cudaMalloc((void**)&g->d_list0, lb)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_list1, lb)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_cand, lb)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
+    if ((e = cudaMallocHost((void**)&g->h_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
+    g->args.args = g->d_args;
+    g->args.runs = g->d_runs;
+    g->args.ctl = g->d_ctl;
+    g->args.list0 = g->d_list0;
+    g->args.list1 = g->d_list1;
+    g->args.cand = g->d_cand;
+    g->args.summary = g->d_summary;
+    g->args.max_runs = max_runs_;
+    groups_[ns] = std::move(g);
+    return groups_[ns].get();
+  }
+
+  int max_runs_;
+  int64_t max_tiles_;
+  std::unique_ptr<Group> groups_[kMaxSolidBuilt + 1];
+  std::vector<Rec> recs_;
+};
+
+template <class R>
+BatchBase* make_batch_impl(int max_runs, int64_t max_tiles, std::string& err) {
+  if (max_runs < 1 || max_runs > 65535) { err = "max_runs must be 1..65535"; return nullptr; }
+  if (max_tiles < 1 || max_tiles > ((int64_t)1 << 31)) { err = "max_cells out of range"; return nullptr; }
+  return new Batch<R>(max_runs, max_tiles);
+}
+
+}  // namespace sflow

@@ -1,0 +1,287 @@
+// sflow_batch_kernels.cuh -- many independent runs advanced together.
+//
+// Every run keeps its own state, geometry, RunState and kernel arguments
+// (KArgs) in device memory.  One batch step is five launches for all runs
+// of a solid-class count together:
+//
+//   k_b_cand    from the active tiles of the previous step (list L[pp]):
+//               every tile within one tile of an active tile becomes a
+//               candidate (deduplicated by a per-tile flag) -> list C;
+//               also the per-run start-of-step work of k_mask (ring inlet
+//               time factor)
+//   k_b_mask    check_solve on the candidate tiles; tiles with an active
+//               cell -> list L[pp^1]
+//   k_b_flux    k_flux on L[pp^1] (persistent blocks, dynamic tile fetch)
+//   k_b_dt      k_dt of every live run (one thread per run); pp ^= 1
+//   k_b_stage2  k_stage2 on L[pp]
+//
+// Why candidates suffice: a cell outside the active set is not updated, so
+// a wet cell (a check_solve seed) was active in the previous step; active
+// cells lie within n_RK <= 4 cells of a seed, and tiles are 32 x 8 cells, so
+// they lie in the 3 x 3 tile neighbourhood of a previously active tile.
+// Border and ring cells are seeds of every step, so their tiles stay in the
+// lists.  A newly admitted run puts all its tiles in L[pp] (full scan for
+// its first step).  Tiles outside the candidate set keep an all-zero mask
+// (they were processed when they last stopped being active), so the flux
+// halo reads them as inactive, as the single-run kernels do.
+//
+// List entries are 64-bit: slot (16 bits) | generation (16 bits) | tile (32
+// bits).  k_b_cand drops entries whose slot is free or holds a newer run,
+// so a slot can be reused at once after its run is collected.
+//
+// The per-cell arithmetic is the single-run code (mask_tile, flux_tile,
+// stage2_tile) on the run's own arguments, so a run gives bit-identical
+// results alone, with the single-run solver, and in any mix.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sflow_kernels.cuh"
+
+namespace sflow {
+
+struct BatchRun {
+  RunState* st;      // the run's device state
+  uint32_t* cand;    // per-tile candidate flag
+  int tiles_x, tiles_y;
+  unsigned gen;      // generation of the run in this slot
+  int live;          // slot holds a run
+  double max_dt;
+};
+
+struct BatchCtl {
+  unsigned count[2];   // entries in tile list 0 / 1
+  unsigned ncand;      // entries in the candidate list
+  unsigned pp;         // list read by k_b_cand
+  unsigned work[3];    // dynamic tile counters of k_b_mask, k_b_flux, k_b_stage2
+  unsigned steps;      // batch steps done
+};
+
+// per-slot summary copied to the host after a batch advance
+struct BatchSummary {
+  long long steps;
+  long long cells_total;
+  double t;
+  unsigned status;
+  int running;
+};
+
+template <class R>
+struct BatchArgs {
+  const KArgs<R>* args;      // [max_runs]
+  BatchRun* runs;            // [max_runs]
+  BatchCtl* ctl;
+  unsigned long long* list0;
+  unsigned long long* list1;
+  unsigned long long* cand;
+  BatchSummary* summary;     // [max_runs]
+  int max_runs;
+};
+
+constexpr int kBatchCandThreads = 256;
+
+__device__ __forceinline__ int entry_slot(unsigned long long e) { return (int)(e >> 48); }
+__device__ __forceinline__ unsigned entry_gen(unsigned long long e) { return (unsigned)(e >> 32) & 0xffffu; }
+__device__ __forceinline__ unsigned entry_tile(unsigned long long e) { return (unsigned)(e & 0xffffffffull); }
+
+// copy one run's kernel arguments into shared memory (all threads)
+template <class R>
+__device__ __forceinline__ void load_args(KArgs<R>* dst, const KArgs<R>* src) {
+  static_assert(sizeof(KArgs<R>) % 8 == 0, "KArgs size");
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(KArgs<R>) / 8); i += blockDim.x) d[i] = s[i];
+}
+
+// next list index for this block (one atomic per tile; block-uniform result)
+__device__ __forceinline__ unsigned next_tile(unsigned* counter, unsigned* s_idx) {
+  __syncthreads();
+  if (threadIdx.x == 0) *s_idx = atomicAdd(counter, 1u);
+  __syncthreads();
+  return *s_idx;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
+  BatchCtl* ctl = b.ctl;
+  const unsigned pp = ctl->pp;
+  const unsigned long long* L = pp ? b.list1 : b.list0;
+  const unsigned n = ctl->count[pp];
+  const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned G = gridDim.x * blockDim.x;
+  if (gt == 0) {
+    ctl->count[pp ^ 1u] = 0u;
+    ctl->work[0] = 0u;
+  }
+  for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
+    const BatchRun br = b.runs[r];
+    if (!br.live) continue;
+    RunState* st = br.st;
+    if (running(st)) {
+      st->src_t_coeff = source_time_coeff(st->tp, st->pi_g, st->t);
+      st->src_t_coeff_f = (float)st->src_t_coeff;
+    }
+  }
+  for (unsigned i = gt; i < n * 9u; i += G) {
+    const unsigned long long e = L[i / 9u];
+    const int slot = entry_slot(e);
+    const BatchRun& br = b.runs[slot];
+    if (!br.live || (br.gen & 0xffffu) != entry_gen(e) || !running(br.st)) continue;
+    const unsigned tile = entry_tile(e);
+    const int nb = (int)(i % 9u);
+    const int tx = (int)(tile % (unsigned)br.tiles_x) + nb % 3 - 1;
+    const int ty = (int)(tile / (unsigned)br.tiles_x) + nb / 3 - 1;
+    if (tx < 0 || ty < 0 || tx >= br.tiles_x || ty >= br.tiles_y) continue;
+    const unsigned t2 = (unsigned)(ty * br.tiles_x + tx);
+    if (atomicExch(&br.cand[t2], 1u) == 0u) {
+      const unsigned pos = atomicAdd(&ctl->ncand, 1u);
+      b.cand[pos] = (e & 0xffffffff00000000ull) | (unsigned long long)t2;
+    }
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(TX* TY) k_b_mask(BatchArgs<R> b) {
+  __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
+  __shared__ unsigned s_idx;
+  KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
+  BatchCtl* ctl = b.ctl;
+  const unsigned pp = ctl->pp;
+  unsigned long long* out = pp ? b.list0 : b.list1;
+  const unsigned n = ctl->ncand;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->work[1] = 0u;
+  int cur = -1;
+  for (;;) {
+    const unsigned i = next_tile(&ctl->work[0], &s_idx);
+    if (i >= n) break;
+    const unsigned long long e = b.cand[i];
+    const int slot = entry_slot(e);
+    const unsigned tile = entry_tile(e);
+    if (slot != cur) {
+      load_args(&a, &b.args[slot]);
+      cur = slot;
+      __syncthreads();
+    }
+    const BatchRun& br = b.runs[slot];
+    if (threadIdx.x == 0) br.cand[tile] = 0u;
+    if (!running(a.st)) continue;
+    const int tx = (int)(tile % (unsigned)br.tiles_x), ty = (int)(tile / (unsigned)br.tiles_x);
+    const int cnt = mask_tile(a, 0, tx, ty, br.tiles_x);
+    if (cnt > 0 && threadIdx.x == 0) {
+      const unsigned pos = atomicAdd(&ctl->count[pp ^ 1u], 1u);
+      out[pos] = e;
+    }
+  }
+}
+
+// 3 blocks per SM (27 warps): without the bound the persistent loop keeps
+// loop-invariant values of the tile body live and needs ~120 registers
+template <class R, int NS>
+__global__ void __launch_bounds__(FLUX_THREADS, 3) k_b_flux(BatchArgs<R> b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
+  __shared__ unsigned s_idx;
+  KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
+  BatchCtl* ctl = b.ctl;
+  const unsigned pp = ctl->pp;
+  const unsigned long long* L = pp ? b.list0 : b.list1;
+  const unsigned n = ctl->count[pp ^ 1u];
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->work[2] = 0u;
+  int cur = -1;
+  for (;;) {
+    const unsigned i = next_tile(&ctl->work[1], &s_idx);
+    if (i >= n) break;
+    const unsigned long long e = L[i];
+    const int slot = entry_slot(e);
+    const unsigned tile = entry_tile(e);
+    if (slot != cur) {
+      load_args(&a, &b.args[slot]);
+      cur = slot;
+      __syncthreads();
+    }
+    if (!running(a.st)) continue;
+    const int tiles_x = (a.g.nx + TX - 1) / TX;
+    flux_tile<R, NS>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
+                     smem_raw);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kBatchCandThreads) k_b_dt(BatchArgs<R> b) {
+  const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned G = gridDim.x * blockDim.x;
+  for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
+    const BatchRun& br = b.runs[r];
+    if (br.live) dt_update(br.st, br.max_dt);
+  }
+  if (gt == 0) {
+    BatchCtl* ctl = b.ctl;
+    ctl->pp ^= 1u;
+    ctl->ncand = 0u;
+    ctl->steps += 1u;
+  }
+}
+
+template <class R, int NS>
+__global__ void __launch_bounds__(TX* TY, 5) k_b_stage2(BatchArgs<R> b) {
+  __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
+  __shared__ unsigned s_idx;
+  KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
+  BatchCtl* ctl = b.ctl;
+  const unsigned pp = ctl->pp;
+  const unsigned long long* L = pp ? b.list1 : b.list0;
+  const unsigned n = ctl->count[pp];
+  int cur = -1;
+  for (;;) {
+    const unsigned i = next_tile(&ctl->work[2], &s_idx);
+    if (i >= n) break;
+    const unsigned long long e = L[i];
+    const int slot = entry_slot(e);
+    const unsigned tile = entry_tile(e);
+    if (slot != cur) {
+      load_args(&a, &b.args[slot]);
+      cur = slot;
+      __syncthreads();
+    }
+    if (!a.st->run_step) continue;
+    const int tiles_x = (a.g.nx + TX - 1) / TX;
+    stage2_tile<R, NS>(a, -1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x));
+  }
+}
+
+// all tiles of a newly admitted run into the list of the next k_b_cand
+template <class R>
+__global__ void __launch_bounds__(256) k_b_admit(BatchArgs<R> b, int slot, unsigned gen, unsigned ntiles) {
+  __shared__ unsigned base;
+  BatchCtl* ctl = b.ctl;
+  const unsigned pp = ctl->pp;
+  unsigned long long* L = pp ? b.list1 : b.list0;
+  if (threadIdx.x == 0) base = atomicAdd(&ctl->count[pp], ntiles);
+  __syncthreads();
+  const unsigned long long hi = ((unsigned long long)(unsigned)slot << 48) |
+                                ((unsigned long long)(gen & 0xffffu) << 32);
+  for (unsigned t = threadIdx.x; t < ntiles; t += blockDim.x) L[base + t] = hi | t;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_b_summary(BatchArgs<R> b) {
+  const unsigned r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (unsigned)b.max_runs) return;
+  const BatchRun& br = b.runs[r];
+  BatchSummary s;
+  s.steps = 0;
+  s.cells_total = 0;
+  s.t = 0.0;
+  s.status = 0u;
+  s.running = 0;
+  if (br.live) {
+    const RunState* st = br.st;
+    s.steps = st->steps;
+    s.cells_total = st->cells_total;
+    s.t = st->t;
+    s.status = st->status;
+    s.running = running(st) ? 1 : 0;
+  }
+  b.summary[r] = s;
+}
+
+}  // namespace sflow

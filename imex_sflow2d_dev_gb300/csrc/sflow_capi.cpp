@@ -7,8 +7,14 @@
 #include "../../include/sflow.h"
 #include "sflow_host.h"
 
+using sflow::BatchBase;
 using sflow::HostSetup;
 using sflow::SolverBase;
+
+struct sflow_batch {
+  BatchBase* impl = nullptr;
+  int precision = 0;
+};
 
 struct sflow_handle {
   SolverBase* solver = nullptr;
@@ -33,6 +39,102 @@ static std::string last_solver_error(const sflow_handle* h);
 extern "C" {
 
 const char* sflow_last_error(void) { return g_err.c_str(); }
+
+int sflow_batch_create(int32_t precision, int32_t max_runs, int64_t max_cells, sflow_batch** out) {
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (precision != SFLOW_PREC_FP32 && precision != SFLOW_PREC_FP64) return fail(SFLOW_EINVAL, "unknown precision");
+  if (max_cells < 1) return fail(SFLOW_EINVAL, "max_cells must be positive");
+  std::string err;
+  // tile lists hold one entry per 32 x 8 tile; small runs waste part of a
+  // tile, so the capacity allows for twice the cells
+  const int64_t max_tiles = 2 * ((max_cells + 255) / 256) + 1024;
+  BatchBase* b = (precision == SFLOW_PREC_FP32) ? sflow::make_batch_fp32(max_runs, max_tiles, err)
+                                                : sflow::make_batch_fp64(max_runs, max_tiles, err);
+  if (!b) return fail(SFLOW_EINVAL, err);
+  sflow_batch* h = new (std::nothrow) sflow_batch;
+  if (!h) {
+    delete b;
+    return fail(SFLOW_ENOMEM, "out of host memory");
+  }
+  h->impl = b;
+  h->precision = precision;
+  *out = h;
+  g_err.clear();
+  return SFLOW_OK;
+}
+
+void sflow_batch_destroy(sflow_batch* b) {
+  if (!b) return;
+  delete b->impl;
+  delete b;
+}
+
+#define BATCH_CHECK(b)                                                   \
+  do {                                                                   \
+    if (!(b) || !(b)->impl) return fail(SFLOW_EINVAL, "null batch");     \
+  } while (0)
+#define BATCH_FORWARD(b, expr)                                           \
+  do {                                                                   \
+    int rc_ = (expr);                                                    \
+    if (rc_ < 0) return fail(rc_, (b)->impl->error());                   \
+    return rc_;                                                          \
+  } while (0)
+
+int sflow_batch_submit(sflow_batch* b, const SflowParams* p, const double* B_cent, const double* q_aos,
+                       int64_t max_steps, int32_t* run_id) {
+  BATCH_CHECK(b);
+  if (!p || !q_aos || !run_id) return fail(SFLOW_EINVAL, "NULL argument");
+  if (p->precision != b->precision) return fail(SFLOW_EINVAL, "run precision differs from the batch precision");
+  HostSetup s;
+  std::string err;
+  int rc = sflow::host_setup(p, B_cent, s, err);
+  if (rc != SFLOW_OK) return fail(rc, err);
+  int id = -1;
+  rc = b->impl->submit(s, q_aos, max_steps, &id);
+  if (rc < 0) return fail(rc, b->impl->error());
+  *run_id = id;
+  return SFLOW_OK;
+}
+
+int sflow_batch_advance(sflow_batch* b, int64_t steps, int32_t* finished) {
+  BATCH_CHECK(b);
+  if (steps < 0) return fail(SFLOW_EINVAL, "steps must be >= 0");
+  int nf = 0;
+  int rc = b->impl->advance(steps, &nf);
+  if (rc < 0) return fail(rc, b->impl->error());
+  if (finished) *finished = nf;
+  return SFLOW_OK;
+}
+
+int sflow_batch_poll(sflow_batch* b, int32_t run_id, SflowStepStats* stats, int32_t* done) {
+  BATCH_CHECK(b);
+  int d = 0;
+  int rc = b->impl->poll(run_id, stats, &d);
+  if (rc < 0) return fail(rc, b->impl->error());
+  if (done) *done = d;
+  return SFLOW_OK;
+}
+
+int sflow_batch_counters(sflow_batch* b, int32_t run_id, int64_t* cell_updates, int64_t* steps) {
+  BATCH_CHECK(b);
+  BATCH_FORWARD(b, b->impl->counters(run_id, cell_updates, steps));
+}
+
+int sflow_batch_download(sflow_batch* b, int32_t run_id, double* q_aos) {
+  BATCH_CHECK(b);
+  if (!q_aos) return fail(SFLOW_EINVAL, "q is NULL");
+  BATCH_FORWARD(b, b->impl->download(run_id, q_aos));
+}
+
+int sflow_batch_collect(sflow_batch* b, int32_t run_id, double* q_aos) {
+  BATCH_CHECK(b);
+  BATCH_FORWARD(b, b->impl->collect(run_id, q_aos));
+}
+
+int32_t sflow_batch_live(const sflow_batch* b) { return (b && b->impl) ? b->impl->live() : 0; }
+
+int64_t sflow_batch_launch_count(const sflow_batch* b) { return (b && b->impl) ? b->impl->launches() : 0; }
 
 const char* sflow_build_info(void) {
   return "sflow GB300: FP64 plain form + FP32 bulk form, N_RK=2, KT fluxes, sm_103a";

@@ -71,4 +71,22 @@ class SolverBase {
 SolverBase* make_solver_fp64(const HostSetup& s, std::string& err);
 SolverBase* make_solver_fp32(const HostSetup& s, std::string& err);
 
+// Many independent runs advanced together (sflow_batch.cuh).
+class BatchBase {
+ public:
+  virtual ~BatchBase() {}
+  virtual int submit(const HostSetup& hs, const double* q_aos, int64_t max_steps, int* id) = 0;
+  virtual int advance(int64_t steps, int* finished) = 0;
+  virtual int poll(int id, SflowStepStats* s, int* done) = 0;
+  virtual int counters(int id, int64_t* cells, int64_t* steps) = 0;
+  virtual int download(int id, double* q_aos) = 0;
+  virtual int collect(int id, double* q_aos) = 0;
+  virtual int live() const = 0;
+  virtual int64_t launches() const = 0;
+  virtual const char* error() const = 0;
+};
+
+BatchBase* make_batch_fp64(int max_runs, int64_t max_tiles, std::string& err);
+BatchBase* make_batch_fp32(int max_runs, int64_t max_tiles, std::string& err);
+
 }  // namespace sflow

@@ -117,13 +117,11 @@ __device__ __forceinline__ Geo<R> load_geo(const KArgs<R>& a, int64_t c) {
 // ring-boundary cell) and is not a ring-interior cell.
 // ---------------------------------------------------------------------------
 template <class R>
-__global__ void __launch_bounds__(TX* TY) k_mask(KArgs<R> a, int solve_all) {
+__device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x) {
   RunState* st = a.st;
-  const double t = st->t;
-  if (!running(st)) return;
   const Grid<R>& g = a.g;
-  const int j = blockIdx.x * TX + threadIdx.x % TX;
-  const int k = blockIdx.y * TY + threadIdx.x / TX;
+  const int j = tx * TX + threadIdx.x % TX;
+  const int k = ty * TY + threadIdx.x / TX;
   const int nrk = a.pd.nrk;
   int act = 0;
   if (j < g.nx && k < g.ny) {
@@ -152,9 +150,18 @@ __global__ void __launch_bounds__(TX* TY) k_mask(KArgs<R> a, int solve_all) {
   }
   int cnt = __syncthreads_count(act);
   if (threadIdx.x == 0) {
-    a.tile_active[blockIdx.y * gridDim.x + blockIdx.x] = cnt > 0;
+    a.tile_active[ty * tiles_x + tx] = cnt > 0;
     if (cnt) atomicAdd((unsigned long long*)&st->cells_acc[st->steps & 1], (unsigned long long)cnt);
   }
+  return cnt;
+}
+
+template <class R>
+__global__ void __launch_bounds__(TX* TY) k_mask(KArgs<R> a, int solve_all) {
+  RunState* st = a.st;
+  const double t = st->t;
+  if (!running(st)) return;
+  mask_tile(a, solve_all, blockIdx.x, blockIdx.y, gridDim.x);
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
     st->src_t_coeff = source_time_coeff(st->tp, st->pi_g, t);
     st->src_t_coeff_f = (float)st->src_t_coeff;
@@ -487,26 +494,23 @@ __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const ui
 // sides, speeds, physical fluxes, KT flux) and finally one cell.
 // ---------------------------------------------------------------------------
 template <class R, int NS>
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
-                                                       R* __restrict__ rout, int want_dt) {
+__device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict__ qin,
+                                          R* __restrict__ rout, int want_dt, int tx, int ty,
+                                          unsigned char* smem_raw) {
   constexpr int nv = 4 + NS, np = nv + 2;
   const RunState* st = a.st;
-  // the timestep pass runs before k_dt advances the clock; the later stage
-  // fluxes of a step run after it and follow its run_step decision
-  if (want_dt ? !running(st) : !st->run_step) return;
-  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
   const Grid<R>& g = a.g;
   const Phys<R>& P = a.pr;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sqp = reinterpret_cast<R*>(smem_raw);                       // np * RX*RY
   R* sHx = sqp + np * RX * RY;                                   // nv * TY*(TX+1)
   R* sHy = sHx + nv * TY * (TX + 1);                             // nv * (TY+1)*TX
   R* sAx = sHy + nv * (TY + 1) * TX;                             // TY*(TX+1)
   R* sAy = sAx + TY * (TX + 1);                                  // (TY+1)*TX
   uint8_t* sfl = reinterpret_cast<uint8_t*>(sAy + (TY + 1) * TX);  // RX*RY
-  const int j0 = blockIdx.x * TX, k0 = blockIdx.y * TY;
+  const int j0 = tx * TX, k0 = ty * TY;
   const int tid = threadIdx.x;
 
+  __syncthreads();   // shared memory of the previous tile of a persistent block is free
   // 1. physical variables of the tile + halo (qc_to_qp; inactive = dry)
   for (int idx = tid; idx < RX * RY; idx += FLUX_THREADS) {
     const int rx = idx % RX, ry = idx / RX;
@@ -649,10 +653,22 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
   }
 }
 
+template <class R, int NS>
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
+                                                       R* __restrict__ rout, int want_dt) {
+  const RunState* st = a.st;
+  // the timestep pass runs before k_dt advances the clock; the later stage
+  // fluxes of a step run after it and follow its run_step decision
+  if (want_dt ? !running(st) : !st->run_step) return;
+  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  flux_tile<R, NS>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
+}
+
 // ---------------------------------------------------------------------------
 // k_dt: dt of this step (timestep + IMEX_SfloW2D.f90:417-439), one thread.
 // ---------------------------------------------------------------------------
-static __global__ void k_dt(RunState* st, double max_dt) {
+__device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   if (!running(st)) { st->run_step = 0; return; }
   double dtmin = __longlong_as_double((long long)st->dtmin_bits);
   double dt = max_dt;
@@ -675,6 +691,8 @@ static __global__ void k_dt(RunState* st, double max_dt) {
   st->steps += 1;
   st->dtmin_bits = dbits(1.0e300);
 }
+
+static __global__ void k_dt(RunState* st, double max_dt) { dt_update(st, max_dt); }
 
 // ---------------------------------------------------------------------------
 // Positivity fixes of assemble_sol (solver_2d.f90:1381-1628) on an FP64 or
@@ -941,14 +959,12 @@ __device__ __forceinline__ void newton_stats(RunState* st, unsigned status, int 
 // 2: maxima only.
 // ---------------------------------------------------------------------------
 template <class R, int NS>
-__global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
+__device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx, int ty) {
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
-  if (!st->run_step) return;
-  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
   const Grid<R>& g = a.g;
-  const int j = blockIdx.x * TX + threadIdx.x % TX;
-  const int k = blockIdx.y * TY + threadIdx.x / TX;
+  const int j = tx * TX + threadIdx.x % TX;
+  const int k = ty * TY + threadIdx.x / TX;
   unsigned status = 0;
   int nit = 0;
   if (j < g.nx && k < g.ny) {
@@ -986,6 +1002,13 @@ __global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
     }
   }
   newton_stats<R>(st, status, nit);
+}
+
+template <class R, int NS>
+__global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
+  if (!a.st->run_step) return;
+  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  stage2_tile<R, NS>(a, mode, blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------

@@ -131,7 +131,6 @@ class Solver : public SolverBase {
     SFLOW_CU(alloc((void**)&pdynmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&mvmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&st_, sizeof(RunState)));
-    SFLOW_CU(alloc((void**)&stage_aos_, sizeof(double) * (size_t)nx * ny * (nv + 2)));
     nstat_blocks_ = 1024;
     SFLOW_CU(alloc((void**)&stat_part_, sizeof(double) * 4 * nstat_blocks_));
     SFLOW_CU(alloc((void**)&stat_out_, sizeof(double) * 4));
@@ -146,10 +145,41 @@ class Solver : public SolverBase {
     return SFLOW_OK;
   }
 
+  // --- used by the batch engine ----------------------------------------------
+  const KArgs<R>& kargs() const { return ka_; }
+  RunState* state_dev() const { return st_; }
+  int tiles_x() const { return tiles_x_; }
+  int tiles_y() const { return tiles_y_; }
+  size_t smem_flux() const { return smem_flux_; }
+  cudaStream_t stream() const { return stream_; }
+  const HostSetup& setup() const { return hs_; }
+  int limits(double t_stop, int64_t step_limit) {
+    SFLOW_CU(set_limits(t_stop, step_limit));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+  // frees the host-layout staging buffer (allocated again when needed)
+  void trim_stage() {
+    if (!stage_aos_) return;
+    cudaStreamSynchronize(stream_);
+    cudaFree(stage_aos_);
+    bytes_ -= (int64_t)(sizeof(double) * (size_t)hs_.nx * hs_.ny * (hs_.nv + 2));
+    stage_aos_ = nullptr;
+  }
+  // device bytes a run of this set-up holds while it is in a batch
+  static int64_t batch_bytes(const HostSetup& hs) {
+    const int64_t pitch = (hs.nx + 31) / 32 * 32, plane = pitch * hs.ny;
+    const int ngeo = hs.p.curvature_term_flag ? 8 : 5;
+    const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + TY - 1) / TY);
+    return plane * (int64_t)sizeof(R) * (2 * hs.nv + ngeo + 3 + 3) + 2 * plane + tiles * 5 +
+           (int64_t)sizeof(double) * 4 * 1024 + 4096;
+  }
+
   // --- SolverBase -----------------------------------------------------------
   int upload(const double* q_aos) override {
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     const size_t N = (size_t)nx * ny;
+    SFLOW_CU(ensure_stage());
     SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
     k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
     ++launches_;
@@ -166,6 +196,7 @@ class Solver : public SolverBase {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     const size_t N = (size_t)nx * ny;
+    SFLOW_CU(ensure_stage());
     SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
     k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
     ++launches_;
@@ -241,6 +272,7 @@ class Solver : public SolverBase {
   int download(double* q_aos) override {
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     const size_t N = (size_t)nx * ny;
+    SFLOW_CU(ensure_stage());
     k_planes_to_aos<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(q_, stage_aos_, nv, nx, ny, pitch_, plane_);
     ++launches_;
     SFLOW_CU(cudaGetLastError());
@@ -251,6 +283,7 @@ class Solver : public SolverBase {
 
   int download_qp(double* qp_aos) override {
     const size_t N = (size_t)hs_.nx * hs_.ny;
+    SFLOW_CU(ensure_stage());
     SFLOW_CU(dispatch_qp((unsigned)((N + 255) / 256)));
     SFLOW_CU(cudaMemcpyAsync(qp_aos, stage_aos_, sizeof(double) * N * (hs_.nv + 2), cudaMemcpyDeviceToHost, stream_));
     SFLOW_CU(cudaStreamSynchronize(stream_));
@@ -260,6 +293,7 @@ class Solver : public SolverBase {
   int download_maps(double* h, double* p, double* v) override {
     const int nx = hs_.nx, ny = hs_.ny;
     const size_t N = (size_t)nx * ny;
+    SFLOW_CU(ensure_stage());
     R* src[3] = {hmax_, pdynmax_, mvmax_};
     double* dst[3] = {h, p, v};
     for (int m = 0; m < 3; ++m) {
@@ -511,7 +545,18 @@ class Solver : public SolverBase {
     if (flush_buf_) cudaFree(flush_buf_);
     for (void* p : allocs_) cudaFree(p);
     allocs_.clear();
+    if (stage_aos_) cudaFree(stage_aos_);
+    stage_aos_ = nullptr;
     if (stream_) cudaStreamDestroy(stream_);
+  }
+
+  // host-layout staging buffer, allocated on first use
+  cudaError_t ensure_stage() {
+    if (stage_aos_) return cudaSuccess;
+    const size_t bytes = sizeof(double) * (size_t)hs_.nx * hs_.ny * (hs_.nv + 2);
+    cudaError_t e = cudaMalloc((void**)&stage_aos_, bytes);
+    if (e == cudaSuccess) bytes_ += (int64_t)bytes;
+    return e;
   }
 
   cudaError_t put_plane(R* dst, const std::vector<double>& src) {

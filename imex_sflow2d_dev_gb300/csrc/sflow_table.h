@@ -11,6 +11,8 @@ namespace sflow {
 
 template <class R>
 struct KArgs;
+template <class R>
+struct BatchArgs;
 
 template <class R>
 struct KernelTable {
@@ -22,6 +24,12 @@ struct KernelTable {
   cudaError_t (*qp)(const KArgs<R>&, unsigned, cudaStream_t, double*) = nullptr;
   cudaError_t (*stats)(const KArgs<R>&, int, cudaStream_t, double*) = nullptr;
   cudaError_t (*set_smem)(size_t) = nullptr;
+  // batched runs (sflow_batch_kernels.cuh): grids[4] = persistent grid sizes
+  // of k_b_cand / k_b_mask / k_b_flux / k_b_stage2 for this device
+  cudaError_t (*b_setup)(size_t smem_flux, int* grids) = nullptr;
+  cudaError_t (*b_step)(const BatchArgs<R>&, cudaStream_t, const int* grids, size_t smem_flux) = nullptr;
+  cudaError_t (*b_admit)(const BatchArgs<R>&, cudaStream_t, int slot, unsigned gen, unsigned ntiles) = nullptr;
+  cudaError_t (*b_summary)(const BatchArgs<R>&, cudaStream_t) = nullptr;
 };
 
 template <class R, int NS>

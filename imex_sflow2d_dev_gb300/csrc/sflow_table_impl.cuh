@@ -1,6 +1,7 @@
 // sflow_table_impl.cuh -- launch wrappers of the class-count-templated
 // kernels; included by the sflow_k_*.cu translation units only.
 #pragma once
+#include "sflow_batch_kernels.cuh"
 #include "sflow_kernels.cuh"
 #include "sflow_table.h"
 
@@ -128,6 +129,48 @@ static cudaError_t tab_smem(size_t bytes) {
 }
 
 template <class R, int NS>
+static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_b_flux<R, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
+  if (e != cudaSuccess) return e;
+  int occ[3] = {0, 0, 0};
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_b_mask<R>, TX * TY, 0);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_b_flux<R, NS>, FLUX_THREADS, smem_flux);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_b_stage2<R, NS>, TX * TY, 0);
+  if (e != cudaSuccess) return e;
+  grids[0] = sms * 4;
+  grids[1] = sms * (occ[0] > 0 ? occ[0] : 1);
+  grids[2] = sms * (occ[1] > 0 ? occ[1] : 1);
+  grids[3] = sms * (occ[2] > 0 ? occ[2] : 1);
+  return cudaSuccess;
+}
+template <class R, int NS>
+static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux) {
+  k_b_cand<R><<<grids[0], kBatchCandThreads, 0, s>>>(b);
+  k_b_mask<R><<<grids[1], TX * TY, 0, s>>>(b);
+  k_b_flux<R, NS><<<grids[2], FLUX_THREADS, smem_flux, s>>>(b);
+  k_b_dt<R><<<1, kBatchCandThreads, 0, s>>>(b);
+  k_b_stage2<R, NS><<<grids[3], TX * TY, 0, s>>>(b);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_b_admit(const BatchArgs<R>& b, cudaStream_t s, int slot, unsigned gen, unsigned ntiles) {
+  k_b_admit<R><<<1, 256, 0, s>>>(b, slot, gen, ntiles);
+  return cudaGetLastError();
+}
+template <class R, int NS>
+static cudaError_t tab_b_summary(const BatchArgs<R>& b, cudaStream_t s) {
+  k_b_summary<R><<<(b.max_runs + 255) / 256, 256, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+template <class R, int NS>
 KernelTable<R> make_table() {
   KernelTable<R> t;
   t.flux = &tab_flux<R, NS>;
@@ -138,6 +181,10 @@ KernelTable<R> make_table() {
   t.qp = &tab_qp<R, NS>;
   t.stats = &tab_stats<R, NS>;
   t.set_smem = &tab_smem<R, NS>;
+  t.b_setup = &tab_b_setup<R, NS>;
+  t.b_step = &tab_b_step<R, NS>;
+  t.b_admit = &tab_b_admit<R, NS>;
+  t.b_summary = &tab_b_summary<R, NS>;
   return t;
 }
 

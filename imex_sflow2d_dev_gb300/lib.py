@@ -69,6 +69,16 @@ def load(build_if_missing=True):
         "sflow_log_sums_noalloc_error": (C.c_char_p, []),
         "sflow_host_geometry": (C.c_int, [P, dp, i32, dp]),
         "sflow_host_scalars": (C.c_int, [P, dp, dp]),
+        "sflow_batch_create": (C.c_int, [i32, i32, i64, C.POINTER(vp)]),
+        "sflow_batch_destroy": (None, [vp]),
+        "sflow_batch_submit": (C.c_int, [vp, P, dp, dp, i64, C.POINTER(i32)]),
+        "sflow_batch_advance": (C.c_int, [vp, i64, C.POINTER(i32)]),
+        "sflow_batch_poll": (C.c_int, [vp, i32, S, C.POINTER(i32)]),
+        "sflow_batch_counters": (C.c_int, [vp, i32, C.POINTER(i64), C.POINTER(i64)]),
+        "sflow_batch_download": (C.c_int, [vp, i32, dp]),
+        "sflow_batch_collect": (C.c_int, [vp, i32, dp]),
+        "sflow_batch_live": (i32, [vp]),
+        "sflow_batch_launch_count": (i64, [vp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -86,7 +96,10 @@ def exported_symbols():
             "sflow_get_stats", "sflow_status", "sflow_clear_status", "sflow_launch_count",
             "sflow_device_bytes", "sflow_counters", "sflow_host_geometry", "sflow_host_scalars",
             "sflow_put_q", "sflow_set_clock", "sflow_advance_timed", "sflow_profile_kernels",
-            "sflow_log_sums_noalloc", "sflow_log_sums_noalloc_error"]
+            "sflow_log_sums_noalloc", "sflow_log_sums_noalloc_error", "sflow_batch_create",
+            "sflow_batch_destroy", "sflow_batch_submit", "sflow_batch_advance", "sflow_batch_poll",
+            "sflow_batch_counters", "sflow_batch_download", "sflow_batch_collect",
+            "sflow_batch_live", "sflow_batch_launch_count"]
 
 
 def log_sums_noalloc(params, q_dev_ptr, sums_dev_ptr, stream_ptr=0):
@@ -265,3 +278,86 @@ class Solver:
 
     def device_bytes(self):
         return self.lib.sflow_device_bytes(self.h)
+
+
+EBUSY = -6
+
+
+class Batch:
+    """Many independent runs resident on the GPU and advanced together
+    (sflow_batch_* of include/sflow.h).  submit() returns a run id, or None
+    when the batch has no slot, list capacity or device memory for the run
+    now (SFLOW_EBUSY); collect() returns the run's q and frees its slot."""
+
+    def __init__(self, precision, max_runs=256, max_cells=1 << 28):
+        self.lib = load()
+        self.h = C.c_void_p()
+        self.precision = precision
+        _check(self.lib.sflow_batch_create(precision, max_runs, max_cells, C.byref(self.h)))
+        self._shape = {}
+
+    def close(self):
+        if self.h:
+            self.lib.sflow_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, params, B_cent, q_aos, max_steps=0):
+        p = params.copy()
+        p.precision = self.precision
+        B = np.ascontiguousarray(B_cent, dtype=np.float64).reshape(-1)
+        q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
+        if B.size != p.comp_cells_x * p.comp_cells_y:
+            raise ValueError("B_cent must have nx*ny values")
+        if q.size != p.n_vars * p.comp_cells_x * p.comp_cells_y:
+            raise ValueError("q must have n_vars*nx*ny values")
+        rid = C.c_int32(-1)
+        rc = self.lib.sflow_batch_submit(self.h, C.byref(p), _dp(B), _dp(q), int(max_steps), C.byref(rid))
+        if rc == EBUSY:
+            return None
+        _check(rc)
+        self._shape[rid.value] = p.n_vars * p.comp_cells_x * p.comp_cells_y
+        return rid.value
+
+    def advance(self, steps):
+        f = C.c_int32(0)
+        _check(self.lib.sflow_batch_advance(self.h, int(steps), C.byref(f)))
+        return f.value
+
+    def poll(self, rid):
+        s = SflowStepStats()
+        d = C.c_int32(0)
+        _check(self.lib.sflow_batch_poll(self.h, rid, C.byref(s), C.byref(d)))
+        return s, bool(d.value)
+
+    def done(self, rid):
+        d = C.c_int32(0)
+        _check(self.lib.sflow_batch_poll(self.h, rid, None, C.byref(d)))
+        return bool(d.value)
+
+    def counters(self, rid):
+        a, b = C.c_int64(), C.c_int64()
+        _check(self.lib.sflow_batch_counters(self.h, rid, C.byref(a), C.byref(b)))
+        return {"cell_updates": a.value, "steps": b.value}
+
+    def download(self, rid):
+        out = np.empty(self._shape[rid])
+        _check(self.lib.sflow_batch_download(self.h, rid, _dp(out)))
+        return out
+
+    def collect(self, rid, want_q=True):
+        out = np.empty(self._shape[rid]) if want_q else None
+        _check(self.lib.sflow_batch_collect(self.h, rid, _dp(out) if want_q else None))
+        del self._shape[rid]
+        return out
+
+    def live(self):
+        return self.lib.sflow_batch_live(self.h)
+
+    def launch_count(self):
+        return self.lib.sflow_batch_launch_count(self.h)

@@ -194,20 +194,22 @@ def _gas_common(p):
 # workloads
 # ---------------------------------------------------------------------------
 
-def dam_break(nx=200, ny=200, dx=1.0, n_rk=2, precision=PREC_FP64, t_end=10.0):
+def dam_break(nx=200, ny=200, dx=1.0, n_rk=2, precision=PREC_FP64, t_end=10.0, n_solid=1):
     """Plain-method dam break on a flat bed with a liquid carrier (a gas-only
     carrier at T_ambient has zero reduced gravity in the reference physics
-    and does not move, constitutive_2d.f90:1470)."""
+    and does not move, constitutive_2d.f90:1470); particle classes at zero
+    concentration."""
     p = default_params()
     p.precision = precision
     p.comp_cells_x, p.comp_cells_y, p.cell_size = nx, ny, dx
     p.x0 = p.y0 = 0.0
-    p.n_solid = 1
+    p.n_solid = n_solid
     p.gas_flag, p.liquid_flag, p.energy_flag = 0, 1, 0
     p.rheology_flag = 0
     _gas_common(p)
     p.rho_l, p.sp_heat_l, p.kin_visc_l, p.loss_rate = 1000.0, 4186.0, 1.0e-6, 0.0
-    p.rho_s[0], p.diam_s[0], p.sp_heat_s[0] = 2500.0, 1.0e-4, 1100.0
+    for i in range(n_solid):
+        p.rho_s[i], p.diam_s[i], p.sp_heat_s[i] = 2500.0, 1.0e-4 * 10 ** i, 1100.0
     p.n_rk = n_rk
     p.cfl, p.dt0, p.max_dt = 0.24, 1.0e-3, 1.0
     p.set_bc_all(1, 0.0)
@@ -216,7 +218,7 @@ def dam_break(nx=200, ny=200, dx=1.0, n_rk=2, precision=PREC_FP64, t_end=10.0):
     B = np.zeros((ny, nx))
     x = (np.arange(nx) + 0.5) * dx
     h = np.where(x[None, :] < 0.5 * nx * dx, 1.0, 0.1) * np.ones((ny, 1))
-    q = rest_state_q(p, h, 300.0, [0.0])
+    q = rest_state_q(p, h, 300.0, [0.0] * n_solid)
     return p, B, q
 
 
@@ -315,3 +317,31 @@ def large_domain(n=8192, dx=2.0, precision=PREC_FP32, seed=5, t_end=1.0e9):
     B = Z[:n, :n].copy()
     q = np.zeros((p.n_vars, n, n))
     return p, B, q
+
+
+def served_job(index, precision=PREC_FP32):
+    """Job `index` of the served request stream (draws use seed = index):
+    a dam break (liquid carrier) or a ring-inlet current with equal odds,
+    grid side log-uniform in [64, 2048], 1-3 particle classes, step count
+    uniform in [500, 5000].  Returns (params, B_cent, q, steps, kind)."""
+    u = uniform01(0x5E4E0000 + index, 4)
+    side = int(round(math.exp(math.log(64) + u[0] * (math.log(2048) - math.log(64)))))
+    ns = 1 + min(int(u[1] * 3), 2)
+    steps = 500 + min(int(u[2] * 4501), 4500)
+    if u[3] < 0.5:
+        p, B, q = dam_break(nx=side, ny=side, dx=1.0, precision=precision, t_end=1.0e9, n_solid=ns)
+        kind = "dam_break"
+    else:
+        dx = 10.0
+        p, B, q = pyroclastic(nx=side, ny=side, dx=dx, precision=precision, t_end=1.0e9,
+                              seed=index + 1, settling=False, n_solid=ns)
+        p.r_source = min(50.0, 0.2 * side * dx)
+        kind = "ring_inlet"
+    return p, B, q, steps, kind
+
+
+def poisson_arrivals(n, rate, seed=0x5E4E):
+    """n arrival times (s) of a Poisson process with the given mean rate."""
+    u = uniform01(seed, n)
+    gaps = -np.log(np.maximum(1.0 - u, 1e-300)) / rate
+    return np.cumsum(gaps) - gaps[0]

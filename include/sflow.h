@@ -43,6 +43,9 @@ extern "C" {
 #define SFLOW_ECUDA (-3)      /* CUDA runtime error                          */
 #define SFLOW_ESTATE (-4)     /* call out of order (e.g. step before upload) */
 #define SFLOW_ERANGE (-5)     /* size beyond a fixed capacity                */
+#define SFLOW_EBUSY (-6)      /* batch: no free slot, tile-list capacity or
+                                 device memory for this run now; retry after
+                                 other runs are collected                    */
 
 /* ---- solver status bits (positive), sticky until sflow_clear_status ------ */
 #define SFLOW_S_NAN 0x1u          /* NaN after assembly (solver_2d.f90:1381)  */
@@ -274,6 +277,44 @@ int sflow_host_scalars(const SflowParams* p, const double* B_cent, double* out4)
  */
 int sflow_log_sums_noalloc(const SflowParams* p, const double* q_dev, double* sums_dev, void* stream);
 const char* sflow_log_sums_noalloc_error(void);
+
+/*
+ * Batched runs.  No counterpart in the reference, which runs ensembles as
+ * separate processes (EXAMPLES/EXAMPLE_ENSEMBLE_ETNA/launch_jobs.py): many
+ * independent runs -- uneven grid sizes, parameters and solid-class counts
+ * -- stay resident on one GPU and advance together, five kernel launches
+ * per batch step for all runs of a class count (persistent kernels over a
+ * device-built queue of active tiles, replayed as CUDA graphs of 16 steps).
+ * Each run follows the N_RK = 2 time step of sflow_step exactly (bitwise the
+ * same result as its own handle, alone or in any mix).  Runs can be
+ * submitted and collected between sflow_batch_advance calls (continuous
+ * batching); a run stops at its t_end or after max_steps steps.
+ *
+ *   sflow_batch_create   precision SFLOW_PREC_FP32 or _FP64 of every run;
+ *                        max_runs slots per class count; max_cells bounds
+ *                        the summed cells of resident runs (tile lists)
+ *   sflow_batch_submit   set-up (as sflow_create) + upload of q (reference
+ *                        layout); SFLOW_EBUSY when no slot, list capacity
+ *                        or device memory (free memory minus 1 GiB) is
+ *                        available now; the run id is returned in *run_id
+ *   sflow_batch_advance  `steps` batch steps; *finished = runs that have
+ *                        stopped and are not yet collected
+ *   sflow_batch_poll     log scalars of the run and whether it has stopped
+ *   sflow_batch_download copy of the run's q (reference layout)
+ *   sflow_batch_collect  optional download, then frees the run's slot
+ */
+typedef struct sflow_batch sflow_batch;
+int sflow_batch_create(int32_t precision, int32_t max_runs, int64_t max_cells, sflow_batch** out);
+void sflow_batch_destroy(sflow_batch* b);
+int sflow_batch_submit(sflow_batch* b, const SflowParams* p, const double* B_cent, const double* q_aos,
+                       int64_t max_steps, int32_t* run_id);
+int sflow_batch_advance(sflow_batch* b, int64_t steps, int32_t* finished);
+int sflow_batch_poll(sflow_batch* b, int32_t run_id, SflowStepStats* stats, int32_t* done);
+int sflow_batch_counters(sflow_batch* b, int32_t run_id, int64_t* cell_updates, int64_t* steps);
+int sflow_batch_download(sflow_batch* b, int32_t run_id, double* q_aos);
+int sflow_batch_collect(sflow_batch* b, int32_t run_id, double* q_aos);
+int32_t sflow_batch_live(const sflow_batch* b);
+int64_t sflow_batch_launch_count(const sflow_batch* b);
 
 /* Build information ("fp64+fp32 sm_103a ..."). */
 const char* sflow_build_info(void);

@@ -1,0 +1,161 @@
+"""Batched runs (sflow_batch_*): many independent runs of uneven sizes and
+parameters advance together on one GPU.  Each run must give exactly the
+result of its own single-run handle, alone and in any mix, including runs
+admitted while others are in flight (continuous batching).  Bitwise
+equality is the tolerance: the per-cell arithmetic is the same code."""
+import numpy as np
+import pytest
+
+from imex_sflow2d_dev_gb300 import lib as L
+from imex_sflow2d_dev_gb300 import workloads as W
+from imex_sflow2d_dev_gb300.params import PREC_FP32, PREC_FP64
+
+pytestmark = pytest.mark.gpu
+
+
+def _pyro(nx, ny, dx, **kw):
+    p, B, q = W.pyroclastic(nx=nx, ny=ny, dx=dx, **kw)
+    p.x_source, p.y_source = 0.5 * nx * dx + 3.0, 0.5 * ny * dx - 4.0
+    return p, B, q
+
+
+def _mix():
+    """Five runs: dam breaks (liquid, 1 class) and ring-inlet currents (gas,
+    2 and 3 classes, different friction) on grids of different shapes."""
+    runs = []
+    p, B, q = W.dam_break(nx=64, ny=48, t_end=100.0)
+    runs.append((p, B, q))
+    p, B, q = _pyro(80, 80, 20.0, settling=True, entrainment=True)
+    runs.append((p, B, q))
+    p, B, q = _pyro(96, 72, 15.0, settling=False, n_solid=3)
+    runs.append((p, B, q))
+    p, B, q = _pyro(130, 70, 12.0, settling=False)
+    p.mu, p.xi = 0.22, 450.0
+    runs.append((p, B, q))
+    p, B, q = W.dam_break(nx=40, ny=200, t_end=100.0)
+    runs.append((p, B, q))
+    return runs
+
+
+def _alone(p, B, q, steps, precision):
+    p = p.copy()
+    p.precision = precision
+    s = L.Solver(p, B)
+    s.upload_q(W.to_aos(q))
+    for _ in range(steps):
+        s.step()
+    out = s.download_q()
+    st = s.stats()
+    s.close()
+    return out, st
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32])
+def test_batch_runs_equal_their_single_run_result(precision):
+    runs = _mix()
+    b = L.Batch(precision, max_runs=8, max_cells=1 << 22)
+    ids = [b.submit(p, B, W.to_aos(q)) for p, B, q in runs]
+    assert all(i is not None for i in ids)
+    assert b.live() == len(runs)
+    b.advance(37)
+    for (p, B, q), rid in zip(runs, ids):
+        ref, st_ref = _alone(p, B, q, 37, precision)
+        st, done = b.poll(rid)
+        assert not done
+        assert st.steps == st_ref.steps == 37
+        assert st.t == st_ref.t
+        np.testing.assert_array_equal(b.collect(rid), ref)
+    assert b.live() == 0
+    b.close()
+
+
+def test_runs_admitted_in_flight_equal_alone():
+    """Continuous batching: B joins after A has run 10 steps, C after 25;
+    each result equals the run alone with its own step count."""
+    runs = _mix()
+    b = L.Batch(PREC_FP32, max_runs=8, max_cells=1 << 22)
+    a = b.submit(*runs[1][:2], W.to_aos(runs[1][2]))
+    b.advance(10)
+    bb = b.submit(*runs[2][:2], W.to_aos(runs[2][2]))
+    b.advance(15)
+    c = b.submit(*runs[0][:2], W.to_aos(runs[0][2]))
+    b.advance(20)
+    for rid, (p, B, q), n in ((a, runs[1], 45), (bb, runs[2], 35), (c, runs[0], 20)):
+        ref, _ = _alone(p, B, q, n, PREC_FP32)
+        np.testing.assert_array_equal(b.collect(rid), ref)
+    b.close()
+
+
+def test_max_steps_and_t_end_stop_each_run():
+    runs = _mix()
+    b = L.Batch(PREC_FP64, max_runs=4, max_cells=1 << 22)
+    r1 = b.submit(*runs[1][:2], W.to_aos(runs[1][2]), max_steps=12)
+    p, B, q = W.dam_break(nx=40, ny=40, t_end=0.05)
+    r2 = b.submit(p, B, W.to_aos(q))
+    finished = b.advance(40)
+    assert finished == 2
+    s1, d1 = b.poll(r1)
+    s2, d2 = b.poll(r2)
+    assert d1 and d2
+    assert s1.steps == 12
+    assert s2.t == pytest.approx(0.05, abs=1e-15)
+    ref, _ = _alone(*runs[1], 12, PREC_FP64)
+    np.testing.assert_array_equal(b.collect(r1), ref)
+    s = L.Solver(p, B)
+    s.upload_q(W.to_aos(q))
+    s.advance()
+    np.testing.assert_array_equal(b.collect(r2), s.download_q())
+    b.close()
+
+
+def test_slots_busy_then_reused():
+    """With 2 slots per solid-class count a third run with 2 classes is
+    refused (None) while one with 1 class is admitted; after a collect the
+    slot is reused at once and the new run is unaffected by the old one's
+    tile-list entries."""
+    runs = _mix()
+    b = L.Batch(PREC_FP32, max_runs=2, max_cells=1 << 22)
+    r0 = b.submit(*runs[1][:2], W.to_aos(runs[1][2]))
+    r1 = b.submit(*runs[3][:2], W.to_aos(runs[3][2]))
+    assert b.submit(*runs[3][:2], W.to_aos(runs[3][2])) is None
+    r3 = b.submit(*runs[0][:2], W.to_aos(runs[0][2]))
+    assert r3 is not None
+    b.advance(8)
+    b.collect(r0, want_q=False)
+    p2, B2, q2 = _pyro(96, 72, 15.0, settling=False)
+    runs[2] = (p2, B2, q2)
+    r2 = b.submit(p2, B2, W.to_aos(q2))
+    assert r2 is not None
+    b.advance(19)
+    ref2, _ = _alone(*runs[2], 19, PREC_FP32)
+    ref1, _ = _alone(*runs[3], 27, PREC_FP32)
+    np.testing.assert_array_equal(b.collect(r2), ref2)
+    np.testing.assert_array_equal(b.collect(r1), ref1)
+    ref3, _ = _alone(*runs[0], 27, PREC_FP32)
+    np.testing.assert_array_equal(b.collect(r3), ref3)
+    b.close()
+
+
+def test_tile_list_capacity_is_enforced():
+    """max_cells = 70000 gives room for 2 * 274 + 1024 = 1572 tiles of 32 x 8;
+    a 512 x 512 run takes 1024.  A collected run's tiles count until the
+    next batch step has dropped its list entries."""
+    p, B, q = _pyro(512, 512, 5.0, settling=False)
+    ps, Bs, qs = _pyro(64, 48, 10.0, settling=False)     # same class count: same group
+    b = L.Batch(PREC_FP32, max_runs=8, max_cells=70000)
+    small = b.submit(ps, Bs, W.to_aos(qs))
+    r0 = b.submit(p, B, W.to_aos(q))
+    assert small is not None and r0 is not None
+    assert b.submit(p, B, W.to_aos(q)) is None
+    b.advance(2)
+    b.collect(r0, want_q=False)
+    assert b.submit(p, B, W.to_aos(q)) is None
+    b.advance(1)
+    r1 = b.submit(p, B, W.to_aos(q))
+    assert r1 is not None
+    b.advance(3)
+    ref, _ = _alone(p, B, q, 3, PREC_FP32)
+    np.testing.assert_array_equal(b.collect(r1), ref)
+    ref, _ = _alone(ps, Bs, qs, 6, PREC_FP32)
+    np.testing.assert_array_equal(b.collect(small), ref)
+    b.close()
