@@ -253,8 +253,11 @@ def ensemble_leg(lib, n_runs, steps):
     together and advanced `steps` steps each by the batched engine (FP32
     bulk form, FP64 Newton).  Inputs are uploaded before the timed region;
     the timed region is the batch advance until every run has stopped."""
+    ts = time.perf_counter()
     members = [W.ensemble_params(i, PREC_FP32, steps) for i in range(n_runs)]
     cells = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members)
+    print(f"[bench] ensemble inputs: {n_runs} runs, {cells} cells, {time.perf_counter() - ts:.1f} s",
+          file=sys.stderr, flush=True)
     b = lib.Batch(PREC_FP32, max_runs=n_runs, max_cells=int(cells * 1.2) + 4096)
     ids = []
     for p, B, q, st in members:
@@ -262,6 +265,7 @@ def ensemble_leg(lib, n_runs, steps):
         if rid is None:
             raise RuntimeError("ensemble member not admitted")
         ids.append(rid)
+    print(f"[bench] ensemble submitted: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
     l0 = b.launch_count()
     t0 = time.perf_counter()
     while True:
@@ -269,6 +273,7 @@ def ensemble_leg(lib, n_runs, steps):
         if fin == len(ids):
             break
     dt = time.perf_counter() - t0
+    print(f"[bench] ensemble advanced: {dt:.1f} s", file=sys.stderr, flush=True)
     launches = b.launch_count() - l0
     cu = sum(b.counters(i)["cell_updates"] for i in ids)
     dense = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members) * steps
@@ -317,12 +322,15 @@ def served_leg(lib, n_requests, rate):
     batching).  Job inputs are prepared before the clock starts; time to
     solution = finish - arrival."""
     from imex_sflow2d_dev_gb300 import serve as S
+    ts = time.perf_counter()
     jobs = [W.served_job(i, PREC_FP32) for i in range(n_requests)]
+    print(f"[bench] served inputs: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
     arr = W.poisson_arrivals(n_requests, rate)
     reqs = [S.Request(i, arr[i], p, B, q, st, kind) for i, (p, B, q, st, kind) in enumerate(jobs)]
     cells = sum(p.comp_cells_x * p.comp_cells_y for p, *_ in jobs)
     loop = S.RequestLoop(PREC_FP32, max_runs=64, max_cells=int(cells * 1.2) + 4096, chunk=16)
     recs = loop.run(reqs)
+    print(f"[bench] served: {max(r['finished_s'] for r in recs):.1f} s", file=sys.stderr, flush=True)
     launches = loop.batch.launch_count()
     loop.close()
     out = S.summarize(recs)

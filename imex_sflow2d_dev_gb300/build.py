@@ -32,6 +32,7 @@ UNITS = [
     ("sflow_fp32.cu", FP32),
     ("sflow_setup.cpp", []),
     ("sflow_capi.cpp", []),
+    ("sflow_io.cpp", []),
 ]
 
 
@@ -76,7 +77,7 @@ def build(force=False, verbose=False, ptxas_verbose=False):
                 cmd += ["-Xptxas", "-v"]
         else:
             cmd = ["g++", "-c", path, "-o", obj, "-std=c++17", "-O2", "-fPIC", "-Wall",
-                   "-I", INC]
+                   "-ffp-contract=off", "-I", INC]
         if verbose:
             print(" ".join(cmd))
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

@@ -49,7 +49,7 @@ class Batch : public BatchBase {
       return SFLOW_EBUSY;
     }
     const int64_t need = Solver<R>::batch_bytes(hs) +
-                         (int64_t)sizeof(double) * hs.nx * hs.ny * (hs.nv + 2);   // staging, freed after upload
+                         (int64_t)sizeof(double) * hs.nx * hs.ny * (hs.nv + 3);   // staging, freed after upload
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
     if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }

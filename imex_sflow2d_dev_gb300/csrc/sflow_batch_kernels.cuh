@@ -243,6 +243,7 @@ __global__ void __launch_bounds__(TX* TY, 5) k_b_stage2(BatchArgs<R> b) {
       __syncthreads();
     }
     if (!a.st->run_step) continue;
+    if (a.tile_active[tile] == 2) continue;   // dry without ring cells (flux_tile)
     const int tiles_x = (a.g.nx + TX - 1) / TX;
     stage2_tile<R, NS>(a, -1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x));
   }

@@ -256,6 +256,34 @@ int sflow_download_qp(sflow_handle* h, double* qp) {
   if (!qp) return fail(SFLOW_EINVAL, "qp is NULL");
   FORWARD(h->solver->download_qp(qp));
 }
+int sflow_download_phys(sflow_handle* h, double* out) {
+  CHECK_HANDLE(h);
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  FORWARD(h->solver->download_phys(out));
+}
+
+int sflow_download_deposit(sflow_handle* h, double* out) {
+  CHECK_HANDLE(h);
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  FORWARD(h->solver->download_deposit(out));
+}
+
+int sflow_upload_deposit(sflow_handle* h, const double* in) {
+  CHECK_HANDLE(h);
+  if (!in) return fail(SFLOW_EINVAL, "in is NULL");
+  FORWARD(h->solver->upload_deposit(in));
+}
+
+int sflow_upload_maps(sflow_handle* h, const double* hmax, const double* pdynmax, const double* mod_vel_max) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->upload_maps(hmax, pdynmax, mod_vel_max));
+}
+
+int sflow_set_output_time(sflow_handle* h, double t_output) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->set_output_time(t_output));
+}
+
 int sflow_download_maps(sflow_handle* h, double* a, double* b, double* c) {
   CHECK_HANDLE(h);
   FORWARD(h->solver->download_maps(a, b, c));

@@ -51,6 +51,11 @@ class SolverBase {
   virtual int download(double* q_aos) = 0;
   virtual int download_qp(double* qp_aos) = 0;
   virtual int download_maps(double* h, double* p, double* v) = 0;
+  virtual int download_deposit(double* out) = 0;
+  virtual int download_phys(double* out) = 0;
+  virtual int upload_deposit(const double* in) = 0;
+  virtual int upload_maps(const double* h, const double* p, const double* v) = 0;
+  virtual int set_output_time(double t_output) = 0;
   virtual int check_solve(int solve_all) = 0;
   virtual int timestep(double* dt_out) = 0;
   virtual int imex_rk(double t, double dt) = 0;

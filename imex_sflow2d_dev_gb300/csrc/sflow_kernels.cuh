@@ -33,6 +33,7 @@ constexpr int FLUX_THREADS = 288;  // 9 warps: covers (TX+1)*TY and TX*(TY+1) fa
 // flag byte bits
 constexpr uint8_t F_SC_MASK = 0x3;  // source_cell (0, 1 ring interior, 2 ring boundary)
 constexpr uint8_t F_E = 0x4, F_W = 0x8, F_N = 0x10, F_S = 0x20;
+constexpr uint8_t F_WET = 0x40;     // set in shared memory only: active and q1 > 0
 constexpr uint8_t F_ACTIVE = 0x80;  // set in shared memory only
 
 template <class R>
@@ -53,6 +54,7 @@ struct KArgs {
   R* hmax;
   R* pdynmax;
   R* mvmax;
+  double* deposit;   // n_solid planes (settling only): accumulated dt * deposition
   RunState* st;
   double tableau_at[16], tableau_ad[16], omega_t[4], omega[4];
   int take_last;
@@ -116,36 +118,56 @@ __device__ __forceinline__ Geo<R> load_geo(const KArgs<R>& a, int64_t c) {
 // within Manhattan distance n_RK of a seed (border cell, wet interior cell,
 // ring-boundary cell) and is not a ring-interior cell.
 // ---------------------------------------------------------------------------
+// Seeds of check_solve (solver_2d.f90:667-858): border cells, wet cells and
+// ring-boundary cells; a cell is active when a seed lies within Manhattan
+// distance n_RK (<= 4) and it is not a ring-interior cell.  The seed bits of
+// the tile and a 4-cell frame are staged in shared memory; a tile with no
+// seed in its frame is inactive without scanning its cells.
+constexpr int MASK_HALO = 4;
+constexpr int MRX = TX + 2 * MASK_HALO, MRY = TY + 2 * MASK_HALO;
+
 template <class R>
 __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x) {
+  __shared__ uint8_t seed[MRY][MRX];
   RunState* st = a.st;
   const Grid<R>& g = a.g;
-  const int j = tx * TX + threadIdx.x % TX;
-  const int k = ty * TY + threadIdx.x / TX;
+  const int j0 = tx * TX, k0 = ty * TY;
   const int nrk = a.pd.nrk;
+  int any = 0;
+  if (!solve_all) {
+    for (int idx = threadIdx.x; idx < MRX * MRY; idx += TX * TY) {
+      const int rx = idx % MRX, ry = idx / MRX;
+      const int jj = j0 + rx - MASK_HALO, kk = k0 + ry - MASK_HALO;
+      uint8_t sd = 0;
+      if (jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
+        if (jj == 0 || jj == g.nx - 1 || kk == 0 || kk == g.ny - 1) sd = 1;
+        else {
+          const int64_t cc = cidx(g, jj, kk);
+          if (a.q[cc] > R(0)) sd = 1;
+          else if (a.pd.radial_source && (a.cflags[cc] & F_SC_MASK) == 2) sd = 1;
+        }
+      }
+      seed[ry][rx] = sd;
+      any |= sd;
+    }
+    any = __syncthreads_or(any);
+  }
+  const int j = j0 + threadIdx.x % TX;
+  const int k = k0 + threadIdx.x / TX;
   int act = 0;
   if (j < g.nx && k < g.ny) {
     const int64_t c = cidx(g, j, k);
-    const uint8_t fl = a.cflags[c];
     if (solve_all) {
       act = 1;
-    } else {
+    } else if (any) {
+      const int cx = threadIdx.x % TX + MASK_HALO, cy = threadIdx.x / TX + MASK_HALO;
       for (int dk = -nrk; dk <= nrk && !act; ++dk) {
-        int kk = k + dk;
-        if (kk < 0 || kk >= g.ny) continue;
-        int rem = nrk - (dk < 0 ? -dk : dk);
-        for (int dj = -rem; dj <= rem; ++dj) {
-          int jj = j + dj;
-          if (jj < 0 || jj >= g.nx) continue;
-          bool border = (jj == 0 || jj == g.nx - 1 || kk == 0 || kk == g.ny - 1);
-          if (border) { act = 1; break; }
-          int64_t cc = cidx(g, jj, kk);
-          if (a.q[cc] > R(0)) { act = 1; break; }
-          if (a.pd.radial_source && (a.cflags[cc] & F_SC_MASK) == 2) { act = 1; break; }
-        }
+        const int rem = nrk - (dk < 0 ? -dk : dk);
+        for (int dj = -rem; dj <= rem; ++dj)
+          if (seed[cy + dk][cx + dj]) { act = 1; break; }
       }
     }
-    if (a.pd.radial_source && (fl & F_SC_MASK) == 1) act = 0;
+    if (act && a.pd.radial_source && (a.cflags[c] & F_SC_MASK) == 1) act = 0;
     a.mask[c] = (uint8_t)act;
   }
   int cnt = __syncthreads_count(act);
@@ -512,6 +534,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
 
   __syncthreads();   // shared memory of the previous tile of a persistent block is free
   // 1. physical variables of the tile + halo (qc_to_qp; inactive = dry)
+  int any_wet = 0, all_wet = 1;
   for (int idx = tid; idx < RX * RY; idx += FLUX_THREADS) {
     const int rx = idx % RX, ry = idx / RX;
     const int j = j0 + rx - HALO, k = k0 + ry - HALO;
@@ -526,7 +549,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
         R q[nv];
 #pragma unroll
         for (int i = 0; i < nv; ++i) q[i] = qin[i * g.plane + c];
-        if (q[0] > R(0)) { qc_to_qp<R, NS>(P, q, qp); wet = true; }
+        if (q[0] > R(0)) { qc_to_qp<R, NS>(P, q, qp); wet = true; fl |= F_WET; }
       }
     }
     if (!wet) {
@@ -537,17 +560,42 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
 #pragma unroll
     for (int i = 0; i < np; ++i) sqp[i * RX * RY + idx] = qp[i];
     sfl[idx] = fl;
+    any_wet |= wet;
+    all_wet &= wet;
   }
-  __syncthreads();
+  // A face whose reconstruction stencil (two cells each side) is dry has
+  // dry states on both sides: zero fluxes, zero speeds, and the KT flux is
+  // exactly 0 (solver_2d.f90 eval_flux_KT with a+ = a- = 0).  Ghost states
+  // beyond the domain edge are dry too when every boundary condition is
+  // (Neumann, 0).  A tile with no wet cell in its halo skips the faces.
+  const bool some_wet = __syncthreads_or(any_wet);
+  const bool inside = j0 - HALO >= 0 && k0 - HALO >= 0 && j0 + TX + HALO <= g.nx && k0 + TY + HALO <= g.ny;
+  const bool tile_dry = !some_wet && (g.dry_bc || inside);
+  // every halo cell wet: no face can have a dry stencil
+  const bool face_checks = !__syncthreads_and(all_wet);
+  if (tile_dry) {
+    // a dry tile without ring cells is left unchanged by the stage kernel
+    // (q stays 0, divFlux - expl = 0, the maxima keep their values)
+    int ring = 0;
+    for (int idx = tid; idx < TX * TY; idx += FLUX_THREADS) {
+      const int rx = idx % TX + HALO, ry = idx / TX + HALO;
+      ring |= (sfl[ry * RX + rx] & F_SC_MASK) != 0;
+    }
+    if (!__syncthreads_or(ring) && tid == 0) a.tile_active[ty * g.tiles_x + tx] = 2;
+  }
 
   // 2. x faces: face f = j0+fx between cells f-1 and f
-  for (int fi = tid; fi < (TX + 1) * TY; fi += FLUX_THREADS) {
+  for (int fi = tid; fi < (TX + 1) * TY && !tile_dry; fi += FLUX_THREADS) {
     const int fx = fi % (TX + 1), fy = fi / (TX + 1);
     const int f = j0 + fx, k = k0 + fy;
     R H[nv];
     R amax = R(0);
     const int ry = fy + HALO, rxl = fx - 1 + HALO, rxh = fx + HALO;
-    const bool any = (k < g.ny && f <= g.nx) &&
+    const bool stencil_dry =
+        face_checks &&
+        !((sfl[ry * RX + rxl - 1] | sfl[ry * RX + rxl] | sfl[ry * RX + rxh] | sfl[ry * RX + rxh + 1]) & F_WET) &&
+        (g.dry_bc || (f >= 2 && f + 1 <= g.nx - 1));
+    const bool any = (k < g.ny && f <= g.nx) && !stencil_dry &&
                      (((f > 0) && (sfl[ry * RX + rxl] & F_ACTIVE)) || ((f < g.nx) && (sfl[ry * RX + rxh] & F_ACTIVE)));
     if (any) {
       const int64_t cl = cidx(g, f > 0 ? f - 1 : 0, k), ch = cidx(g, f < g.nx ? f : g.nx - 1, k);
@@ -566,13 +614,19 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   }
 
   // 3. y faces: face f = k0+fy between cells f-1 and f
-  for (int fi = tid; fi < TX * (TY + 1); fi += FLUX_THREADS) {
+  // (one-row domains have no y fluxes: solver_2d.f90 eval_hyperbolic_terms
+  // skips the y direction when comp_cells_y = 1)
+  for (int fi = tid; fi < TX * (TY + 1) && !tile_dry && g.ny > 1; fi += FLUX_THREADS) {
     const int fx = fi % TX, fy = fi / TX;
     const int j = j0 + fx, f = k0 + fy;
     R H[nv];
     R amax = R(0);
     const int rx = fx + HALO, ryl = fy - 1 + HALO, ryh = fy + HALO;
-    const bool any = (j < g.nx && f <= g.ny) &&
+    const bool stencil_dry =
+        face_checks &&
+        !((sfl[(ryl - 1) * RX + rx] | sfl[ryl * RX + rx] | sfl[ryh * RX + rx] | sfl[(ryh + 1) * RX + rx]) & F_WET) &&
+        (g.dry_bc || (f >= 2 && f + 1 <= g.ny - 1));
+    const bool any = (j < g.nx && f <= g.ny) && !stencil_dry &&
                      (((f > 0) && (sfl[ryl * RX + rx] & F_ACTIVE)) || ((f < g.ny) && (sfl[ryh * RX + rx] & F_ACTIVE)));
     if (any) {
       const int64_t cl = cidx(g, j, f > 0 ? f - 1 : 0), ch = cidx(g, j, f < g.ny ? f : g.ny - 1);
@@ -618,13 +672,16 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
 #pragma unroll
       for (int i = 0; i < nv; ++i) {
         R d = R(0);
-        d = d + (sHx[i * TY * (TX + 1) + cy * (TX + 1) + cx + 1] - sHx[i * TY * (TX + 1) + cy * (TX + 1) + cx]) * g.one_by_dx;
-        d = d + (sHy[i * (TY + 1) * TX + (cy + 1) * TX + cx] - sHy[i * (TY + 1) * TX + cy * TX + cx]) * g.one_by_dy;
+        if (!tile_dry) {
+          d = d + (sHx[i * TY * (TX + 1) + cy * (TX + 1) + cx + 1] - sHx[i * TY * (TX + 1) + cy * (TX + 1) + cx]) * g.one_by_dx;
+          if (g.ny > 1)
+            d = d + (sHy[i * (TY + 1) * TX + (cy + 1) * TX + cx] - sHy[i * (TY + 1) * TX + cy * TX + cx]) * g.one_by_dy;
+        }
         if (rout) rout[i * g.plane + c] = d - e[i];
       }
-      if (want_dt) {
+      if (want_dt && !tile_dry) {
         R ax = rmax(sAx[cy * (TX + 1) + cx], sAx[cy * (TX + 1) + cx + 1]);
-        R ay = rmax(sAy[cy * TX + cx], sAy[(cy + 1) * TX + cx]);
+        R ay = (g.ny > 1) ? rmax(sAy[cy * TX + cx], sAy[(cy + 1) * TX + cx]) : R(0);
         if constexpr (sizeof(R) == 8) {
           double dtx = (ax > 0.0) ? g.cfl * g.dx / ax : 1.0e300;
           double dty = (ay > 0.0) ? g.cfl * g.dy / ay : 1.0e300;
@@ -752,7 +809,7 @@ __device__ __forceinline__ unsigned assemble_fixes(const Phys<R>& P, R* q) {
 // update_erosion_deposition_cell (solver_2d.f90:2382-2597) for one cell
 template <class R, int NS>
 __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const Geo<R>& geo, R dt,
-                                                       R* q) {
+                                                       R* q, R* dep_out) {
   constexpr int nv = 4 + NS, ns = NS;
   unsigned st = 0;
   R qp[nv + 2], dep[kMaxSolid], eqn[nv];
@@ -763,6 +820,8 @@ __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const G
     qp[3] = P.T_ambient;
   }
   mass_exchange<R, NS>(P, qp, geo.Bx, geo.By, dt, dep, eqn);
+#pragma unroll
+  for (int i = 0; i < ns; ++i) dep_out[i] = dep[i];
 #pragma unroll
   for (int i = 0; i < nv; ++i) q[i] = q[i] + dt * eqn[i];
 #pragma unroll
@@ -805,6 +864,14 @@ __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const G
     for (int i = 0; i < nv; ++i) q[i] = R(0);
   }
   return st;
+}
+
+// deposit(j,k,:) += dt * deposition_term (solver_2d.f90:2476-2477), FP64
+template <class R, int NS>
+__device__ __forceinline__ void add_deposit(const KArgs<R>& a, int64_t c, double dt, const R* dep) {
+  if (!a.deposit) return;
+#pragma unroll
+  for (int i = 0; i < NS; ++i) a.deposit[i * a.g.plane + c] += dt * (double)dep[i];
 }
 
 // post-step maxima (IMEX_SfloW2D.f90:449-505)
@@ -977,7 +1044,9 @@ __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx,
       if (mode > 0) {
         if (mode == 1) {
           const Geo<R> geo = load_geo(a, c);
-          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q);
+          R dep[NS];
+          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+          add_deposit<R, NS>(a, c, dt, dep);
 #pragma unroll
           for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
         } else {
@@ -993,8 +1062,11 @@ __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx,
         }
         status |= stage_cell<R, NS>(a, geo, q, s1, s2, dt, 1.0, q, rn, nit);
         status |= assemble_fixes<R, NS>(a.pr, q);
-        if (mode < 0 && (a.pd.settling || a.pd.entrain))
-          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q);
+        if (mode < 0 && (a.pd.settling || a.pd.entrain)) {
+          R dep[NS];
+          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+          add_deposit<R, NS>(a, c, dt, dep);
+        }
 #pragma unroll
         for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
         if (mode < 0) post_step_maps<R, NS>(a, c, q);
@@ -1007,7 +1079,8 @@ __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx,
 template <class R, int NS>
 __global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
   if (!a.st->run_step) return;
-  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  const uint8_t ta = a.tile_active[blockIdx.y * gridDim.x + blockIdx.x];
+  if (ta == 0 || ta == 2) return;   // inactive, or dry without ring cells (k_flux)
   stage2_tile<R, NS>(a, mode, blockIdx.x, blockIdx.y);
 }
 
@@ -1100,7 +1173,9 @@ __global__ void __launch_bounds__(TX* TY) k_assemble(KArgs<R> a) {
       status |= assemble_fixes<R, NS>(a.pr, q);
       if (a.pd.settling || a.pd.entrain) {
         const Geo<R> geo = load_geo(a, c);
-        status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q);
+        R dep[NS];
+        status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+        add_deposit<R, NS>(a, c, dt, dep);
       }
 #pragma unroll
       for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];

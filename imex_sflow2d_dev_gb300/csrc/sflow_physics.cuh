@@ -810,36 +810,33 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, fl
   float dKf;
   float K = Kf(S, dKf);
   float s = 2.0f * S / (1.0f + sqrtf(fmaxf(1.0f + 4.0f * dtaf * K * S, 0.0f)));
+  float gdf = 1.0f + 2.0f * dtaf * K * s;
   if (varT) {
     for (int it = 0; it < 8; ++it) {
       K = Kf(s, dKf);
       const float gv = s + dtaf * K * s * s - S;
-      const float gd = 1.0f + dtaf * (dKf * s * s + 2.0f * K * s);
-      const float ds = gv / gd;
+      gdf = 1.0f + dtaf * (dKf * s * s + 2.0f * K * s);
+      const float ds = gv / gdf;
       s -= ds;
       if (!(fabsf(ds) > 1.0e-7f * s)) break;
     }
   }
-  // One FP64 Newton step from the FP32 root.  The FP32 root is within
-  // ~1e-7 relative of the solution, so the step leaves an error of order
-  // 1e-14, far below the float the result is stored in; residual and
-  // derivative are evaluated in FP64 (rho_m to ~1e-14 by one refinement of
-  // the float reciprocal; the step itself needs only ~1e-7 relative).
-  const double Sd = S, cg = cgeo, bi = base_inv, ra = rho_a;
+  // One FP64 Newton step from the FP32 root: the residual g(s) in FP64
+  // (rho_m to ~1e-14 by one refinement of the float reciprocal), the
+  // derivative from the last FP32 iteration.  The FP32 root is within ~1e-7
+  // relative of the solution and g' is known to ~1e-7, so the step leaves an
+  // error of order 1e-14, far below the float the result is stored in.
   double sd = s;
   {
-    double T = (double)a_T - (double)b_T * sd * sd;
-    double dT = -2.0 * (double)b_T * sd;
-    if (T <= 0.0) { T = (double)P.T_ambient; dT = 0.0; }
-    const double ci = c_inv;
-    const double x = bi + ci * T;
+    const double sd2 = sd * sd;
+    double T = (double)a_T - (double)b_T * sd2;
+    if (T <= 0.0) T = (double)P.T_ambient;
+    const double x = (double)base_inv + (double)c_inv * T;
     double rho_m = (double)__frcp_rn((float)x);
     rho_m = rho_m * (2.0 - x * rho_m);
-    const double Kd = cg * (rho_m - ra);
-    const double dKd = cg * (-rho_m * rho_m * ci * dT);
-    const double gv = sd + dta * Kd * sd * sd - Sd;
-    const double gd = 1.0 + dta * (dKd * sd * sd + 2.0 * Kd * sd);
-    sd -= gv * (double)__frcp_rn((float)gd);
+    const double Kd = (double)cgeo * (rho_m - (double)rho_a);
+    const double gv = (sd - (double)S) + dta * Kd * sd2;
+    sd -= gv * (double)__frcp_rn(gdf);
     iters = 1;
   }
   return sd > 0.0 ? (float)sd : 0.0f;

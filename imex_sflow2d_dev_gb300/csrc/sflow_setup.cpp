@@ -73,6 +73,21 @@ static void topography(HostSetup& s, const double* B) {
   auto at = [&](std::vector<double>& v, int j, int k) -> double& { return v[(size_t)k * nx + j]; };
   std::vector<double>* arr[5] = {&s.Bx, &s.By, &s.Bxx, &s.Byy, &s.Bxy};
   for (auto* a : arr) a->assign(N, 0.0);
+  // one row: x derivatives only (geometry_2d.f90:600-640)
+  if (ny == 1) {
+    for (int j = 2; j <= nx - 3; ++j) {
+      double px = 0.0, sxx = 0.0;
+      for (int m = 0; m < 5; ++m) {
+        px = px + c1[m] * Bc(j + m - 2, 0);
+        sxx = sxx + c2[m] * Bc(j + m - 2, 0);
+      }
+      at(s.Bx, j, 0) = px / n1x;
+      at(s.By, j, 0) = 0.0 / n1y;
+      at(s.Bxx, j, 0) = sxx / n2x;
+      at(s.Byy, j, 0) = 0.0 / n2y;
+      at(s.Bxy, j, 0) = 0.0;
+    }
+  }
   // five-point centred derivatives (geometry_2d.f90:730-790)
   for (int k = 2; k <= ny - 3; ++k) {
     for (int j = 2; j <= nx - 3; ++j) {
@@ -102,13 +117,14 @@ static void topography(HostSetup& s, const double* B) {
       at(*a, nx - 2, k) = at(*a, nx - 3, k);
       at(*a, nx - 1, k) = at(*a, nx - 3, k);
     }
-  for (int j = 0; j < nx; ++j)
-    for (auto* a : arr) {
-      at(*a, j, 0) = at(*a, j, 2);
-      at(*a, j, 1) = at(*a, j, 2);
-      at(*a, j, ny - 2) = at(*a, j, ny - 3);
-      at(*a, j, ny - 1) = at(*a, j, ny - 3);
-    }
+  if (ny >= 3)
+    for (int j = 0; j < nx; ++j)
+      for (auto* a : arr) {
+        at(*a, j, 0) = at(*a, j, 2);
+        at(*a, j, 1) = at(*a, j, 2);
+        at(*a, j, ny - 2) = at(*a, j, ny - 3);
+        at(*a, j, ny - 1) = at(*a, j, ny - 3);
+      }
   s.gc.assign(N, 1.0);
   s.dgcx.assign(N, 0.0);
   s.dgcy.assign(N, 0.0);
@@ -237,7 +253,11 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   SflowParams& p = s.p;
   if (p.abi_version != SFLOW_ABI_VERSION) { err = "abi_version mismatch"; return SFLOW_EINVAL; }
   if (p.precision != SFLOW_PREC_FP64 && p.precision != SFLOW_PREC_FP32) { err = "precision must be SFLOW_PREC_FP64 or SFLOW_PREC_FP32"; return SFLOW_EINVAL; }
-  if (p.comp_cells_x < 5 || p.comp_cells_y < 5) { err = "comp_cells_x and comp_cells_y must be >= 5"; return SFLOW_EINVAL; }
+  if (p.comp_cells_x < 5 || (p.comp_cells_y < 5 && p.comp_cells_y != 1)) {
+    err = "comp_cells_x must be >= 5 and comp_cells_y 1 or >= 5";
+    return SFLOW_EINVAL;
+  }
+  if (p.comp_cells_y == 1 && p.radial_source_flag) { err = "a radial source needs comp_cells_y > 1"; return SFLOW_EINVAL; }
   if ((int64_t)p.comp_cells_x * p.comp_cells_y > (int64_t)1 << 31) { err = "domain larger than 2^31 cells"; return SFLOW_ERANGE; }
   if (p.n_solid < 1 || p.n_solid > 3) { err = "the GPU kernels are built for n_solid = 1, 2 or 3"; return SFLOW_EINVAL; }
   if (p.n_rk < 1 || p.n_rk > 4) { err = "N_RK must be 1, 2, 3 or 4"; return SFLOW_EINVAL; }
@@ -265,7 +285,7 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   s.nv = 4 + p.n_solid;
   s.nrk = p.n_rk;
   s.dx = p.cell_size;
-  s.dy = p.cell_size;
+  s.dy = p.comp_cells_y > 1 ? p.cell_size : 1.0;   // geometry_2d.f90:288-298
   s.eps_sing = std::fmin(std::fmin(std::pow(s.dx, 4.0), std::pow(s.dy, 4.0)), 1.0e-10);
   {
     double e2 = s.eps_sing * s.eps_sing;

@@ -130,6 +130,10 @@ class Solver : public SolverBase {
     SFLOW_CU(alloc((void**)&hmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&pdynmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&mvmax_, sizeof(R) * plane_));
+    if (hs_.p.settling_flag || hs_.p.entrainment_flag) {
+      SFLOW_CU(alloc((void**)&deposit_, sizeof(double) * plane_ * hs_.ns));
+      SFLOW_CU(cudaMemset(deposit_, 0, sizeof(double) * plane_ * hs_.ns));
+    }
     SFLOW_CU(alloc((void**)&st_, sizeof(RunState)));
     nstat_blocks_ = 1024;
     SFLOW_CU(alloc((void**)&stat_part_, sizeof(double) * 4 * nstat_blocks_));
@@ -163,7 +167,7 @@ class Solver : public SolverBase {
     if (!stage_aos_) return;
     cudaStreamSynchronize(stream_);
     cudaFree(stage_aos_);
-    bytes_ -= (int64_t)(sizeof(double) * (size_t)hs_.nx * hs_.ny * (hs_.nv + 2));
+    bytes_ -= (int64_t)(sizeof(double) * (size_t)hs_.nx * hs_.ny * (hs_.nv + 3));
     stage_aos_ = nullptr;
   }
   // device bytes a run of this set-up holds while it is in a batch
@@ -187,6 +191,7 @@ class Solver : public SolverBase {
     init_state_host();
     SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
+    if (deposit_) SFLOW_CU(cudaMemsetAsync(deposit_, 0, sizeof(double) * plane_ * hs_.ns, stream_));
     SFLOW_CU(cudaStreamSynchronize(stream_));
     uploaded_ = true;
     return SFLOW_OK;
@@ -290,6 +295,17 @@ class Solver : public SolverBase {
     return SFLOW_OK;
   }
 
+  // .p_2d fields per cell: h, u, v, T, alphas, rho_m, red_grav, Ri
+  int download_phys(double* out) override {
+    const size_t N = (size_t)hs_.nx * hs_.ny;
+    SFLOW_CU(ensure_stage());
+    ++launches_;
+    SFLOW_CU(tab_.phys(ka_, (unsigned)((N + 255) / 256), stream_, stage_aos_));
+    SFLOW_CU(cudaMemcpyAsync(out, stage_aos_, sizeof(double) * N * (hs_.ns + 7), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+
   int download_maps(double* h, double* p, double* v) override {
     const int nx = hs_.nx, ny = hs_.ny;
     const size_t N = (size_t)nx * ny;
@@ -303,6 +319,61 @@ class Solver : public SolverBase {
       SFLOW_CU(cudaGetLastError());
       SFLOW_CU(cudaMemcpyAsync(dst[m], stage_aos_, sizeof(double) * N, cudaMemcpyDeviceToHost, stream_));
       SFLOW_CU(cudaStreamSynchronize(stream_));
+    }
+    return SFLOW_OK;
+  }
+
+  // deposit(1:nx,1:ny,1:n_solid) in the reference layout (column-major, class
+  // slowest); zeros when the run has no settling
+  int download_deposit(double* out) override {
+    const int nx = hs_.nx, ny = hs_.ny;
+    const size_t N = (size_t)nx * ny;
+    if (!deposit_) {
+      std::memset(out, 0, sizeof(double) * N * hs_.ns);
+      return SFLOW_OK;
+    }
+    std::vector<double> buf((size_t)plane_);
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    for (int i = 0; i < hs_.ns; ++i) {
+      SFLOW_CU(cudaMemcpy(buf.data(), deposit_ + (size_t)i * plane_, sizeof(double) * plane_, cudaMemcpyDeviceToHost));
+      for (int k = 0; k < ny; ++k)
+        for (int j = 0; j < nx; ++j) out[(size_t)i * N + (size_t)k * nx + j] = buf[(size_t)k * pitch_ + j];
+    }
+    return SFLOW_OK;
+  }
+  int upload_deposit(const double* in) override {
+    if (!deposit_) { err_ = "the run has no settling: no deposit to set"; return SFLOW_EINVAL; }
+    const int nx = hs_.nx, ny = hs_.ny;
+    const size_t N = (size_t)nx * ny;
+    std::vector<double> buf((size_t)plane_, 0.0);
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    for (int i = 0; i < hs_.ns; ++i) {
+      for (int k = 0; k < ny; ++k)
+        for (int j = 0; j < nx; ++j) buf[(size_t)k * pitch_ + j] = in[(size_t)i * N + (size_t)k * nx + j];
+      SFLOW_CU(cudaMemcpy(deposit_ + (size_t)i * plane_, buf.data(), sizeof(double) * plane_, cudaMemcpyHostToDevice));
+    }
+    return SFLOW_OK;
+  }
+  int set_output_time(double t_output) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    SFLOW_CU(cudaMemcpyAsync(&st_->t_output, &t_output, sizeof(double), cudaMemcpyHostToDevice, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    hst_.t_output = t_output;
+    return SFLOW_OK;
+  }
+
+  // maxima maps from the host (restart.bin), reference layout
+  int upload_maps(const double* h, const double* p, const double* v) override {
+    const int nx = hs_.nx, ny = hs_.ny;
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    R* dst[3] = {hmax_, pdynmax_, mvmax_};
+    const double* src[3] = {h, p, v};
+    std::vector<R> buf((size_t)plane_, R(0));
+    for (int m = 0; m < 3; ++m) {
+      if (!src[m]) continue;
+      for (int k = 0; k < ny; ++k)
+        for (int j = 0; j < nx; ++j) buf[(size_t)k * pitch_ + j] = (R)src[m][(size_t)k * nx + j];
+      SFLOW_CU(cudaMemcpy(dst[m], buf.data(), sizeof(R) * plane_, cudaMemcpyHostToDevice));
     }
     return SFLOW_OK;
   }
@@ -459,6 +530,7 @@ class Solver : public SolverBase {
   int tiles_x_ = 0, tiles_y_ = 0;
   cudaStream_t stream_ = nullptr;
   R *q_ = nullptr, *rd_ = nullptr, *rn_ = nullptr, *qs_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
+  double* deposit_ = nullptr;
   R* geo_[8];
   uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr;
   RunState* st_ = nullptr;
@@ -553,7 +625,7 @@ class Solver : public SolverBase {
   // host-layout staging buffer, allocated on first use
   cudaError_t ensure_stage() {
     if (stage_aos_) return cudaSuccess;
-    const size_t bytes = sizeof(double) * (size_t)hs_.nx * hs_.ny * (hs_.nv + 2);
+    const size_t bytes = sizeof(double) * (size_t)hs_.nx * hs_.ny * (hs_.nv + 3);
     cudaError_t e = cudaMalloc((void**)&stage_aos_, bytes);
     if (e == cudaSuccess) bytes_ += (int64_t)bytes;
     return e;
@@ -643,12 +715,19 @@ class Solver : public SolverBase {
         ka_.bc.flag[sd][i] = p.bc[sd][i].flag;
         ka_.bc.value[sd][i] = (R)p.bc[sd][i].value;
       }
+    g.dry_bc = 1;
+    for (int sd = 0; sd < 4; ++sd) {
+      if ((sd < 2 && hs_.nx < 2) || (sd >= 2 && hs_.ny < 2)) continue;
+      for (int i = 0; i < hs_.nv; ++i)
+        if (!(p.bc[sd][i].flag == 1 && p.bc[sd][i].value == 0.0)) g.dry_bc = 0;
+    }
     ka_.q = q_; ka_.rd = rd_; ka_.rn = rn_; ka_.qs = qs_;
     for (int i = 0; i < 16; ++i) { ka_.tableau_at[i] = hs_.a_tilde[i]; ka_.tableau_ad[i] = hs_.a_dirk[i]; }
     for (int i = 0; i < 4; ++i) { ka_.omega_t[i] = hs_.omega_tilde[i]; ka_.omega[i] = hs_.omega[i]; }
     for (int i = 0; i < 8; ++i) ka_.geo[i] = geo_[i];
     ka_.cflags = cflags_; ka_.arc = arc_; ka_.mask = mask_; ka_.tile_active = tile_active_;
     ka_.hmax = hmax_; ka_.pdynmax = pdynmax_; ka_.mvmax = mvmax_; ka_.st = st_;
+    ka_.deposit = deposit_;
     ka_.take_last = hs_.take_last;
   }
 

@@ -22,6 +22,7 @@ struct KernelTable {
   cudaError_t (*assemble)(const KArgs<R>&, dim3, cudaStream_t) = nullptr;
   cudaError_t (*init_maps)(const KArgs<R>&, unsigned, cudaStream_t) = nullptr;
   cudaError_t (*qp)(const KArgs<R>&, unsigned, cudaStream_t, double*) = nullptr;
+  cudaError_t (*phys)(const KArgs<R>&, unsigned, cudaStream_t, double*) = nullptr;
   cudaError_t (*stats)(const KArgs<R>&, int, cudaStream_t, double*) = nullptr;
   cudaError_t (*set_smem)(size_t) = nullptr;
   // batched runs (sflow_batch_kernels.cuh): grids[4] = persistent grid sizes

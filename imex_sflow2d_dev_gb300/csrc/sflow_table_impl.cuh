@@ -26,6 +26,37 @@ __global__ void k_qp_to_aos(KArgs<R> a, double* __restrict__ aos) {
   for (int i = 0; i < np; ++i) aos[c * np + i] = (double)qp[i];
 }
 
+// per-cell physical fields of the .p_2d output (inpout_2d.f90:6150-6200):
+// h, u, v, T, alphas (NS), rho_m, red_grav, Ri -- qc_to_qp and mixt_var of
+// every cell, in host layout
+template <class R, int NS>
+__global__ void k_phys_to_aos(KArgs<R> a, double* __restrict__ aos) {
+  constexpr int nv = 4 + NS, np = nv + 2, nf = 7 + NS;
+  const Grid<R>& g = a.g;
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)g.nx * g.ny) return;
+  int j = (int)(c % g.nx), k = (int)(c / g.nx);
+  int64_t d = cidx(g, j, k);
+  R q[nv], qp[np];
+  for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + d];
+  if (q[0] > R(0)) qc_to_qp<R, NS>(a.pr, q, qp);
+  else {
+    for (int i = 0; i < np; ++i) qp[i] = R(0);
+    qp[3] = a.pr.T_ambient;
+  }
+  const Mixt<R> m = mixt_var<R, NS>(a.pr, qp, false);
+  double* o = aos + c * nf;
+  const R h = qp[0];
+  o[0] = (double)h;
+  o[1] = (double)qp[nv];
+  o[2] = (double)qp[nv + 1];
+  o[3] = (double)qp[3];
+  for (int i = 0; i < NS; ++i) o[4 + i] = (h > R(0)) ? (double)(a.pr.alpha ? qp[4 + i] : qp[4 + i] / h) : 0.0;
+  o[4 + NS] = (double)m.rho_m;
+  o[5 + NS] = (double)m.red_grav;
+  o[6 + NS] = (double)m.Ri;
+}
+
 // initial maxima after the initial check_solve(.TRUE.) (IMEX_SfloW2D.f90:307-368)
 template <class R, int NS>
 __global__ void k_init_maps(KArgs<R> a) {
@@ -119,6 +150,11 @@ static cudaError_t tab_qp(const KArgs<R>& a, unsigned blocks, cudaStream_t s, do
   return cudaGetLastError();
 }
 template <class R, int NS>
+static cudaError_t tab_phys(const KArgs<R>& a, unsigned blocks, cudaStream_t s, double* out) {
+  k_phys_to_aos<R, NS><<<blocks, 256, 0, s>>>(a, out);
+  return cudaGetLastError();
+}
+template <class R, int NS>
 static cudaError_t tab_stats(const KArgs<R>& a, int blocks, cudaStream_t s, double* part) {
   k_stats_partial<R, NS><<<blocks, 256, 0, s>>>(a, part);
   return cudaGetLastError();
@@ -179,6 +215,7 @@ KernelTable<R> make_table() {
   t.assemble = &tab_assemble<R, NS>;
   t.init_maps = &tab_init_maps<R, NS>;
   t.qp = &tab_qp<R, NS>;
+  t.phys = &tab_phys<R, NS>;
   t.stats = &tab_stats<R, NS>;
   t.set_smem = &tab_smem<R, NS>;
   t.b_setup = &tab_b_setup<R, NS>;

@@ -61,6 +61,8 @@ struct Grid {
   R cfl_dx, cfl_dy;
   int limiter[kMaxVars + 2];
   double cfl, max_dt;
+  int dry_bc;       // every boundary condition is (Neumann, 0): a dry inside keeps dry ghosts
+  int pad;
 };
 
 // Device-resident run state (one per domain).

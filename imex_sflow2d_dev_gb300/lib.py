@@ -9,7 +9,7 @@ import os
 
 import numpy as np
 
-from .params import SflowParams, SflowStepStats
+from .params import SflowParams, SflowRunInfo, SflowStepStats
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libsflow_gb300.so")
@@ -69,6 +69,20 @@ def load(build_if_missing=True):
         "sflow_log_sums_noalloc_error": (C.c_char_p, []),
         "sflow_host_geometry": (C.c_int, [P, dp, i32, dp]),
         "sflow_host_scalars": (C.c_int, [P, dp, dp]),
+        "sflow_io_error": (C.c_char_p, []),
+        "sflow_read_input": (C.c_int, [C.c_char_p, P, C.POINTER(SflowRunInfo)]),
+        "sflow_read_dem": (C.c_int, [C.c_char_p, P, dp, C.POINTER(C.c_uint8)]),
+        "sflow_read_q2d": (C.c_int, [C.c_char_p, P, dp, C.POINTER(i32)]),
+        "sflow_write_q2d": (C.c_int, [C.c_char_p, P, dp]),
+        "sflow_write_p2d": (C.c_int, [C.c_char_p, P, dp, dp, dp, dp, dp, dp]),
+        "sflow_write_restart": (C.c_int, [C.c_char_p, P, C.c_double, C.c_double, dp, dp, dp, dp, dp, dp]),
+        "sflow_read_restart": (C.c_int, [C.c_char_p, P, dp, dp, dp, dp, dp, dp, dp, dp]),
+        "sflow_output_name": (C.c_int, [C.c_char_p, i32, C.c_char_p, C.c_char_p, i32]),
+        "sflow_download_phys": (C.c_int, [vp, dp]),
+        "sflow_download_deposit": (C.c_int, [vp, dp]),
+        "sflow_upload_deposit": (C.c_int, [vp, dp]),
+        "sflow_upload_maps": (C.c_int, [vp, dp, dp, dp]),
+        "sflow_set_output_time": (C.c_int, [vp, C.c_double]),
         "sflow_batch_create": (C.c_int, [i32, i32, i64, C.POINTER(vp)]),
         "sflow_batch_destroy": (None, [vp]),
         "sflow_batch_submit": (C.c_int, [vp, P, dp, dp, i64, C.POINTER(i32)]),
@@ -99,7 +113,11 @@ def exported_symbols():
             "sflow_log_sums_noalloc", "sflow_log_sums_noalloc_error", "sflow_batch_create",
             "sflow_batch_destroy", "sflow_batch_submit", "sflow_batch_advance", "sflow_batch_poll",
             "sflow_batch_counters", "sflow_batch_download", "sflow_batch_collect",
-            "sflow_batch_live", "sflow_batch_launch_count"]
+            "sflow_batch_live", "sflow_batch_launch_count", "sflow_io_error", "sflow_read_input",
+            "sflow_read_dem", "sflow_read_q2d", "sflow_write_q2d", "sflow_write_p2d",
+            "sflow_write_restart", "sflow_read_restart", "sflow_output_name",
+            "sflow_download_phys", "sflow_download_deposit", "sflow_upload_deposit",
+            "sflow_upload_maps", "sflow_set_output_time"]
 
 
 def log_sums_noalloc(params, q_dev_ptr, sums_dev_ptr, stream_ptr=0):
@@ -135,7 +153,93 @@ def host_scalars(params, B_cent):
 
 
 def _dp(a):
-    return a.ctypes.data_as(C.POINTER(C.c_double))
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _io_check(rc):
+    if rc < 0:
+        raise SflowError(rc, _lib.sflow_io_error().decode())
+    return rc
+
+
+def _path(p):
+    return os.fsencode(p)
+
+
+# --- host I/O of the reference's files (no GPU needed) ----------------------
+def read_input(path):
+    """IMEX_SfloW2D.inp -> (SflowParams, run info dict)."""
+    lib = load()
+    p = SflowParams()
+    r = SflowRunInfo()
+    _io_check(lib.sflow_read_input(_path(path), C.byref(p), C.byref(r)))
+    run = {f: getattr(r, f) for f, _ in SflowRunInfo._fields_ if f != "pad"}
+    for k in ("run_name", "restart_file", "topography_file"):
+        run[k] = run[k].decode()
+    return p, run
+
+
+def read_dem(path, params):
+    """ESRI ASCII DEM -> (B_cent (ny, nx), nodata mask (ny, nx) bool)."""
+    lib = load()
+    nx, ny = params.comp_cells_x, params.comp_cells_y
+    B = np.empty(nx * ny)
+    nd = np.zeros(nx * ny, dtype=np.uint8)
+    _io_check(lib.sflow_read_dem(_path(path), C.byref(params), _dp(B),
+                                 nd.ctypes.data_as(C.POINTER(C.c_uint8))))
+    return B.reshape(ny, nx), nd.reshape(ny, nx).astype(bool)
+
+
+def read_q2d(path, params):
+    """.q_2d restart -> (q in reference layout (flat), output index)."""
+    lib = load()
+    q = np.empty(params.n_vars * params.comp_cells_x * params.comp_cells_y)
+    idx = C.c_int32(0)
+    _io_check(lib.sflow_read_q2d(_path(path), C.byref(params), _dp(q), C.byref(idx)))
+    return q, idx.value
+
+
+def write_q2d(path, params, q_aos):
+    """Writes .q_2d; like the reference, zeroes |q| < 1e-20 in q_aos itself."""
+    lib = load()
+    if q_aos.dtype != np.float64 or not q_aos.flags.c_contiguous:
+        raise ValueError("q_aos must be a contiguous float64 array")
+    _io_check(lib.sflow_write_q2d(_path(path), C.byref(params), _dp(q_aos)))
+
+
+def write_p2d(path, params, phys, B_cent, deposit, hmax, pdynmax, mod_vel_max):
+    lib = load()
+    arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) if a is not None else None
+            for a in (phys, B_cent, deposit, hmax, pdynmax, mod_vel_max)]
+    _io_check(lib.sflow_write_p2d(_path(path), C.byref(params), *[_dp(a) for a in arrs]))
+
+
+def write_restart(path, params, t, dt, q_aos, B_cent, deposit, hmax, pdynmax, mod_vel_max):
+    lib = load()
+    arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) if a is not None else None
+            for a in (q_aos, B_cent, deposit, hmax, pdynmax, mod_vel_max)]
+    _io_check(lib.sflow_write_restart(_path(path), C.byref(params), float(t), float(dt),
+                                      *[_dp(a) for a in arrs]))
+
+
+def read_restart(path, params):
+    lib = load()
+    nx, ny, nv, ns = params.comp_cells_x, params.comp_cells_y, params.n_vars, params.n_solid
+    N = nx * ny
+    t, dt = C.c_double(), C.c_double()
+    q, B, dep = np.empty(N * nv), np.empty(N), np.empty(N * ns)
+    h, pd, v = np.empty(N), np.empty(N), np.empty(N)
+    _io_check(lib.sflow_read_restart(_path(path), C.byref(params), C.byref(t), C.byref(dt), _dp(q),
+                                     _dp(B), _dp(dep), _dp(h), _dp(pd), _dp(v)))
+    return {"t": t.value, "dt": dt.value, "q": q, "B_cent": B.reshape(ny, nx), "deposit": dep,
+            "hmax": h, "pdynmax": pd, "mod_vel_max": v}
+
+
+def output_name(run_name, index, ext):
+    lib = load()
+    buf = C.create_string_buffer(512)
+    _io_check(lib.sflow_output_name(run_name.encode(), index, ext.encode(), buf, 512))
+    return buf.value.decode()
 
 
 def _check(rc):
@@ -275,6 +379,30 @@ class Solver:
 
     def launch_count(self):
         return self.lib.sflow_launch_count(self.h)
+
+    def download_phys(self):
+        """Per cell h, u, v, T, alphas, rho_m, red_grav, Ri (the .p_2d fields)."""
+        nx, ny = self.p.comp_cells_x, self.p.comp_cells_y
+        out = np.empty(nx * ny * (7 + self.p.n_solid))
+        _check(self.lib.sflow_download_phys(self.h, _dp(out)))
+        return out
+
+    def download_deposit(self):
+        out = np.empty(self.p.comp_cells_x * self.p.comp_cells_y * self.p.n_solid)
+        _check(self.lib.sflow_download_deposit(self.h, _dp(out)))
+        return out
+
+    def upload_deposit(self, dep):
+        d = np.ascontiguousarray(dep, dtype=np.float64).reshape(-1)
+        _check(self.lib.sflow_upload_deposit(self.h, _dp(d)))
+
+    def upload_maps(self, hmax=None, pdynmax=None, mod_vel_max=None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) if a is not None else None
+                for a in (hmax, pdynmax, mod_vel_max)]
+        _check(self.lib.sflow_upload_maps(self.h, *[_dp(a) for a in arrs]))
+
+    def set_output_time(self, t_output):
+        _check(self.lib.sflow_set_output_time(self.h, float(t_output)))
 
     def device_bytes(self):
         return self.lib.sflow_device_bytes(self.h)

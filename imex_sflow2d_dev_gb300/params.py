@@ -90,6 +90,48 @@ class SflowParams(C.Structure):
                 self.bc[s][i].value = value
 
 
+def params_to_dict(p):
+    """Plain-Python copy of SflowParams (arrays as lists, BCs as
+    [side][var] = [flag, value])."""
+    out = {}
+    for name, _ in SflowParams._fields_:
+        v = getattr(p, name)
+        if name == "bc":
+            out[name] = [[[v[s][i].flag, v[s][i].value] for i in range(MAX_VARS)] for s in range(4)]
+        elif hasattr(v, "__len__"):
+            out[name] = list(v)
+        else:
+            out[name] = v
+    return out
+
+
+def params_from_dict(d):
+    p = SflowParams()
+    for name, _ in SflowParams._fields_:
+        v = d[name]
+        if name == "bc":
+            for s in range(4):
+                for i in range(MAX_VARS):
+                    p.bc[s][i].flag, p.bc[s][i].value = int(v[s][i][0]), float(v[s][i][1])
+        elif isinstance(v, list):
+            arr = getattr(p, name)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(p, name, v)
+    return p
+
+
+class SflowRunInfo(C.Structure):
+    _fields_ = [
+        ("run_name", C.c_char * 128), ("restart_file", C.c_char * 256),
+        ("topography_file", C.c_char * 256), ("restart", C.c_int32),
+        ("output_cons_flag", C.c_int32), ("output_phys_flag", C.c_int32),
+        ("output_esri_flag", C.c_int32), ("output_netcdf_flag", C.c_int32),
+        ("output_runout_flag", C.c_int32), ("verbose_level", C.c_int32), ("pad", C.c_int32),
+    ]
+
+
 class SflowStepStats(C.Structure):
     _fields_ = [
         ("t", C.c_double), ("dt", C.c_double), ("mass", C.c_double),

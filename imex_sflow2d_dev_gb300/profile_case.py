@@ -1,8 +1,14 @@
 """A short run of the pyroclastic workload for profilers (ncu).
 
     python -m imex_sflow2d_dev_gb300.profile_case --n 2048 --steps 6 --precision fp32
+    python -m imex_sflow2d_dev_gb300.profile_case --ensemble 256 --steps 64
 
-Builds the n x n version of the benchmark workload (cone + fBm DEM with
+--ensemble N: the first N members of the batched ensemble (side
+log-uniform in [128, 1024], own DEM and parameters) submitted to one batch
+and advanced `steps` batch steps (FP32 bulk form), for a launch list of the
+batched kernels.
+
+Otherwise: builds the n x n version of the benchmark workload (cone + fBm DEM with
 dx = 10240/n m, seeded developed-current state), uploads it and runs
 `steps` driver iterations one at a time (no graph, so every kernel is a
 separate launch).  With n = 2048 the FP32 working set (~400 MB) exceeds the
@@ -20,7 +26,18 @@ def main():
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--ensemble", type=int, default=0)
     a = ap.parse_args()
+    if a.ensemble > 0:
+        members = [W.ensemble_params(i, PREC_FP32, 100000) for i in range(a.ensemble)]
+        cells = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members)
+        b = lib.Batch(PREC_FP32, max_runs=a.ensemble, max_cells=int(cells * 1.2) + 4096)
+        ids = [b.submit(p, B, W.to_aos(q), max_steps=st) for p, B, q, st in members]
+        b.advance(a.steps)
+        cu = sum(b.counters(i)["cell_updates"] for i in ids)
+        print(f"ensemble runs={a.ensemble} cells={cells} steps={a.steps} cell_updates={cu}")
+        b.close()
+        return
     prec = PREC_FP32 if a.precision == "fp32" else PREC_FP64
     p, B, _ = W.pyroclastic(nx=a.n, ny=a.n, dx=10240.0 / a.n, settling=False, precision=prec,
                             t_end=1.0e9)

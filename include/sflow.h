@@ -316,6 +316,85 @@ int sflow_batch_collect(sflow_batch* b, int32_t run_id, double* q_aos);
 int32_t sflow_batch_live(const sflow_batch* b);
 int64_t sflow_batch_launch_count(const sflow_batch* b);
 
+/*
+ * Host I/O of the reference's files (host only, no GPU needed), so a run
+ * keeps its input file, restart files and output formats.  Errors:
+ * sflow_io_error().
+ *
+ * sflow_read_input   IMEX_SfloW2D.inp -> p (from the init_param defaults,
+ *                    inpout_2d.f90:408-970) and run; the namelists and
+ *                    boundary-condition rules of read_param (986-5134) for
+ *                    the subset the GPU path runs; any key that would switch
+ *                    on physics outside it is rejected with its line.  A
+ *                    restart is required (RESTART = T).  RESTART_FILE is
+ *                    accepted as RESTART_FILES(1): the reference's TESTS
+ *                    inputs use that name, which the current reference
+ *                    namelist no longer declares.
+ * sflow_read_dem     ESRI ASCII DEM -> B_cent(nx,ny) at the cell centres
+ *                    (bilinear, values clipped at 0) and the no-data mask
+ *                    (1 where a surrounding DEM value is NODATA_value);
+ *                    nodata may be NULL (inpout_2d.f90:3684-3760,
+ *                    geometry_2d.f90:312-350, 1395-1517)
+ * sflow_read_q2d     .q_2d restart -> q (reference layout), cells with
+ *                    q(1) <= 0 zeroed, negative solids zeroed; the output
+ *                    index of the file name (inpout_2d.f90:5674-5722)
+ * sflow_write_q2d    .q_2d output (inpout_2d.f90:6000-6110); like the
+ *                    reference it sets |q| < 1e-20 to zero in q itself
+ * sflow_write_p2d    .p_2d output (inpout_2d.f90:6124-6400) from the
+ *                    per-cell fields of sflow_download_phys, B_cent, the
+ *                    deposit (may be NULL: zeros) and the maxima maps
+ * sflow_write_restart / sflow_read_restart
+ *                    restart.bin (inpout_2d.f90:8037-8179), Fortran
+ *                    unformatted sequential records with 4-byte markers;
+ *                    q records above 2 GiB are refused (SFLOW_ERANGE)
+ * sflow_output_name  RUN_NAME_dddd.ext (lettera, inpout_2d.f90:6893-6912)
+ */
+typedef struct {
+  char run_name[128];
+  char restart_file[256];
+  char topography_file[256];
+  int32_t restart;
+  int32_t output_cons_flag, output_phys_flag, output_esri_flag, output_netcdf_flag, output_runout_flag;
+  int32_t verbose_level;
+  int32_t pad;
+} SflowRunInfo;
+
+const char* sflow_io_error(void);
+int sflow_read_input(const char* path, SflowParams* p, SflowRunInfo* run);
+int sflow_read_dem(const char* path, const SflowParams* p, double* B_cent, uint8_t* nodata);
+int sflow_read_q2d(const char* path, const SflowParams* p, double* q_aos, int32_t* output_idx);
+int sflow_write_q2d(const char* path, const SflowParams* p, double* q_aos);
+int sflow_write_p2d(const char* path, const SflowParams* p, const double* phys, const double* B_cent,
+                    const double* deposit, const double* hmax, const double* pdynmax, const double* mod_vel_max);
+int sflow_write_restart(const char* path, const SflowParams* p, double t, double dt, const double* q_aos,
+                        const double* B_cent, const double* deposit, const double* hmax, const double* pdynmax,
+                        const double* mod_vel_max);
+int sflow_read_restart(const char* path, const SflowParams* p, double* t, double* dt, double* q_aos, double* B_cent,
+                       double* deposit, double* hmax, double* pdynmax, double* mod_vel_max);
+int sflow_output_name(const char* run_name, int32_t index, const char* ext, char* out, int32_t out_len);
+
+/*
+ * Device-side fields for the writers and for restarts:
+ *   sflow_download_phys     per cell (reference order) h, u, v, T,
+ *                           alphas(1:n_solid), rho_m, red_grav, Ri: the
+ *                           qc_to_qp and mixt_var values output_solution
+ *                           writes (7 + n_solid doubles per cell)
+ *   sflow_download_deposit  deposit(1:nx,1:ny,1:n_solid), the accumulated
+ *                           dt * deposition of update_erosion_deposition_cell
+ *                           (solver_2d.f90:2476); zeros without settling
+ *   sflow_upload_deposit    sets it (restart.bin)
+ *   sflow_upload_maps       sets hmax, pdynmax, mod_vel_max (restart.bin);
+ *                           a NULL map is left unchanged
+ *   sflow_set_output_time   the next output time t_output that the dt clamp
+ *                           stops at (IMEX_SfloW2D.f90:417-422); the reference
+ *                           sets t_output = t + dt_output after each output
+ */
+int sflow_download_phys(sflow_handle* h, double* out);
+int sflow_download_deposit(sflow_handle* h, double* out);
+int sflow_upload_deposit(sflow_handle* h, const double* in);
+int sflow_upload_maps(sflow_handle* h, const double* hmax, const double* pdynmax, const double* mod_vel_max);
+int sflow_set_output_time(sflow_handle* h, double t_output);
+
 /* Build information ("fp64+fp32 sm_103a ..."). */
 const char* sflow_build_info(void);
 

@@ -32,6 +32,7 @@ def _load():
         getattr(lib, "sflow_oracle_" + f).argtypes = [vp, dp]
     lib.sflow_oracle_get_maps.argtypes = [vp, dp, dp, dp]
     lib.sflow_oracle_get_mask.argtypes = [vp, C.POINTER(C.c_uint8)]
+    lib.sflow_oracle_get_deposit.argtypes = [vp, dp]
     lib.sflow_oracle_get_geometry.argtypes = [vp, ip, dp]
     lib.sflow_oracle_stats.argtypes = [vp, vp]
     lib.sflow_oracle_time.restype = C.c_double
@@ -135,6 +136,12 @@ class Oracle:
         a = [np.empty(self.nx * self.ny) for _ in range(3)]
         self.lib.sflow_oracle_get_maps(self.h, *[_dp(x) for x in a])
         return a
+
+    def deposit(self):
+        """deposit(1:nx,1:ny,1:n_solid), column-major (class slowest)."""
+        out = np.empty(self.nx * self.ny * (self.nv - 4))
+        self.lib.sflow_oracle_get_deposit(self.h, _dp(out))
+        return out
 
     def mask(self):
         m = np.empty(self.nx * self.ny, dtype=np.uint8)

@@ -2089,6 +2089,11 @@ void sflow_oracle_get_maps(const oracle_t* o, double* hmax, double* pdynmax, dou
   memcpy(mvmax, o->mod_vel_max, sizeof(double) * o->N);
 }
 void sflow_oracle_get_mask(const oracle_t* o, unsigned char* m) { memcpy(m, o->mask, o->N); }
+/* deposit(1:nx,1:ny,1:n_solid), column-major (class slowest) */
+void sflow_oracle_get_deposit(const oracle_t* o, double* out) {
+  for (int i = 0; i < o->P.ns; ++i)
+    for (size_t c = 0; c < (size_t)o->N; ++c) out[(size_t)i * o->N + c] = o->deposit[c * MAXS + i];
+}
 
 /* which: 0 Bx_geom 1 By_geom 2 Bxx 3 Bxy 4 Byy 5 grav_coeff 6 dgc/dx 7 dgc/dy
  * 8 arc_perim 9 arc_nx 10 arc_ny 11 source_cell 12 src flags (E|W<<1|N<<2|S<<3) */

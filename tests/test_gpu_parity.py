@@ -314,3 +314,16 @@ def test_other_tableaux_refuse_per_call_site_entry_points():
     with pytest.raises(Exception):
         s.timestep()
     assert s.step() == 0
+
+
+def test_fp64_dam_break_dry_bed_is_bitwise_equal():
+    """Dam break onto a dry bed: the wet/dry front crosses tiles whose halo is
+    dry (zero-flux fast path) and faces with dry stencils; no Newton, so the
+    FP64 form must equal the oracle bit for bit."""
+    p, B, _ = W.dam_break(nx=96, ny=40, t_end=100.0)
+    x = (np.arange(96) + 0.5) * p.cell_size
+    h = np.where(x[None, :] < 30.0, 1.0, 0.0) * np.ones((40, 1))
+    q = W.rest_state_q(p, h, 300.0, [0.0])
+    o, s = run_pair(p, B, q, 60)
+    assert s.stats().status == 0
+    np.testing.assert_array_equal(s.download_q(), o.q())
