@@ -315,6 +315,41 @@ def form_errors(lib, p, B, q, steps):
     return out
 
 
+def large_leg(lib, n, steps, warmup):
+    """Large single domain: n x n cells, dx = 2 m, diamond-square DEM
+    (Hurst 0.8, relief 2000 m, seed 5), 3 particle classes (1e-5, 1e-4,
+    1e-3 m), entrainment and settling on, one ring inlet, from a seeded
+    developed current of radius 3.5 km (workloads.large_domain).  The
+    working set (~12 GB in FP32) is far larger than L2, so steps are timed
+    back to back; the plain FP64 form is timed beside it on fewer steps and
+    the FP32-vs-FP64 errors are taken after `steps` steps."""
+    ts = time.perf_counter()
+    p32, B, _ = W.large_domain(n=n, precision=PREC_FP32)
+    q = W.developed_current_state(p32, B, radius=min(3500.0, 0.2 * n * p32.cell_size))
+    qa = W.to_aos(q)
+    del q
+    print(f"[bench] large inputs {n}x{n}: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
+    out = {"cells": n * n, "steps": steps, "workload":
+           f"{n}x{n} dx=2m diamond-square DEM, 3 classes, entrainment + settling, ring inlet, developed current"}
+    for name, prec, nst in (("fp32", PREC_FP32, steps), ("fp64_plain", PREC_FP64, max(steps // 5, 2))):
+        pp = p32.copy()
+        pp.precision = prec
+        s = lib.Solver(pp, B)
+        s.upload_q(qa)
+        s.advance(max_steps=warmup)
+        c0 = s.counters()
+        ms = s.advance_timed(nst, flush_l2=False)
+        c1 = s.counters()
+        cu = c1["cell_updates"] - c0["cell_updates"]
+        out[name] = {"value": cu / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / nst, "steps": nst,
+                     "active_cells_per_step": cu / nst}
+        s.close()
+    out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64_plain"]["value"]
+    out["error_vs_fp64"] = {"steps": steps, **form_errors(lib, p32, B, W.from_aos(qa, p32.n_vars, n, n), steps)}
+    print(f"[bench] large done: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
+    return out
+
+
 def served_leg(lib, n_requests, rate):
     """Served solves: Poisson arrivals (mean `rate` per s) of dam-break and
     ring-inlet jobs (side log-uniform in [64, 2048], 1-3 classes, 500-5000
@@ -451,6 +486,9 @@ def run_gb300(args, d):
         pe, Be, qe, _ = W.ensemble_params(0, PREC_FP32, 300)
         ens["error_vs_fp64"] = {"member": 0, "side": pe.comp_cells_x, "steps": 300,
                                 **form_errors(lib, pe, Be, qe, 300)}
+    large = None
+    if d.rank == 0 and args.large_n > 0:
+        large = large_leg(lib, args.large_n, args.large_steps, args.warmup)
     srv = None
     if d.rank == 0 and args.served_requests > 0:
         srv, recs = served_leg(lib, args.served_requests, args.served_rate)
@@ -486,6 +524,7 @@ def run_gb300(args, d):
             "gpu_launches": r32["launches"],
             "ensemble": ens,
             "served": srv,
+            "large_domain": large,
             "clocks": clk,
             "wall_s_timed_region": t_wall1 - t_wall0,
         }
@@ -507,6 +546,8 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=2000)
     ap.add_argument("--served-requests", type=int, default=24)
     ap.add_argument("--served-rate", type=float, default=20.0)
+    ap.add_argument("--large-n", type=int, default=8192)
+    ap.add_argument("--large-steps", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -82,6 +82,14 @@ class Batch : public BatchBase {
     br.live = 1;
     br.max_dt = hs.p.max_dt;
     const KArgs<R> ka = sv->kargs();
+    if (ka.g.lim_all != 1 && g->lim == 1) {
+      // the group needs the generic limiter kernel from now on: re-capture
+      g->lim = -1;
+      if (g->graph_exec) cudaGraphExecDestroy(g->graph_exec);
+      if (g->graph) cudaGraphDestroy(g->graph);
+      g->graph_exec = nullptr;
+      g->graph = nullptr;
+    }
     if (g->smem_flux < sv->smem_flux()) { err_ = "flux shared memory mismatch"; cudaFree(cand); return SFLOW_EINVAL; }
     // the batch stream is idle here (every advance ends synchronised)
     if (cudaMemcpy(g->d_args + slot, &ka, sizeof(ka), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -122,7 +130,7 @@ class Batch : public BatchBase {
         left -= kChunk;
       }
       for (; left > 0; --left) {
-        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux);
+        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux, g->lim);
         if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
         g->launches += 5;
       }
@@ -258,6 +266,7 @@ class Batch : public BatchBase {
     BatchArgs<R> args;
     int grids[4] = {0, 0, 0, 0};
     size_t smem_flux = 0;
+    int lim = 1;   // 1 while every submitted run uses minmod everywhere, else -1
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<Slot> slots;
@@ -268,7 +277,7 @@ class Batch : public BatchBase {
       cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
       for (int i = 0; i < kChunk; ++i) {
-        e = tab.b_step(args, stream, grids, smem_flux);
+        e = tab.b_step(args, stream, grids, smem_flux, lim);
         if (e != cudaSuccess) {
           cudaGraph_t g0 = nullptr;
           cudaStreamEndCapture(stream, &g0);

@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(TX* TY) k_b_mask(BatchArgs<R> b) {
 
 // 3 blocks per SM (27 warps): without the bound the persistent loop keeps
 // loop-invariant values of the tile body live and needs ~120 registers
-template <class R, int NS>
+template <class R, int NS, int LIM>
 __global__ void __launch_bounds__(FLUX_THREADS, 3) k_b_flux(BatchArgs<R> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(FLUX_THREADS, 3) k_b_flux(BatchArgs<R> b) {
     }
     if (!running(a.st)) continue;
     const int tiles_x = (a.g.nx + TX - 1) / TX;
-    flux_tile<R, NS>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
+    flux_tile<R, NS, LIM>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
                      smem_raw);
   }
 }

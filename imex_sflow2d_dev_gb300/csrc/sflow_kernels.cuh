@@ -225,12 +225,13 @@ __device__ __forceinline__ float maxmod_f(float a, float b) {
   return 0.5f * (copysignf(1.0f, a) + copysignf(1.0f, b)) * fmaxf(fabsf(a), fabsf(b));
 }
 
-template <class R>
+template <class R, int LIM>
 __device__ __forceinline__ R slope(R v0, R v1, R v2, const Spacing<R>& s, int lim, R theta) {
   if constexpr (sizeof(R) == 8) {
-    return limit(v0, v1, v2, s.z0, s.z1, s.z2, lim, theta);
+    return limit<R, LIM>(v0, v1, v2, s.z0, s.z1, s.z2, lim, theta);
   } else {
     const float a = (v2 - v1) * s.r12, b = (v1 - v0) * s.r01;
+    if constexpr (LIM >= 0) lim = LIM;
     switch (lim) {
       case 0: return 0.0f;
       case 1: return minmod_f(a, b);
@@ -254,7 +255,7 @@ __device__ __forceinline__ R slope(R v0, R v1, R v2, const Spacing<R>& s, int li
 // reference's use of y_stag in the x slope of v at ring cells with a ring
 // face to the north only (solver_2d.f90:3605, kept as is).
 // ---------------------------------------------------------------------------
-template <class R, int NS, int DIR>
+template <class R, int NS, int DIR, int LIM>
 __device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, const uint8_t* sfl,
                                            int rx, int ry, int j, int k, int plus, R* out) {
   constexpr int nv = 4 + NS, np = nv + 2;
@@ -308,19 +309,19 @@ __device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, cons
     const int bl = a.bc.flag[side_lo][i], bh = a.bc.flag[side_hi][i];
     R sl;
     if (b0) {
-      if (DIR == 1 && sc == 2) sl = slope(cell[i], v1, QP(i, 1), sp, g.limiter[i], g.theta);
-      else if (bl == 0) sl = slope(a.bc.value[side_lo][i], v1, QP(i, 1), sp, g.limiter[i], g.theta);
+      if (DIR == 1 && sc == 2) sl = slope<R, LIM>(cell[i], v1, QP(i, 1), sp, g.limiter[i], g.theta);
+      else if (bl == 0) sl = slope<R, LIM>(a.bc.value[side_lo][i], v1, QP(i, 1), sp, g.limiter[i], g.theta);
       else if (bl == 1) sl = a.bc.value[side_lo][i];
       else sl = (QP(i, 1) - QP(i, 0)) * inv_d;
     } else if (b1) {
-      if (DIR == 1 && sc == 2) sl = slope(QP(i, -1), v1, cell[i], sp, g.limiter[i], g.theta);
-      else if (bh == 0) sl = slope(QP(i, -1), v1, a.bc.value[side_hi][i], sp, g.limiter[i], g.theta);
+      if (DIR == 1 && sc == 2) sl = slope<R, LIM>(QP(i, -1), v1, cell[i], sp, g.limiter[i], g.theta);
+      else if (bh == 0) sl = slope<R, LIM>(QP(i, -1), v1, a.bc.value[side_hi][i], sp, g.limiter[i], g.theta);
       else if (bh == 1) sl = a.bc.value[side_hi][i];
       else sl = (QP(i, 0) - QP(i, -1)) * inv_d;
     } else {
       R v0 = QP(i, -1), v2 = QP(i, 1);
       if (src2) { if (use_hi) v2 = cell[i]; else if (use_lo) v0 = cell[i]; }
-      sl = slope(v0, v1, v2, sp, g.limiter[i], g.theta);
+      sl = slope<R, LIM>(v0, v1, v2, sp, g.limiter[i], g.theta);
     }
     const R dq = g.rc * d2 * sl;
     R l_ = v1 - dq, h_ = v1 + dq;
@@ -360,7 +361,7 @@ __device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, cons
       v2 = QP(i, 1);
       if (src2) { if (use_hi) v2 = cell[i]; else if (use_lo) v0 = cell[i]; }
     }
-    const R sl = slope(v0, v1, v2, (m == 1) ? spv : sp, g.limiter[i], g.theta);
+    const R sl = slope<R, LIM>(v0, v1, v2, (m == 1) ? spv : sp, g.limiter[i], g.theta);
     const R dq = g.rc * d2 * sl;
     R val = plus ? v1 + dq : v1 - dq;
     if (b0 && !plus) val = ul;
@@ -382,6 +383,7 @@ struct Side {
   R f[4 + NS];
   R vmin, vmax;
   R hu_p;   // qp(2): x zero-velocity test
+  R un;     // upwind test of eval_flux_UP: qp u (x faces) or q hv (y faces)
 };
 
 template <class R, int NS, int DIR>
@@ -394,13 +396,39 @@ __device__ __forceinline__ void side_from_qp(const KArgs<R>& a, const R* qp, R g
   local_speeds<R, NS>(P, qp, m.red_grav, gcs, DIR, s.vmin, s.vmax);
   eval_fluxes<R, NS>(P, s.q, qp, m, gcs, DIR, s.f);
   s.hu_p = qp[1];
+  s.un = (DIR == 1) ? qp[4 + NS] : s.q[2];
 }
 
 template <class R, int NS>
 __device__ __forceinline__ void side_zero(Side<R, NS>& s) {
 #pragma unroll
   for (int i = 0; i < 4 + NS; ++i) { s.q[i] = R(0); s.f[i] = R(0); }
-  s.vmin = R(0); s.vmax = R(0); s.hu_p = R(0);
+  s.vmin = R(0); s.vmax = R(0); s.hu_p = R(0); s.un = R(0);
+}
+
+// Upwind flux (solver_2d.f90:2705-2821, SOLVER_SCHEME = 'UP'): the side the
+// normal velocity comes from, or the mean; on y faces with zero hv on both
+// sides the mass, energy and solid fluxes are zero.  (The x counterpart of
+// that test reads q_interfaceL(n_vars+1), past the conservative vector, and
+// is not reproduced.)  The local speeds still give the CFL bound.
+template <class R, int NS, int DIR>
+__device__ __forceinline__ R up_flux(const Side<R, NS>& L, const Side<R, NS>& Rt, R* H) {
+  constexpr int nv = 4 + NS;
+  const R ul = L.un, ur = Rt.un;
+#pragma unroll
+  for (int i = 0; i < nv; ++i) {
+    if (ul > R(0) && ur >= R(0)) H[i] = L.f[i];
+    else if (ul <= R(0) && ur < R(0)) H[i] = Rt.f[i];
+    else H[i] = cst<R>(0.5) * (L.f[i] + Rt.f[i]);
+  }
+  if (DIR == 2 && ul == R(0) && ur == R(0)) {
+    H[0] = R(0);
+#pragma unroll
+    for (int i = 3; i < nv; ++i) H[i] = R(0);
+  }
+  const R a1 = rmin(rmin(L.vmin, Rt.vmin), R(0));
+  const R a2 = rmax(rmax(L.vmax, Rt.vmax), R(0));
+  return rmax(a2, -a1);
 }
 
 // KT flux across one face (solver_2d.f90:2834-3049).  H has n_vars entries.
@@ -457,7 +485,7 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
 // reconstruction of both sides, the domain-edge copies and the wall mirror
 // at ring-inlet faces (solver_2d.f90:3716-3920), KT flux.  Returns the
 // largest |speed| at the face (a_interface_*_max).
-template <class R, int NS, int DIR>
+template <class R, int NS, int DIR, int LIM>
 __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const uint8_t* sfl, int f,
                                        int o, int rxl, int ryl, int rxh, int ryh, R gcs, R* H) {
   constexpr int nv = 4 + NS, np = nv + 2;
@@ -475,8 +503,8 @@ __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const ui
   bool hl = false, hh = false;
   const int jl = (DIR == 1) ? f - 1 : o, kl = (DIR == 1) ? o : f - 1;
   const int jh = (DIR == 1) ? f : o, kh = (DIR == 1) ? o : f;
-  if (f > 0 && actl) { recon_side<R, NS, DIR>(a, sqp, sfl, rxl, ryl, jl, kl, 1, qpl); hl = true; }
-  if (f < n && acth && !mirror_h) { recon_side<R, NS, DIR>(a, sqp, sfl, rxh, ryh, jh, kh, 0, qph); hh = true; }
+  if (f > 0 && actl) { recon_side<R, NS, DIR, LIM>(a, sqp, sfl, rxl, ryl, jl, kl, 1, qpl); hl = true; }
+  if (f < n && acth && !mirror_h) { recon_side<R, NS, DIR, LIM>(a, sqp, sfl, rxh, ryh, jh, kh, 0, qph); hh = true; }
   if (f == 0) {
 #pragma unroll
     for (int i = 0; i < np; ++i) qpl[i] = qph[i];
@@ -504,6 +532,7 @@ __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const ui
   else side_zero(L);
   if (hh) side_from_qp<R, NS, DIR>(a, qph, gcs, Hs, mirror_h);
   else side_zero(Hs);
+  if (a.pr.scheme == SFLOW_SCHEME_UP) return up_flux<R, NS, DIR>(L, Hs, H);
   return kt_flux<R, NS, DIR>(L, Hs, H);
 }
 
@@ -515,7 +544,7 @@ __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const ui
 // shared memory; each thread then evaluates one face (both reconstructed
 // sides, speeds, physical fluxes, KT flux) and finally one cell.
 // ---------------------------------------------------------------------------
-template <class R, int NS>
+template <class R, int NS, int LIM>
 __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict__ qin,
                                           R* __restrict__ rout, int want_dt, int tx, int ty,
                                           unsigned char* smem_raw) {
@@ -603,7 +632,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
       if (f == 0) gcs = __ldg(a.geo[5] + ch);
       else if (f == g.nx) gcs = __ldg(a.geo[5] + cl);
       else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cl) + __ldg(a.geo[5] + ch));
-      amax = face_flux<R, NS, 1>(a, sqp, sfl, f, k, rxl, ry, rxh, ry, gcs, H);
+      amax = face_flux<R, NS, 1, LIM>(a, sqp, sfl, f, k, rxl, ry, rxh, ry, gcs, H);
     } else {
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = R(0);
@@ -634,7 +663,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
       if (f == 0) gcs = __ldg(a.geo[5] + ch);
       else if (f == g.ny) gcs = __ldg(a.geo[5] + cl);
       else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cl) + __ldg(a.geo[5] + ch));
-      amax = face_flux<R, NS, 2>(a, sqp, sfl, f, j, rx, ryl, rx, ryh, gcs, H);
+      amax = face_flux<R, NS, 2, LIM>(a, sqp, sfl, f, j, rx, ryl, rx, ryh, gcs, H);
     } else {
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = R(0);
@@ -710,7 +739,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   }
 }
 
-template <class R, int NS>
+template <class R, int NS, int LIM>
 __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
                                                        R* __restrict__ rout, int want_dt) {
   const RunState* st = a.st;
@@ -719,7 +748,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
   if (want_dt ? !running(st) : !st->run_step) return;
   if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  flux_tile<R, NS>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
+  flux_tile<R, NS, LIM>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // ---------------------------------------------------------------------------

@@ -46,10 +46,12 @@ __device__ __forceinline__ R maxmod(R a, R b) {
   R sa = a / fabs(a), sb = b / fabs(b);
   return cst<R>(0.5) * (sa + sb) * rmax(fabs(a), fabs(b));
 }
-template <class R>
+// LIM >= 0: the limiter of every variable, known at compile time; -1: lim
+template <class R, int LIM = -1>
 __device__ __forceinline__ R limit(R v0, R v1, R v2, R z0, R z1, R z2, int lim, R theta) {
   R a = (v2 - v1) / (z2 - z1);
   R b = (v1 - v0) / (z1 - z0);
+  if constexpr (LIM >= 0) lim = LIM;
   switch (lim) {
     case 0: return R(0);
     case 1: return minmod(a, b);

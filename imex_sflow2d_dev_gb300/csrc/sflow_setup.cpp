@@ -265,7 +265,10 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   if (!p.gas_flag && !p.liquid_flag) { err = "one of gas_flag / liquid_flag must be set"; return SFLOW_EINVAL; }
   if (p.rheology_flag && p.rheology_model != 1 && p.rheology_model != 6) { err = "rheology_model must be 1 or 6"; return SFLOW_EINVAL; }
   if (p.erosion_coeff != 0.0) { err = "erosion_coeff must be 0"; return SFLOW_EINVAL; }
-  if (p.solver_scheme != SFLOW_SCHEME_KT) { err = "only SOLVER_SCHEME = KT is implemented on the GPU"; return SFLOW_EINVAL; }
+  if (p.solver_scheme != SFLOW_SCHEME_KT && p.solver_scheme != SFLOW_SCHEME_UP) {
+    err = "SOLVER_SCHEME must be KT or UP";
+    return SFLOW_EINVAL;
+  }
   if (!(p.cell_size > 0.0) || !(p.cfl > 0.0) || !(p.max_dt > 0.0) || !(p.dt0 > 0.0)) { err = "cell_size, cfl, max_dt, dt0 must be > 0"; return SFLOW_EINVAL; }
   if (!(p.pres > 0.0) || !(p.sp_gas_const_a > 0.0) || !(p.T_ambient > 0.0)) { err = "pres, sp_gas_const_a, T_ambient must be > 0"; return SFLOW_EINVAL; }
   for (int i = 0; i < p.n_solid; ++i)

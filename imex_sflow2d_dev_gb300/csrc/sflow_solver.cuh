@@ -707,6 +707,9 @@ class Solver : public SolverBase {
     for (int i = 0; i < hs_.nv; ++i) g.limiter[i] = p.limiter[i];
     g.limiter[hs_.nv] = p.limiter[1];
     g.limiter[hs_.nv + 1] = p.limiter[2];
+    g.lim_all = g.limiter[0];
+    for (int i = 1; i < hs_.nv + 2; ++i)
+      if (g.limiter[i] != g.lim_all) g.lim_all = -1;
     g.cfl = p.cfl; g.max_dt = p.max_dt;
     fill_phys(ka_.pr);
     fill_phys(ka_.pd);

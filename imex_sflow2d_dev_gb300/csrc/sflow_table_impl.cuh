@@ -121,7 +121,10 @@ __global__ void k_stats_partial(KArgs<R> a, double* __restrict__ part) {
 template <class R, int NS>
 static cudaError_t tab_flux(const KArgs<R>& a, dim3 grid, size_t smem, cudaStream_t s, const R* qin,
                             R* rout, int want_dt) {
-  k_flux<R, NS><<<grid, FLUX_THREADS, smem, s>>>(a, qin, rout, want_dt);
+  // minmod everywhere (the reference default) has its own instantiation:
+  // one limiter case instead of eight per variable keeps the code small
+  if (a.g.lim_all == 1) k_flux<R, NS, 1><<<grid, FLUX_THREADS, smem, s>>>(a, qin, rout, want_dt);
+  else k_flux<R, NS, -1><<<grid, FLUX_THREADS, smem, s>>>(a, qin, rout, want_dt);
   return cudaGetLastError();
 }
 template <class R, int NS>
@@ -161,7 +164,9 @@ static cudaError_t tab_stats(const KArgs<R>& a, int blocks, cudaStream_t s, doub
 }
 template <class R, int NS>
 static cudaError_t tab_smem(size_t bytes) {
-  return cudaFuncSetAttribute(k_flux<R, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = cudaFuncSetAttribute(k_flux<R, NS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_flux<R, NS, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 template <class R, int NS>
@@ -171,12 +176,14 @@ static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_b_flux<R, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
+  e = cudaFuncSetAttribute(k_b_flux<R, NS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_b_flux<R, NS, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
   if (e != cudaSuccess) return e;
   int occ[3] = {0, 0, 0};
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_b_mask<R>, TX * TY, 0);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_b_flux<R, NS>, FLUX_THREADS, smem_flux);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_b_flux<R, NS, -1>, FLUX_THREADS, smem_flux);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_b_stage2<R, NS>, TX * TY, 0);
   if (e != cudaSuccess) return e;
@@ -187,10 +194,11 @@ static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
   return cudaSuccess;
 }
 template <class R, int NS>
-static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux) {
+static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux, int lim) {
   k_b_cand<R><<<grids[0], kBatchCandThreads, 0, s>>>(b);
   k_b_mask<R><<<grids[1], TX * TY, 0, s>>>(b);
-  k_b_flux<R, NS><<<grids[2], FLUX_THREADS, smem_flux, s>>>(b);
+  if (lim == 1) k_b_flux<R, NS, 1><<<grids[2], FLUX_THREADS, smem_flux, s>>>(b);
+  else k_b_flux<R, NS, -1><<<grids[2], FLUX_THREADS, smem_flux, s>>>(b);
   k_b_dt<R><<<1, kBatchCandThreads, 0, s>>>(b);
   k_b_stage2<R, NS><<<grids[3], TX * TY, 0, s>>>(b);
   return cudaGetLastError();

@@ -62,7 +62,7 @@ struct Grid {
   int limiter[kMaxVars + 2];
   double cfl, max_dt;
   int dry_bc;       // every boundary condition is (Neumann, 0): a dry inside keeps dry ghosts
-  int pad;
+  int lim_all;      // the limiter of every variable when they are all equal, else -1
 };
 
 // Device-resident run state (one per domain).

@@ -327,3 +327,22 @@ def test_fp64_dam_break_dry_bed_is_bitwise_equal():
     o, s = run_pair(p, B, q, 60)
     assert s.stats().status == 0
     np.testing.assert_array_equal(s.download_q(), o.q())
+
+
+def test_upwind_scheme_matches_oracle():
+    """SOLVER_SCHEME = 'UP' (eval_flux_UP): bitwise on the dam break (no
+    Newton), 1e-10 on the ring-inlet current; the FP32 form within 1e-4."""
+    from imex_sflow2d_dev_gb300.params import SCHEME_UP
+    p, B, q = W.dam_break(nx=64, ny=48, t_end=100.0)
+    p.solver_scheme = SCHEME_UP
+    o, s = run_pair(p, B, q, 40)
+    assert s.stats().status == 0
+    np.testing.assert_array_equal(s.download_q(), o.q())
+    p, B, q = _pyro(settling=False)
+    p.solver_scheme = SCHEME_UP
+    o, s = run_pair(p, B, q, 50)
+    assert s.stats().status == 0
+    err = rel_err(s.download_q(), o.q(), p.n_vars, p.comp_cells_x, p.comp_cells_y)
+    assert max(err) <= FP64_TOL, err
+    o, s = run_pair(p, B, q, 50, precision=PREC_FP32)
+    assert l1_err(s.download_q(), o.q(), p.n_vars, p.comp_cells_x, p.comp_cells_y) <= FP32_L1_TOL
