@@ -256,7 +256,7 @@ __device__ __forceinline__ R slope(R v0, R v1, R v2, const Spacing<R>& s, int li
 // face to the north only (solver_2d.f90:3605, kept as is).
 // ---------------------------------------------------------------------------
 template <class R, int NS, int DIR, int LIM>
-__device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, const uint8_t* sfl,
+__device__ __noinline__ void recon_side_edge(const KArgs<R>& a, const R* sqp, const uint8_t* sfl,
                                            int rx, int ry, int j, int k, int plus, R* out) {
   constexpr int nv = 4 + NS, np = nv + 2;
   const Grid<R>& g = a.g;
@@ -374,6 +374,41 @@ __device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, cons
   }
 #pragma unroll
   for (int i = 0; i < np; ++i) out[i] = qm[i];
+}
+
+// Interior cells without a ring face (almost every cell): three-point
+// slopes on the uniform grid, no boundary or wall rule.  The same operations
+// as recon_side_edge takes for such a cell, so both give identical values;
+// the edge version is a separate (not inlined) function so that the face
+// code every thread runs stays small.
+template <class R, int NS, int DIR, int LIM>
+__device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, const uint8_t* sfl,
+                                           int rx, int ry, int j, int k, int plus, R* out) {
+  constexpr int nv = 4 + NS, np = nv + 2;
+  const Grid<R>& g = a.g;
+  constexpr int plane = RX * RY;
+  const int n = (DIR == 1) ? g.nx : g.ny;
+  const int c = (DIR == 1) ? j : k;
+  const uint8_t fl = sfl[ry * RX + rx];
+  const bool src2 = a.pr.radial_source && (fl & F_SC_MASK) == 2;
+  if (c == 0 || c == n - 1 || src2) {
+    recon_side_edge<R, NS, DIR, LIM>(a, sqp, sfl, rx, ry, j, k, plus, out);
+    return;
+  }
+  auto QP = [&](int i, int o) -> R {
+    return (DIR == 1) ? sqp[i * plane + ry * RX + (rx + o)] : sqp[i * plane + (ry + o) * RX + rx];
+  };
+  auto comp = [&](int m) -> R { return (DIR == 1) ? xcomp(g, m) : ycomp(g, m); };
+  const R inv_d = (DIR == 1) ? g.one_by_dx : g.one_by_dy;
+  const R d2 = (DIR == 1) ? g.dx2 : g.dy2;
+  const Spacing<R> sp = spacing<R>(comp(c - 1), comp(c), comp(c + 1), true, inv_d);
+#pragma unroll
+  for (int i = 0; i < np; ++i) {
+    const R v1 = QP(i, 0);
+    const R sl = slope<R, LIM>(QP(i, -1), v1, QP(i, 1), sp, g.limiter[i], g.theta);
+    const R dq = g.rc * d2 * sl;
+    out[i] = plus ? v1 + dq : v1 - dq;
+  }
 }
 
 // One side of a face reduced to what the KT flux needs.
