@@ -101,6 +101,13 @@ class Dist:
             self.dist.destroy_process_group()
 
 
+def aggregate(d, cells, ms):
+    """Whole-job rate of the replicas: cells of all ranks over the slowest
+    rank's time (ms).  Returns (cell-updates/s, max ms)."""
+    ms_max = d.max(ms)
+    return d.sum(cells) / (ms_max / 1e3), ms_max
+
+
 def read_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -408,9 +415,7 @@ def run_gb300(args, d):
     t_wall1 = time.perf_counter()
     clk = clocks.stop()
     d.barrier()
-    ms_max = d.max(r32["ms"])
-    cells_all = d.sum(r32["cells"])
-    value = cells_all / (ms_max / 1e3)
+    value, ms_max = aggregate(d, r32["cells"], r32["ms"])
 
     # plain FP64 form, same start state and step count
     s64, r64 = timed_form(lib, p64, B, q, max(args.steps // 5, 3), args.warmup)

@@ -2,7 +2,9 @@
 
 nvcc compiles the CUDA translation units for sm_103a only; the FP64 plain
 form is compiled with --fmad=false so that its arithmetic follows the
-reference operation order.  The host set-up and the C ABI are plain C++.
+reference operation order; the FP32 bulk form with fused multiply-add,
+flush-to-zero and the approximate (<= 2 ulp) single-precision division and
+square root (its FP64 Newton step and sums are unaffected).  The host set-up and the C ABI are plain C++.
 Translation units compile in parallel; the library links the CUDA runtime
 statically so it loads without a torch or CUDA toolkit environment.
 """
@@ -18,7 +20,7 @@ LIB = os.path.join(HERE, "libsflow_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 FP64 = ["--fmad=false"]
-FP32 = ["--fmad=true", "-ftz=true"]
+FP32 = ["--fmad=true", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
 UNITS = [
     # (source, extra flags); the class-count kernels are the slow units
     ("sflow_k_fp64_ns2.cu", FP64),

@@ -69,13 +69,27 @@ class Batch : public BatchBase {
       err_ = "cudaMemset failed";
       return SFLOW_ECUDA;
     }
+    uint8_t* tile_seed = nullptr;
+    {
+      const std::vector<uint8_t> ts = sv->tile_seed_host();
+      if (cudaMalloc((void**)&tile_seed, ts.size()) != cudaSuccess) { cudaFree(cand); err_ = "cudaMalloc failed"; return SFLOW_ENOMEM; }
+      if (cudaMemcpy(tile_seed, ts.data(), ts.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(cand);
+        cudaFree(tile_seed);
+        err_ = "cudaMemcpy failed";
+        return SFLOW_ECUDA;
+      }
+    }
     Slot& s = g->slots[slot];
     s.gen = (s.gen + 1u) & 0xffffu;
     s.cand = cand;
+    s.tile_seed = tile_seed;
     s.tiles = tiles;
     BatchRun br;
     br.st = sv->state_dev();
     br.cand = cand;
+    br.tile_wet = sv->tile_wet_dev();
+    br.tile_seed = tile_seed;
     br.tiles_x = sv->tiles_x();
     br.tiles_y = sv->tiles_y();
     br.gen = s.gen;
@@ -200,6 +214,8 @@ class Batch : public BatchBase {
     s->solver.reset();
     cudaFree(s->cand);
     s->cand = nullptr;
+    cudaFree(s->tile_seed);
+    s->tile_seed = nullptr;
     g->tiles_live -= s->tiles;
     g->tiles_draining += s->tiles;
     g->live -= 1;
@@ -245,6 +261,7 @@ class Batch : public BatchBase {
   struct Slot {
     std::unique_ptr<Solver<R>> solver;
     uint32_t* cand = nullptr;
+    uint8_t* tile_seed = nullptr;
     int64_t tiles = 0;
     unsigned gen = 0;
     bool done = false;
@@ -294,7 +311,9 @@ class Batch : public BatchBase {
       for (auto& s : slots) {
         s.solver.reset();
         if (s.cand) cudaFree(s.cand);
+        if (s.tile_seed) cudaFree(s.tile_seed);
         s.cand = nullptr;
+        s.tile_seed = nullptr;
       }
       if (graph_exec) cudaGraphExecDestroy(graph_exec);
       if (graph) cudaGraphDestroy(graph);

@@ -18,9 +18,12 @@
 // Why candidates suffice: a cell outside the active set is not updated, so
 // a wet cell (a check_solve seed) was active in the previous step; active
 // cells lie within n_RK <= 4 cells of a seed, and tiles are 32 x 8 cells, so
-// they lie in the 3 x 3 tile neighbourhood of a previously active tile.
-// Border and ring cells are seeds of every step, so their tiles stay in the
-// lists.  A newly admitted run puts all its tiles in L[pp] (full scan for
+// they lie in the 3 x 3 tile neighbourhood of a previously active tile that
+// held mass (tile_wet, written by the stage kernel).  Border and ring cells
+// are seeds of every step, so their tiles stay in the lists; a border seed
+// reaches into the neighbouring tile only when the edge tile is narrower
+// than n_RK + 1 cells, and ring seeds may reach any neighbour, so those
+// tiles are dilated too (tile_seed).  A newly admitted run puts all its tiles in L[pp] (full scan for
 // its first step).  Tiles outside the candidate set keep an all-zero mask
 // (they were processed when they last stopped being active), so the flux
 // halo reads them as inactive, as the single-run kernels do.
@@ -42,6 +45,8 @@ namespace sflow {
 struct BatchRun {
   RunState* st;      // the run's device state
   uint32_t* cand;    // per-tile candidate flag
+  const uint8_t* tile_wet;    // tile held mass after the last step (or unknown: 1)
+  const uint8_t* tile_seed;   // tile holds ring-boundary cells, or is a narrow edge tile
   int tiles_x, tiles_y;
   unsigned gen;      // generation of the run in this slot
   int live;          // slot holds a run
@@ -128,6 +133,10 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
     if (!br.live || (br.gen & 0xffffu) != entry_gen(e) || !running(br.st)) continue;
     const unsigned tile = entry_tile(e);
     const int nb = (int)(i % 9u);
+    // only tiles with mass, ring cells or a narrow domain edge can activate
+    // cells of their neighbours; a dry tile kept active by the border rule
+    // is its own only candidate
+    if (nb != 4 && !br.tile_wet[tile] && !br.tile_seed[tile]) continue;
     const int tx = (int)(tile % (unsigned)br.tiles_x) + nb % 3 - 1;
     const int ty = (int)(tile / (unsigned)br.tiles_x) + nb / 3 - 1;
     if (tx < 0 || ty < 0 || tx >= br.tiles_x || ty >= br.tiles_y) continue;
@@ -243,7 +252,10 @@ __global__ void __launch_bounds__(TX* TY, 5) k_b_stage2(BatchArgs<R> b) {
       __syncthreads();
     }
     if (!a.st->run_step) continue;
-    if (a.tile_active[tile] == 2) continue;   // dry without ring cells (flux_tile)
+    if (a.tile_active[tile] == 2) {   // dry without ring cells (flux_tile)
+      if (threadIdx.x == 0) a.tile_wet[tile] = 0;
+      continue;
+    }
     const int tiles_x = (a.g.nx + TX - 1) / TX;
     stage2_tile<R, NS>(a, -1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x));
   }

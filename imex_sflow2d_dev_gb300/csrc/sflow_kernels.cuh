@@ -51,6 +51,7 @@ struct KArgs {
   const R* arc;      // 3 planes: perimeter, n_x, n_y
   uint8_t* mask;
   uint8_t* tile_active;
+  uint8_t* tile_wet;   // a cell of the tile holds mass after the step (stage kernel)
   R* hmax;
   R* pdynmax;
   R* mvmax;
@@ -135,17 +136,34 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
   const int nrk = a.pd.nrk;
   int any = 0;
   if (!solve_all) {
-    for (int idx = threadIdx.x; idx < MRX * MRY; idx += TX * TY) {
+    // all frame loads of a thread are issued before any is used
+    constexpr int NIT = (MRX * MRY + TX * TY - 1) / (TX * TY);
+    R qv[NIT];
+    uint8_t fv[NIT];
+#pragma unroll
+    for (int it = 0; it < NIT; ++it) {
+      const int idx = threadIdx.x + it * TX * TY;
+      const int rx = idx % MRX, ry = idx / MRX;
+      const int jj = j0 + rx - MASK_HALO, kk = k0 + ry - MASK_HALO;
+      qv[it] = R(0);
+      fv[it] = 0;
+      if (idx < MRX * MRY && jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
+        const int64_t cc = cidx(g, jj, kk);
+        qv[it] = a.q[cc];
+        fv[it] = a.cflags[cc];
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < NIT; ++it) {
+      const int idx = threadIdx.x + it * TX * TY;
+      if (idx >= MRX * MRY) break;
       const int rx = idx % MRX, ry = idx / MRX;
       const int jj = j0 + rx - MASK_HALO, kk = k0 + ry - MASK_HALO;
       uint8_t sd = 0;
       if (jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
         if (jj == 0 || jj == g.nx - 1 || kk == 0 || kk == g.ny - 1) sd = 1;
-        else {
-          const int64_t cc = cidx(g, jj, kk);
-          if (a.q[cc] > R(0)) sd = 1;
-          else if (a.pd.radial_source && (a.cflags[cc] & F_SC_MASK) == 2) sd = 1;
-        }
+        else if (qv[it] > R(0)) sd = 1;
+        else if (a.pd.radial_source && (fv[it] & F_SC_MASK) == 2) sd = 1;
       }
       seed[ry][rx] = sd;
       any |= sd;
@@ -425,9 +443,8 @@ template <class R, int NS, int DIR>
 __device__ __forceinline__ void side_from_qp(const KArgs<R>& a, const R* qp, R gcs, Side<R, NS>& s,
                                              bool mirrored) {
   const Phys<R>& P = a.pr;
-  qp_to_qc<R, NS>(P, qp, s.q);
+  Mixt<R> m = qp_to_qc_mixt<R, NS>(P, qp, s.q);
   if (mirrored) s.q[DIR] = -s.q[DIR];   // hu (x) / hv (y) of the wall mirror
-  Mixt<R> m = mixt_var<R, NS>(P, qp, false);
   local_speeds<R, NS>(P, qp, m.red_grav, gcs, DIR, s.vmin, s.vmax);
   eval_fluxes<R, NS>(P, s.q, qp, m, gcs, DIR, s.f);
   s.hu_p = qp[1];
@@ -1098,6 +1115,7 @@ __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx,
   const int k = ty * TY + threadIdx.x / TX;
   unsigned status = 0;
   int nit = 0;
+  int wet = 0;
   if (j < g.nx && k < g.ny) {
     const int64_t c = cidx(g, j, k);
     if (a.mask[c]) {
@@ -1135,9 +1153,14 @@ __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx,
         for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
         if (mode < 0) post_step_maps<R, NS>(a, c, q);
       }
+      wet = q[0] > R(0);
     }
   }
   newton_stats<R>(st, status, nit);
+  if (mode < 0) {
+    wet = __syncthreads_or(wet);
+    if (threadIdx.x == 0) a.tile_wet[ty * g.tiles_x + tx] = (uint8_t)wet;
+  }
 }
 
 template <class R, int NS>

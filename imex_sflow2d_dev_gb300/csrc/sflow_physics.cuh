@@ -251,6 +251,65 @@ __device__ __forceinline__ Mixt<R> mixt_var(const Phys<R>& P, const R* qpj, bool
   return m;
 }
 
+// qp_to_qc together with the densities and the reduced gravity of mixt_var
+// (no Richardson number, no specific heats) for a face state: the carrier
+// and mixture densities are formed once, with exactly the operations both
+// routines use, so qc, rho_m and red_grav equal those of the two calls.
+template <class R, int NS>
+__device__ __forceinline__ Mixt<R> qp_to_qc_mixt(const Phys<R>& P, const R* qp, R* qc) {
+  constexpr int ns = NS, nv = 4 + NS;
+  Mixt<R> m;
+  m.Ri = R(0);
+  m.cp_c = R(0);
+  m.cp_mix = R(0);
+  R r_h = qp[0];
+  if (!(r_h > P.thr_eps)) {
+    for (int i = 0; i < nv; ++i) qc[i] = R(0);
+    m.red_grav = R(0); m.rho_m = P.rho_a_amb; m.rho_c = P.rho_a_amb;
+    return m;
+  }
+  R r_hu = qp[1], r_hv = qp[2], r_u = qp[nv], r_v = qp[nv + 1], r_T = qp[3];
+  R arhos[kMaxSolid];
+  R at = R(0);
+  for (int i = 0; i < ns; ++i) {
+    R al = P.alpha ? qp[4 + i] : qp[4 + i] / qp[0];
+    at += al;
+    arhos[i] = al * P.rho_s[i];
+  }
+  R rho_c;
+  if (P.gas) {
+    R rho_a = P.pres / (P.sp_gas_const_a * r_T);
+    rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
+  } else {
+    rho_c = P.rho_l;
+  }
+  R alphac = R(1) - at;
+  R sa = R(0);
+  for (int i = 0; i < ns; ++i) sa += arhos[i];
+  R rho_m = alphac * rho_c + sa;
+  R inv_rhom = R(1) / rho_m;
+  R xc = alphac * rho_c * inv_rhom;
+  R cp_c;
+  if (P.gas) cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
+  else cp_c = P.sp_heat_l;
+  R dcp = R(0);
+  for (int i = 0; i < ns; ++i) dcp += (arhos[i] * inv_rhom) * P.sp_heat_s[i];
+  R cmix = dcp + xc * cp_c;
+  qc[0] = rho_m * r_h;
+  qc[1] = rho_m * r_hu;
+  qc[2] = rho_m * r_hv;
+  if (P.energy) {
+    qc[3] = (r_h > R(0)) ? r_h * rho_m * (cmix * r_T + cst<R>(0.5) * (sq(r_u) + sq(r_v))) : R(0);
+  } else {
+    qc[3] = r_h * rho_m * cmix * r_T;
+  }
+  for (int i = 0; i < ns; ++i) qc[4 + i] = (arhos[i] * inv_rhom) * qc[0];
+  m.rho_m = rho_m;
+  m.rho_c = rho_c;
+  m.red_grav = (rho_m - P.rho_a_amb) / rho_m * P.grav;
+  return m;
+}
+
 // constitutive_2d.f90:2203-2307 eval_local_speeds_x / _y.  dir 1 = x, 2 = y.
 template <class R, int NS>
 __device__ __forceinline__ void local_speeds(const Phys<R>& P, const R* qpj, R red_grav, R gc,

@@ -127,6 +127,8 @@ class Solver : public SolverBase {
     SFLOW_CU(alloc((void**)&mask_, plane_));
     SFLOW_CU(cudaMemset(mask_, 0, plane_));
     SFLOW_CU(alloc((void**)&tile_active_, (size_t)tiles_x_ * tiles_y_));
+    SFLOW_CU(alloc((void**)&tile_wet_, (size_t)tiles_x_ * tiles_y_));
+    SFLOW_CU(cudaMemset(tile_wet_, 1, (size_t)tiles_x_ * tiles_y_));
     SFLOW_CU(alloc((void**)&hmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&pdynmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&mvmax_, sizeof(R) * plane_));
@@ -170,12 +172,32 @@ class Solver : public SolverBase {
     bytes_ -= (int64_t)(sizeof(double) * (size_t)hs_.nx * hs_.ny * (hs_.nv + 3));
     stage_aos_ = nullptr;
   }
+  // per tile: 1 when its cells can activate neighbouring tiles whatever the
+  // flow (ring-boundary cells, or an edge tile narrower than n_RK + 1 cells)
+  std::vector<uint8_t> tile_seed_host() const {
+    std::vector<uint8_t> ts((size_t)tiles_x_ * tiles_y_, 0);
+    const int nx = hs_.nx, ny = hs_.ny, nrk = hs_.nrk;
+    const int wlast = nx - (tiles_x_ - 1) * TX, hlast = ny - (tiles_y_ - 1) * TY;
+    for (int ty = 0; ty < tiles_y_; ++ty)
+      for (int tx = 0; tx < tiles_x_; ++tx) {
+        uint8_t v = 0;
+        if ((tx == tiles_x_ - 1 && wlast <= nrk) || (ty == tiles_y_ - 1 && hlast <= nrk)) v = 1;
+        if (hs_.p.radial_source_flag)
+          for (int k = ty * TY; k < std::min(ny, (ty + 1) * TY) && !v; ++k)
+            for (int j = tx * TX; j < std::min(nx, (tx + 1) * TX); ++j)
+              if ((hs_.cflags[(size_t)k * nx + j] & 3) == 2) { v = 1; break; }
+        ts[(size_t)ty * tiles_x_ + tx] = v;
+      }
+    return ts;
+  }
+  uint8_t* tile_wet_dev() const { return tile_wet_; }
+
   // device bytes a run of this set-up holds while it is in a batch
   static int64_t batch_bytes(const HostSetup& hs) {
     const int64_t pitch = (hs.nx + 31) / 32 * 32, plane = pitch * hs.ny;
     const int ngeo = hs.p.curvature_term_flag ? 8 : 5;
     const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + TY - 1) / TY);
-    return plane * (int64_t)sizeof(R) * (2 * hs.nv + ngeo + 3 + 3) + 2 * plane + tiles * 5 +
+    return plane * (int64_t)sizeof(R) * (2 * hs.nv + ngeo + 3 + 3) + 2 * plane + tiles * 7 +
            (int64_t)sizeof(double) * 4 * 1024 + 4096;
   }
 
@@ -192,6 +214,7 @@ class Solver : public SolverBase {
     SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
     if (deposit_) SFLOW_CU(cudaMemsetAsync(deposit_, 0, sizeof(double) * plane_ * hs_.ns, stream_));
+    SFLOW_CU(cudaMemsetAsync(tile_wet_, 1, (size_t)tiles_x_ * tiles_y_, stream_));
     SFLOW_CU(cudaStreamSynchronize(stream_));
     uploaded_ = true;
     return SFLOW_OK;
@@ -532,7 +555,7 @@ class Solver : public SolverBase {
   R *q_ = nullptr, *rd_ = nullptr, *rn_ = nullptr, *qs_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
   double* deposit_ = nullptr;
   R* geo_[8];
-  uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr;
+  uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr, *tile_wet_ = nullptr;
   RunState* st_ = nullptr;
   double *stage_aos_ = nullptr, *stat_part_ = nullptr, *stat_out_ = nullptr;
   int nstat_blocks_ = 0;
@@ -729,6 +752,7 @@ class Solver : public SolverBase {
     for (int i = 0; i < 4; ++i) { ka_.omega_t[i] = hs_.omega_tilde[i]; ka_.omega[i] = hs_.omega[i]; }
     for (int i = 0; i < 8; ++i) ka_.geo[i] = geo_[i];
     ka_.cflags = cflags_; ka_.arc = arc_; ka_.mask = mask_; ka_.tile_active = tile_active_;
+    ka_.tile_wet = tile_wet_;
     ka_.hmax = hmax_; ka_.pdynmax = pdynmax_; ka_.mvmax = mvmax_; ka_.st = st_;
     ka_.deposit = deposit_;
     ka_.take_last = hs_.take_last;
