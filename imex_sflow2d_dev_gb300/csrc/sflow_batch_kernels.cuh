@@ -182,10 +182,11 @@ __global__ void __launch_bounds__(TX* TY) k_b_mask(BatchArgs<R> b) {
   }
 }
 
-// 3 blocks per SM (27 warps): without the bound the persistent loop keeps
-// loop-invariant values of the tile body live and needs ~120 registers
+// 4 blocks per SM (36 warps, 56 registers, a few spills): without the bound
+// the persistent loop keeps loop-invariant values of the tile body live and
+// needs ~120 registers; 4 blocks measured 4 % faster than 3 on the ensemble
 template <class R, int NS, int LIM>
-__global__ void __launch_bounds__(FLUX_THREADS, 3) k_b_flux(BatchArgs<R> b) {
+__global__ void __launch_bounds__(FLUX_THREADS, 4) k_b_flux(BatchArgs<R> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx;
