@@ -20,6 +20,19 @@ plain FP64 form is timed the same way and reported beside it, with the L1
 error of h between the two forms.  `e2e` is the same metric through the C
 ABI with the state in pinned host memory copied in and out every step.
 
+Further legs on rank 0, each a key of the same JSON line:
+  ensemble      the 256-run mixed ensemble (sides 128-1024, own DEMs and
+                draws) in one batch of persistent kernels, FP32 bulk form;
+                its speed-up is taken against the plain FP64 form's
+                cell-updates/s of the main leg, and the L1/Linf errors of
+                h, hu, hv, T and alpha_s of the two forms on member 0;
+  served        Poisson arrivals of short jobs through the request loop
+                (admission by free HBM), p50/p99 submit-to-done latency;
+  large_domain  one 8192x8192 domain (3 classes, entrainment), FP32 bulk
+                against FP64 on a few steps, with the same error norms.
+Each leg is switched off by a zero size (--ensemble-runs 0,
+--served-requests 0, --large-n 0).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
 import argparse
