@@ -614,24 +614,40 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   const int tid = threadIdx.x;
 
   __syncthreads();   // shared memory of the previous tile of a persistent block is free
-  // 1. physical variables of the tile + halo (qc_to_qp; inactive = dry)
+  // 1. physical variables of the tile + halo (qc_to_qp; inactive = dry).
+  // Each thread covers two region cells; all their loads (flags, mask,
+  // state) are issued before any is used.
   int any_wet = 0, all_wet = 1;
-  for (int idx = tid; idx < RX * RY; idx += FLUX_THREADS) {
+  constexpr int NIT = (RX * RY + FLUX_THREADS - 1) / FLUX_THREADS;
+  R qv[NIT][nv];
+  uint8_t flv[NIT], mv[NIT];
+#pragma unroll
+  for (int it = 0; it < NIT; ++it) {
+    const int idx = tid + it * FLUX_THREADS;
     const int rx = idx % RX, ry = idx / RX;
     const int j = j0 + rx - HALO, k = k0 + ry - HALO;
-    R qp[np];
-    uint8_t fl = 0;
-    bool wet = false;
-    if (j >= 0 && j < g.nx && k >= 0 && k < g.ny) {
-      const int64_t c = cidx(g, j, k);
-      fl = a.cflags[c];
-      if (a.mask[c]) {
-        fl |= F_ACTIVE;
-        R q[nv];
+    flv[it] = 0;
+    mv[it] = 0;
 #pragma unroll
-        for (int i = 0; i < nv; ++i) q[i] = qin[i * g.plane + c];
-        if (q[0] > R(0)) { qc_to_qp<R, NS>(P, q, qp); wet = true; fl |= F_WET; }
-      }
+    for (int i = 0; i < nv; ++i) qv[it][i] = R(0);
+    if (idx < RX * RY && j >= 0 && j < g.nx && k >= 0 && k < g.ny) {
+      const int64_t c = cidx(g, j, k);
+      flv[it] = a.cflags[c];
+      mv[it] = a.mask[c];
+#pragma unroll
+      for (int i = 0; i < nv; ++i) qv[it][i] = qin[i * g.plane + c];
+    }
+  }
+#pragma unroll
+  for (int it = 0; it < NIT; ++it) {
+    const int idx = tid + it * FLUX_THREADS;
+    if (idx >= RX * RY) break;
+    R qp[np];
+    uint8_t fl = flv[it];
+    bool wet = false;
+    if (mv[it]) {
+      fl |= F_ACTIVE;
+      if (qv[it][0] > R(0)) { qc_to_qp<R, NS>(P, qv[it], qp); wet = true; fl |= F_WET; }
     }
     if (!wet) {
 #pragma unroll
