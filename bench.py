@@ -251,9 +251,29 @@ def run_reference(args, d):
     return 0
 
 
-def timed_form(lib, p, B, q, steps, warmup, flush=True):
+def autotune_run(s, qa, warmup, steps):
+    """Tile-shape autotuner on the run itself (sflow_autotune), from the
+    start state after `warmup` steps; the run is then reset to the start
+    state and keeps the chosen tile height."""
+    t0 = time.perf_counter()
+    s.upload_q(qa)
+    s.advance(max_steps=warmup)
+    best, tab = s.autotune(steps)
+    s.upload_q(qa)
+    return {"tile_h": best, "ms_per_mcu": {str(k): v for k, v in tab.items()},
+            "steps_per_height": steps, "seconds": time.perf_counter() - t0,
+            "tuner": "sflow_autotune (CUDA events over graph-replayed steps of this run)"}
+
+
+def timed_form(lib, p, B, q, steps, warmup, flush=True, tune_steps=0, tile_h=None):
     s = lib.Solver(p, B)
-    s.upload_q(W.to_aos(q))
+    qa = W.to_aos(q)
+    tune = None
+    if tune_steps > 0:
+        tune = autotune_run(s, qa, warmup, tune_steps)
+    elif tile_h:
+        s.set_tile_shape(tile_h)
+    s.upload_q(qa)
     s.advance(max_steps=warmup)
     c0 = s.counters()
     l0 = s.launch_count()
@@ -263,10 +283,10 @@ def timed_form(lib, p, B, q, steps, warmup, flush=True):
     cells = c1["cell_updates"] - c0["cell_updates"]
     return s, {"ms": ms, "cells": cells, "steps": c1["steps"] - c0["steps"],
                "launches": l1 - l0, "newton_iters": c1["newton_iters"] - c0["newton_iters"],
-               "newton_max": c1["newton_max"]}
+               "newton_max": c1["newton_max"], "autotune": tune, "tile_h": s.tile_shape()}
 
 
-def ensemble_leg(lib, n_runs, steps):
+def ensemble_leg(lib, n_runs, steps, tune=True):
     """Batched ensemble: n_runs independent ring-inlet runs (side log-uniform
     in [128, 1024], dx U[5, 20] m, own DEM seed, mu, xi, source radius and
     temperature, particle fractions; workloads.ensemble_params) resident
@@ -278,7 +298,20 @@ def ensemble_leg(lib, n_runs, steps):
     cells = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members)
     print(f"[bench] ensemble inputs: {n_runs} runs, {cells} cells, {time.perf_counter() - ts:.1f} s",
           file=sys.stderr, flush=True)
+    tuned = None
+    if tune:
+        # every 8th member, 128 batch steps per tile height, in a scratch batch
+        from imex_sflow2d_dev_gb300 import autotune as A
+        t0 = time.perf_counter()
+        sample = [(p, B, W.to_aos(q)) for p, B, q, _ in members[::8]]
+        best, rates = A.tune_batch(PREC_FP32, sample, steps=128)
+        tuned = {"tile_h": best, "cell_updates_per_s": {str(k): v for k, v in rates.items()},
+                 "sample": f"{len(sample)} runs (every 8th member), 16 + 128 batch steps per height",
+                 "seconds": time.perf_counter() - t0, "tuner": "autotune.tune_batch"}
+        print(f"[bench] ensemble autotune: {tuned}", file=sys.stderr, flush=True)
     b = lib.Batch(PREC_FP32, max_runs=n_runs, max_cells=int(cells * 1.2) + 4096)
+    if tuned:
+        b.set_tile_shape(tuned["tile_h"])
     ids = []
     for p, B, q, st in members:
         rid = b.submit(p, B, W.to_aos(q), max_steps=st)
@@ -301,7 +334,8 @@ def ensemble_leg(lib, n_runs, steps):
     return {"runs": n_runs, "steps_per_run": steps, "cells_total": cells,
             "cell_updates": cu, "dense_cell_steps": dense, "seconds": dt,
             "value": cu / dt, "unit": UNIT, "gpu_launches": launches,
-            "timing": "host clock around the batch advance calls (each ends synchronised)"}
+            "timing": "host clock around the batch advance calls (each ends synchronised)",
+            "autotune": tuned}
 
 
 def form_errors(lib, p, B, q, steps):
@@ -335,7 +369,7 @@ def form_errors(lib, p, B, q, steps):
     return out
 
 
-def large_leg(lib, n, steps, warmup):
+def large_leg(lib, n, steps, warmup, tune_steps=16):
     """Large single domain: n x n cells, dx = 2 m, diamond-square DEM
     (Hurst 0.8, relief 2000 m, seed 5), 3 particle classes (1e-5, 1e-4,
     1e-3 m), entrainment and settling on, one ring inlet, from a seeded
@@ -355,6 +389,8 @@ def large_leg(lib, n, steps, warmup):
         pp = p32.copy()
         pp.precision = prec
         s = lib.Solver(pp, B)
+        if prec == PREC_FP32 and tune_steps > 0:
+            out["autotune"] = autotune_run(s, qa, warmup, tune_steps)
         s.upload_q(qa)
         s.advance(max_steps=warmup)
         c0 = s.counters()
@@ -362,7 +398,7 @@ def large_leg(lib, n, steps, warmup):
         c1 = s.counters()
         cu = c1["cell_updates"] - c0["cell_updates"]
         out[name] = {"value": cu / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / nst, "steps": nst,
-                     "active_cells_per_step": cu / nst}
+                     "active_cells_per_step": cu / nst, "tile_h": s.tile_shape()}
         s.close()
     out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64_plain"]["value"]
     out["error_vs_fp64"] = {"steps": steps, **form_errors(lib, p32, B, W.from_aos(qa, p32.n_vars, n, n), steps)}
@@ -370,7 +406,7 @@ def large_leg(lib, n, steps, warmup):
     return out
 
 
-def served_leg(lib, n_requests, rate):
+def served_leg(lib, n_requests, rate, tile_h=None):
     """Served solves: Poisson arrivals (mean `rate` per s) of dam-break and
     ring-inlet jobs (side log-uniform in [64, 2048], 1-3 classes, 500-5000
     steps; workloads.served_job) through the request loop (continuous
@@ -383,13 +419,14 @@ def served_leg(lib, n_requests, rate):
     arr = W.poisson_arrivals(n_requests, rate)
     reqs = [S.Request(i, arr[i], p, B, q, st, kind) for i, (p, B, q, st, kind) in enumerate(jobs)]
     cells = sum(p.comp_cells_x * p.comp_cells_y for p, *_ in jobs)
-    loop = S.RequestLoop(PREC_FP32, max_runs=64, max_cells=int(cells * 1.2) + 4096, chunk=16)
+    loop = S.RequestLoop(PREC_FP32, max_runs=64, max_cells=int(cells * 1.2) + 4096, chunk=16,
+                         tile_h=tile_h)
     recs = loop.run(reqs)
     print(f"[bench] served: {max(r['finished_s'] for r in recs):.1f} s", file=sys.stderr, flush=True)
     launches = loop.batch.launch_count()
     loop.close()
     out = S.summarize(recs)
-    out.update({"rate_per_s": rate, "gpu_launches": launches,
+    out.update({"rate_per_s": rate, "gpu_launches": launches, "tile_h": tile_h or 8,
                 "jobs": [{k: r[k] for k in ("kind", "cells", "n_solid", "steps", "tts_s")} for r in recs]})
     return out, recs
 
@@ -420,11 +457,18 @@ def run_gb300(args, d):
     p64.precision = PREC_FP64
     nx, ny, nv = p32.comp_cells_x, p32.comp_cells_y, p32.n_vars
 
+    # tile height of the FP32 form: autotuned on the workload before the
+    # timed region (the plain FP64 form has one compiled height)
+    tune = None
+    if args.tune_steps > 0:
+        st = lib.Solver(p32, B)
+        tune = autotune_run(st, W.to_aos(q), args.warmup, args.tune_steps)
+        st.close()
     clocks = ClockSampler(d.local)
     d.barrier()
     clocks.start()
     t_wall0 = time.perf_counter()
-    s32, r32 = timed_form(lib, p32, B, q, args.steps, args.warmup)
+    s32, r32 = timed_form(lib, p32, B, q, args.steps, args.warmup, tile_h=tune["tile_h"] if tune else None)
     t_wall1 = time.perf_counter()
     clk = clocks.stop()
     d.barrier()
@@ -439,6 +483,7 @@ def run_gb300(args, d):
 
     # per-kernel device time (events between the kernels of each step)
     pk = lib.Solver(p32, B)
+    pk.set_tile_shape(r32["tile_h"])
     pk.upload_q(W.to_aos(q))
     pk.advance(max_steps=args.warmup)
     c0 = pk.counters()
@@ -472,6 +517,7 @@ def run_gb300(args, d):
         pinned = torch.empty(nx * ny * nv, dtype=torch.float64, pin_memory=True)
         pinned.numpy()[:] = W.to_aos(q)
         se = lib.Solver(p32, B)
+        se.set_tile_shape(r32["tile_h"])
         se.upload_q(W.to_aos(q))
         se.advance(max_steps=args.warmup)
         ptr = pinned.data_ptr()
@@ -499,17 +545,19 @@ def run_gb300(args, d):
 
     ens = None
     if d.rank == 0 and args.ensemble_runs > 0:
-        ens = ensemble_leg(lib, args.ensemble_runs, args.ensemble_steps)
+        ens = ensemble_leg(lib, args.ensemble_runs, args.ensemble_steps, tune=args.tune_steps > 0)
         ens["speedup_vs_fp64_plain"] = ens["value"] / value64 if value64 else None
         pe, Be, qe, _ = W.ensemble_params(0, PREC_FP32, 300)
         ens["error_vs_fp64"] = {"member": 0, "side": pe.comp_cells_x, "steps": 300,
                                 **form_errors(lib, pe, Be, qe, 300)}
     large = None
     if d.rank == 0 and args.large_n > 0:
-        large = large_leg(lib, args.large_n, args.large_steps, args.warmup)
+        large = large_leg(lib, args.large_n, args.large_steps, args.warmup,
+                          tune_steps=16 if args.tune_steps > 0 else 0)
     srv = None
     if d.rank == 0 and args.served_requests > 0:
-        srv, recs = served_leg(lib, args.served_requests, args.served_rate)
+        srv, recs = served_leg(lib, args.served_requests, args.served_rate,
+                               tile_h=ens["autotune"]["tile_h"] if ens and ens.get("autotune") else None)
         srv["fp64_one_at_a_time"] = fp64_one_at_a_time(recs, value64)
 
     if d.rank == 0:
@@ -524,7 +572,9 @@ def run_gb300(args, d):
                        "form": "FP32 bulk + FP64 implicit solve",
                        "l2": "flushed between timed steps (512 MB write), one step per "
                              "event-timed interval",
-                       "parallelism": f"replicas x{args.gpus}"},
+                       "parallelism": f"replicas x{args.gpus}",
+                       "tile": f"32x{r32['tile_h']} cells"},
+            "autotune": tune,
             "fp64_plain": {"value": value64, "ms_per_step": r64["ms"] / max(r64["steps"], 1),
                            "steps": r64["steps"], "newton_iters_per_cell":
                            r64["newton_iters"] / max(r64["cells"], 1)},
@@ -566,6 +616,8 @@ def main():
     ap.add_argument("--served-rate", type=float, default=20.0)
     ap.add_argument("--large-n", type=int, default=8192)
     ap.add_argument("--large-steps", type=int, default=10)
+    ap.add_argument("--tune-steps", type=int, default=64,
+                    help="steps per tile height of the autotuner (0: default 32x8 tiles)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -22,13 +22,17 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FP64 = ["--fmad=false"]
 FP32 = ["--fmad=true", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
 UNITS = [
-    # (source, extra flags); the class-count kernels are the slow units
+    # (source, extra flags); the class-count / tile-height kernels are the
+    # slow units and start first
     ("sflow_k_fp64_ns2.cu", FP64),
     ("sflow_k_fp32_ns2.cu", FP32),
+    ("sflow_k_fp32_ns2_t16.cu", FP32),
     ("sflow_k_fp64_ns3.cu", FP64),
     ("sflow_k_fp32_ns3.cu", FP32),
+    ("sflow_k_fp32_ns3_t16.cu", FP32),
     ("sflow_k_fp64_ns1.cu", FP64),
     ("sflow_k_fp32_ns1.cu", FP32),
+    ("sflow_k_fp32_ns1_t16.cu", FP32),
     ("sflow_noalloc.cu", FP64),
     ("sflow_fp64.cu", FP64),
     ("sflow_fp32.cu", FP32),

@@ -43,18 +43,18 @@ class Batch : public BatchBase {
     for (int i = 0; i < max_runs_; ++i)
       if (!g->slots[i].solver) { slot = i; break; }
     if (slot < 0) { err_ = "no free run slot"; return SFLOW_EBUSY; }
-    const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + TY - 1) / TY);
+    const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + tile_h_ - 1) / tile_h_);
     if (g->tiles_live + g->tiles_draining + tiles > max_tiles_) {
       err_ = "tile-list capacity of the batch is in use";
       return SFLOW_EBUSY;
     }
-    const int64_t need = Solver<R>::batch_bytes(hs) +
+    const int64_t need = Solver<R>::batch_bytes(hs, tile_h_) +
                          (int64_t)sizeof(double) * hs.nx * hs.ny * (hs.nv + 3);   // staging, freed after upload
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
     if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
 
-    std::unique_ptr<Solver<R>> sv(new Solver<R>(hs));
+    std::unique_ptr<Solver<R>> sv(new Solver<R>(hs, tile_h_));
     int rc = sv->init();
     if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
     rc = sv->upload(q_aos);
@@ -241,6 +241,22 @@ class Batch : public BatchBase {
     return SFLOW_OK;
   }
 
+  // Tile height of every run admitted from now on; only while the batch
+  // holds no run (the groups' lists and graphs are made for one height).
+  int set_tile_shape(int th) override {
+    if (th == tile_h_) return SFLOW_OK;
+    if (!tile_h_built<R>(th)) { err_ = "no kernels built for this tile height"; return SFLOW_EINVAL; }
+    if (live() > 0) { err_ = "the tile height changes only while the batch holds no run"; return SFLOW_ESTATE; }
+    for (auto& g : groups_)
+      if (g) {
+        g->release();
+        g.reset();
+      }
+    tile_h_ = th;
+    return SFLOW_OK;
+  }
+  int tile_shape() const override { return tile_h_; }
+
   int live() const override {
     int n = 0;
     for (auto& g : groups_)
@@ -338,16 +354,12 @@ class Batch : public BatchBase {
   Group* group(int ns) {
     if (groups_[ns]) return groups_[ns].get();
     std::unique_ptr<Group> g(new Group());
-    g->tab = kernel_table<R>(ns);
-    if (!g->tab.b_step) { err_ = "no batch kernels for this class count"; return nullptr; }
+    g->tab = kernel_table<R>(ns, tile_h_);
+    if (!g->tab.b_step) { err_ = "no batch kernels for this class count and tile height"; return nullptr; }
     g->slots.resize(max_runs_);
     // shared memory of the flux kernel for this class count (the largest
     // any run of the group needs: it depends on n_vars only)
-    const int nv = 4 + ns, np = nv + 2;
-    g->smem_flux = sizeof(R) * ((size_t)np * RX * RY + (size_t)nv * TY * (TX + 1) + (size_t)nv * (TY + 1) * TX +
-                                (size_t)TY * (TX + 1) + (size_t)(TY + 1) * TX) +
-                   (size_t)RX * RY;
-    g->smem_flux = (g->smem_flux + 15) / 16 * 16;
+    g->smem_flux = Solver<R>::flux_smem_bytes(4 + ns, tile_h_);
     auto fail = [&](cudaError_t e) -> Group* {
       err_ = cudaGetErrorString(e);
       g->release();
@@ -381,6 +393,7 @@ class Batch : public BatchBase {
 
   int max_runs_;
   int64_t max_tiles_;
+  int tile_h_ = kTileHDefault;
   std::unique_ptr<Group> groups_[kMaxSolidBuilt + 1];
   std::vector<Rec> recs_;
 };

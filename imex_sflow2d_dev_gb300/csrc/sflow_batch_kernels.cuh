@@ -17,8 +17,8 @@
 //
 // Why candidates suffice: a cell outside the active set is not updated, so
 // a wet cell (a check_solve seed) was active in the previous step; active
-// cells lie within n_RK <= 4 cells of a seed, and tiles are 32 x 8 cells, so
-// they lie in the 3 x 3 tile neighbourhood of a previously active tile that
+// cells lie within n_RK = 2 cells of a seed, and tiles are 32 x TH cells
+// with TH >= 4, so they lie in the 3 x 3 tile neighbourhood of a previously active tile that
 // held mass (tile_wet, written by the stage kernel).  Border and ring cells
 // are seeds of every step, so their tiles stay in the lists; a border seed
 // reaches into the neighbouring tile only when the edge tile is narrower
@@ -148,8 +148,8 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
   }
 }
 
-template <class R>
-__global__ void __launch_bounds__(TX* TY) k_b_mask(BatchArgs<R> b) {
+template <class R, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx;
   KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(TX* TY) k_b_mask(BatchArgs<R> b) {
     if (threadIdx.x == 0) br.cand[tile] = 0u;
     if (!running(a.st)) continue;
     const int tx = (int)(tile % (unsigned)br.tiles_x), ty = (int)(tile / (unsigned)br.tiles_x);
-    const int cnt = mask_tile(a, 0, tx, ty, br.tiles_x);
+    const int cnt = mask_tile<R, TH>(a, 0, tx, ty, br.tiles_x);
     if (cnt > 0 && threadIdx.x == 0) {
       const unsigned pos = atomicAdd(&ctl->count[pp ^ 1u], 1u);
       out[pos] = e;
@@ -182,11 +182,13 @@ __global__ void __launch_bounds__(TX* TY) k_b_mask(BatchArgs<R> b) {
   }
 }
 
-// 4 blocks per SM (36 warps, 56 registers, a few spills): without the bound
-// the persistent loop keeps loop-invariant values of the tile body live and
-// needs ~120 registers; 4 blocks measured 4 % faster than 3 on the ensemble
-template <class R, int NS, int LIM>
-__global__ void __launch_bounds__(FLUX_THREADS, 4) k_b_flux(BatchArgs<R> b) {
+// 32 x 8 tiles: 4 blocks per SM (36 warps, 56 registers, a few spills):
+// without the bound the persistent loop keeps loop-invariant values of the
+// tile body live and needs ~120 registers; 4 blocks measured 4 % faster
+// than 3 on the ensemble
+template <class R, int NS, int LIM, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FLUX_MIN_BLOCKS)
+    k_b_flux(BatchArgs<R> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx;
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(FLUX_THREADS, 4) k_b_flux(BatchArgs<R> b) {
     }
     if (!running(a.st)) continue;
     const int tiles_x = (a.g.nx + TX - 1) / TX;
-    flux_tile<R, NS, LIM>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
+    flux_tile<R, NS, LIM, TH>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
                      smem_raw);
   }
 }
@@ -231,8 +233,9 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_dt(BatchArgs<R> b) {
   }
 }
 
-template <class R, int NS>
-__global__ void __launch_bounds__(TX* TY, 5) k_b_stage2(BatchArgs<R> b) {
+template <class R, int NS, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, TileShape<TH>::STAGE_MIN_BLOCKS)
+    k_b_stage2(BatchArgs<R> b) {
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx;
   KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
@@ -258,7 +261,7 @@ __global__ void __launch_bounds__(TX* TY, 5) k_b_stage2(BatchArgs<R> b) {
       continue;
     }
     const int tiles_x = (a.g.nx + TX - 1) / TX;
-    stage2_tile<R, NS>(a, -1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x));
+    stage2_tile<R, NS, TH>(a, -1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x));
   }
 }
 

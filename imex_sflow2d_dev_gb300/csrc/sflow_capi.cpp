@@ -46,8 +46,9 @@ int sflow_batch_create(int32_t precision, int32_t max_runs, int64_t max_cells, s
   if (precision != SFLOW_PREC_FP32 && precision != SFLOW_PREC_FP64) return fail(SFLOW_EINVAL, "unknown precision");
   if (max_cells < 1) return fail(SFLOW_EINVAL, "max_cells must be positive");
   std::string err;
-  // tile lists hold one entry per 32 x 8 tile; small runs waste part of a
-  // tile, so the capacity allows for twice the cells
+  // tile lists hold one entry per tile (32 x 8 cells at the smallest
+  // compiled height); small runs waste part of a tile, so the capacity
+  // allows for twice the cells
   const int64_t max_tiles = 2 * ((max_cells + 255) / 256) + 1024;
   BatchBase* b = (precision == SFLOW_PREC_FP32) ? sflow::make_batch_fp32(max_runs, max_tiles, err)
                                                 : sflow::make_batch_fp64(max_runs, max_tiles, err);
@@ -135,6 +136,29 @@ int sflow_batch_collect(sflow_batch* b, int32_t run_id, double* q_aos) {
 int32_t sflow_batch_live(const sflow_batch* b) { return (b && b->impl) ? b->impl->live() : 0; }
 
 int64_t sflow_batch_launch_count(const sflow_batch* b) { return (b && b->impl) ? b->impl->launches() : 0; }
+
+int sflow_batch_set_tile_shape(sflow_batch* b, int32_t tile_h) {
+  BATCH_CHECK(b);
+  BATCH_FORWARD(b, b->impl->set_tile_shape(tile_h));
+}
+
+int sflow_batch_get_tile_shape(const sflow_batch* b, int32_t* tile_h) {
+  if (!b || !b->impl) return fail(SFLOW_EINVAL, "null batch");
+  if (!tile_h) return fail(SFLOW_EINVAL, "tile_h is NULL");
+  *tile_h = b->impl->tile_shape();
+  return SFLOW_OK;
+}
+
+int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count) {
+  if (!count) return fail(SFLOW_EINVAL, "count is NULL");
+  if (precision != SFLOW_PREC_FP32 && precision != SFLOW_PREC_FP64) return fail(SFLOW_EINVAL, "unknown precision");
+  const int32_t fp32[2] = {8, 16}, fp64[1] = {8};
+  const int32_t* v = (precision == SFLOW_PREC_FP32) ? fp32 : fp64;
+  const int32_t n = (precision == SFLOW_PREC_FP32) ? 2 : 1;
+  for (int32_t i = 0; i < n && i < capacity && heights; ++i) heights[i] = v[i];
+  *count = n;
+  return SFLOW_OK;
+}
 
 const char* sflow_build_info(void) {
   return "sflow GB300: FP64 plain form + FP32 bulk form, N_RK=2, KT fluxes, sm_103a";
@@ -341,6 +365,28 @@ int sflow_clear_status(sflow_handle* h) {
   CHECK_HANDLE(h);
   FORWARD(h->solver->clear_status());
 }
+int sflow_set_tile_shape(sflow_handle* h, int32_t tile_h) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->set_tile_shape(tile_h));
+}
+int sflow_get_tile_shape(const sflow_handle* h, int32_t* tile_h) {
+  CHECK_HANDLE(h);
+  if (!tile_h) return fail(SFLOW_EINVAL, "tile_h is NULL");
+  *tile_h = h->solver->tile_shape();
+  return SFLOW_OK;
+}
+int sflow_autotune(sflow_handle* h, int64_t steps_per_shape, int32_t* best, double* ms_per_mcu, int32_t n) {
+  CHECK_HANDLE(h);
+  if (!best) return fail(SFLOW_EINVAL, "best is NULL");
+  double v[SFLOW_TILE_CANDIDATES];
+  int b = 0;
+  const int rc = h->solver->autotune(steps_per_shape, &b, v);
+  if (rc < 0) return fail(rc, last_solver_error(h));
+  *best = b;
+  for (int32_t i = 0; i < n && i < SFLOW_TILE_CANDIDATES && ms_per_mcu; ++i) ms_per_mcu[i] = v[i];
+  return SFLOW_OK;
+}
+
 int64_t sflow_launch_count(const sflow_handle* h) {
   return (h && h->solver) ? h->solver->launches() : -1;
 }

@@ -70,6 +70,9 @@ class SolverBase {
   virtual int64_t device_bytes() const = 0;
   virtual int newton_stats(int64_t* total, int* maxit) = 0;
   virtual int64_t cells_total() = 0;
+  virtual int tile_shape() const = 0;
+  virtual int set_tile_shape(int tile_h) = 0;
+  virtual int autotune(int64_t steps, int* best, double* ms_per_mcu) = 0;
   virtual const char* error() const = 0;
 };
 
@@ -88,6 +91,8 @@ class BatchBase {
   virtual int collect(int id, double* q_aos) = 0;
   virtual int live() const = 0;
   virtual int64_t launches() const = 0;
+  virtual int tile_shape() const = 0;
+  virtual int set_tile_shape(int tile_h) = 0;
   virtual const char* error() const = 0;
 };
 

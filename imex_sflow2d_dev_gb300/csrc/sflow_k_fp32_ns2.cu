@@ -1,6 +1,8 @@
-// sflow_k_fp32_ns2.cu -- kernels of the FP32 form with 2 solid classes.
+// sflow_k_fp32_ns2.cu -- kernels of the FP32 form with 2 solid classes:
+// the entries independent of the tile height and the 32 x 8 tiled kernels.
 #include "sflow_table_impl.cuh"
 
 namespace sflow {
 template KernelTable<float> make_table<float, 2>();
+template void fill_tile_entries<float, 2, 8>(KernelTable<float>&);
 }  // namespace sflow

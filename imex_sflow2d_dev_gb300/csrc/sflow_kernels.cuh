@@ -23,12 +23,29 @@
 
 namespace sflow {
 
-constexpr int TX = 32;   // tile width  (cells)
-constexpr int TY = 8;    // tile height (cells)
+constexpr int TX = 32;   // tile width (cells): one warp per tile row
 constexpr int HALO = 2;  // reconstruction stencil reach for a cell's faces
 constexpr int RX = TX + 2 * HALO;
-constexpr int RY = TY + 2 * HALO;
-constexpr int FLUX_THREADS = 288;  // 9 warps: covers (TX+1)*TY and TX*(TY+1) faces
+
+// A tile is TX x TH cells; the tile height TH is a template parameter of
+// every tiled kernel (the tile-shape autotuner picks it per run or batch).
+// The results of a step do not depend on TH: every face and cell is
+// computed from the same stencil whatever tile it falls in.
+template <int TH>
+struct TileShape {
+  static constexpr int TY = TH;
+  static constexpr int RY = TH + 2 * HALO;
+  // whole warps covering the (TX+1)*TH x-faces and the TX*(TH+1) y-faces
+  static constexpr int FLUX_THREADS = (TX * (TH + 1) + 31) / 32 * 32;
+  // resident blocks per SM the persistent flux kernel is compiled for
+  static constexpr int FLUX_MIN_BLOCKS = (TH >= 16) ? 2 : (TH >= 8 ? 4 : 6);
+  // pointwise kernels: 32 x 8 threads, one cell each (a single run's
+  // blocks cover 32 x 8 cells; a batched block walks a tile 8 rows at a time)
+  static constexpr int STAGE_THREADS = TX * 8;
+  static constexpr int STAGE_MIN_BLOCKS = 5;
+  static constexpr int MASK_THREADS = TX * TH;
+};
+constexpr int kTileHDefault = 8;
 
 // flag byte bits
 constexpr uint8_t F_SC_MASK = 0x3;  // source_cell (0, 1 ring interior, 2 ring boundary)
@@ -125,10 +142,11 @@ __device__ __forceinline__ Geo<R> load_geo(const KArgs<R>& a, int64_t c) {
 // the tile and a 4-cell frame are staged in shared memory; a tile with no
 // seed in its frame is inactive without scanning its cells.
 constexpr int MASK_HALO = 4;
-constexpr int MRX = TX + 2 * MASK_HALO, MRY = TY + 2 * MASK_HALO;
+constexpr int MRX = TX + 2 * MASK_HALO;
 
-template <class R>
+template <class R, int TH>
 __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x) {
+  constexpr int TY = TH, MRY = TH + 2 * MASK_HALO;
   __shared__ uint8_t seed[MRY][MRX];
   RunState* st = a.st;
   const Grid<R>& g = a.g;
@@ -196,12 +214,12 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
   return cnt;
 }
 
-template <class R>
-__global__ void __launch_bounds__(TX* TY) k_mask(KArgs<R> a, int solve_all) {
+template <class R, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_mask(KArgs<R> a, int solve_all) {
   RunState* st = a.st;
   const double t = st->t;
   if (!running(st)) return;
-  mask_tile(a, solve_all, blockIdx.x, blockIdx.y, gridDim.x);
+  mask_tile<R, TH>(a, solve_all, blockIdx.x, blockIdx.y, gridDim.x);
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
     st->src_t_coeff = source_time_coeff(st->tp, st->pi_g, t);
     st->src_t_coeff_f = (float)st->src_t_coeff;
@@ -273,12 +291,12 @@ __device__ __forceinline__ R slope(R v0, R v1, R v2, const Spacing<R>& s, int li
 // reference's use of y_stag in the x slope of v at ring cells with a ring
 // face to the north only (solver_2d.f90:3605, kept as is).
 // ---------------------------------------------------------------------------
-template <class R, int NS, int DIR, int LIM>
+template <class R, int NS, int DIR, int LIM, int TH>
 __device__ __noinline__ void recon_side_edge(const KArgs<R>& a, const R* sqp, const uint8_t* sfl,
                                            int rx, int ry, int j, int k, int plus, R* out) {
   constexpr int nv = 4 + NS, np = nv + 2;
   const Grid<R>& g = a.g;
-  constexpr int plane = RX * RY;
+  constexpr int plane = RX * TileShape<TH>::RY;
   constexpr int side_lo = (DIR == 1) ? SFLOW_W : SFLOW_S;
   constexpr int side_hi = (DIR == 1) ? SFLOW_E : SFLOW_N;
   constexpr int mom = DIR;   // hu (x) or hv (y) in the conservative/physical index
@@ -399,18 +417,18 @@ __device__ __noinline__ void recon_side_edge(const KArgs<R>& a, const R* sqp, co
 // as recon_side_edge takes for such a cell, so both give identical values;
 // the edge version is a separate (not inlined) function so that the face
 // code every thread runs stays small.
-template <class R, int NS, int DIR, int LIM>
+template <class R, int NS, int DIR, int LIM, int TH>
 __device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, const uint8_t* sfl,
                                            int rx, int ry, int j, int k, int plus, R* out) {
   constexpr int nv = 4 + NS, np = nv + 2;
   const Grid<R>& g = a.g;
-  constexpr int plane = RX * RY;
+  constexpr int plane = RX * TileShape<TH>::RY;
   const int n = (DIR == 1) ? g.nx : g.ny;
   const int c = (DIR == 1) ? j : k;
   const uint8_t fl = sfl[ry * RX + rx];
   const bool src2 = a.pr.radial_source && (fl & F_SC_MASK) == 2;
   if (c == 0 || c == n - 1 || src2) {
-    recon_side_edge<R, NS, DIR, LIM>(a, sqp, sfl, rx, ry, j, k, plus, out);
+    recon_side_edge<R, NS, DIR, LIM, TH>(a, sqp, sfl, rx, ry, j, k, plus, out);
     return;
   }
   auto QP = [&](int i, int o) -> R {
@@ -537,7 +555,7 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
 // reconstruction of both sides, the domain-edge copies and the wall mirror
 // at ring-inlet faces (solver_2d.f90:3716-3920), KT flux.  Returns the
 // largest |speed| at the face (a_interface_*_max).
-template <class R, int NS, int DIR, int LIM>
+template <class R, int NS, int DIR, int LIM, int TH>
 __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const uint8_t* sfl, int f,
                                        int o, int rxl, int ryl, int rxh, int ryh, R gcs, R* H) {
   constexpr int nv = 4 + NS, np = nv + 2;
@@ -555,8 +573,8 @@ __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const ui
   bool hl = false, hh = false;
   const int jl = (DIR == 1) ? f - 1 : o, kl = (DIR == 1) ? o : f - 1;
   const int jh = (DIR == 1) ? f : o, kh = (DIR == 1) ? o : f;
-  if (f > 0 && actl) { recon_side<R, NS, DIR, LIM>(a, sqp, sfl, rxl, ryl, jl, kl, 1, qpl); hl = true; }
-  if (f < n && acth && !mirror_h) { recon_side<R, NS, DIR, LIM>(a, sqp, sfl, rxh, ryh, jh, kh, 0, qph); hh = true; }
+  if (f > 0 && actl) { recon_side<R, NS, DIR, LIM, TH>(a, sqp, sfl, rxl, ryl, jl, kl, 1, qpl); hl = true; }
+  if (f < n && acth && !mirror_h) { recon_side<R, NS, DIR, LIM, TH>(a, sqp, sfl, rxh, ryh, jh, kh, 0, qph); hh = true; }
   if (f == 0) {
 #pragma unroll
     for (int i = 0; i < np; ++i) qpl[i] = qph[i];
@@ -590,16 +608,17 @@ __device__ __forceinline__ R face_flux(const KArgs<R>& a, const R* sqp, const ui
 
 // ---------------------------------------------------------------------------
 // k_flux: divFlux - expl_terms of one explicit stage for every active cell
-// of a 32x8 tile (eval_hyperbolic_terms, solver_2d.f90:2616-2693, and
+// of a 32 x TH tile (eval_hyperbolic_terms, solver_2d.f90:2616-2693, and
 // eval_expl_terms), plus the CFL minimum of timestep (solver_2d.f90:873-1006)
 // when want_dt.  The tile's qp (with a 2-cell halo) is computed once into
 // shared memory; each thread then evaluates one face (both reconstructed
 // sides, speeds, physical fluxes, KT flux) and finally one cell.
 // ---------------------------------------------------------------------------
-template <class R, int NS, int LIM>
+template <class R, int NS, int LIM, int TH>
 __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict__ qin,
                                           R* __restrict__ rout, int want_dt, int tx, int ty,
                                           unsigned char* smem_raw) {
+  constexpr int TY = TH, RY = TileShape<TH>::RY, FLUX_THREADS = TileShape<TH>::FLUX_THREADS;
   constexpr int nv = 4 + NS, np = nv + 2;
   const RunState* st = a.st;
   const Grid<R>& g = a.g;
@@ -700,7 +719,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
       if (f == 0) gcs = __ldg(a.geo[5] + ch);
       else if (f == g.nx) gcs = __ldg(a.geo[5] + cl);
       else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cl) + __ldg(a.geo[5] + ch));
-      amax = face_flux<R, NS, 1, LIM>(a, sqp, sfl, f, k, rxl, ry, rxh, ry, gcs, H);
+      amax = face_flux<R, NS, 1, LIM, TH>(a, sqp, sfl, f, k, rxl, ry, rxh, ry, gcs, H);
     } else {
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = R(0);
@@ -731,7 +750,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
       if (f == 0) gcs = __ldg(a.geo[5] + ch);
       else if (f == g.ny) gcs = __ldg(a.geo[5] + cl);
       else gcs = cst<R>(0.5) * (__ldg(a.geo[5] + cl) + __ldg(a.geo[5] + ch));
-      amax = face_flux<R, NS, 2, LIM>(a, sqp, sfl, f, j, rx, ryl, rx, ryh, gcs, H);
+      amax = face_flux<R, NS, 2, LIM, TH>(a, sqp, sfl, f, j, rx, ryl, rx, ryh, gcs, H);
     } else {
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = R(0);
@@ -757,14 +776,14 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
       const Geo<R> geo = load_geo(a, c);
       const uint8_t fl = sfl[ry * RX + rx];
       R ap = R(0), anx = R(0), any_ = R(0);
+      R tcoef = R(0);   // read at ring cells only (arc perimeter > 0)
       if (P.radial_source && (fl & F_SC_MASK) == 2) {
         ap = __ldg(a.arc + c);
         anx = __ldg(a.arc + g.plane + c);
         any_ = __ldg(a.arc + 2 * g.plane + c);
+        if constexpr (sizeof(R) == 8) tcoef = st->src_t_coeff;
+        else tcoef = st->src_t_coeff_f;
       }
-      R tcoef;
-      if constexpr (sizeof(R) == 8) tcoef = st->src_t_coeff;
-      else tcoef = st->src_t_coeff_f;
       expl_terms<R, NS>(P, geo, qp, tcoef, ap, anx, any_, e);
 #pragma unroll
       for (int i = 0; i < nv; ++i) {
@@ -807,16 +826,16 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   }
 }
 
-template <class R, int NS, int LIM>
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
+template <class R, int NS, int LIM, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
                                                        R* __restrict__ rout, int want_dt) {
   const RunState* st = a.st;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   // the timestep pass runs before k_dt advances the clock; the later stage
   // fluxes of a step run after it and follow its run_step decision
   if (want_dt ? !running(st) : !st->run_step) return;
   if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  flux_tile<R, NS, LIM>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
+  flux_tile<R, NS, LIM, TH>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -824,7 +843,9 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux(KArgs<R> a, const R* __re
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   if (!running(st)) { st->run_step = 0; return; }
-  double dtmin = __longlong_as_double((long long)st->dtmin_bits);
+  // the CFL minimum and the active count were accumulated with atomics by
+  // the blocks of the kernels before: read and reset them with atomics
+  double dtmin = __longlong_as_double((long long)atomicExch(&st->dtmin_bits, dbits(1.0e300)));
   double dt = max_dt;
   if (dtmin < dt) dt = dtmin;
   if (st->t_end - st->t_output < 1.0e-7) st->t_output = st->t_end;
@@ -839,11 +860,10 @@ __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   st->t = st->t + dt;
   st->run_step = 1;
   const int p = (int)(st->steps & 1);
-  st->last_cells = (long long)st->cells_acc[p];
-  st->cells_total += (long long)st->cells_acc[p];
-  st->cells_acc[p] = 0ull;
+  const unsigned long long cells = atomicExch(&st->cells_acc[p], 0ull);
+  st->last_cells = (long long)cells;
+  st->cells_total += (long long)cells;
   st->steps += 1;
-  st->dtmin_bits = dbits(1.0e300);
 }
 
 static __global__ void k_dt(RunState* st, double max_dt) { dt_update(st, max_dt); }
@@ -1101,11 +1121,11 @@ __device__ __forceinline__ unsigned stage_cell(const KArgs<R>& a, const Geo<R>& 
 }
 
 template <class R>
-__device__ __forceinline__ void newton_stats(RunState* st, unsigned status, int nit) {
+__device__ __forceinline__ void newton_stats(RunState* st, unsigned status, int nit_sum, int nit_max) {
   if (status) atomicOr(&st->status, status);
-  int wsum = nit;
+  int wsum = nit_sum;
   for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
-  int wmax = nit;
+  int wmax = nit_max;
   for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
   if ((threadIdx.x & 31) == 0 && wsum > 0) {
     atomicAdd((unsigned long long*)&st->newton_iters, (unsigned long long)wsum);
@@ -1122,69 +1142,88 @@ __device__ __forceinline__ void newton_stats(RunState* st, unsigned status, int 
 // 0: stage + assembly (imex_RK_solver); 1: erosion/deposition only;
 // 2: maxima only.
 // ---------------------------------------------------------------------------
+// One cell (j, k) of the pointwise step; returns 1 when the cell is active
+// and holds mass afterwards.  One cell per thread in every caller, so the
+// cell's arithmetic is the same code whatever the tile height.
 template <class R, int NS>
-__device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx, int ty) {
+__device__ __forceinline__ int stage2_cell(const KArgs<R>& a, int mode, int j, int k, unsigned& status,
+                                           int& nit) {
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
   const Grid<R>& g = a.g;
-  const int j = tx * TX + threadIdx.x % TX;
-  const int k = ty * TY + threadIdx.x / TX;
-  unsigned status = 0;
-  int nit = 0;
-  int wet = 0;
-  if (j < g.nx && k < g.ny) {
-    const int64_t c = cidx(g, j, k);
-    if (a.mask[c]) {
-      const double dt = st->dt;
-      R q[nv];
+  nit = 0;
+  if (j >= g.nx || k >= g.ny) return 0;
+  const int64_t c = cidx(g, j, k);
+  if (!a.mask[c]) return 0;
+  const double dt = st->dt;
+  R q[nv];
 #pragma unroll
-      for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + c];
-      if (mode > 0) {
-        if (mode == 1) {
-          const Geo<R> geo = load_geo(a, c);
-          R dep[NS];
-          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
-          add_deposit<R, NS>(a, c, dt, dep);
+  for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + c];
+  if (mode > 0) {
+    if (mode == 1) {
+      const Geo<R> geo = load_geo(a, c);
+      R dep[NS];
+      status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+      add_deposit<R, NS>(a, c, dt, dep);
 #pragma unroll
-          for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
-        } else {
-          post_step_maps<R, NS>(a, c, q);
-        }
-      } else {
-        const Geo<R> geo = load_geo(a, c);
-        R s1[nv], s2[nv], rn[nv];
-#pragma unroll
-        for (int i = 0; i < nv; ++i) {
-          s1[i] = R(0) + a.rd[i * g.plane + c] * R(1);
-          s2[i] = R(0);
-        }
-        status |= stage_cell<R, NS>(a, geo, q, s1, s2, dt, 1.0, q, rn, nit);
-        status |= assemble_fixes<R, NS>(a.pr, q);
-        if (mode < 0 && (a.pd.settling || a.pd.entrain)) {
-          R dep[NS];
-          status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
-          add_deposit<R, NS>(a, c, dt, dep);
-        }
-#pragma unroll
-        for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
-        if (mode < 0) post_step_maps<R, NS>(a, c, q);
-      }
-      wet = q[0] > R(0);
+      for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
+    } else {
+      post_step_maps<R, NS>(a, c, q);
     }
+  } else {
+    const Geo<R> geo = load_geo(a, c);
+    R s1[nv], s2[nv], rn[nv];
+#pragma unroll
+    for (int i = 0; i < nv; ++i) {
+      s1[i] = R(0) + a.rd[i * g.plane + c] * R(1);
+      s2[i] = R(0);
+    }
+    status |= stage_cell<R, NS>(a, geo, q, s1, s2, dt, 1.0, q, rn, nit);
+    status |= assemble_fixes<R, NS>(a.pr, q);
+    if (mode < 0 && (a.pd.settling || a.pd.entrain)) {
+      R dep[NS];
+      status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+      add_deposit<R, NS>(a, c, dt, dep);
+    }
+#pragma unroll
+    for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
+    if (mode < 0) post_step_maps<R, NS>(a, c, q);
   }
-  newton_stats<R>(st, status, nit);
+  return q[0] > R(0);
+}
+
+// A whole 32 x TH tile with 32 x 8 threads, 8 rows at a time (batched
+// runs), then the tile's wet flag for the candidate rule (mode -1).
+template <class R, int NS, int TH>
+__device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx, int ty) {
+  static_assert(TH % 8 == 0, "stage tiles are processed 8 rows at a time");
+  unsigned status = 0;
+  int nit_sum = 0, nit_max = 0, wet = 0;
+#pragma unroll 1
+  for (int r0 = 0; r0 < TH; r0 += 8) {
+    int nit = 0;
+    wet |= stage2_cell<R, NS>(a, mode, tx * TX + threadIdx.x % TX, ty * TH + r0 + threadIdx.x / TX, status, nit);
+    nit_sum += nit;
+    nit_max = max(nit_max, nit);
+  }
+  newton_stats<R>(a.st, status, nit_sum, nit_max);
   if (mode < 0) {
     wet = __syncthreads_or(wet);
-    if (threadIdx.x == 0) a.tile_wet[ty * g.tiles_x + tx] = (uint8_t)wet;
+    if (threadIdx.x == 0) a.tile_wet[ty * a.g.tiles_x + tx] = (uint8_t)wet;
   }
 }
 
-template <class R, int NS>
-__global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
+// single run: one block per 32 x 8 cells (grid tiles_x x ceil(ny/8)); the
+// activity byte is the one of the 32 x TH tile holding the block
+template <class R, int NS, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage2(KArgs<R> a, int mode) {
   if (!a.st->run_step) return;
-  const uint8_t ta = a.tile_active[blockIdx.y * gridDim.x + blockIdx.x];
+  const uint8_t ta = a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x];
   if (ta == 0 || ta == 2) return;   // inactive, or dry without ring cells (k_flux)
-  stage2_tile<R, NS>(a, mode, blockIdx.x, blockIdx.y);
+  unsigned status = 0;
+  int nit = 0;
+  stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, blockIdx.y * 8 + threadIdx.x / TX, status, nit);
+  newton_stats<R>(a.st, status, nit, nit);
 }
 
 // ---------------------------------------------------------------------------
@@ -1193,15 +1232,15 @@ __global__ void __launch_bounds__(TX* TY) k_stage2(KArgs<R> a, int mode) {
 // rd holds divFlux - expl and rn holds NH + SI of every stage (n_vars planes
 // per stage); qs holds the state of the running stage.
 // ---------------------------------------------------------------------------
-template <class R, int NS>
-__global__ void __launch_bounds__(TX* TY) k_stage(KArgs<R> a, int irk) {
+template <class R, int NS, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage(KArgs<R> a, int irk) {
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
   if (!st->run_step) return;
-  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  if (!a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x]) return;
   const Grid<R>& g = a.g;
   const int j = blockIdx.x * TX + threadIdx.x % TX;
-  const int k = blockIdx.y * TY + threadIdx.x / TX;
+  const int k = blockIdx.y * 8 + threadIdx.x / TX;
   unsigned status = 0;
   int nit = 0;
   if (j < g.nx && k < g.ny) {
@@ -1233,19 +1272,19 @@ __global__ void __launch_bounds__(TX* TY) k_stage(KArgs<R> a, int irk) {
       }
     }
   }
-  newton_stats<R>(st, status, nit);
+  newton_stats<R>(st, status, nit, nit);
 }
 
 // assemble_sol (solver_2d.f90:1342-1630) + erosion/deposition + maxima
-template <class R, int NS>
-__global__ void __launch_bounds__(TX* TY) k_assemble(KArgs<R> a) {
+template <class R, int NS, int TH>
+__global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_assemble(KArgs<R> a) {
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
   if (!st->run_step) return;
-  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  if (!a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x]) return;
   const Grid<R>& g = a.g;
   const int j = blockIdx.x * TX + threadIdx.x % TX;
-  const int k = blockIdx.y * TY + threadIdx.x / TX;
+  const int k = blockIdx.y * 8 + threadIdx.x / TX;
   unsigned status = 0;
   if (j < g.nx && k < g.ny) {
     const int64_t c = cidx(g, j, k);

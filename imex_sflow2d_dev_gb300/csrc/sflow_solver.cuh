@@ -83,18 +83,20 @@ static __global__ void k_stats_final(const double* __restrict__ part, int nblk, 
 template <class R>
 class Solver : public SolverBase {
  public:
-  explicit Solver(const HostSetup& s) : hs_(s) { tab_ = kernel_table<R>(s.ns); }
+  explicit Solver(const HostSetup& s, int tile_h = kTileHDefault) : hs_(s), tile_h_(tile_h) {
+    tab_ = kernel_table<R>(s.ns, tile_h);
+  }
   ~Solver() override { release(); }
 
   std::string err_;
 
   int init() {
-    if (!tab_.flux) { err_ = "no kernels built for this number of solid classes"; return SFLOW_EINVAL; }
+    if (!tab_.flux) { err_ = "no kernels built for this number of solid classes and tile height"; return SFLOW_EINVAL; }
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     pitch_ = (nx + 31) / 32 * 32;
     plane_ = (int64_t)pitch_ * ny;
     tiles_x_ = (nx + TX - 1) / TX;
-    tiles_y_ = (ny + TY - 1) / TY;
+    tiles_y_ = (ny + tile_h_ - 1) / tile_h_;
     SFLOW_CU(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     SFLOW_CU(alloc((void**)&q_, sizeof(R) * plane_ * nv));
     const int nstage = (hs_.nrk == 2) ? 1 : hs_.nrk;
@@ -126,9 +128,7 @@ class Solver : public SolverBase {
     SFLOW_CU(put_plane(arc_ + 2 * plane_, hs_.arc_ny));
     SFLOW_CU(alloc((void**)&mask_, plane_));
     SFLOW_CU(cudaMemset(mask_, 0, plane_));
-    SFLOW_CU(alloc((void**)&tile_active_, (size_t)tiles_x_ * tiles_y_));
-    SFLOW_CU(alloc((void**)&tile_wet_, (size_t)tiles_x_ * tiles_y_));
-    SFLOW_CU(cudaMemset(tile_wet_, 1, (size_t)tiles_x_ * tiles_y_));
+    SFLOW_CU(alloc_tiles());
     SFLOW_CU(alloc((void**)&hmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&pdynmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&mvmax_, sizeof(R) * plane_));
@@ -143,7 +143,7 @@ class Solver : public SolverBase {
     SFLOW_CU(cudaMemset(q_, 0, sizeof(R) * plane_ * nv));
     fill_args();
     // shared memory of the flux kernel
-    smem_flux_ = flux_smem_bytes();
+    smem_flux_ = flux_smem_bytes(hs_.nv, tile_h_);
     SFLOW_CU(set_smem_attr());
     std::memset(&hst_, 0, sizeof(hst_));
     init_state_host();
@@ -157,6 +157,15 @@ class Solver : public SolverBase {
   int tiles_x() const { return tiles_x_; }
   int tiles_y() const { return tiles_y_; }
   size_t smem_flux() const { return smem_flux_; }
+  // dynamic shared memory of flux_tile: qp of the tile + halo, x- and
+  // y-face fluxes and speeds, flag bytes of the tile + halo
+  static size_t flux_smem_bytes(int nv, int th) {
+    const int np = nv + 2;
+    const size_t ry = (size_t)th + 2 * HALO;
+    const size_t r = (size_t)np * RX * ry + (size_t)nv * th * (TX + 1) + (size_t)nv * (th + 1) * TX +
+                     (size_t)th * (TX + 1) + (size_t)(th + 1) * TX;
+    return (r * sizeof(R) + RX * ry + 15) / 16 * 16;
+  }
   cudaStream_t stream() const { return stream_; }
   const HostSetup& setup() const { return hs_; }
   int limits(double t_stop, int64_t step_limit) {
@@ -177,6 +186,7 @@ class Solver : public SolverBase {
   std::vector<uint8_t> tile_seed_host() const {
     std::vector<uint8_t> ts((size_t)tiles_x_ * tiles_y_, 0);
     const int nx = hs_.nx, ny = hs_.ny, nrk = hs_.nrk;
+    const int TY = tile_h_;
     const int wlast = nx - (tiles_x_ - 1) * TX, hlast = ny - (tiles_y_ - 1) * TY;
     for (int ty = 0; ty < tiles_y_; ++ty)
       for (int tx = 0; tx < tiles_x_; ++tx) {
@@ -193,10 +203,10 @@ class Solver : public SolverBase {
   uint8_t* tile_wet_dev() const { return tile_wet_; }
 
   // device bytes a run of this set-up holds while it is in a batch
-  static int64_t batch_bytes(const HostSetup& hs) {
+  static int64_t batch_bytes(const HostSetup& hs, int tile_h) {
     const int64_t pitch = (hs.nx + 31) / 32 * 32, plane = pitch * hs.ny;
     const int ngeo = hs.p.curvature_term_flag ? 8 : 5;
-    const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + TY - 1) / TY);
+    const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + tile_h - 1) / tile_h);
     return plane * (int64_t)sizeof(R) * (2 * hs.nv + ngeo + 3 + 3) + 2 * plane + tiles * 7 +
            (int64_t)sizeof(double) * 4 * 1024 + 4096;
   }
@@ -462,6 +472,84 @@ class Solver : public SolverBase {
     return s ? stats(s) : SFLOW_OK;
   }
 
+  // tile shape ----------------------------------------------------------------
+  int tile_shape() const override { return tile_h_; }
+
+  // Switch the tiled kernels to tiles of TX x th cells.  The step's results
+  // do not depend on the tile height, so a run may switch between steps: the
+  // per-tile arrays are re-made (wet flags unknown = 1; activity is
+  // recomputed by the next check_solve) and the captured graphs dropped.
+  int set_tile_shape(int th) override {
+    if (th == tile_h_) return SFLOW_OK;
+    KernelTable<R> t = kernel_table<R>(hs_.ns, th);
+    if (!t.flux) { err_ = "no kernels built for this tile height"; return SFLOW_EINVAL; }
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    drop_graphs();
+    const size_t n_old = (size_t)tiles_x_ * tiles_y_;
+    free_tracked(tile_active_, n_old);
+    free_tracked(tile_wet_, n_old);
+    tile_active_ = tile_wet_ = nullptr;
+    tab_ = t;
+    tile_h_ = th;
+    tiles_y_ = (hs_.ny + th - 1) / th;
+    SFLOW_CU(alloc_tiles());
+    ka_.g.tiles_y = tiles_y_;
+    ka_.tile_active = tile_active_;
+    ka_.tile_wet = tile_wet_;
+    smem_flux_ = flux_smem_bytes(hs_.nv, th);
+    SFLOW_CU(set_smem_attr());
+    return SFLOW_OK;
+  }
+
+  // Tile-shape autotuner: times `steps` graph-replayed steps of this run
+  // with every compiled tile height (after one untimed chunk that captures
+  // the graph) and keeps the height with the least time per active-cell
+  // update.  The steps are real steps of the run (the results are the same
+  // with every height); ms_per_mcu[i] receives the time per 10^6 cell
+  // updates of candidate i of kTileCandidates (-1 when not compiled).
+  int autotune(int64_t steps, int* best, double* ms_per_mcu) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    if (steps < 1) { err_ = "autotune needs at least one step per tile height"; return SFLOW_EINVAL; }
+    SFLOW_CU(prepare_timing(0));
+    int best_th = tile_h_;
+    double best_v = -1.0;
+    for (int i = 0; i < kTileCandidates; ++i) {
+      const int th = kTileCandidate[i];
+      ms_per_mcu[i] = -1.0;
+      if (!tile_h_built<R>(th)) continue;
+      int rc = set_tile_shape(th);
+      if (rc != SFLOW_OK) return rc;
+      SFLOW_CU(set_limits(hs_.p.t_end, -1));
+      if (!graph_exec_) SFLOW_CU(build_graph());
+      SFLOW_CU(cudaGraphLaunch(graph_exec_, stream_));   // warm-up chunk
+      launches_ += kChunk * steps_launches();
+      RunState h0, h1;
+      SFLOW_CU(cudaMemcpyAsync(&h0, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+      SFLOW_CU(cudaEventRecord(ev_[0], stream_));
+      const int64_t chunks = (steps + kChunk - 1) / kChunk;
+      for (int64_t c = 0; c < chunks; ++c) {
+        SFLOW_CU(cudaGraphLaunch(graph_exec_, stream_));
+        launches_ += kChunk * steps_launches();
+      }
+      SFLOW_CU(cudaEventRecord(ev_[1], stream_));
+      SFLOW_CU(cudaMemcpyAsync(&h1, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+      SFLOW_CU(cudaStreamSynchronize(stream_));
+      float m = 0.0f;
+      SFLOW_CU(cudaEventElapsedTime(&m, ev_[0], ev_[1]));
+      const long long cells = h1.cells_total - h0.cells_total;
+      if (cells <= 0) continue;   // the run stopped: nothing measured
+      ms_per_mcu[i] = (double)m / ((double)cells * 1.0e-6);
+      if (best_v < 0.0 || ms_per_mcu[i] < best_v) {
+        best_v = ms_per_mcu[i];
+        best_th = th;
+      }
+    }
+    int rc = set_tile_shape(best_th);
+    if (rc != SFLOW_OK) return rc;
+    *best = best_th;
+    return SFLOW_OK;
+  }
+
   // fused driver iteration -----------------------------------------------------
   int step() override {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
@@ -550,6 +638,7 @@ class Solver : public SolverBase {
   HostSetup hs_;
   int pitch_ = 0;
   int64_t plane_ = 0;
+  int tile_h_ = kTileHDefault;   // cells per tile column (TileShape)
   int tiles_x_ = 0, tiles_y_ = 0;
   cudaStream_t stream_ = nullptr;
   R *q_ = nullptr, *rd_ = nullptr, *rn_ = nullptr, *qs_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
@@ -628,6 +717,35 @@ class Solver : public SolverBase {
       bytes_ += (int64_t)bytes;
     }
     return e;
+  }
+
+  // per-tile bytes (activity, wet flag) for the current tile height
+  cudaError_t alloc_tiles() {
+    const size_t n = (size_t)tiles_x_ * tiles_y_;
+    cudaError_t e = alloc((void**)&tile_active_, n);
+    if (e == cudaSuccess) e = alloc((void**)&tile_wet_, n);
+    if (e == cudaSuccess) e = cudaMemset(tile_active_, 0, n);
+    if (e == cudaSuccess) e = cudaMemset(tile_wet_, 1, n);
+    return e;
+  }
+  void free_tracked(void* p, size_t bytes) {
+    for (auto it = allocs_.begin(); it != allocs_.end(); ++it)
+      if (*it == p) {
+        allocs_.erase(it);
+        break;
+      }
+    cudaFree(p);
+    bytes_ -= (int64_t)bytes;
+  }
+  void drop_graphs() {
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    if (graph1_exec_) cudaGraphExecDestroy(graph1_exec_);
+    if (graph1_) cudaGraphDestroy(graph1_);
+    graph_exec_ = nullptr;
+    graph_ = nullptr;
+    graph1_exec_ = nullptr;
+    graph1_ = nullptr;
   }
 
   void release() {
@@ -785,20 +903,12 @@ class Solver : public SolverBase {
     return cudaStreamSynchronize(stream_);
   }
 
-  size_t flux_smem_bytes() const {
-    const int nv = hs_.nv, np = nv + 2;
-    size_t r = (size_t)np * RX * RY + (size_t)nv * TY * (TX + 1) + (size_t)nv * (TY + 1) * TX + TY * (TX + 1) +
-               (TY + 1) * TX;
-    return r * sizeof(R) + RX * RY;
-  }
 
   cudaError_t set_smem_attr() { return tab_.set_smem(smem_flux_); }
 
   cudaError_t launch_mask(int solve_all) {
-    dim3 grid(tiles_x_, tiles_y_);
-    k_mask<R><<<grid, TX * TY, 0, stream_>>>(ka_, solve_all);
     ++launches_;
-    return cudaGetLastError();
+    return tab_.mask(ka_, dim3(tiles_x_, tiles_y_), stream_, solve_all);
   }
   cudaError_t launch_flux(int want_dt) {
     ++launches_;

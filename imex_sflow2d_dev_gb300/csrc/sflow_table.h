@@ -1,9 +1,13 @@
-// sflow_table.h -- per-(precision, solid-class count) kernel entry points.
-// The class count is a compile-time parameter of the heavy kernels so their
-// per-variable arrays stay in registers; each (precision, count) pair is its
-// own translation unit (sflow_k_*.cu) so the build parallelises.
+// sflow_table.h -- per-(precision, solid-class count, tile height) kernel
+// entry points.  The class count is a compile-time parameter of the heavy
+// kernels so their per-variable arrays stay in registers, and the tile
+// height (cells per tile column) one of every tiled kernel; each
+// (precision, count, height) triple is its own translation unit
+// (sflow_k_*.cu) so the build parallelises.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "sflow_types.cuh"
 
@@ -16,6 +20,8 @@ struct BatchArgs;
 
 template <class R>
 struct KernelTable {
+  int tile_h = 0;   // tile height of the tiled entries
+  cudaError_t (*mask)(const KArgs<R>&, dim3, cudaStream_t, int) = nullptr;
   cudaError_t (*flux)(const KArgs<R>&, dim3, size_t, cudaStream_t, const R*, R*, int) = nullptr;
   cudaError_t (*stage2)(const KArgs<R>&, dim3, cudaStream_t, int) = nullptr;
   cudaError_t (*stage)(const KArgs<R>&, dim3, cudaStream_t, int) = nullptr;
@@ -36,19 +42,41 @@ struct KernelTable {
 
 template <class R, int NS>
 KernelTable<R> make_table();
+template <class R, int NS, int TH>
+void fill_tile_entries(KernelTable<R>& t);
 
 // solid-class counts with compiled kernels
 constexpr int kMinSolidBuilt = 1;
 constexpr int kMaxSolidBuilt = 3;
 
+// tile heights the autotuner tries, and those with compiled kernels: 8 and
+// 16 for the FP32 bulk form, 8 for the FP64 plain form
+constexpr int kTileCandidates = 2;
+constexpr int kTileCandidate[kTileCandidates] = {8, 16};
 template <class R>
-inline KernelTable<R> kernel_table(int ns) {
-  switch (ns) {
-    case 1: return make_table<R, 1>();
-    case 2: return make_table<R, 2>();
-    case 3: return make_table<R, 3>();
+inline bool tile_h_built(int th) {
+  return th == 8 || (std::is_same<R, float>::value && th == 16);
+}
+
+template <class R, int NS>
+inline void fill_tiles(KernelTable<R>& t, int th) {
+  if (th == 8) fill_tile_entries<R, NS, 8>(t);
+  if constexpr (std::is_same<R, float>::value) {
+    if (th == 16) fill_tile_entries<R, NS, 16>(t);
   }
-  return KernelTable<R>();
+}
+
+// the table of (ns, th); entries are null when either has no kernels
+template <class R>
+inline KernelTable<R> kernel_table(int ns, int th) {
+  KernelTable<R> t;
+  if (!tile_h_built<R>(th)) return t;
+  switch (ns) {
+    case 1: t = make_table<R, 1>(); fill_tiles<R, 1>(t, th); break;
+    case 2: t = make_table<R, 2>(); fill_tiles<R, 2>(t, th); break;
+    case 3: t = make_table<R, 3>(); fill_tiles<R, 3>(t, th); break;
+  }
+  return t;
 }
 
 }  // namespace sflow

@@ -118,30 +118,97 @@ __global__ void k_stats_partial(KArgs<R> a, double* __restrict__ part) {
 }
 
 
-template <class R, int NS>
+// ---- tile-height dependent entries (one translation unit per height) ----
+// pointwise kernels of a single run: one block per 32 x 8 cells
+static inline dim3 stage_grid(dim3 tiles, int ny) { return dim3(tiles.x, (unsigned)((ny + 7) / 8)); }
+
+template <class R, int NS, int TH>
+static cudaError_t tab_mask(const KArgs<R>& a, dim3 grid, cudaStream_t s, int solve_all) {
+  k_mask<R, TH><<<grid, TileShape<TH>::MASK_THREADS, 0, s>>>(a, solve_all);
+  return cudaGetLastError();
+}
+template <class R, int NS, int TH>
 static cudaError_t tab_flux(const KArgs<R>& a, dim3 grid, size_t smem, cudaStream_t s, const R* qin,
                             R* rout, int want_dt) {
   // minmod everywhere (the reference default) has its own instantiation:
   // one limiter case instead of eight per variable keeps the code small
-  if (a.g.lim_all == 1) k_flux<R, NS, 1><<<grid, FLUX_THREADS, smem, s>>>(a, qin, rout, want_dt);
-  else k_flux<R, NS, -1><<<grid, FLUX_THREADS, smem, s>>>(a, qin, rout, want_dt);
+  constexpr int T = TileShape<TH>::FLUX_THREADS;
+  if (a.g.lim_all == 1) k_flux<R, NS, 1, TH><<<grid, T, smem, s>>>(a, qin, rout, want_dt);
+  else k_flux<R, NS, -1, TH><<<grid, T, smem, s>>>(a, qin, rout, want_dt);
   return cudaGetLastError();
 }
-template <class R, int NS>
+template <class R, int NS, int TH>
 static cudaError_t tab_stage2(const KArgs<R>& a, dim3 grid, cudaStream_t s, int mode) {
-  k_stage2<R, NS><<<grid, TX * TY, 0, s>>>(a, mode);
+  k_stage2<R, NS, TH><<<stage_grid(grid, a.g.ny), TileShape<TH>::STAGE_THREADS, 0, s>>>(a, mode);
   return cudaGetLastError();
 }
-template <class R, int NS>
+template <class R, int NS, int TH>
 static cudaError_t tab_stage(const KArgs<R>& a, dim3 grid, cudaStream_t s, int irk) {
-  k_stage<R, NS><<<grid, TX * TY, 0, s>>>(a, irk);
+  k_stage<R, NS, TH><<<stage_grid(grid, a.g.ny), TileShape<TH>::STAGE_THREADS, 0, s>>>(a, irk);
   return cudaGetLastError();
 }
-template <class R, int NS>
+template <class R, int NS, int TH>
 static cudaError_t tab_assemble(const KArgs<R>& a, dim3 grid, cudaStream_t s) {
-  k_assemble<R, NS><<<grid, TX * TY, 0, s>>>(a);
+  k_assemble<R, NS, TH><<<stage_grid(grid, a.g.ny), TileShape<TH>::STAGE_THREADS, 0, s>>>(a);
   return cudaGetLastError();
 }
+template <class R, int NS, int TH>
+static cudaError_t tab_smem(size_t bytes) {
+  cudaError_t e = cudaFuncSetAttribute(k_flux<R, NS, 1, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_flux<R, NS, -1, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+template <class R, int NS, int TH>
+static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_b_flux<R, NS, 1, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_b_flux<R, NS, -1, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
+  if (e != cudaSuccess) return e;
+  int occ[3] = {0, 0, 0};
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_b_mask<R, TH>, TileShape<TH>::MASK_THREADS, 0);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_b_flux<R, NS, -1, TH>, TileShape<TH>::FLUX_THREADS,
+                                                    smem_flux);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_b_stage2<R, NS, TH>, TileShape<TH>::STAGE_THREADS, 0);
+  if (e != cudaSuccess) return e;
+  grids[0] = sms * 4;
+  grids[1] = sms * (occ[0] > 0 ? occ[0] : 1);
+  grids[2] = sms * (occ[1] > 0 ? occ[1] : 1);
+  grids[3] = sms * (occ[2] > 0 ? occ[2] : 1);
+  return cudaSuccess;
+}
+template <class R, int NS, int TH>
+static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux, int lim) {
+  constexpr int T = TileShape<TH>::FLUX_THREADS;
+  k_b_cand<R><<<grids[0], kBatchCandThreads, 0, s>>>(b);
+  k_b_mask<R, TH><<<grids[1], TileShape<TH>::MASK_THREADS, 0, s>>>(b);
+  if (lim == 1) k_b_flux<R, NS, 1, TH><<<grids[2], T, smem_flux, s>>>(b);
+  else k_b_flux<R, NS, -1, TH><<<grids[2], T, smem_flux, s>>>(b);
+  k_b_dt<R><<<1, kBatchCandThreads, 0, s>>>(b);
+  k_b_stage2<R, NS, TH><<<grids[3], TileShape<TH>::STAGE_THREADS, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+template <class R, int NS, int TH>
+void fill_tile_entries(KernelTable<R>& t) {
+  t.tile_h = TH;
+  t.mask = &tab_mask<R, NS, TH>;
+  t.flux = &tab_flux<R, NS, TH>;
+  t.stage2 = &tab_stage2<R, NS, TH>;
+  t.stage = &tab_stage<R, NS, TH>;
+  t.assemble = &tab_assemble<R, NS, TH>;
+  t.set_smem = &tab_smem<R, NS, TH>;
+  t.b_setup = &tab_b_setup<R, NS, TH>;
+  t.b_step = &tab_b_step<R, NS, TH>;
+}
+
+// ---- entries that do not depend on the tile height ----
 template <class R, int NS>
 static cudaError_t tab_init_maps(const KArgs<R>& a, unsigned blocks, cudaStream_t s) {
   k_init_maps<R, NS><<<blocks, 256, 0, s>>>(a);
@@ -163,47 +230,6 @@ static cudaError_t tab_stats(const KArgs<R>& a, int blocks, cudaStream_t s, doub
   return cudaGetLastError();
 }
 template <class R, int NS>
-static cudaError_t tab_smem(size_t bytes) {
-  cudaError_t e = cudaFuncSetAttribute(k_flux<R, NS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_flux<R, NS, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
-template <class R, int NS>
-static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
-  int dev = 0, sms = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_b_flux<R, NS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_b_flux<R, NS, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_flux);
-  if (e != cudaSuccess) return e;
-  int occ[3] = {0, 0, 0};
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_b_mask<R>, TX * TY, 0);
-  if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_b_flux<R, NS, -1>, FLUX_THREADS, smem_flux);
-  if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_b_stage2<R, NS>, TX * TY, 0);
-  if (e != cudaSuccess) return e;
-  grids[0] = sms * 4;
-  grids[1] = sms * (occ[0] > 0 ? occ[0] : 1);
-  grids[2] = sms * (occ[1] > 0 ? occ[1] : 1);
-  grids[3] = sms * (occ[2] > 0 ? occ[2] : 1);
-  return cudaSuccess;
-}
-template <class R, int NS>
-static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux, int lim) {
-  k_b_cand<R><<<grids[0], kBatchCandThreads, 0, s>>>(b);
-  k_b_mask<R><<<grids[1], TX * TY, 0, s>>>(b);
-  if (lim == 1) k_b_flux<R, NS, 1><<<grids[2], FLUX_THREADS, smem_flux, s>>>(b);
-  else k_b_flux<R, NS, -1><<<grids[2], FLUX_THREADS, smem_flux, s>>>(b);
-  k_b_dt<R><<<1, kBatchCandThreads, 0, s>>>(b);
-  k_b_stage2<R, NS><<<grids[3], TX * TY, 0, s>>>(b);
-  return cudaGetLastError();
-}
-template <class R, int NS>
 static cudaError_t tab_b_admit(const BatchArgs<R>& b, cudaStream_t s, int slot, unsigned gen, unsigned ntiles) {
   k_b_admit<R><<<1, 256, 0, s>>>(b, slot, gen, ntiles);
   return cudaGetLastError();
@@ -217,17 +243,10 @@ static cudaError_t tab_b_summary(const BatchArgs<R>& b, cudaStream_t s) {
 template <class R, int NS>
 KernelTable<R> make_table() {
   KernelTable<R> t;
-  t.flux = &tab_flux<R, NS>;
-  t.stage2 = &tab_stage2<R, NS>;
-  t.stage = &tab_stage<R, NS>;
-  t.assemble = &tab_assemble<R, NS>;
   t.init_maps = &tab_init_maps<R, NS>;
   t.qp = &tab_qp<R, NS>;
   t.phys = &tab_phys<R, NS>;
   t.stats = &tab_stats<R, NS>;
-  t.set_smem = &tab_smem<R, NS>;
-  t.b_setup = &tab_b_setup<R, NS>;
-  t.b_step = &tab_b_step<R, NS>;
   t.b_admit = &tab_b_admit<R, NS>;
   t.b_summary = &tab_b_summary<R, NS>;
   return t;

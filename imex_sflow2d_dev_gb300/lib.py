@@ -93,6 +93,12 @@ def load(build_if_missing=True):
         "sflow_batch_collect": (C.c_int, [vp, i32, dp]),
         "sflow_batch_live": (i32, [vp]),
         "sflow_batch_launch_count": (i64, [vp]),
+        "sflow_tile_shapes": (C.c_int, [i32, C.POINTER(i32), i32, C.POINTER(i32)]),
+        "sflow_set_tile_shape": (C.c_int, [vp, i32]),
+        "sflow_get_tile_shape": (C.c_int, [vp, C.POINTER(i32)]),
+        "sflow_autotune": (C.c_int, [vp, i64, C.POINTER(i32), dp, i32]),
+        "sflow_batch_set_tile_shape": (C.c_int, [vp, i32]),
+        "sflow_batch_get_tile_shape": (C.c_int, [vp, C.POINTER(i32)]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -117,7 +123,21 @@ def exported_symbols():
             "sflow_read_dem", "sflow_read_q2d", "sflow_write_q2d", "sflow_write_p2d",
             "sflow_write_restart", "sflow_read_restart", "sflow_output_name",
             "sflow_download_phys", "sflow_download_deposit", "sflow_upload_deposit",
-            "sflow_upload_maps", "sflow_set_output_time"]
+            "sflow_upload_maps", "sflow_set_output_time", "sflow_tile_shapes",
+            "sflow_set_tile_shape", "sflow_get_tile_shape", "sflow_autotune",
+            "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape"]
+
+
+TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
+
+
+def tile_shapes(precision):
+    """Tile heights (cells per tile column) with compiled kernels."""
+    lib = load()
+    h = (C.c_int32 * 8)()
+    n = C.c_int32(0)
+    _check(lib.sflow_tile_shapes(precision, h, 8, C.byref(n)))
+    return [h[i] for i in range(n.value)]
 
 
 def log_sums_noalloc(params, q_dev_ptr, sums_dev_ptr, stream_ptr=0):
@@ -407,6 +427,23 @@ class Solver:
     def device_bytes(self):
         return self.lib.sflow_device_bytes(self.h)
 
+    def tile_shape(self):
+        v = C.c_int32(0)
+        _check(self.lib.sflow_get_tile_shape(self.h, C.byref(v)))
+        return v.value
+
+    def set_tile_shape(self, tile_h):
+        _check(self.lib.sflow_set_tile_shape(self.h, int(tile_h)))
+
+    def autotune(self, steps_per_shape=64):
+        """Time the compiled tile heights on this run (the steps advance
+        the run) and keep the fastest; returns (best height, {height: ms
+        per 10^6 cell updates})."""
+        best = C.c_int32(0)
+        v = (C.c_double * len(TILE_CANDIDATES))()
+        _check(self.lib.sflow_autotune(self.h, int(steps_per_shape), C.byref(best), v, len(TILE_CANDIDATES)))
+        return best.value, {th: v[i] for i, th in enumerate(TILE_CANDIDATES) if v[i] >= 0}
+
 
 EBUSY = -6
 
@@ -489,3 +526,12 @@ class Batch:
 
     def launch_count(self):
         return self.lib.sflow_batch_launch_count(self.h)
+
+    def tile_shape(self):
+        v = C.c_int32(0)
+        _check(self.lib.sflow_batch_get_tile_shape(self.h, C.byref(v)))
+        return v.value
+
+    def set_tile_shape(self, tile_h):
+        """Tile height of the runs admitted from now on (no run may be live)."""
+        _check(self.lib.sflow_batch_set_tile_shape(self.h, int(tile_h)))

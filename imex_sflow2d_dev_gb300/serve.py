@@ -33,8 +33,11 @@ class Request:
 
 
 class RequestLoop:
-    def __init__(self, precision, max_runs=256, max_cells=1 << 28, chunk=16, keep_results=False):
+    def __init__(self, precision, max_runs=256, max_cells=1 << 28, chunk=16, keep_results=False,
+                 tile_h=None):
         self.batch = L.Batch(precision, max_runs=max_runs, max_cells=max_cells)
+        if tile_h:
+            self.batch.set_tile_shape(tile_h)
         self.chunk = chunk
         self.keep = keep_results
 

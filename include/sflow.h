@@ -234,6 +234,33 @@ int64_t sflow_launch_count(const sflow_handle* h);
 /* Device bytes held by the handle. */
 int64_t sflow_device_bytes(const sflow_handle* h);
 
+/*
+ * Tile shape and its autotuner (no counterpart in the reference, whose loops
+ * run over cells: the tiling is how this library maps the step onto the
+ * GPU).  The tiled kernels work on tiles of 32 x tile_h cells; the results
+ * of a step are the same for every tile height.  Heights with compiled
+ * kernels: 8 and 16 in the FP32 bulk form, 8 in the FP64 plain form
+ * (sflow_tile_shapes lists them; the default is 8).
+ *
+ * sflow_set_tile_shape  switch a run between steps (SFLOW_EINVAL for a
+ *                       height without kernels)
+ * sflow_autotune        runs `steps_per_shape` steps of the run (after one
+ *                       untimed 16-step graph chunk) with each candidate
+ *                       height, times them with CUDA events, keeps the
+ *                       fastest per active-cell update and returns it in
+ *                       *best; ms_per_mcu[i] (n entries, candidates in the
+ *                       order of sflow_tile_shapes' full list 8, 16) gets
+ *                       the ms per 10^6 cell updates, -1 where not
+ *                       compiled or nothing ran.  The steps advance the run.
+ * sflow_batch_set_tile_shape  height of the batch's runs; only while the
+ *                       batch holds no run (SFLOW_ESTATE otherwise)
+ */
+#define SFLOW_TILE_CANDIDATES 2
+int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count);
+int sflow_set_tile_shape(sflow_handle* h, int32_t tile_h);
+int sflow_get_tile_shape(const sflow_handle* h, int32_t* tile_h);
+int sflow_autotune(sflow_handle* h, int64_t steps_per_shape, int32_t* best, double* ms_per_mcu, int32_t n);
+
 /* Work counters since the last upload: cell updates (sum over steps of the
  * active cells), steps, Newton iterations and the largest per-cell count. */
 int sflow_counters(sflow_handle* h, int64_t* cell_updates, int64_t* steps,
@@ -315,6 +342,8 @@ int sflow_batch_download(sflow_batch* b, int32_t run_id, double* q_aos);
 int sflow_batch_collect(sflow_batch* b, int32_t run_id, double* q_aos);
 int32_t sflow_batch_live(const sflow_batch* b);
 int64_t sflow_batch_launch_count(const sflow_batch* b);
+int sflow_batch_set_tile_shape(sflow_batch* b, int32_t tile_h);
+int sflow_batch_get_tile_shape(const sflow_batch* b, int32_t* tile_h);
 
 /*
  * Host I/O of the reference's files (host only, no GPU needed), so a run
