@@ -148,28 +148,25 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
   }
 }
 
+// check_solve reads a handful of the run's arguments (grid sizes, n_RK,
+// the ring flag, four pointers), so they come straight from the argument
+// table in global memory (L1-cached) instead of a shared-memory copy of the
+// whole KArgs per run change: candidate lists interleave the runs' tiles.
 template <class R, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
-  __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx;
-  KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   unsigned long long* out = pp ? b.list0 : b.list1;
   const unsigned n = ctl->ncand;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->work[1] = 0u;
-  int cur = -1;
   for (;;) {
     const unsigned i = next_tile(&ctl->work[0], &s_idx);
     if (i >= n) break;
     const unsigned long long e = b.cand[i];
     const int slot = entry_slot(e);
     const unsigned tile = entry_tile(e);
-    if (slot != cur) {
-      load_args(&a, &b.args[slot]);
-      cur = slot;
-      __syncthreads();
-    }
+    const KArgs<R>& a = b.args[slot];
     const BatchRun& br = b.runs[slot];
     if (threadIdx.x == 0) br.cand[tile] = 0u;
     if (!running(a.st)) continue;
