@@ -1102,7 +1102,7 @@ __device__ __forceinline__ unsigned stage_cell(const KArgs<R>& a, const Geo<R>& 
 #pragma unroll
         for (int i = 0; i < nv; ++i) { si[i] = (qsi[i] - qfv[i]) * idta; qg[i] = qsi[i]; }
         float e1, e2;
-        const float sv = reduced_friction_solve<NS>(P, geo.Bx, geo.By, qsi, dt * a_diag, e1, e2, nit);
+        const float sv = reduced_friction_solve<NS>(P, a.pd, geo.Bx, geo.By, qsi, dt * a_diag, e1, e2, nit);
         qg[1] = sv * e1;
         qg[2] = sv * e2;
         if (a.g.ny == 1) qg[2] = R(0);

@@ -818,7 +818,8 @@ __device__ __forceinline__ double rcp64(double x) {
 }
 
 template <int NS>
-__device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, float Bx, float By,
+__device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, const Phys<double>& PD,
+                                                        float Bx, float By,
                                                         const float* q, double dta, float& e1,
                                                         float& e2, int& iters) {
   constexpr int ns = NS;
@@ -891,11 +892,11 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, fl
   {
     const double sd2 = sd * sd;
     double T = (double)a_T - (double)b_T * sd2;
-    if (T <= 0.0) T = (double)P.T_ambient;
+    if (T <= 0.0) T = PD.T_ambient;   // FP64 constants: no conversion on the FP64 pipe
     const double x = (double)base_inv + (double)c_inv * T;
     double rho_m = (double)__frcp_rn((float)x);
     rho_m = rho_m * (2.0 - x * rho_m);
-    const double Kd = (double)cgeo * (rho_m - (double)rho_a);
+    const double Kd = (double)cgeo * (rho_m - ((P.rheo_model == 1) ? PD.rho_a_amb : 0.0));
     const double gv = (sd - (double)S) + dta * Kd * sd2;
     sd -= gv * (double)__frcp_rn(gdf);
     iters = 1;

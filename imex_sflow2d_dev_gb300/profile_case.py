@@ -27,11 +27,13 @@ def main():
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--ensemble", type=int, default=0)
+    ap.add_argument("--tile-h", type=int, default=8, help="tile height (8, or 16 in FP32)")
     a = ap.parse_args()
     if a.ensemble > 0:
         members = [W.ensemble_params(i, PREC_FP32, 100000) for i in range(a.ensemble)]
         cells = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members)
         b = lib.Batch(PREC_FP32, max_runs=a.ensemble, max_cells=int(cells * 1.2) + 4096)
+        b.set_tile_shape(a.tile_h)
         ids = [b.submit(p, B, W.to_aos(q), max_steps=st) for p, B, q, st in members]
         b.advance(a.steps)
         cu = sum(b.counters(i)["cell_updates"] for i in ids)
@@ -43,12 +45,13 @@ def main():
                             t_end=1.0e9)
     q = W.developed_current_state(p, B)
     s = lib.Solver(p, B)
+    s.set_tile_shape(a.tile_h)
     s.upload_q(W.to_aos(q))
     for _ in range(a.steps):
         s.step()
     st = s.stats()
     c = s.counters()
-    print(f"n={a.n} precision={a.precision} steps={st.steps} t={st.t:.4f} "
+    print(f"n={a.n} precision={a.precision} tile=32x{a.tile_h} steps={st.steps} t={st.t:.4f} "
           f"active/step={c['cell_updates'] / max(c['steps'], 1):.0f} status={st.status}")
     s.close()
 
