@@ -13,6 +13,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <memory>
 #include <string>
 #include <vector>
@@ -144,7 +145,7 @@ class Batch : public BatchBase {
         left -= kChunk;
       }
       for (; left > 0; --left) {
-        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux, g->lim);
+        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux, g->lim, g->pdl);
         if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
         g->launches += 5;
       }
@@ -300,6 +301,7 @@ class Batch : public BatchBase {
     int grids[4] = {0, 0, 0, 0};
     size_t smem_flux = 0;
     int lim = 1;   // 1 while every submitted run uses minmod everywhere, else -1
+    int pdl = 1;   // programmatic dependent launch of the step kernels (SFLOW_PDL=0: off)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<Slot> slots;
@@ -310,7 +312,7 @@ class Batch : public BatchBase {
       cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
       for (int i = 0; i < kChunk; ++i) {
-        e = tab.b_step(args, stream, grids, smem_flux, lim);
+        e = tab.b_step(args, stream, grids, smem_flux, lim, pdl);
         if (e != cudaSuccess) {
           cudaGraph_t g0 = nullptr;
           cudaStreamEndCapture(stream, &g0);
@@ -355,6 +357,10 @@ class Batch : public BatchBase {
     if (groups_[ns]) return groups_[ns].get();
     std::unique_ptr<Group> g(new Group());
     g->tab = kernel_table<R>(ns, tile_h_);
+    {
+      const char* pdl_env = std::getenv("SFLOW_PDL");
+      g->pdl = (pdl_env && pdl_env[0] == '0') ? 0 : 1;
+    }
     if (!g->tab.b_step) { err_ = "no batch kernels for this class count and tile height"; return nullptr; }
     g->slots.resize(max_runs_);
     // shared memory of the flux kernel for this class count (the largest

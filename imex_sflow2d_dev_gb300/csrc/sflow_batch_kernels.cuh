@@ -107,6 +107,7 @@ __device__ __forceinline__ unsigned next_tile(unsigned* counter, unsigned* s_idx
 
 template <class R>
 __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
+  step_kernel_entry();
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   const unsigned long long* L = pp ? b.list1 : b.list0;
@@ -155,6 +156,7 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
 template <class R, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
   __shared__ unsigned s_idx;
+  step_kernel_entry();
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   unsigned long long* out = pp ? b.list0 : b.list1;
@@ -189,6 +191,7 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FL
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx;
+  step_kernel_entry();
   KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
@@ -216,6 +219,7 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FL
 
 template <class R>
 __global__ void __launch_bounds__(kBatchCandThreads) k_b_dt(BatchArgs<R> b) {
+  step_kernel_entry();
   const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned G = gridDim.x * blockDim.x;
   for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
@@ -235,6 +239,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, TileShape<TH>::S
     k_b_stage2(BatchArgs<R> b) {
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx;
+  step_kernel_entry();
   KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;

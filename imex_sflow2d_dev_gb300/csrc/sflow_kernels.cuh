@@ -81,9 +81,37 @@ struct KArgs {
 // ---------------------------------------------------------------------------
 // helpers
 // ---------------------------------------------------------------------------
+// Launch with programmatic stream serialisation (see step_kernel_entry);
+// pdl = 0 gives an ordinary launch.
+template <typename... KParams, typename... Args>
+static cudaError_t launch_step_kernel(void (*kern)(KParams...), dim3 grid, dim3 block, size_t smem,
+                                      cudaStream_t s, int pdl, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
 template <class R>
 __device__ __forceinline__ int64_t cidx(const Grid<R>& g, int j, int k) {
   return (int64_t)k * g.pitch + j;
+}
+
+// Programmatic dependent launch: the kernels of a step are launched with
+// programmatic stream serialisation, so a kernel's blocks may be scheduled
+// while the previous kernel still runs.  Every kernel first waits for the
+// previous grid to complete and its memory to be visible (a no-op when the
+// launch had no programmatic dependency), then lets the next kernel's
+// launch begin.
+__device__ __forceinline__ void step_kernel_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 __device__ __forceinline__ bool running(const RunState* st) {
@@ -138,69 +166,81 @@ __device__ __forceinline__ Geo<R> load_geo(const KArgs<R>& a, int64_t c) {
 // ---------------------------------------------------------------------------
 // Seeds of check_solve (solver_2d.f90:667-858): border cells, wet cells and
 // ring-boundary cells; a cell is active when a seed lies within Manhattan
-// distance n_RK (<= 4) and it is not a ring-interior cell.  The seed bits of
-// the tile and a 4-cell frame are staged in shared memory; a tile with no
-// seed in its frame is inactive without scanning its cells.
+// distance n_RK (<= 4) and it is not a ring-interior cell.  The seeds of
+// the tile and a 4-cell frame (40 columns) become one 64-bit mask per frame
+// row (warp ballots); the distance test of a cell is then one shifted mask
+// test per row within n_RK, and a tile with no seed in its frame is
+// inactive without scanning its cells.
 constexpr int MASK_HALO = 4;
 constexpr int MRX = TX + 2 * MASK_HALO;
+static_assert(MRX <= 64, "a frame row must fit one 64-bit mask");
 
 template <class R, int TH>
 __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x) {
   constexpr int TY = TH, MRY = TH + 2 * MASK_HALO;
-  __shared__ uint8_t seed[MRY][MRX];
+  constexpr int RPW = (MRY + TH - 1) / TH;   // frame rows per warp (TH warps)
+  __shared__ unsigned long long srow[MRY];   // bit x: seed at frame column x
   RunState* st = a.st;
   const Grid<R>& g = a.g;
   const int j0 = tx * TX, k0 = ty * TY;
   const int nrk = a.pd.nrk;
+  const int lane = threadIdx.x % TX, warp = threadIdx.x / TX;
   int any = 0;
   if (!solve_all) {
-    // all frame loads of a thread are issued before any is used
-    constexpr int NIT = (MRX * MRY + TX * TY - 1) / (TX * TY);
-    R qv[NIT];
-    uint8_t fv[NIT];
+    // frame row y = warp + r*TH; columns lane and 32 + lane (lane < 8); all
+    // loads of a thread are issued before any is used
+    R qv[RPW][2];
+    uint8_t fv[RPW][2];
 #pragma unroll
-    for (int it = 0; it < NIT; ++it) {
-      const int idx = threadIdx.x + it * TX * TY;
-      const int rx = idx % MRX, ry = idx / MRX;
-      const int jj = j0 + rx - MASK_HALO, kk = k0 + ry - MASK_HALO;
-      qv[it] = R(0);
-      fv[it] = 0;
-      if (idx < MRX * MRY && jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
-        const int64_t cc = cidx(g, jj, kk);
-        qv[it] = a.q[cc];
-        fv[it] = a.cflags[cc];
-      }
-    }
+    for (int r = 0; r < RPW; ++r)
 #pragma unroll
-    for (int it = 0; it < NIT; ++it) {
-      const int idx = threadIdx.x + it * TX * TY;
-      if (idx >= MRX * MRY) break;
-      const int rx = idx % MRX, ry = idx / MRX;
-      const int jj = j0 + rx - MASK_HALO, kk = k0 + ry - MASK_HALO;
-      uint8_t sd = 0;
-      if (jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
-        if (jj == 0 || jj == g.nx - 1 || kk == 0 || kk == g.ny - 1) sd = 1;
-        else if (qv[it] > R(0)) sd = 1;
-        else if (a.pd.radial_source && (fv[it] & F_SC_MASK) == 2) sd = 1;
+      for (int h = 0; h < 2; ++h) {
+        const int y = warp + r * TH, x = lane + TX * h;
+        const int jj = j0 + x - MASK_HALO, kk = k0 + y - MASK_HALO;
+        qv[r][h] = R(0);
+        fv[r][h] = 0;
+        if (y < MRY && x < MRX && jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
+          const int64_t cc = cidx(g, jj, kk);
+          qv[r][h] = a.q[cc];
+          fv[r][h] = a.cflags[cc];
+        }
       }
-      seed[ry][rx] = sd;
-      any |= sd;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int y = warp + r * TH;
+      if (y >= MRY) break;   // warp-uniform
+      unsigned bits[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int x = lane + TX * h;
+        const int jj = j0 + x - MASK_HALO, kk = k0 + y - MASK_HALO;
+        int sd = 0;
+        if (x < MRX && jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
+          if (jj == 0 || jj == g.nx - 1 || kk == 0 || kk == g.ny - 1) sd = 1;
+          else if (qv[r][h] > R(0)) sd = 1;
+          else if (a.pd.radial_source && (fv[r][h] & F_SC_MASK) == 2) sd = 1;
+        }
+        bits[h] = __ballot_sync(0xffffffffu, sd);
+      }
+      if (lane == 0) srow[y] = (unsigned long long)bits[0] | ((unsigned long long)bits[1] << 32);
+      any |= (bits[0] | bits[1]) != 0u;
     }
     any = __syncthreads_or(any);
   }
-  const int j = j0 + threadIdx.x % TX;
-  const int k = k0 + threadIdx.x / TX;
+  const int j = j0 + lane;
+  const int k = k0 + warp;
   int act = 0;
   if (j < g.nx && k < g.ny) {
     const int64_t c = cidx(g, j, k);
     if (solve_all) {
       act = 1;
     } else if (any) {
-      const int cx = threadIdx.x % TX + MASK_HALO, cy = threadIdx.x / TX + MASK_HALO;
-      for (int dk = -nrk; dk <= nrk && !act; ++dk) {
-        const int rem = nrk - (dk < 0 ? -dk : dk);
-        for (int dj = -rem; dj <= rem; ++dj)
-          if (seed[cy + dk][cx + dj]) { act = 1; break; }
+      // seeds within Manhattan distance n_RK: in frame row cy + dk, the
+      // columns cx - r .. cx + r with r = n_RK - |dk|
+      const int cx = lane + MASK_HALO, cy = warp + MASK_HALO;
+      for (int dk = -nrk; dk <= nrk; ++dk) {
+        const int r = nrk - (dk < 0 ? -dk : dk);
+        if ((srow[cy + dk] >> (cx - r)) & ((2ull << (2 * r)) - 1ull)) act = 1;
       }
     }
     if (act && a.pd.radial_source && (a.cflags[c] & F_SC_MASK) == 1) act = 0;
@@ -216,6 +256,7 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
 
 template <class R, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_mask(KArgs<R> a, int solve_all) {
+  step_kernel_entry();
   RunState* st = a.st;
   const double t = st->t;
   if (!running(st)) return;
@@ -829,6 +870,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
 template <class R, int NS, int LIM, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
                                                        R* __restrict__ rout, int want_dt) {
+  step_kernel_entry();
   const RunState* st = a.st;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // the timestep pass runs before k_dt advances the clock; the later stage
@@ -866,7 +908,10 @@ __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   st->steps += 1;
 }
 
-static __global__ void k_dt(RunState* st, double max_dt) { dt_update(st, max_dt); }
+static __global__ void k_dt(RunState* st, double max_dt) {
+  step_kernel_entry();
+  dt_update(st, max_dt);
+}
 
 // ---------------------------------------------------------------------------
 // Positivity fixes of assemble_sol (solver_2d.f90:1381-1628) on an FP64 or
@@ -1217,6 +1262,7 @@ __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx,
 // activity byte is the one of the 32 x TH tile holding the block
 template <class R, int NS, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage2(KArgs<R> a, int mode) {
+  step_kernel_entry();
   if (!a.st->run_step) return;
   const uint8_t ta = a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x];
   if (ta == 0 || ta == 2) return;   // inactive, or dry without ring cells (k_flux)
@@ -1234,6 +1280,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage2(KArgs<R
 // ---------------------------------------------------------------------------
 template <class R, int NS, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage(KArgs<R> a, int irk) {
+  step_kernel_entry();
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
   if (!st->run_step) return;
@@ -1278,6 +1325,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage(KArgs<R>
 // assemble_sol (solver_2d.f90:1342-1630) + erosion/deposition + maxima
 template <class R, int NS, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_assemble(KArgs<R> a) {
+  step_kernel_entry();
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
   if (!st->run_step) return;

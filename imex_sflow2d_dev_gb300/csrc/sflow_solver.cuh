@@ -6,6 +6,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -290,7 +291,7 @@ class Solver : public SolverBase {
       SFLOW_CU(cudaEventRecord(ev_[1], stream_));
       SFLOW_CU(launch_flux(1));
       SFLOW_CU(cudaEventRecord(ev_[2], stream_));
-      k_dt<<<1, 1, 0, stream_>>>(st_, hs_.p.max_dt);
+      SFLOW_CU(launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt));
       ++launches_;
       SFLOW_CU(cudaGetLastError());
       SFLOW_CU(cudaEventRecord(ev_[3], stream_));
@@ -852,6 +853,9 @@ class Solver : public SolverBase {
     for (int i = 1; i < hs_.nv + 2; ++i)
       if (g.limiter[i] != g.lim_all) g.lim_all = -1;
     g.cfl = p.cfl; g.max_dt = p.max_dt;
+    // programmatic dependent launch of the step kernels (SFLOW_PDL=0: off)
+    const char* pdl_env = std::getenv("SFLOW_PDL");
+    g.pdl = (pdl_env && pdl_env[0] == '0') ? 0 : 1;
     fill_phys(ka_.pr);
     fill_phys(ka_.pd);
     for (int sd = 0; sd < 4; ++sd)
@@ -926,9 +930,8 @@ class Solver : public SolverBase {
       if (e != cudaSuccess) return e;
       e = launch_flux(1);
       if (e != cudaSuccess) return e;
-      k_dt<<<1, 1, 0, stream_>>>(st_, hs_.p.max_dt);
+      e = launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt);
       ++launches_;
-      e = cudaGetLastError();
       if (e != cudaSuccess) return e;
       return launch_stage2(-1);
     }
@@ -948,9 +951,8 @@ class Solver : public SolverBase {
     ++launches_;
     e = tab_.flux(ka_, grid, smem_flux_, stream_, q_, fused0 ? rd_ : nullptr, 1);
     if (e != cudaSuccess) return e;
-    k_dt<<<1, 1, 0, stream_>>>(st_, hs_.p.max_dt);
+    e = launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt);
     ++launches_;
-    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     for (int i = 0; i < hs_.nrk; ++i) {
       ++launches_;

@@ -35,7 +35,9 @@ struct KernelTable {
   // of k_b_cand / k_b_mask / k_b_flux / k_b_stage2 for this device
   cudaError_t (*b_setup)(size_t smem_flux, int* grids) = nullptr;
   // lim = 1: every run of the group uses minmod for every variable
-  cudaError_t (*b_step)(const BatchArgs<R>&, cudaStream_t, const int* grids, size_t smem_flux, int lim) = nullptr;
+  // pdl: launch with programmatic dependent launch
+  cudaError_t (*b_step)(const BatchArgs<R>&, cudaStream_t, const int* grids, size_t smem_flux, int lim,
+                        int pdl) = nullptr;
   cudaError_t (*b_admit)(const BatchArgs<R>&, cudaStream_t, int slot, unsigned gen, unsigned ntiles) = nullptr;
   cudaError_t (*b_summary)(const BatchArgs<R>&, cudaStream_t) = nullptr;
 };

@@ -124,33 +124,31 @@ static inline dim3 stage_grid(dim3 tiles, int ny) { return dim3(tiles.x, (unsign
 
 template <class R, int NS, int TH>
 static cudaError_t tab_mask(const KArgs<R>& a, dim3 grid, cudaStream_t s, int solve_all) {
-  k_mask<R, TH><<<grid, TileShape<TH>::MASK_THREADS, 0, s>>>(a, solve_all);
-  return cudaGetLastError();
+  return launch_step_kernel(k_mask<R, TH>, grid, dim3(TileShape<TH>::MASK_THREADS), 0, s, a.g.pdl, a, solve_all);
 }
 template <class R, int NS, int TH>
 static cudaError_t tab_flux(const KArgs<R>& a, dim3 grid, size_t smem, cudaStream_t s, const R* qin,
                             R* rout, int want_dt) {
   // minmod everywhere (the reference default) has its own instantiation:
   // one limiter case instead of eight per variable keeps the code small
-  constexpr int T = TileShape<TH>::FLUX_THREADS;
-  if (a.g.lim_all == 1) k_flux<R, NS, 1, TH><<<grid, T, smem, s>>>(a, qin, rout, want_dt);
-  else k_flux<R, NS, -1, TH><<<grid, T, smem, s>>>(a, qin, rout, want_dt);
-  return cudaGetLastError();
+  const dim3 T(TileShape<TH>::FLUX_THREADS);
+  if (a.g.lim_all == 1) return launch_step_kernel(k_flux<R, NS, 1, TH>, grid, T, smem, s, a.g.pdl, a, qin, rout, want_dt);
+  return launch_step_kernel(k_flux<R, NS, -1, TH>, grid, T, smem, s, a.g.pdl, a, qin, rout, want_dt);
 }
 template <class R, int NS, int TH>
 static cudaError_t tab_stage2(const KArgs<R>& a, dim3 grid, cudaStream_t s, int mode) {
-  k_stage2<R, NS, TH><<<stage_grid(grid, a.g.ny), TileShape<TH>::STAGE_THREADS, 0, s>>>(a, mode);
-  return cudaGetLastError();
+  return launch_step_kernel(k_stage2<R, NS, TH>, stage_grid(grid, a.g.ny), dim3(TileShape<TH>::STAGE_THREADS), 0, s,
+                            a.g.pdl, a, mode);
 }
 template <class R, int NS, int TH>
 static cudaError_t tab_stage(const KArgs<R>& a, dim3 grid, cudaStream_t s, int irk) {
-  k_stage<R, NS, TH><<<stage_grid(grid, a.g.ny), TileShape<TH>::STAGE_THREADS, 0, s>>>(a, irk);
-  return cudaGetLastError();
+  return launch_step_kernel(k_stage<R, NS, TH>, stage_grid(grid, a.g.ny), dim3(TileShape<TH>::STAGE_THREADS), 0, s,
+                            a.g.pdl, a, irk);
 }
 template <class R, int NS, int TH>
 static cudaError_t tab_assemble(const KArgs<R>& a, dim3 grid, cudaStream_t s) {
-  k_assemble<R, NS, TH><<<stage_grid(grid, a.g.ny), TileShape<TH>::STAGE_THREADS, 0, s>>>(a);
-  return cudaGetLastError();
+  return launch_step_kernel(k_assemble<R, NS, TH>, stage_grid(grid, a.g.ny), dim3(TileShape<TH>::STAGE_THREADS), 0,
+                            s, a.g.pdl, a);
 }
 template <class R, int NS, int TH>
 static cudaError_t tab_smem(size_t bytes) {
@@ -184,15 +182,20 @@ static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
   return cudaSuccess;
 }
 template <class R, int NS, int TH>
-static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux, int lim) {
-  constexpr int T = TileShape<TH>::FLUX_THREADS;
-  k_b_cand<R><<<grids[0], kBatchCandThreads, 0, s>>>(b);
-  k_b_mask<R, TH><<<grids[1], TileShape<TH>::MASK_THREADS, 0, s>>>(b);
-  if (lim == 1) k_b_flux<R, NS, 1, TH><<<grids[2], T, smem_flux, s>>>(b);
-  else k_b_flux<R, NS, -1, TH><<<grids[2], T, smem_flux, s>>>(b);
-  k_b_dt<R><<<1, kBatchCandThreads, 0, s>>>(b);
-  k_b_stage2<R, NS, TH><<<grids[3], TileShape<TH>::STAGE_THREADS, 0, s>>>(b);
-  return cudaGetLastError();
+static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux, int lim,
+                              int pdl) {
+  const dim3 T(TileShape<TH>::FLUX_THREADS);
+  cudaError_t e = launch_step_kernel(k_b_cand<R>, dim3(grids[0]), dim3(kBatchCandThreads), 0, s, pdl, b);
+  if (e == cudaSuccess)
+    e = launch_step_kernel(k_b_mask<R, TH>, dim3(grids[1]), dim3(TileShape<TH>::MASK_THREADS), 0, s, pdl, b);
+  if (e == cudaSuccess) {
+    if (lim == 1) e = launch_step_kernel(k_b_flux<R, NS, 1, TH>, dim3(grids[2]), T, smem_flux, s, pdl, b);
+    else e = launch_step_kernel(k_b_flux<R, NS, -1, TH>, dim3(grids[2]), T, smem_flux, s, pdl, b);
+  }
+  if (e == cudaSuccess) e = launch_step_kernel(k_b_dt<R>, dim3(1), dim3(kBatchCandThreads), 0, s, pdl, b);
+  if (e == cudaSuccess)
+    e = launch_step_kernel(k_b_stage2<R, NS, TH>, dim3(grids[3]), dim3(TileShape<TH>::STAGE_THREADS), 0, s, pdl, b);
+  return e;
 }
 
 template <class R, int NS, int TH>

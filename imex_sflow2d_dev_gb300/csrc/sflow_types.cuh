@@ -63,6 +63,7 @@ struct Grid {
   double cfl, max_dt;
   int dry_bc;       // every boundary condition is (Neumann, 0): a dry inside keeps dry ghosts
   int lim_all;      // the limiter of every variable when they are all equal, else -1
+  int pdl;          // launch the step kernels with programmatic dependent launch
 };
 
 // Device-resident run state (one per domain).
