@@ -38,6 +38,44 @@ __global__ void k_planes_to_aos(const R* __restrict__ q, double* __restrict__ ao
   for (int i = 0; i < nv; ++i) aos[c * nv + i] = (double)q[i * plane + (int64_t)k * pitch + j];
 }
 
+// The same through host memory mapped into the device address space (read
+// or written over NVLink-C2C): a block moves 256 cells of the host layout
+// as one contiguous run of doubles (coalesced, every cache line used once)
+// through shared memory, then converts cell by cell.
+constexpr int kHostChunk = 256;
+template <class R>
+__global__ void __launch_bounds__(kHostChunk) k_host_aos_to_planes(const double* __restrict__ aos, R* __restrict__ q,
+                                                                   int nv, int nx, int ny, int pitch, int64_t plane) {
+  extern __shared__ double sbuf[];
+  const int64_t N = (int64_t)nx * ny;
+  const int64_t c0 = (int64_t)blockIdx.x * kHostChunk;
+  const int ncell = (int)((N - c0) < kHostChunk ? (N - c0) : kHostChunk);
+  const int nval = ncell * nv;
+  for (int i = threadIdx.x; i < nval; i += kHostChunk) sbuf[i] = aos[c0 * nv + i];
+  __syncthreads();
+  if (threadIdx.x < ncell) {
+    const int64_t c = c0 + threadIdx.x;
+    const int j = (int)(c % nx), k = (int)(c / nx);
+    for (int i = 0; i < nv; ++i) q[i * plane + (int64_t)k * pitch + j] = (R)sbuf[threadIdx.x * nv + i];
+  }
+}
+template <class R>
+__global__ void __launch_bounds__(kHostChunk) k_host_planes_to_aos(const R* __restrict__ q, double* __restrict__ aos,
+                                                                   int nv, int nx, int ny, int pitch, int64_t plane) {
+  extern __shared__ double sbuf[];
+  const int64_t N = (int64_t)nx * ny;
+  const int64_t c0 = (int64_t)blockIdx.x * kHostChunk;
+  const int ncell = (int)((N - c0) < kHostChunk ? (N - c0) : kHostChunk);
+  if (threadIdx.x < ncell) {
+    const int64_t c = c0 + threadIdx.x;
+    const int j = (int)(c % nx), k = (int)(c / nx);
+    for (int i = 0; i < nv; ++i) sbuf[threadIdx.x * nv + i] = (double)q[i * plane + (int64_t)k * pitch + j];
+  }
+  __syncthreads();
+  const int nval = ncell * nv;
+  for (int i = threadIdx.x; i < nval; i += kHostChunk) aos[c0 * nv + i] = sbuf[i];
+}
+
 template <class R>
 __global__ void k_map_to_host(const R* __restrict__ m, double* __restrict__ out, int nx, int ny,
                               int pitch) {
@@ -231,13 +269,33 @@ class Solver : public SolverBase {
     return SFLOW_OK;
   }
 
+  // Pinned (page-locked) host memory is mapped into the device address
+  // space; on a Grace-Blackwell node the layout kernels then read or write
+  // it over NVLink-C2C directly, with no staging copy.  Other host memory
+  // goes through the device staging buffer and the copy engines.
+  static const double* mapped_host(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return static_cast<const double*>(at.devicePointer);
+  }
+
   int put(const double* q_aos) override {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     const size_t N = (size_t)nx * ny;
-    SFLOW_CU(ensure_stage());
-    SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
-    k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
+    const double* src = mapped_host(q_aos);
+    if (src) {
+      k_host_aos_to_planes<R><<<(unsigned)((N + kHostChunk - 1) / kHostChunk), kHostChunk,
+                                sizeof(double) * kHostChunk * nv, stream_>>>(src, q_, nv, nx, ny, pitch_, plane_);
+    } else {
+      SFLOW_CU(ensure_stage());
+      SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
+      k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
+    }
     ++launches_;
     SFLOW_CU(cudaGetLastError());
     SFLOW_CU(cudaStreamSynchronize(stream_));
@@ -311,6 +369,15 @@ class Solver : public SolverBase {
   int download(double* q_aos) override {
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     const size_t N = (size_t)nx * ny;
+    double* dst = const_cast<double*>(mapped_host(q_aos));
+    if (dst) {
+      k_host_planes_to_aos<R><<<(unsigned)((N + kHostChunk - 1) / kHostChunk), kHostChunk,
+                                sizeof(double) * kHostChunk * nv, stream_>>>(q_, dst, nv, nx, ny, pitch_, plane_);
+      ++launches_;
+      SFLOW_CU(cudaGetLastError());
+      SFLOW_CU(cudaStreamSynchronize(stream_));
+      return SFLOW_OK;
+    }
     SFLOW_CU(ensure_stage());
     k_planes_to_aos<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(q_, stage_aos_, nv, nx, ny, pitch_, plane_);
     ++launches_;
