@@ -149,6 +149,15 @@ int sflow_batch_get_tile_shape(const sflow_batch* b, int32_t* tile_h) {
   return SFLOW_OK;
 }
 
+int sflow_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
+  if (!mismatches || n < 0) return fail(SFLOW_EINVAL, "bad argument");
+  long long m = 0;
+  const int rc = sflow::check_conversions((long long)n, (unsigned long long)seed, &m);
+  if (rc != SFLOW_OK) return fail(rc, "conversion check failed to run");
+  *mismatches = (int64_t)m;
+  return SFLOW_OK;
+}
+
 int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count) {
   if (!count) return fail(SFLOW_EINVAL, "count is NULL");
   if (precision != SFLOW_PREC_FP32 && precision != SFLOW_PREC_FP64) return fail(SFLOW_EINVAL, "unknown precision");

@@ -98,5 +98,7 @@ class BatchBase {
 
 BatchBase* make_batch_fp64(int max_runs, int64_t max_tiles, std::string& err);
 BatchBase* make_batch_fp32(int max_runs, int64_t max_tiles, std::string& err);
+// self-check of the integer-pipe float <-> double conversions (sflow_fp32.cu)
+int check_conversions(long long n, unsigned long long seed, long long* mismatches);
 
 }  // namespace sflow

@@ -1033,7 +1033,12 @@ template <class R, int NS>
 __device__ __forceinline__ void add_deposit(const KArgs<R>& a, int64_t c, double dt, const R* dep) {
   if (!a.deposit) return;
 #pragma unroll
-  for (int i = 0; i < NS; ++i) a.deposit[i * a.g.plane + c] += dt * (double)dep[i];
+  for (int i = 0; i < NS; ++i) {
+    double d;
+    if constexpr (sizeof(R) == 4) d = f2d_exact(dep[i]);
+    else d = dep[i];
+    a.deposit[i * a.g.plane + c] += dt * d;
+  }
 }
 
 // post-step maxima (IMEX_SfloW2D.f90:449-505)
@@ -1121,8 +1126,8 @@ __device__ __forceinline__ unsigned stage_cell(const KArgs<R>& a, const Geo<R>& 
   } else {
     // ---- FP32 bulk form: FP32 explicit part, FP64 scalar Newton ----
     const Phys<R>& P = a.pr;
-    const R dtr = (R)dt;
-    const R dta = (R)(dt * a_diag);
+    const R dtr = from_double<R>(dt);
+    const R dta = from_double<R>(dt * a_diag);
     R qfv[nv], qp[nv + 2], si[nv], qsi[nv], qg[nv];
 #pragma unroll
     for (int i = 0; i < nv; ++i) qfv[i] = q0[i] - dtr * (s1[i] - s2[i]);
@@ -1208,7 +1213,7 @@ __device__ __forceinline__ int stage2_cell(const KArgs<R>& a, int mode, int j, i
     if (mode == 1) {
       const Geo<R> geo = load_geo(a, c);
       R dep[NS];
-      status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+      status |= erosion_deposition<R, NS>(a.pr, geo, from_double<R>(dt), q, dep);
       add_deposit<R, NS>(a, c, dt, dep);
 #pragma unroll
       for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
@@ -1227,7 +1232,7 @@ __device__ __forceinline__ int stage2_cell(const KArgs<R>& a, int mode, int j, i
     status |= assemble_fixes<R, NS>(a.pr, q);
     if (mode < 0 && (a.pd.settling || a.pd.entrain)) {
       R dep[NS];
-      status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+      status |= erosion_deposition<R, NS>(a.pr, geo, from_double<R>(dt), q, dep);
       add_deposit<R, NS>(a, c, dt, dep);
     }
 #pragma unroll
@@ -1356,7 +1361,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_assemble(KArgs
             s2[i] = s2[i] + a.rn[r * sv + i * g.plane + c] * om;
           }
         }
-        const R dtr = (R)dt;
+        const R dtr = from_double<R>(dt);
 #pragma unroll
         for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + c] - dtr * (s1[i] - s2[i]);
       }
@@ -1364,7 +1369,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_assemble(KArgs
       if (a.pd.settling || a.pd.entrain) {
         const Geo<R> geo = load_geo(a, c);
         R dep[NS];
-        status |= erosion_deposition<R, NS>(a.pr, geo, (R)dt, q, dep);
+        status |= erosion_deposition<R, NS>(a.pr, geo, from_double<R>(dt), q, dep);
         add_deposit<R, NS>(a, c, dt, dep);
       }
 #pragma unroll

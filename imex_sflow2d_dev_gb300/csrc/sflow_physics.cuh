@@ -31,6 +31,46 @@ template <class R>
 __device__ __forceinline__ R sq(R a) { return a * a; }
 
 // ---------------------------------------------------------------------------
+// float <-> double conversions on the integer pipe.  GB300 executes FP64
+// instructions, conversions to and from FP64 included, at 1/64 of the FP32
+// rate; the FP32 form's FP64 Newton step and FP64 sums use these instead, so
+// the FP64 pipe only does FP64 arithmetic.  Both follow IEEE 754 with the
+// FP32 form's flush-to-zero: f2d_exact is exact (subnormal floats, which the
+// FP32 form flushes, give +-0); d2f_rn rounds to nearest even and flushes
+// results below the float normal range to +-0.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  unsigned long long bits = sign;
+  if (e == 0xffu) bits |= 0x7ff0000000000000ull | ((unsigned long long)(u & 0x7fffffu) << 29);
+  else if (e != 0u) bits |= ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ float d2f_rn(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int ed = (int)((b >> 52) & 0x7ffull);
+  const unsigned long long frac = b & 0xfffffffffffffull;
+  if (ed == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (frac ? 0x400000u : 0u));
+  int e = ed - 896;                                      // biased float exponent
+  unsigned long long m = (frac | 0x10000000000000ull) >> 29;   // 24 significant bits
+  const unsigned long long rest = frac & 0x1fffffffull;        // 29 dropped bits
+  if (rest > 0x10000000ull || (rest == 0x10000000ull && (m & 1ull))) ++m;
+  if (m == 0x1000000ull) { m >>= 1; ++e; }              // carry into the exponent
+  if (ed == 0 || e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((unsigned)e << 23) | ((unsigned)m & 0x7fffffu));
+}
+// (R)x of a double for either form
+template <class R>
+__device__ __forceinline__ R from_double(double x) {
+  if constexpr (sizeof(R) == 4) return d2f_rn(x);
+  else return x;
+}
+
+// ---------------------------------------------------------------------------
 // geometry_2d.f90:1855-1876 minmod, 1878-1897 maxmod, 1776-1841 limit
 // ---------------------------------------------------------------------------
 template <class R>
@@ -868,7 +908,7 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, co
     dK = cgeo * (-rho_m * rho_m * c_inv * dT);
     return cgeo * (rho_m - rho_a);
   };
-  const float dtaf = (float)dta;
+  const float dtaf = d2f_rn(dta);
   float dKf;
   float K = Kf(S, dKf);
   float s = 2.0f * S / (1.0f + sqrtf(fmaxf(1.0f + 4.0f * dtaf * K * S, 0.0f)));
@@ -888,20 +928,25 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, co
   // derivative from the last FP32 iteration.  The FP32 root is within ~1e-7
   // relative of the solution and g' is known to ~1e-7, so the step leaves an
   // error of order 1e-14, far below the float the result is stored in.
-  double sd = s;
+  // FP32 values enter through f2d_exact and leave through d2f_rn, and the
+  // sign tests read the sign bit, so the FP64 pipe only does the FP64
+  // arithmetic (FP64 constants come from the FP64 parameter block).
+  double sd = f2d_exact(s);
   {
     const double sd2 = sd * sd;
-    double T = (double)a_T - (double)b_T * sd2;
-    if (T <= 0.0) T = PD.T_ambient;   // FP64 constants: no conversion on the FP64 pipe
-    const double x = (double)base_inv + (double)c_inv * T;
-    double rho_m = (double)__frcp_rn((float)x);
+    double T = f2d_exact(a_T) - f2d_exact(b_T) * sd2;
+    if (__double_as_longlong(T) <= 0) T = PD.T_ambient;   // T <= 0 (sign bit or zero)
+    const double x = f2d_exact(base_inv) + f2d_exact(c_inv) * T;
+    double rho_m = f2d_exact(__frcp_rn(d2f_rn(x)));
     rho_m = rho_m * (2.0 - x * rho_m);
-    const double Kd = (double)cgeo * (rho_m - ((P.rheo_model == 1) ? PD.rho_a_amb : 0.0));
-    const double gv = (sd - (double)S) + dta * Kd * sd2;
-    sd -= gv * (double)__frcp_rn(gdf);
+    const double Kd = f2d_exact(cgeo) * (rho_m - ((P.rheo_model == 1) ? PD.rho_a_amb : 0.0));
+    const double gv = (sd - f2d_exact(S)) + dta * Kd * sd2;
+    sd -= gv * f2d_exact(__frcp_rn(gdf));
     iters = 1;
   }
-  return sd > 0.0 ? (float)sd : 0.0f;
+  // sd > 0 (finite or +inf): positive sign and not a NaN
+  const long long sb = __double_as_longlong(sd);
+  return (sb > 0 && sb <= 0x7ff0000000000000ll) ? d2f_rn(sd) : 0.0f;
 }
 
 }  // namespace sflow

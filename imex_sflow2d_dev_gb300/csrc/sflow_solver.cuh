@@ -186,6 +186,7 @@ class Solver : public SolverBase {
     SFLOW_CU(set_smem_attr());
     std::memset(&hst_, 0, sizeof(hst_));
     init_state_host();
+    limits_known_ = false;
     SFLOW_CU(cudaMemcpy(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice));
     return SFLOW_OK;
   }
@@ -260,6 +261,7 @@ class Solver : public SolverBase {
     ++launches_;
     SFLOW_CU(cudaGetLastError());
     init_state_host();
+    limits_known_ = false;
     SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
     if (deposit_) SFLOW_CU(cudaMemsetAsync(deposit_, 0, sizeof(double) * plane_ * hs_.ns, stream_));
@@ -310,6 +312,7 @@ class Solver : public SolverBase {
     hst_.t_prev = t;
     hst_.dt_old = dt_old;
     hst_.dt_old_old = dt_old_old;
+    limits_known_ = false;
     SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(cudaStreamSynchronize(stream_));
     return SFLOW_OK;
@@ -517,6 +520,7 @@ class Solver : public SolverBase {
     h.cells_total += (long long)h.cells_acc[p];
     h.cells_acc[p] = 0;
     h.dtmin_bits = bits_of(1.0e300);
+    limits_known_ = false;
     SFLOW_CU(cudaMemcpyAsync(st_, &h, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(launch_stage2(0));
     flux_ready_ = false;
@@ -536,6 +540,7 @@ class Solver : public SolverBase {
     h.t = h.t + h.dt;
     h.steps += 1;
     h.run_step = 0;
+    limits_known_ = false;
     SFLOW_CU(cudaMemcpyAsync(st_, &h, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     return s ? stats(s) : SFLOW_OK;
   }
@@ -722,6 +727,11 @@ class Solver : public SolverBase {
   size_t smem_flux_ = 0;
   RunState hst_;
   bool uploaded_ = false, flux_ready_ = false;
+  // t_stop / step_limit last written to the device (whole-state writes
+  // clear limits_known_)
+  bool limits_known_ = false;
+  double limits_t_stop_ = 0.0;
+  long long limits_steps_ = 0;
   double pending_dt_ = -1.0;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
@@ -964,14 +974,21 @@ class Solver : public SolverBase {
 
   cudaError_t set_limits(double t_stop, int64_t step_limit) {
     // write t_stop and step_limit into the device state without touching
-    // the rest (the device owns t, dt and the counters)
+    // the rest (the device owns t, dt and the counters); skipped when the
+    // device already holds these values (only the host writes them)
+    long long lim = step_limit < 0 ? ((long long)1 << 62) : (long long)step_limit;
+    if (limits_known_ && t_stop == limits_t_stop_ && lim == limits_steps_) return cudaSuccess;
     cudaError_t e = cudaMemcpyAsync(&st_->t_stop, &t_stop, sizeof(double), cudaMemcpyHostToDevice, stream_);
     if (e != cudaSuccess) return e;
-    long long lim = step_limit < 0 ? ((long long)1 << 62) : (long long)step_limit;
     static_assert(sizeof(lim) == sizeof(st_->step_limit), "step_limit size");
     e = cudaMemcpyAsync(&st_->step_limit, &lim, sizeof(lim), cudaMemcpyHostToDevice, stream_);
     if (e != cudaSuccess) return e;
-    return cudaStreamSynchronize(stream_);
+    e = cudaStreamSynchronize(stream_);
+    if (e != cudaSuccess) return e;
+    limits_known_ = true;
+    limits_t_stop_ = t_stop;
+    limits_steps_ = lim;
+    return cudaSuccess;
   }
 
 

@@ -94,6 +94,7 @@ def load(build_if_missing=True):
         "sflow_batch_live": (i32, [vp]),
         "sflow_batch_launch_count": (i64, [vp]),
         "sflow_tile_shapes": (C.c_int, [i32, C.POINTER(i32), i32, C.POINTER(i32)]),
+        "sflow_check_conversions": (C.c_int, [i64, C.c_uint64, C.POINTER(i64)]),
         "sflow_set_tile_shape": (C.c_int, [vp, i32]),
         "sflow_get_tile_shape": (C.c_int, [vp, C.POINTER(i32)]),
         "sflow_autotune": (C.c_int, [vp, i64, C.POINTER(i32), dp, i32]),
@@ -125,10 +126,19 @@ def exported_symbols():
             "sflow_download_phys", "sflow_download_deposit", "sflow_upload_deposit",
             "sflow_upload_maps", "sflow_set_output_time", "sflow_tile_shapes",
             "sflow_set_tile_shape", "sflow_get_tile_shape", "sflow_autotune",
-            "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape"]
+            "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape", "sflow_check_conversions"]
 
 
 TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
+
+
+def check_conversions(n=1 << 22, seed=12345):
+    """Mismatches of the integer-pipe float <-> double conversions against
+    the hardware conversions on n seeded bit patterns (0 expected)."""
+    lib = load()
+    m = C.c_int64(-1)
+    _check(lib.sflow_check_conversions(int(n), int(seed), C.byref(m)))
+    return m.value
 
 
 def tile_shapes(precision):

@@ -255,6 +255,11 @@ int64_t sflow_device_bytes(const sflow_handle* h);
  * sflow_batch_set_tile_shape  height of the batch's runs; only while the
  *                       batch holds no run (SFLOW_ESTATE otherwise)
  */
+/* Self-check of the device's integer-pipe float <-> double conversions
+ * (used by the FP32 form's FP64 Newton step and FP64 sums) against the
+ * hardware conversions on n seeded bit patterns; *mismatches must be 0. */
+int sflow_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
+
 #define SFLOW_TILE_CANDIDATES 2
 int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count);
 int sflow_set_tile_shape(sflow_handle* h, int32_t tile_h);

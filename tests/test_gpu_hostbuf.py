@@ -36,3 +36,11 @@ def test_pinned_and_pageable_host_buffers_agree(precision):
         runs.append(s.download_q())
         s.close()
     np.testing.assert_array_equal(runs[0], runs[1])
+
+
+def test_integer_pipe_conversions_match_hardware():
+    """The FP32 form's FP64 Newton step converts between float and double
+    with integer operations (FP64 conversions run at the FP64 rate on
+    GB300); they must give the hardware conversions' results."""
+    assert L.check_conversions(1 << 22, 12345) == 0
+    assert L.check_conversions(1 << 20, 987654321) == 0
