@@ -69,6 +69,11 @@ struct KArgs {
   uint8_t* mask;
   uint8_t* tile_active;
   uint8_t* tile_wet;   // a cell of the tile holds mass after the step (stage kernel)
+  // single runs: the same per step parity (2 x tiles; written by the
+  // N_RK = 2 stage kernel) and the tiles within n_RK cells of a static seed
+  // (border or ring-boundary cell); check_solve skips the other tiles
+  uint8_t* tile_wet_step;
+  const uint8_t* tile_static;
   R* hmax;
   R* pdynmax;
   R* mvmax;
@@ -114,8 +119,18 @@ __device__ __forceinline__ void step_kernel_entry() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Order-preserving integer key of a double (for non-NaN values: a < b iff
+// key(a) < key(b); -0 maps to +0).  Every thread of the step kernels tests
+// the run clock, and a double comparison runs on GB300's FP64 pipe at 1/64
+// of the FP32 rate; the key comparison runs on the integer pipe.
+__device__ __forceinline__ long long order_key(double x) {
+  long long b = __double_as_longlong(x);
+  if (b == (long long)0x8000000000000000ull) b = 0;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+
 __device__ __forceinline__ bool running(const RunState* st) {
-  return st->t < st->t_stop && st->steps < st->step_limit;
+  return order_key(st->t) < order_key(st->t_stop) && st->steps < st->step_limit;
 }
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
@@ -238,9 +253,17 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
       // seeds within Manhattan distance n_RK: in frame row cy + dk, the
       // columns cx - r .. cx + r with r = n_RK - |dk|
       const int cx = lane + MASK_HALO, cy = warp + MASK_HALO;
-      for (int dk = -nrk; dk <= nrk; ++dk) {
-        const int r = nrk - (dk < 0 ? -dk : dk);
-        if ((srow[cy + dk] >> (cx - r)) & ((2ull << (2 * r)) - 1ull)) act = 1;
+      if ((srow[cy] >> cx) & 1ull) {
+        act = 1;                       // the cell is a seed itself
+      } else if (nrk == 2) {
+        act = (((srow[cy - 2] >> cx) & 1ull) | ((srow[cy + 2] >> cx) & 1ull) |
+               ((srow[cy - 1] >> (cx - 1)) & 7ull) | ((srow[cy + 1] >> (cx - 1)) & 7ull) |
+               ((srow[cy] >> (cx - 2)) & 31ull)) != 0ull;
+      } else {
+        for (int dk = -nrk; dk <= nrk; ++dk) {
+          const int r = nrk - (dk < 0 ? -dk : dk);
+          if ((srow[cy + dk] >> (cx - r)) & ((2ull << (2 * r)) - 1ull)) act = 1;
+        }
       }
     }
     if (act && a.pd.radial_source && (a.cflags[c] & F_SC_MASK) == 1) act = 0;
@@ -254,17 +277,42 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
   return cnt;
 }
 
+// A tile without a static seed within n_RK cells, with no tile of its 3 x 3
+// neighbourhood holding mass after the last step and inactive in the last
+// step cannot have an active cell (a seed within n_RK <= 4 cells of it lies
+// in that neighbourhood) and already has an all-zero mask: check_solve
+// skips it.  The tile also clears its wet flag of the buffer that this
+// step's stage kernel sets.
+template <class R>
+__device__ __forceinline__ bool mask_tile_skippable(const KArgs<R>& a, int tx, int ty, int tiles_x, int tiles_y) {
+  const int nt = tiles_x * tiles_y, t = ty * tiles_x + tx;
+  const unsigned par = (unsigned)(a.st->steps & 1);
+  if (threadIdx.x == 0) a.tile_wet_step[(par ^ 1u) * nt + t] = 0;
+  if (a.tile_active[t] || a.tile_static[t]) return false;
+  const uint8_t* w = a.tile_wet_step + par * nt;
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int x = tx + dx, y = ty + dy;
+      if (x >= 0 && x < tiles_x && y >= 0 && y < tiles_y && w[y * tiles_x + x]) return false;
+    }
+  return true;
+}
+
+// mode 0: check_solve(.FALSE.); 1: check_solve(.TRUE.) (solve_all); 2: as 0
+// with the tile skip of mask_tile_skippable (the N_RK = 2 step, whose stage
+// kernel keeps the wet flags)
 template <class R, int TH>
-__global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_mask(KArgs<R> a, int solve_all) {
+__global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_mask(KArgs<R> a, int mode) {
   step_kernel_entry();
   RunState* st = a.st;
   const double t = st->t;
   if (!running(st)) return;
-  mask_tile<R, TH>(a, solve_all, blockIdx.x, blockIdx.y, gridDim.x);
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
     st->src_t_coeff = source_time_coeff(st->tp, st->pi_g, t);
     st->src_t_coeff_f = (float)st->src_t_coeff;
   }
+  if (mode == 2 && mask_tile_skippable(a, blockIdx.x, blockIdx.y, gridDim.x, gridDim.y)) return;
+  mask_tile<R, TH>(a, mode == 1, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1269,12 +1317,23 @@ template <class R, int NS, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage2(KArgs<R> a, int mode) {
   step_kernel_entry();
   if (!a.st->run_step) return;
-  const uint8_t ta = a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x];
+  const int tile = (blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x;
+  const uint8_t ta = a.tile_active[tile];
   if (ta == 0 || ta == 2) return;   // inactive, or dry without ring cells (k_flux)
   unsigned status = 0;
   int nit = 0;
-  stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, blockIdx.y * 8 + threadIdx.x / TX, status, nit);
+  int wet = stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, blockIdx.y * 8 + threadIdx.x / TX,
+                               status, nit);
   newton_stats<R>(a.st, status, nit, nit);
+  if (mode < 0) {
+    // wet flag of the tile for the next check_solve (buffer of the new
+    // step count's parity; set only, the check_solve of this step cleared it)
+    wet = __syncthreads_or(wet);
+    if (wet && threadIdx.x == 0) {
+      const int nt = gridDim.x * a.g.tiles_y;
+      a.tile_wet_step[(unsigned)(a.st->steps & 1) * nt + tile] = 1;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

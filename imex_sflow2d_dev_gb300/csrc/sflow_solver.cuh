@@ -265,7 +265,7 @@ class Solver : public SolverBase {
     SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
     if (deposit_) SFLOW_CU(cudaMemsetAsync(deposit_, 0, sizeof(double) * plane_ * hs_.ns, stream_));
-    SFLOW_CU(cudaMemsetAsync(tile_wet_, 1, (size_t)tiles_x_ * tiles_y_, stream_));
+    SFLOW_CU(cudaMemsetAsync(tile_wet_, 1, 3 * (size_t)tiles_x_ * tiles_y_, stream_));
     SFLOW_CU(cudaStreamSynchronize(stream_));
     uploaded_ = true;
     return SFLOW_OK;
@@ -298,6 +298,7 @@ class Solver : public SolverBase {
       SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
       k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
     }
+    SFLOW_CU(reset_wet_flags());
     ++launches_;
     SFLOW_CU(cudaGetLastError());
     SFLOW_CU(cudaStreamSynchronize(stream_));
@@ -348,7 +349,7 @@ class Solver : public SolverBase {
     for (int64_t i = 0; i < steps; ++i) {
       if (flush) SFLOW_CU(flush_l2());
       SFLOW_CU(cudaEventRecord(ev_[0], stream_));
-      SFLOW_CU(launch_mask(0));
+      SFLOW_CU(launch_mask(2));
       SFLOW_CU(cudaEventRecord(ev_[1], stream_));
       SFLOW_CU(launch_flux(1));
       SFLOW_CU(cudaEventRecord(ev_[2], stream_));
@@ -505,6 +506,7 @@ class Solver : public SolverBase {
     return SFLOW_OK;
   }
   int imex_rk(double t, double dt) override {
+    SFLOW_CU(reset_wet_flags());   // stage kernel of mode 0 keeps no wet flags
     if (!flux_ready_) { err_ = "sflow_imex_rk needs sflow_timestep on the same state first"; return SFLOW_ESTATE; }
     RunState h;
     SFLOW_CU(cudaMemcpyAsync(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
@@ -528,6 +530,7 @@ class Solver : public SolverBase {
     return SFLOW_OK;
   }
   int erosion_deposition(double dt) override {
+    SFLOW_CU(reset_wet_flags());
     if (dt != pending_dt_) { err_ = "dt differs from the last sflow_imex_rk"; return SFLOW_ESTATE; }
     if (hs_.p.settling_flag || hs_.p.entrainment_flag) SFLOW_CU(launch_stage2(1));
     return SFLOW_OK;
@@ -560,8 +563,9 @@ class Solver : public SolverBase {
     drop_graphs();
     const size_t n_old = (size_t)tiles_x_ * tiles_y_;
     free_tracked(tile_active_, n_old);
-    free_tracked(tile_wet_, n_old);
-    tile_active_ = tile_wet_ = nullptr;
+    free_tracked(tile_wet_, 3 * n_old);
+    free_tracked(tile_static_, n_old);
+    tile_active_ = tile_wet_ = tile_static_ = nullptr;
     tab_ = t;
     tile_h_ = th;
     tiles_y_ = (hs_.ny + th - 1) / th;
@@ -569,6 +573,8 @@ class Solver : public SolverBase {
     ka_.g.tiles_y = tiles_y_;
     ka_.tile_active = tile_active_;
     ka_.tile_wet = tile_wet_;
+    ka_.tile_wet_step = tile_wet_ + (size_t)tiles_x_ * tiles_y_;
+    ka_.tile_static = tile_static_;
     smem_flux_ = flux_smem_bytes(hs_.nv, th);
     SFLOW_CU(set_smem_attr());
     return SFLOW_OK;
@@ -717,7 +723,8 @@ class Solver : public SolverBase {
   R *q_ = nullptr, *rd_ = nullptr, *rn_ = nullptr, *qs_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
   double* deposit_ = nullptr;
   R* geo_[8];
-  uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr, *tile_wet_ = nullptr;
+  uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr, *tile_wet_ = nullptr,
+          *tile_static_ = nullptr;
   RunState* st_ = nullptr;
   double *stage_aos_ = nullptr, *stat_part_ = nullptr, *stat_out_ = nullptr;
   int nstat_blocks_ = 0;
@@ -797,14 +804,45 @@ class Solver : public SolverBase {
     return e;
   }
 
-  // per-tile bytes (activity, wet flag) for the current tile height
+  // per-tile bytes for the current tile height: activity; wet flags (the
+  // batch's, then the single run's two step-parity buffers: 3 x tiles, all
+  // "unknown" = 1); static-seed flags (host computed)
   cudaError_t alloc_tiles() {
     const size_t n = (size_t)tiles_x_ * tiles_y_;
     cudaError_t e = alloc((void**)&tile_active_, n);
-    if (e == cudaSuccess) e = alloc((void**)&tile_wet_, n);
+    if (e == cudaSuccess) e = alloc((void**)&tile_wet_, 3 * n);
+    if (e == cudaSuccess) e = alloc((void**)&tile_static_, n);
     if (e == cudaSuccess) e = cudaMemset(tile_active_, 0, n);
-    if (e == cudaSuccess) e = cudaMemset(tile_wet_, 1, n);
+    if (e == cudaSuccess) e = cudaMemset(tile_wet_, 1, 3 * n);
+    if (e == cudaSuccess) {
+      const std::vector<uint8_t> ts = tile_static_host();
+      e = cudaMemcpy(tile_static_, ts.data(), n, cudaMemcpyHostToDevice);
+    }
     return e;
+  }
+  // tiles with a border cell or a ring-boundary cell (seeds of every
+  // check_solve) within n_RK cells
+  std::vector<uint8_t> tile_static_host() const {
+    const int nx = hs_.nx, ny = hs_.ny, r = hs_.nrk, th = tile_h_;
+    std::vector<uint8_t> ts((size_t)tiles_x_ * tiles_y_, 0);
+    for (int ty = 0; ty < tiles_y_; ++ty)
+      for (int tx = 0; tx < tiles_x_; ++tx) {
+        const int j0 = tx * TX - r, j1 = std::min(nx, (tx + 1) * TX) - 1 + r;
+        const int k0 = ty * th - r, k1 = std::min(ny, (ty + 1) * th) - 1 + r;
+        uint8_t v = (j0 <= 0 || j1 >= nx - 1 || k0 <= 0 || k1 >= ny - 1) ? 1 : 0;
+        if (!v && hs_.p.radial_source_flag)
+          for (int k = std::max(k0, 0); k <= std::min(k1, ny - 1) && !v; ++k)
+            for (int j = std::max(j0, 0); j <= std::min(j1, nx - 1); ++j)
+              if ((hs_.cflags[(size_t)k * nx + j] & 3) == 2) { v = 1; break; }
+        ts[(size_t)ty * tiles_x_ + tx] = v;
+      }
+    return ts;
+  }
+  // the single run's wet flags back to "unknown" (the state changed on the
+  // host, or a per-call entry point ran kernels that do not keep them)
+  cudaError_t reset_wet_flags() {
+    const size_t n = (size_t)tiles_x_ * tiles_y_;
+    return cudaMemsetAsync(tile_wet_ + n, 1, 2 * n, stream_);
   }
   void free_tracked(void* p, size_t bytes) {
     for (auto it = allocs_.begin(); it != allocs_.end(); ++it)
@@ -952,6 +990,8 @@ class Solver : public SolverBase {
     for (int i = 0; i < 8; ++i) ka_.geo[i] = geo_[i];
     ka_.cflags = cflags_; ka_.arc = arc_; ka_.mask = mask_; ka_.tile_active = tile_active_;
     ka_.tile_wet = tile_wet_;
+    ka_.tile_wet_step = tile_wet_ + (size_t)tiles_x_ * tiles_y_;
+    ka_.tile_static = tile_static_;
     ka_.hmax = hmax_; ka_.pdynmax = pdynmax_; ka_.mvmax = mvmax_; ka_.st = st_;
     ka_.deposit = deposit_;
     ka_.take_last = hs_.take_last;
@@ -1010,7 +1050,7 @@ class Solver : public SolverBase {
 
   cudaError_t launch_step() {
     if (hs_.nrk == 2) {
-      cudaError_t e = launch_mask(0);
+      cudaError_t e = launch_mask(2);
       if (e != cudaSuccess) return e;
       e = launch_flux(1);
       if (e != cudaSuccess) return e;
