@@ -717,11 +717,31 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   R* sHy = sHx + nv * TY * (TX + 1);                             // nv * (TY+1)*TX
   R* sAx = sHy + nv * (TY + 1) * TX;                             // TY*(TX+1)
   R* sAy = sAx + TY * (TX + 1);                                  // (TY+1)*TX
-  uint8_t* sfl = reinterpret_cast<uint8_t*>(sAy + (TY + 1) * TX);  // RX*RY
+  R* sgeo = sAy + (TY + 1) * TX;                                 // 5 * TX*TY
+  uint8_t* sfl = reinterpret_cast<uint8_t*>(sgeo + 5 * TX * TY);  // RX*RY
   const int j0 = tx * TX, k0 = ty * TY;
   const int tid = threadIdx.x;
 
   __syncthreads();   // shared memory of the previous tile of a persistent block is free
+  // 0. the topography terms of the cell this thread finishes in step 4
+  // (B'x, B'y, g_c, dg_c/dx, dg_c/dy) start on their way to shared memory
+  // now (asynchronous copies); the thread waits for its own copies in step 4
+  if (tid < TX * TY) {
+    const int j = j0 + tid % TX, k = k0 + tid / TX;
+    if (j < g.nx && k < g.ny) {
+      const int64_t c = cidx(g, j, k);
+      const R* src[5] = {a.geo[0] + c, a.geo[1] + c, a.geo[5] + c, a.geo[6] + c, a.geo[7] + c};
+#pragma unroll
+      for (int p = 0; p < 5; ++p) {
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(sgeo + p * TX * TY + tid);
+        if constexpr (sizeof(R) == 4)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src[p]) : "memory");
+        else
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src[p]) : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   // 1. physical variables of the tile + halo (qc_to_qp; inactive = dry).
   // Each thread covers two region cells; all their loads (flags, mask,
   // state) are issued before any is used.
@@ -850,7 +870,10 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   }
   __syncthreads();
 
-  // 4. cells: divergence, explicit terms, CFL step
+  // 4. cells: divergence, explicit terms, CFL step.  Every thread first
+  // waits for its own copies of step 0 (also those of cells it does not
+  // finish: none may land after the tile is left)
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   R dtloc = R(3.0e38);
   if (tid < TX * TY) {
     const int cx = tid % TX, cy = tid / TX;
@@ -862,7 +885,15 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
 #pragma unroll
       for (int i = 0; i < np; ++i) qp[i] = sqp[i * RX * RY + ry * RX + rx];
       R e[nv];
-      const Geo<R> geo = load_geo(a, c);
+      Geo<R> geo;   // this thread's copies of step 0
+      geo.Bx = sgeo[tid];
+      geo.By = sgeo[TX * TY + tid];
+      geo.gc = sgeo[2 * TX * TY + tid];
+      geo.dgcx = sgeo[3 * TX * TY + tid];
+      geo.dgcy = sgeo[4 * TX * TY + tid];
+      geo.Bxx = a.geo[2] ? __ldg(a.geo[2] + c) : R(0);
+      geo.Bxy = a.geo[3] ? __ldg(a.geo[3] + c) : R(0);
+      geo.Byy = a.geo[4] ? __ldg(a.geo[4] + c) : R(0);
       const uint8_t fl = sfl[ry * RX + rx];
       R ap = R(0), anx = R(0), any_ = R(0);
       R tcoef = R(0);   // read at ring cells only (arc perimeter > 0)

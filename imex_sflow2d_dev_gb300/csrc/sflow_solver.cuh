@@ -198,12 +198,13 @@ class Solver : public SolverBase {
   int tiles_y() const { return tiles_y_; }
   size_t smem_flux() const { return smem_flux_; }
   // dynamic shared memory of flux_tile: qp of the tile + halo, x- and
-  // y-face fluxes and speeds, flag bytes of the tile + halo
+  // y-face fluxes and speeds, the tile's 5 topography planes, flag bytes of
+  // the tile + halo
   static size_t flux_smem_bytes(int nv, int th) {
     const int np = nv + 2;
     const size_t ry = (size_t)th + 2 * HALO;
     const size_t r = (size_t)np * RX * ry + (size_t)nv * th * (TX + 1) + (size_t)nv * (th + 1) * TX +
-                     (size_t)th * (TX + 1) + (size_t)(th + 1) * TX;
+                     (size_t)th * (TX + 1) + (size_t)(th + 1) * TX + (size_t)5 * TX * th;
     return (r * sizeof(R) + RX * ry + 15) / 16 * 16;
   }
   cudaStream_t stream() const { return stream_; }
