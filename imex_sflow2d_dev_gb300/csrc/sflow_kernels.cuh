@@ -1343,9 +1343,12 @@ __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx,
 }
 
 // single run: one block per 32 x 8 cells (grid tiles_x x ceil(ny/8)); the
-// activity byte is the one of the 32 x TH tile holding the block
+// activity byte is the one of the 32 x TH tile holding the block.  The FP32
+// form is compiled for 6 resident blocks per SM (40 registers): the kernel
+// waits on memory, and more warps hide more of it.
 template <class R, int NS, int TH>
-__global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage2(KArgs<R> a, int mode) {
+__global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, sizeof(R) == 4 ? 6 : 1)
+    k_stage2(KArgs<R> a, int mode) {
   step_kernel_entry();
   if (!a.st->run_step) return;
   const int tile = (blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x;
