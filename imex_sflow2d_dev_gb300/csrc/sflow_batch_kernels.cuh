@@ -18,8 +18,10 @@
 // Why candidates suffice: a cell outside the active set is not updated, so
 // a wet cell (a check_solve seed) was active in the previous step; active
 // cells lie within n_RK = 2 cells of a seed, and tiles are 32 x TH cells
-// with TH >= 4, so they lie in the 3 x 3 tile neighbourhood of a previously active tile that
-// held mass (tile_wet, written by the stage kernel).  Border and ring cells
+// with TH >= 4, so they lie in the 3 x 3 tile neighbourhood of a previously
+// active tile that held mass within n_RK cells of the edge (or corner) they
+// share (tile_wet, written by the stage kernel: one bit per edge).  Border
+// and ring cells
 // are seeds of every step, so their tiles stay in the lists; a border seed
 // reaches into the neighbouring tile only when the edge tile is narrower
 // than n_RK + 1 cells, and ring seeds may reach any neighbour, so those
@@ -45,7 +47,7 @@ namespace sflow {
 struct BatchRun {
   RunState* st;      // the run's device state
   uint32_t* cand;    // per-tile candidate flag
-  const uint8_t* tile_wet;    // tile held mass after the last step (or unknown: 1)
+  const uint8_t* tile_wet;    // wet byte of the tile after the last step (TW_*; 0xff: unknown)
   const uint8_t* tile_seed;   // tile holds ring-boundary cells, or is a narrow edge tile
   int tiles_x, tiles_y;
   unsigned gen;      // generation of the run in this slot
@@ -134,12 +136,18 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
     if (!br.live || (br.gen & 0xffffu) != entry_gen(e) || !running(br.st)) continue;
     const unsigned tile = entry_tile(e);
     const int nb = (int)(i % 9u);
-    // only tiles with mass, ring cells or a narrow domain edge can activate
-    // cells of their neighbours; a dry tile kept active by the border rule
-    // is its own only candidate
-    if (nb != 4 && !br.tile_wet[tile] && !br.tile_seed[tile]) continue;
-    const int tx = (int)(tile % (unsigned)br.tiles_x) + nb % 3 - 1;
-    const int ty = (int)(tile / (unsigned)br.tiles_x) + nb / 3 - 1;
+    // only tiles with mass near the shared edge, ring cells or a narrow
+    // domain edge can activate cells of their neighbours; a dry tile kept
+    // active by the border rule is its own only candidate
+    const int dx = nb % 3 - 1, dy = nb / 3 - 1;
+    if (nb != 4 && !br.tile_seed[tile]) {
+      const unsigned tw = br.tile_wet[tile];
+      const unsigned need = TW_ANY | (dx < 0 ? TW_W : 0u) | (dx > 0 ? TW_E : 0u) | (dy < 0 ? TW_S : 0u) |
+                            (dy > 0 ? TW_N : 0u);
+      if ((tw & need) != need) continue;
+    }
+    const int tx = (int)(tile % (unsigned)br.tiles_x) + dx;
+    const int ty = (int)(tile / (unsigned)br.tiles_x) + dy;
     if (tx < 0 || ty < 0 || tx >= br.tiles_x || ty >= br.tiles_y) continue;
     const unsigned t2 = (unsigned)(ty * br.tiles_x + tx);
     if (atomicExch(&br.cand[t2], 1u) == 0u) {

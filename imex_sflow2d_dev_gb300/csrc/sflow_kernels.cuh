@@ -1321,24 +1321,43 @@ __device__ __forceinline__ int stage2_cell(const KArgs<R>& a, int mode, int j, i
   return q[0] > R(0);
 }
 
+// Wet byte of a batched run's tile after the step (read by the candidate
+// rule): bit 0 a cell holds mass; bits 1-4 a cell holding mass lies within
+// n_RK = 2 cells of the west / east / south / north tile edge, so only the
+// neighbours across those edges can gain active cells.  0xff: unknown.
+constexpr uint8_t TW_ANY = 1, TW_W = 2, TW_E = 4, TW_S = 8, TW_N = 16;
+
 // A whole 32 x TH tile with 32 x 8 threads, 8 rows at a time (batched
-// runs), then the tile's wet flag for the candidate rule (mode -1).
+// runs), then the tile's wet byte for the candidate rule (mode -1).
 template <class R, int NS, int TH>
 __device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx, int ty) {
   static_assert(TH % 8 == 0, "stage tiles are processed 8 rows at a time");
+  __shared__ unsigned s_bits[8];
   unsigned status = 0;
-  int nit_sum = 0, nit_max = 0, wet = 0;
+  int nit_sum = 0, nit_max = 0;
+  unsigned bits = 0;
+  const int lane = threadIdx.x % TX;
 #pragma unroll 1
   for (int r0 = 0; r0 < TH; r0 += 8) {
     int nit = 0;
-    wet |= stage2_cell<R, NS>(a, mode, tx * TX + threadIdx.x % TX, ty * TH + r0 + threadIdx.x / TX, status, nit);
+    const int row = r0 + threadIdx.x / TX;
+    const int wet = stage2_cell<R, NS>(a, mode, tx * TX + lane, ty * TH + row, status, nit);
+    if (wet)
+      bits |= TW_ANY | (lane < 2 ? TW_W : 0u) | (lane >= TX - 2 ? TW_E : 0u) | (row < 2 ? TW_S : 0u) |
+              (row >= TH - 2 ? TW_N : 0u);
     nit_sum += nit;
     nit_max = max(nit_max, nit);
   }
   newton_stats<R>(a.st, status, nit_sum, nit_max);
   if (mode < 0) {
-    wet = __syncthreads_or(wet);
-    if (threadIdx.x == 0) a.tile_wet[ty * a.g.tiles_x + tx] = (uint8_t)wet;
+    bits = __reduce_or_sync(0xffffffffu, bits);
+    if (lane == 0) s_bits[threadIdx.x / TX] = bits;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned b = 0;
+      for (int w = 0; w < 8; ++w) b |= s_bits[w];
+      a.tile_wet[ty * a.g.tiles_x + tx] = (uint8_t)b;
+    }
   }
 }
 

@@ -266,7 +266,7 @@ class Solver : public SolverBase {
     SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
     if (deposit_) SFLOW_CU(cudaMemsetAsync(deposit_, 0, sizeof(double) * plane_ * hs_.ns, stream_));
-    SFLOW_CU(cudaMemsetAsync(tile_wet_, 1, 3 * (size_t)tiles_x_ * tiles_y_, stream_));
+    SFLOW_CU(cudaMemsetAsync(tile_wet_, 0xff, 3 * (size_t)tiles_x_ * tiles_y_, stream_));
     SFLOW_CU(cudaStreamSynchronize(stream_));
     uploaded_ = true;
     return SFLOW_OK;
@@ -814,7 +814,7 @@ class Solver : public SolverBase {
     if (e == cudaSuccess) e = alloc((void**)&tile_wet_, 3 * n);
     if (e == cudaSuccess) e = alloc((void**)&tile_static_, n);
     if (e == cudaSuccess) e = cudaMemset(tile_active_, 0, n);
-    if (e == cudaSuccess) e = cudaMemset(tile_wet_, 1, 3 * n);
+    if (e == cudaSuccess) e = cudaMemset(tile_wet_, 0xff, 3 * n);   // unknown
     if (e == cudaSuccess) {
       const std::vector<uint8_t> ts = tile_static_host();
       e = cudaMemcpy(tile_static_, ts.data(), n, cudaMemcpyHostToDevice);
@@ -843,7 +843,7 @@ class Solver : public SolverBase {
   // host, or a per-call entry point ran kernels that do not keep them)
   cudaError_t reset_wet_flags() {
     const size_t n = (size_t)tiles_x_ * tiles_y_;
-    return cudaMemsetAsync(tile_wet_ + n, 1, 2 * n, stream_);
+    return cudaMemsetAsync(tile_wet_ + n, 0xff, 2 * n, stream_);
   }
   void free_tracked(void* p, size_t bytes) {
     for (auto it = allocs_.begin(); it != allocs_.end(); ++it)
