@@ -99,13 +99,32 @@ __device__ __forceinline__ void load_args(KArgs<R>* dst, const KArgs<R>* src) {
   for (int i = threadIdx.x; i < (int)(sizeof(KArgs<R>) / 8); i += blockDim.x) d[i] = s[i];
 }
 
-// next list index for this block (one atomic per tile; block-uniform result)
-__device__ __forceinline__ unsigned next_tile(unsigned* counter, unsigned* s_idx) {
-  __syncthreads();
-  if (threadIdx.x == 0) *s_idx = atomicAdd(counter, 1u);
-  __syncthreads();
-  return *s_idx;
-}
+// Tiles of a persistent kernel come from a counter in global memory.
+// Thread 0 claims the next index as soon as the block starts on a tile, so
+// the atomic's latency overlaps the tile's work, and one barrier per tile
+// hands the claimed index to the block (which also frees the block's shared
+// memory for the next tile).
+struct TileQueue {
+  unsigned* counter;
+  unsigned* s_idx;   // shared, 2 entries
+  unsigned par = 0;
+  unsigned claim = 0;
+  __device__ __forceinline__ unsigned first() {
+    if (threadIdx.x == 0) s_idx[0] = atomicAdd(counter, 1u);
+    __syncthreads();
+    return s_idx[0];
+  }
+  // first statement of the loop body, before any continue
+  __device__ __forceinline__ void prefetch() {
+    if (threadIdx.x == 0) claim = atomicAdd(counter, 1u);
+  }
+  __device__ __forceinline__ unsigned next() {
+    if (threadIdx.x == 0) s_idx[par ^ 1u] = claim;
+    __syncthreads();
+    par ^= 1u;
+    return s_idx[par];
+  }
+};
 
 template <class R>
 __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
@@ -163,23 +182,23 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
 // whole KArgs per run change: candidate lists interleave the runs' tiles.
 template <class R, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
-  __shared__ unsigned s_idx;
+  __shared__ unsigned s_idx[2];
   step_kernel_entry();
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   unsigned long long* out = pp ? b.list0 : b.list1;
   const unsigned n = ctl->ncand;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->work[1] = 0u;
-  for (;;) {
-    const unsigned i = next_tile(&ctl->work[0], &s_idx);
-    if (i >= n) break;
+  TileQueue tq{&ctl->work[0], s_idx};
+  for (unsigned i = tq.first(); i < n; i = tq.next()) {
+    tq.prefetch();
     const unsigned long long e = b.cand[i];
     const int slot = entry_slot(e);
     const unsigned tile = entry_tile(e);
     const KArgs<R>& a = b.args[slot];
     const BatchRun& br = b.runs[slot];
     if (threadIdx.x == 0) br.cand[tile] = 0u;
-    if (!running(a.st)) continue;
+    // k_b_cand listed only running runs, and no run's clock moves before k_b_dt
     const int tx = (int)(tile % (unsigned)br.tiles_x), ty = (int)(tile / (unsigned)br.tiles_x);
     const int cnt = mask_tile<R, TH>(a, 0, tx, ty, br.tiles_x);
     if (cnt > 0 && threadIdx.x == 0) {
@@ -198,7 +217,7 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FL
     k_b_flux(BatchArgs<R> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
-  __shared__ unsigned s_idx;
+  __shared__ unsigned s_idx[2];
   step_kernel_entry();
   KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
   BatchCtl* ctl = b.ctl;
@@ -207,9 +226,9 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FL
   const unsigned n = ctl->count[pp ^ 1u];
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->work[2] = 0u;
   int cur = -1;
-  for (;;) {
-    const unsigned i = next_tile(&ctl->work[1], &s_idx);
-    if (i >= n) break;
+  TileQueue tq{&ctl->work[1], s_idx};
+  for (unsigned i = tq.first(); i < n; i = tq.next()) {
+    tq.prefetch();
     const unsigned long long e = L[i];
     const int slot = entry_slot(e);
     const unsigned tile = entry_tile(e);
@@ -218,7 +237,7 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FL
       cur = slot;
       __syncthreads();
     }
-    if (!running(a.st)) continue;
+    // the list holds tiles of running runs only (k_b_cand, k_b_mask)
     const int tiles_x = (a.g.nx + TX - 1) / TX;
     flux_tile<R, NS, LIM, TH>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
                      smem_raw);
@@ -246,7 +265,7 @@ template <class R, int NS, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, TileShape<TH>::STAGE_MIN_BLOCKS)
     k_b_stage2(BatchArgs<R> b) {
   __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
-  __shared__ unsigned s_idx;
+  __shared__ unsigned s_idx[2];
   step_kernel_entry();
   KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
   BatchCtl* ctl = b.ctl;
@@ -254,9 +273,9 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, TileShape<TH>::S
   const unsigned long long* L = pp ? b.list1 : b.list0;
   const unsigned n = ctl->count[pp];
   int cur = -1;
-  for (;;) {
-    const unsigned i = next_tile(&ctl->work[2], &s_idx);
-    if (i >= n) break;
+  TileQueue tq{&ctl->work[2], s_idx};
+  for (unsigned i = tq.first(); i < n; i = tq.next()) {
+    tq.prefetch();
     const unsigned long long e = L[i];
     const int slot = entry_slot(e);
     const unsigned tile = entry_tile(e);
