@@ -1,7 +1,10 @@
 """Served solves: a request loop over the batched engine (continuous
 batching).  Requests that arrive while others run are admitted as slots and
-memory free up; each result must equal the same job solved alone (bitwise:
-the per-cell arithmetic is the same code in both paths)."""
+memory free up; each result must equal the same job solved alone: the
+per-cell arithmetic is the same source in both paths; in the FP32 form the
+batched kernels are other compilations of it (the compiler may fuse a
+different multiply-add), so the bar is an L1 relative difference <= 1e-5
+per variable."""
 import numpy as np
 import pytest
 
@@ -52,7 +55,11 @@ def test_served_results_equal_alone(max_runs):
         assert r["steps"] == steps
         assert r["status"] == 0
         assert r["finished_s"] >= r["admitted_s"] >= r["arrival_s"] - 1e-9
-        np.testing.assert_array_equal(r["q"], _alone(p, B, q, steps))
+        ref = _alone(p, B, q, steps).reshape(-1, p.n_vars)
+        got = r["q"].reshape(-1, p.n_vars)
+        for i in range(p.n_vars):
+            l1 = np.abs(got[:, i] - ref[:, i]).sum() / max(np.abs(ref[:, i]).sum(), 1e-300)
+            assert l1 <= 1e-5, (i, l1)
     s = S.summarize(recs)
     assert s["p99_s"] >= s["p50_s"] > 0.0
     assert s["cell_updates"] == sum(r["cell_updates"] for r in recs)
