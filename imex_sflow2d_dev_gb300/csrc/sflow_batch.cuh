@@ -295,6 +295,7 @@ class Batch : public BatchBase {
     BatchRun* d_runs = nullptr;
     BatchCtl* d_ctl = nullptr;
     unsigned long long *d_list0 = nullptr, *d_list1 = nullptr, *d_cand = nullptr;
+    unsigned long long *d_dlist0 = nullptr, *d_dlist1 = nullptr;
     BatchSummary* d_summary = nullptr;
     BatchSummary* h_summary = nullptr;
     BatchArgs<R> args;
@@ -335,7 +336,7 @@ class Batch : public BatchBase {
       }
       if (graph_exec) cudaGraphExecDestroy(graph_exec);
       if (graph) cudaGraphDestroy(graph);
-      void* bufs[7] = {d_args, d_runs, d_ctl, d_list0, d_list1, d_cand, d_summary};
+      void* bufs[9] = {d_args, d_runs, d_ctl, d_list0, d_list1, d_dlist0, d_dlist1, d_cand, d_summary};
       for (void* p : bufs)
         if (p) cudaFree(p);
       if (h_summary) cudaFreeHost(h_summary);
@@ -383,6 +384,8 @@ class Batch : public BatchBase {
     if ((e = cudaMalloc((void**)&g->d_list0, lb)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&g->d_list1, lb)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&g->d_cand, lb)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_dlist0, lb)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_dlist1, lb)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&g->d_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
     if ((e = cudaMallocHost((void**)&g->h_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
     g->args.args = g->d_args;
@@ -391,6 +394,8 @@ class Batch : public BatchBase {
     g->args.list0 = g->d_list0;
     g->args.list1 = g->d_list1;
     g->args.cand = g->d_cand;
+    g->args.dlist0 = g->d_dlist0;
+    g->args.dlist1 = g->d_dlist1;
     g->args.summary = g->d_summary;
     g->args.max_runs = max_runs_;
     groups_[ns] = std::move(g);

@@ -57,6 +57,7 @@ struct BatchRun {
 
 struct BatchCtl {
   unsigned count[2];   // entries in tile list 0 / 1
+  unsigned dcount[2];  // entries in dry-border list 0 / 1
   unsigned ncand;      // entries in the candidate list
   unsigned pp;         // list read by k_b_cand
   unsigned work[3];    // dynamic tile counters of k_b_mask, k_b_flux, k_b_stage2
@@ -79,6 +80,10 @@ struct BatchArgs {
   BatchCtl* ctl;
   unsigned long long* list0;
   unsigned long long* list1;
+  // active tiles whose only seeds are border cells (tile code 3): check_solve
+  // keeps evaluating them (candidates of the next step), flux and stage skip
+  unsigned long long* dlist0;
+  unsigned long long* dlist1;
   unsigned long long* cand;
   BatchSummary* summary;     // [max_runs]
   int max_runs;
@@ -132,11 +137,13 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   const unsigned long long* L = pp ? b.list1 : b.list0;
-  const unsigned n = ctl->count[pp];
+  const unsigned long long* Ld = pp ? b.dlist1 : b.dlist0;
+  const unsigned n = ctl->count[pp], nd = ctl->dcount[pp];
   const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned G = gridDim.x * blockDim.x;
   if (gt == 0) {
     ctl->count[pp ^ 1u] = 0u;
+    ctl->dcount[pp ^ 1u] = 0u;
     ctl->work[0] = 0u;
   }
   for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
@@ -148,8 +155,9 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
       st->src_t_coeff_f = (float)st->src_t_coeff;
     }
   }
-  for (unsigned i = gt; i < n * 9u; i += G) {
-    const unsigned long long e = L[i / 9u];
+  for (unsigned i = gt; i < (n + nd) * 9u; i += G) {
+    const unsigned k = i / 9u;
+    const unsigned long long e = k < n ? L[k] : Ld[k - n];
     const int slot = entry_slot(e);
     const BatchRun& br = b.runs[slot];
     if (!br.live || (br.gen & 0xffffu) != entry_gen(e) || !running(br.st)) continue;
@@ -187,6 +195,7 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArg
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   unsigned long long* out = pp ? b.list0 : b.list1;
+  unsigned long long* dout = pp ? b.dlist0 : b.dlist1;
   const unsigned n = ctl->ncand;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->work[1] = 0u;
   TileQueue tq{&ctl->work[0], s_idx};
@@ -200,10 +209,14 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArg
     if (threadIdx.x == 0) br.cand[tile] = 0u;
     // k_b_cand listed only running runs, and no run's clock moves before k_b_dt
     const int tx = (int)(tile % (unsigned)br.tiles_x), ty = (int)(tile / (unsigned)br.tiles_x);
-    const int cnt = mask_tile<R, TH>(a, 0, tx, ty, br.tiles_x);
-    if (cnt > 0 && threadIdx.x == 0) {
+    const int code = mask_tile<R, TH>(a, 0, tx, ty, br.tiles_x, true);
+    if (code == 1 && threadIdx.x == 0) {
       const unsigned pos = atomicAdd(&ctl->count[pp ^ 1u], 1u);
       out[pos] = e;
+    } else if (code == TILE_DRY_BORDER && threadIdx.x == 0) {
+      const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
+      dout[pos] = e;
+      a.tile_wet[tile] = 0;   // dry; the stage kernel does not visit it
     }
   }
 }
@@ -264,26 +277,21 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_dt(BatchArgs<R> b) {
 template <class R, int NS, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, TileShape<TH>::STAGE_MIN_BLOCKS)
     k_b_stage2(BatchArgs<R> b) {
-  __shared__ __align__(16) unsigned char sa_raw[sizeof(KArgs<R>)];
   __shared__ unsigned s_idx[2];
   step_kernel_entry();
-  KArgs<R>& a = *reinterpret_cast<KArgs<R>*>(sa_raw);
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   const unsigned long long* L = pp ? b.list1 : b.list0;
   const unsigned n = ctl->count[pp];
-  int cur = -1;
   TileQueue tq{&ctl->work[2], s_idx};
   for (unsigned i = tq.first(); i < n; i = tq.next()) {
     tq.prefetch();
     const unsigned long long e = L[i];
     const int slot = entry_slot(e);
     const unsigned tile = entry_tile(e);
-    if (slot != cur) {
-      load_args(&a, &b.args[slot]);
-      cur = slot;
-      __syncthreads();
-    }
+    // the run's arguments straight from the argument table (L1-cached);
+    // unlike the flux kernel's, the stage code reads them few times per tile
+    const KArgs<R>& a = b.args[slot];
     if (!a.st->run_step) continue;
     if (a.tile_active[tile] == 2) {   // dry without ring cells (flux_tile)
       if (threadIdx.x == 0) a.tile_wet[tile] = 0;

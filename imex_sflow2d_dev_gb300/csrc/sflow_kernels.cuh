@@ -190,17 +190,30 @@ constexpr int MASK_HALO = 4;
 constexpr int MRX = TX + 2 * MASK_HALO;
 static_assert(MRX <= 64, "a frame row must fit one 64-bit mask");
 
+// Tile codes of tile_active: 0 inactive; 1 active; 2 active, dry and
+// without ring cells (found by the flux kernel: the stage kernel leaves it
+// unchanged); 3 active through border seeds only (found by check_solve with
+// mark_dry: no cell of its 4-cell frame holds mass or belongs to the ring
+// inlet, and its ghosts are dry or it lies 2 cells inside the domain) --
+// the flux and stage kernels would compute zero fluxes and no change, and
+// skip it.
+constexpr uint8_t TILE_DRY_BORDER = 3;
+
+// Returns the tile code (block-uniform).
 template <class R, int TH>
-__device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x) {
+__device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x,
+                                         bool mark_dry = false) {
   constexpr int TY = TH, MRY = TH + 2 * MASK_HALO;
   constexpr int RPW = (MRY + TH - 1) / TH;   // frame rows per warp (TH warps)
   __shared__ unsigned long long srow[MRY];   // bit x: seed at frame column x
+  __shared__ unsigned s_spec[TH];            // per warp: a frame cell with mass or a ring cell
   RunState* st = a.st;
   const Grid<R>& g = a.g;
   const int j0 = tx * TX, k0 = ty * TY;
   const int nrk = a.pd.nrk;
   const int lane = threadIdx.x % TX, warp = threadIdx.x / TX;
   int any = 0;
+  unsigned wspec = 0u;
   if (!solve_all) {
     // frame row y = warp + r*TH; columns lane and 32 + lane (lane < 8); all
     // loads of a thread are issued before any is used
@@ -229,17 +242,20 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
       for (int h = 0; h < 2; ++h) {
         const int x = lane + TX * h;
         const int jj = j0 + x - MASK_HALO, kk = k0 + y - MASK_HALO;
-        int sd = 0;
+        int sd = 0, sp = 0;
         if (x < MRX && jj >= 0 && jj < g.nx && kk >= 0 && kk < g.ny) {
           if (jj == 0 || jj == g.nx - 1 || kk == 0 || kk == g.ny - 1) sd = 1;
           else if (qv[r][h] > R(0)) sd = 1;
           else if (a.pd.radial_source && (fv[r][h] & F_SC_MASK) == 2) sd = 1;
+          sp = (qv[r][h] > R(0)) || (a.pd.radial_source && (fv[r][h] & F_SC_MASK) != 0);
         }
         bits[h] = __ballot_sync(0xffffffffu, sd);
+        wspec |= __ballot_sync(0xffffffffu, sp);
       }
       if (lane == 0) srow[y] = (unsigned long long)bits[0] | ((unsigned long long)bits[1] << 32);
       any |= (bits[0] | bits[1]) != 0u;
     }
+    if (lane == 0) s_spec[warp] = wspec;
     any = __syncthreads_or(any);
   }
   const int j = j0 + lane;
@@ -270,11 +286,19 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
     a.mask[c] = (uint8_t)act;
   }
   int cnt = __syncthreads_count(act);
+  int code = cnt > 0 ? 1 : 0;
+  if (code && mark_dry && !solve_all) {
+    unsigned spec = 0u;
+#pragma unroll
+    for (int w = 0; w < TH; ++w) spec |= s_spec[w];
+    const bool inside = j0 - HALO >= 0 && k0 - HALO >= 0 && j0 + TX + HALO <= g.nx && k0 + TY + HALO <= g.ny;
+    if (!spec && (g.dry_bc || inside)) code = TILE_DRY_BORDER;
+  }
   if (threadIdx.x == 0) {
-    a.tile_active[ty * tiles_x + tx] = cnt > 0;
+    a.tile_active[ty * tiles_x + tx] = (uint8_t)code;
     if (cnt) atomicAdd((unsigned long long*)&st->cells_acc[st->steps & 1], (unsigned long long)cnt);
   }
-  return cnt;
+  return code;
 }
 
 // A tile without a static seed within n_RK cells, with no tile of its 3 x 3
@@ -312,7 +336,7 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_mask(KArgs<R> a
     st->src_t_coeff_f = (float)st->src_t_coeff;
   }
   if (mode == 2 && mask_tile_skippable(a, blockIdx.x, blockIdx.y, gridDim.x, gridDim.y)) return;
-  mask_tile<R, TH>(a, mode == 1, blockIdx.x, blockIdx.y, gridDim.x);
+  mask_tile<R, TH>(a, mode == 1, blockIdx.x, blockIdx.y, gridDim.x, mode == 2);
 }
 
 // ---------------------------------------------------------------------------
@@ -955,7 +979,8 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS) k_flux(KArgs<R> a
   // the timestep pass runs before k_dt advances the clock; the later stage
   // fluxes of a step run after it and follow its run_step decision
   if (want_dt ? !running(st) : !st->run_step) return;
-  if (!a.tile_active[blockIdx.y * gridDim.x + blockIdx.x]) return;
+  const uint8_t ta = a.tile_active[blockIdx.y * gridDim.x + blockIdx.x];
+  if (ta == 0 || ta == TILE_DRY_BORDER) return;
   flux_tile<R, NS, LIM, TH>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
 }
 
@@ -1372,7 +1397,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, sizeof(R) == 4 ?
   if (!a.st->run_step) return;
   const int tile = (blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x;
   const uint8_t ta = a.tile_active[tile];
-  if (ta == 0 || ta == 2) return;   // inactive, or dry without ring cells (k_flux)
+  if (ta == 0 || ta == 2 || ta == TILE_DRY_BORDER) return;   // inactive, or left unchanged (k_flux, k_mask)
   unsigned status = 0;
   int nit = 0;
   int wet = stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, blockIdx.y * 8 + threadIdx.x / TX,
