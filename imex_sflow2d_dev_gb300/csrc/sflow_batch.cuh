@@ -90,6 +90,7 @@ class Batch : public BatchBase {
     br.st = sv->state_dev();
     br.cand = cand;
     br.tile_wet = sv->tile_wet_dev();
+    br.tile_count = sv->tile_count_dev();
     br.tile_seed = tile_seed;
     br.tiles_x = sv->tiles_x();
     br.tiles_y = sv->tiles_y();

@@ -49,6 +49,7 @@ struct BatchRun {
   uint32_t* cand;    // per-tile candidate flag
   const uint8_t* tile_wet;    // wet byte of the tile after the last step (TW_*; 0xff: unknown)
   const uint8_t* tile_seed;   // tile holds ring-boundary cells, or is a narrow edge tile
+  const uint16_t* tile_count; // active cells of a tile of code 3
   int tiles_x, tiles_y;
   unsigned gen;      // generation of the run in this slot
   int live;          // slot holds a run
@@ -141,9 +142,9 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
   const unsigned n = ctl->count[pp], nd = ctl->dcount[pp];
   const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned G = gridDim.x * blockDim.x;
+  unsigned long long* Ldout = pp ? b.dlist0 : b.dlist1;   // cleared by k_b_dt
   if (gt == 0) {
     ctl->count[pp ^ 1u] = 0u;
-    ctl->dcount[pp ^ 1u] = 0u;
     ctl->work[0] = 0u;
   }
   for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
@@ -163,10 +164,34 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
     if (!br.live || (br.gen & 0xffffu) != entry_gen(e) || !running(br.st)) continue;
     const unsigned tile = entry_tile(e);
     const int nb = (int)(i % 9u);
+    const int dx = nb % 3 - 1, dy = nb / 3 - 1;
+    if (k >= n && nb == 4) {
+      // a tile of code 3 (dry border strip) with no mass in its 3 x 3
+      // neighbourhood keeps its code, mask and count (see
+      // mask_tile_skippable): carried to the next dry-border list.  Not when
+      // a neighbour dilates to every neighbour (tile_seed): the tile is a
+      // candidate of this step then, and must not be listed twice.
+      const int tx0 = (int)(tile % (unsigned)br.tiles_x), ty0 = (int)(tile / (unsigned)br.tiles_x);
+      bool keep = true;
+      for (int yy = ty0 - 1; yy <= ty0 + 1 && keep; ++yy)
+        for (int xx = tx0 - 1; xx <= tx0 + 1; ++xx) {
+          if (xx < 0 || yy < 0 || xx >= br.tiles_x || yy >= br.tiles_y) continue;
+          const int t3 = yy * br.tiles_x + xx;
+          if ((br.tile_wet[t3] & TW_ANY) || (t3 != (int)tile && br.tile_seed[t3])) {
+            keep = false;
+            break;
+          }
+        }
+      if (keep) {
+        const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
+        Ldout[pos] = e;
+        atomicAdd((unsigned long long*)&br.st->cells_acc[br.st->steps & 1], (unsigned long long)br.tile_count[tile]);
+        continue;
+      }
+    }
     // only tiles with mass near the shared edge, ring cells or a narrow
     // domain edge can activate cells of their neighbours; a dry tile kept
     // active by the border rule is its own only candidate
-    const int dx = nb % 3 - 1, dy = nb / 3 - 1;
     if (nb != 4 && !br.tile_seed[tile]) {
       const unsigned tw = br.tile_wet[tile];
       const unsigned need = TW_ANY | (dx < 0 ? TW_W : 0u) | (dx > 0 ? TW_E : 0u) | (dy < 0 ? TW_S : 0u) |
@@ -217,6 +242,8 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArg
       const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
       dout[pos] = e;
       a.tile_wet[tile] = 0;   // dry; the stage kernel does not visit it
+    } else if (code == 0 && threadIdx.x == 0) {
+      a.tile_wet[tile] = 0;   // an inactive tile holds no mass
     }
   }
 }
@@ -269,6 +296,10 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_dt(BatchArgs<R> b) {
   if (gt == 0) {
     BatchCtl* ctl = b.ctl;
     ctl->pp ^= 1u;
+    // the next step's k_b_cand and k_b_mask append dry-border tiles to the
+    // lists this step read (k_b_cand carries tiles there while it runs, so
+    // the count is cleared here, not by it)
+    ctl->dcount[ctl->pp ^ 1u] = 0u;
     ctl->ncand = 0u;
     ctl->steps += 1u;
   }

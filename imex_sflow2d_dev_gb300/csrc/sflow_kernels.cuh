@@ -74,6 +74,7 @@ struct KArgs {
   // (border or ring-boundary cell); check_solve skips the other tiles
   uint8_t* tile_wet_step;
   const uint8_t* tile_static;
+  uint16_t* tile_count;   // active cells of a tile of code 3 (dry border)
   R* hmax;
   R* pdynmax;
   R* mvmax;
@@ -296,6 +297,7 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
   }
   if (threadIdx.x == 0) {
     a.tile_active[ty * tiles_x + tx] = (uint8_t)code;
+    if (code == TILE_DRY_BORDER) a.tile_count[ty * tiles_x + tx] = (uint16_t)cnt;
     if (cnt) atomicAdd((unsigned long long*)&st->cells_acc[st->steps & 1], (unsigned long long)cnt);
   }
   return code;
@@ -307,18 +309,26 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
 // in that neighbourhood) and already has an all-zero mask: check_solve
 // skips it.  The tile also clears its wet flag of the buffer that this
 // step's stage kernel sets.
+//
+// A tile of code 3 (active through border seeds only, dry frame) keeps its
+// code, mask and active count while no tile of its 3 x 3 neighbourhood
+// holds mass: its 4-cell frame then stays dry, and its seeds are static.
+// Only its count is added.
 template <class R>
 __device__ __forceinline__ bool mask_tile_skippable(const KArgs<R>& a, int tx, int ty, int tiles_x, int tiles_y) {
   const int nt = tiles_x * tiles_y, t = ty * tiles_x + tx;
   const unsigned par = (unsigned)(a.st->steps & 1);
   if (threadIdx.x == 0) a.tile_wet_step[(par ^ 1u) * nt + t] = 0;
-  if (a.tile_active[t] || a.tile_static[t]) return false;
+  const uint8_t ta = a.tile_active[t];
+  if (!(ta == TILE_DRY_BORDER || (ta == 0 && !a.tile_static[t]))) return false;
   const uint8_t* w = a.tile_wet_step + par * nt;
   for (int dy = -1; dy <= 1; ++dy)
     for (int dx = -1; dx <= 1; ++dx) {
       const int x = tx + dx, y = ty + dy;
       if (x >= 0 && x < tiles_x && y >= 0 && y < tiles_y && w[y * tiles_x + x]) return false;
     }
+  if (ta == TILE_DRY_BORDER && threadIdx.x == 0)
+    atomicAdd((unsigned long long*)&a.st->cells_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
   return true;
 }
 

@@ -242,6 +242,7 @@ class Solver : public SolverBase {
     return ts;
   }
   uint8_t* tile_wet_dev() const { return tile_wet_; }
+  const uint16_t* tile_count_dev() const { return tile_count_; }
 
   // device bytes a run of this set-up holds while it is in a batch
   static int64_t batch_bytes(const HostSetup& hs, int tile_h) {
@@ -566,7 +567,9 @@ class Solver : public SolverBase {
     free_tracked(tile_active_, n_old);
     free_tracked(tile_wet_, 3 * n_old);
     free_tracked(tile_static_, n_old);
+    free_tracked(tile_count_, n_old * sizeof(uint16_t));
     tile_active_ = tile_wet_ = tile_static_ = nullptr;
+    tile_count_ = nullptr;
     tab_ = t;
     tile_h_ = th;
     tiles_y_ = (hs_.ny + th - 1) / th;
@@ -576,6 +579,7 @@ class Solver : public SolverBase {
     ka_.tile_wet = tile_wet_;
     ka_.tile_wet_step = tile_wet_ + (size_t)tiles_x_ * tiles_y_;
     ka_.tile_static = tile_static_;
+    ka_.tile_count = tile_count_;
     smem_flux_ = flux_smem_bytes(hs_.nv, th);
     SFLOW_CU(set_smem_attr());
     return SFLOW_OK;
@@ -726,6 +730,7 @@ class Solver : public SolverBase {
   R* geo_[8];
   uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr, *tile_wet_ = nullptr,
           *tile_static_ = nullptr;
+  uint16_t* tile_count_ = nullptr;
   RunState* st_ = nullptr;
   double *stage_aos_ = nullptr, *stat_part_ = nullptr, *stat_out_ = nullptr;
   int nstat_blocks_ = 0;
@@ -813,6 +818,8 @@ class Solver : public SolverBase {
     cudaError_t e = alloc((void**)&tile_active_, n);
     if (e == cudaSuccess) e = alloc((void**)&tile_wet_, 3 * n);
     if (e == cudaSuccess) e = alloc((void**)&tile_static_, n);
+    if (e == cudaSuccess) e = alloc((void**)&tile_count_, n * sizeof(uint16_t));
+    if (e == cudaSuccess) e = cudaMemset(tile_count_, 0, n * sizeof(uint16_t));
     if (e == cudaSuccess) e = cudaMemset(tile_active_, 0, n);
     if (e == cudaSuccess) e = cudaMemset(tile_wet_, 0xff, 3 * n);   // unknown
     if (e == cudaSuccess) {
@@ -993,6 +1000,7 @@ class Solver : public SolverBase {
     ka_.tile_wet = tile_wet_;
     ka_.tile_wet_step = tile_wet_ + (size_t)tiles_x_ * tiles_y_;
     ka_.tile_static = tile_static_;
+    ka_.tile_count = tile_count_;
     ka_.hmax = hmax_; ka_.pdynmax = pdynmax_; ka_.mvmax = mvmax_; ka_.st = st_;
     ka_.deposit = deposit_;
     ka_.take_last = hs_.take_last;
