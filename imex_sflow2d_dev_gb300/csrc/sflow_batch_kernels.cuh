@@ -156,55 +156,67 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
       st->src_t_coeff_f = (float)st->src_t_coeff;
     }
   }
-  for (unsigned i = gt; i < (n + nd) * 9u; i += G) {
-    const unsigned k = i / 9u;
-    const unsigned long long e = k < n ? L[k] : Ld[k - n];
+  auto add_cand = [&](const BatchRun& br, unsigned long long e, int tx, int ty) {
+    if (tx < 0 || ty < 0 || tx >= br.tiles_x || ty >= br.tiles_y) return;
+    const unsigned t2 = (unsigned)(ty * br.tiles_x + tx);
+    if (atomicExch(&br.cand[t2], 1u) == 0u) {
+      const unsigned pos = atomicAdd(&ctl->ncand, 1u);
+      b.cand[pos] = (e & 0xffffffff00000000ull) | (unsigned long long)t2;
+    }
+  };
+  // active tiles of the last step: one thread per (tile, neighbour)
+  for (unsigned i = gt; i < n * 9u; i += G) {
+    const unsigned long long e = L[i / 9u];
     const int slot = entry_slot(e);
     const BatchRun& br = b.runs[slot];
     if (!br.live || (br.gen & 0xffffu) != entry_gen(e) || !running(br.st)) continue;
     const unsigned tile = entry_tile(e);
     const int nb = (int)(i % 9u);
     const int dx = nb % 3 - 1, dy = nb / 3 - 1;
-    if (k >= n && nb == 4) {
-      // a tile of code 3 (dry border strip) with no mass in its 3 x 3
-      // neighbourhood keeps its code, mask and count (see
-      // mask_tile_skippable): carried to the next dry-border list.  Not when
-      // a neighbour dilates to every neighbour (tile_seed): the tile is a
-      // candidate of this step then, and must not be listed twice.
-      const int tx0 = (int)(tile % (unsigned)br.tiles_x), ty0 = (int)(tile / (unsigned)br.tiles_x);
-      bool keep = true;
-      for (int yy = ty0 - 1; yy <= ty0 + 1 && keep; ++yy)
-        for (int xx = tx0 - 1; xx <= tx0 + 1; ++xx) {
-          if (xx < 0 || yy < 0 || xx >= br.tiles_x || yy >= br.tiles_y) continue;
-          const int t3 = yy * br.tiles_x + xx;
-          if ((br.tile_wet[t3] & TW_ANY) || (t3 != (int)tile && br.tile_seed[t3])) {
-            keep = false;
-            break;
-          }
-        }
-      if (keep) {
-        const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
-        Ldout[pos] = e;
-        atomicAdd((unsigned long long*)&br.st->cells_acc[br.st->steps & 1], (unsigned long long)br.tile_count[tile]);
-        continue;
-      }
-    }
     // only tiles with mass near the shared edge, ring cells or a narrow
-    // domain edge can activate cells of their neighbours; a dry tile kept
-    // active by the border rule is its own only candidate
+    // domain edge can activate cells of their neighbours
     if (nb != 4 && !br.tile_seed[tile]) {
       const unsigned tw = br.tile_wet[tile];
       const unsigned need = TW_ANY | (dx < 0 ? TW_W : 0u) | (dx > 0 ? TW_E : 0u) | (dy < 0 ? TW_S : 0u) |
                             (dy > 0 ? TW_N : 0u);
       if ((tw & need) != need) continue;
     }
-    const int tx = (int)(tile % (unsigned)br.tiles_x) + dx;
-    const int ty = (int)(tile / (unsigned)br.tiles_x) + dy;
-    if (tx < 0 || ty < 0 || tx >= br.tiles_x || ty >= br.tiles_y) continue;
-    const unsigned t2 = (unsigned)(ty * br.tiles_x + tx);
-    if (atomicExch(&br.cand[t2], 1u) == 0u) {
-      const unsigned pos = atomicAdd(&ctl->ncand, 1u);
-      b.cand[pos] = (e & 0xffffffff00000000ull) | (unsigned long long)t2;
+    add_cand(br, e, (int)(tile % (unsigned)br.tiles_x) + dx, (int)(tile / (unsigned)br.tiles_x) + dy);
+  }
+  // dry border strips (code 3) of the last step: one thread per tile.  With
+  // no mass in its 3 x 3 neighbourhood the tile keeps its code, mask and
+  // count (see mask_tile_skippable) and is carried to the next dry-border
+  // list -- not when a neighbour dilates to every neighbour (tile_seed): it
+  // is a candidate of this step then and must not be listed twice.  Else it
+  // is its own candidate (it holds no mass, so it dilates only as a
+  // tile_seed tile).
+  for (unsigned k = gt; k < nd; k += G) {
+    const unsigned long long e = Ld[k];
+    const int slot = entry_slot(e);
+    const BatchRun& br = b.runs[slot];
+    if (!br.live || (br.gen & 0xffffu) != entry_gen(e) || !running(br.st)) continue;
+    const unsigned tile = entry_tile(e);
+    const int tx0 = (int)(tile % (unsigned)br.tiles_x), ty0 = (int)(tile / (unsigned)br.tiles_x);
+    bool keep = true;
+    for (int yy = ty0 - 1; yy <= ty0 + 1 && keep; ++yy)
+      for (int xx = tx0 - 1; xx <= tx0 + 1; ++xx) {
+        if (xx < 0 || yy < 0 || xx >= br.tiles_x || yy >= br.tiles_y) continue;
+        const int t3 = yy * br.tiles_x + xx;
+        if ((br.tile_wet[t3] & TW_ANY) || (t3 != (int)tile && br.tile_seed[t3])) {
+          keep = false;
+          break;
+        }
+      }
+    if (keep) {
+      const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
+      Ldout[pos] = e;
+      atomicAdd((unsigned long long*)&br.st->cells_acc[br.st->steps & 1], (unsigned long long)br.tile_count[tile]);
+      continue;
+    }
+    if (br.tile_seed[tile]) {
+      for (int nb = 0; nb < 9; ++nb) add_cand(br, e, tx0 + nb % 3 - 1, ty0 + nb / 3 - 1);
+    } else {
+      add_cand(br, e, tx0, ty0);
     }
   }
 }
