@@ -314,22 +314,31 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
 // code, mask and active count while no tile of its 3 x 3 neighbourhood
 // holds mass: its 4-cell frame then stays dry, and its seeds are static.
 // Only its count is added.
+// The test is made by thread 0 and shared with one barrier (block-uniform).
 template <class R>
 __device__ __forceinline__ bool mask_tile_skippable(const KArgs<R>& a, int tx, int ty, int tiles_x, int tiles_y) {
-  const int nt = tiles_x * tiles_y, t = ty * tiles_x + tx;
-  const unsigned par = (unsigned)(a.st->steps & 1);
-  if (threadIdx.x == 0) a.tile_wet_step[(par ^ 1u) * nt + t] = 0;
-  const uint8_t ta = a.tile_active[t];
-  if (!(ta == TILE_DRY_BORDER || (ta == 0 && !a.tile_static[t]))) return false;
-  const uint8_t* w = a.tile_wet_step + par * nt;
-  for (int dy = -1; dy <= 1; ++dy)
-    for (int dx = -1; dx <= 1; ++dx) {
-      const int x = tx + dx, y = ty + dy;
-      if (x >= 0 && x < tiles_x && y >= 0 && y < tiles_y && w[y * tiles_x + x]) return false;
+  int skip = 0;
+  if (threadIdx.x == 0) {
+    const int nt = tiles_x * tiles_y, t = ty * tiles_x + tx;
+    const unsigned par = (unsigned)(a.st->steps & 1);
+    a.tile_wet_step[(par ^ 1u) * nt + t] = 0;
+    const uint8_t ta = a.tile_active[t];
+    if (ta == TILE_DRY_BORDER || (ta == 0 && !a.tile_static[t])) {
+      const uint8_t* w = a.tile_wet_step + par * nt;
+      skip = 1;
+      for (int dy = -1; dy <= 1 && skip; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int x = tx + dx, y = ty + dy;
+          if (x >= 0 && x < tiles_x && y >= 0 && y < tiles_y && w[y * tiles_x + x]) {
+            skip = 0;
+            break;
+          }
+        }
+      if (skip && ta == TILE_DRY_BORDER)
+        atomicAdd((unsigned long long*)&a.st->cells_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
     }
-  if (ta == TILE_DRY_BORDER && threadIdx.x == 0)
-    atomicAdd((unsigned long long*)&a.st->cells_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
-  return true;
+  }
+  return __syncthreads_or(skip) != 0;
 }
 
 // mode 0: check_solve(.FALSE.); 1: check_solve(.TRUE.) (solve_all); 2: as 0
