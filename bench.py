@@ -18,7 +18,9 @@ one step per timed interval with a 512 MB write between steps to flush L2
 (the working set, ~100 MB, would otherwise stay in the 126 MB L2).  The
 plain FP64 form is timed the same way and reported beside it, with the L1
 error of h between the two forms.  `e2e` is the same metric through the C
-ABI with the state in pinned host memory copied in and out every step.
+ABI with the state in pinned host memory copied in and out every step;
+its `transfers` split times the two copies alone and, for the host link's
+rate, copy-engine copies of the same pinned buffer.
 
 Further legs on rank 0, each a key of the same JSON line:
   ensemble      the 256-run mixed ensemble (sides 128-1024, own DEMs and
@@ -531,10 +533,33 @@ def run_gb300(args, d):
             se.download_q_ptr(ptr)
         te = time.perf_counter() - t0
         c1 = se.counters()
+        nbytes = nx * ny * nv * 8
         e2e = {"value": d.sum((c1["cell_updates"] - c0["cell_updates"])) / d.max(te),
-               "unit": UNIT, "h2d_bytes_per_step": nx * ny * nv * 8,
-               "d2h_bytes_per_step": nx * ny * nv * 8, "steps": ne,
-               "path": "sflow_put_q + sflow_step + sflow_download_q, pinned host buffers"}
+               "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "steps": ne,
+               "path": "sflow_put_q + sflow_step + sflow_download_q, pinned host buffers",
+               "ms_per_step": te / ne * 1e3}
+        # where the time goes: the two host transfers alone, and plain
+        # copy-engine copies of the same pinned buffer (the host link's rate)
+        dev = torch.empty(nx * ny * nv, dtype=torch.float64, device="cuda")
+
+        def wall_ms(fn, n=8):
+            fn()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for _ in range(n):
+                fn()
+            torch.cuda.synchronize()
+            return (time.perf_counter() - t) / n * 1e3
+
+        split = {"put_ms": wall_ms(lambda: se.put_q_ptr(ptr)),
+                 "download_ms": wall_ms(lambda: se.download_q_ptr(ptr)),
+                 "dma_h2d_ms": wall_ms(lambda: dev.copy_(pinned, non_blocking=True)),
+                 "dma_d2h_ms": wall_ms(lambda: pinned.copy_(dev, non_blocking=True))}
+        for k in list(split):
+            split[k.replace("_ms", "_GBs")] = nbytes / (split[k] * 1e-3) / 1e9
+        e2e["transfers"] = split
+        del dev
         se.close()
     except Exception as exc:  # pragma: no cover - reported, not hidden
         e2e = {"value": None, "unit": UNIT, "error": str(exc)}
@@ -587,7 +612,7 @@ def run_gb300(args, d):
                          "traffic": traffic, "alg_bytes_per_active_cell": alg[dom],
                          "kernel_ms_per_step": {k: v / max(pk_steps, 1) for k, v in kms.items()},
                          "limiter": ("SM instruction issue, not HBM: ncu on the 2048^2 case shows "
-                                     "k_flux issuing on 73 % of cycles at 8.8 % of DRAM throughput "
+                                     "k_flux issuing on 74 % of cycles at 7.6 % of DRAM throughput "
                                      "(profiles/k_flux_k_stage2_pyroclastic_2048.md)")},
             "cpu_baseline": ({k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
                              if cb else None),
