@@ -656,9 +656,18 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
   if (ns > 0) {
     if (DIR == 1) {
       R s = R(0), s2 = R(0);
+      if constexpr (sizeof(R) == 4) {
+        // one reciprocal of the mass flux for the FP32 form
+        const R inv0 = R(1) / H[0];
 #pragma unroll
-      for (int i = 0; i < ns; ++i) { s += H[4 + i] / H[0]; s2 += H[4 + i]; }
-      if (s2 / H[0] >= R(1)) {
+        for (int i = 0; i < ns; ++i) { s += H[4 + i] * inv0; s2 += H[4 + i]; }
+        s2 = s2 * inv0;
+      } else {
+#pragma unroll
+        for (int i = 0; i < ns; ++i) { s += H[4 + i] / H[0]; s2 += H[4 + i]; }
+        s2 = s2 / H[0];
+      }
+      if (s2 >= R(1)) {
 #pragma unroll
         for (int i = 0; i < ns; ++i) H[4 + i] = H[4 + i] / s;
       }

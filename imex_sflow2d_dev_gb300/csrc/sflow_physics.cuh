@@ -145,7 +145,11 @@ __device__ __forceinline__ R qc_to_qp(const Phys<R>& P, const R* q, R* qp) {
   }
   R inv_rho_c;
   if (P.gas) {
-    R Rc = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_gas_const_a + R(0)) / xc : P.sp_gas_const_a;
+    // carrier of air alone: (x_c R_a) / x_c is R_a (the FP32 form uses it
+    // as such; the FP64 form keeps the reference's operations)
+    R Rc;
+    if constexpr (sizeof(R) == 4) Rc = P.sp_gas_const_a;
+    else Rc = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_gas_const_a + R(0)) / xc : P.sp_gas_const_a;
     inv_rho_c = Rc * T * P.inv_pres;
   } else {
     inv_rho_c = P.inv_rho_l;
@@ -207,7 +211,9 @@ __device__ __forceinline__ void qp_to_qc(const Phys<R>& P, const R* qp, R* qc) {
   R rho_c;
   if (P.gas) {
     R rho_a = P.pres / (P.sp_gas_const_a * r_T);
-    rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
+    // carrier of air alone: ((1 - at) rho_a) / (1 - at) is rho_a
+    if constexpr (sizeof(R) == 4) rho_c = rho_a;
+    else rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
   } else {
     rho_c = P.rho_l;
   }
@@ -218,8 +224,12 @@ __device__ __forceinline__ void qp_to_qc(const Phys<R>& P, const R* qp, R* qc) {
   R inv_rhom = R(1) / rho_m;
   R xc = alphac * rho_c * inv_rhom;
   R cp_c;
-  if (P.gas) cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
-  else cp_c = P.sp_heat_l;
+  if (P.gas) {
+    if constexpr (sizeof(R) == 4) cp_c = P.sp_heat_a;   // (x_c c_a) / x_c
+    else cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
+  } else {
+    cp_c = P.sp_heat_l;
+  }
   R dcp = R(0);
   for (int i = 0; i < ns; ++i) dcp += (arhos[i] * inv_rhom) * P.sp_heat_s[i];
   R cmix = dcp + xc * cp_c;
@@ -259,7 +269,9 @@ __device__ __forceinline__ Mixt<R> mixt_var(const Phys<R>& P, const R* qpj, bool
   R rho_c;
   if (P.gas) {
     R rho_a = P.pres / (P.sp_gas_const_a * r_T);
-    rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
+    // carrier of air alone: ((1 - at) rho_a) / (1 - at) is rho_a
+    if constexpr (sizeof(R) == 4) rho_c = rho_a;
+    else rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
   } else {
     rho_c = P.rho_l;
   }
@@ -267,7 +279,9 @@ __device__ __forceinline__ Mixt<R> mixt_var(const Phys<R>& P, const R* qpj, bool
   for (int i = 0; i < ns; ++i) d += al[i] * P.rho_s[i];
   R rho_m = (R(1) - at) * rho_c + d;
   R inv_rhom = R(1) / rho_m;
-  R red_grav = (rho_m - P.rho_a_amb) / rho_m * P.grav;
+  R red_grav;
+  if constexpr (sizeof(R) == 4) red_grav = (rho_m - P.rho_a_amb) * inv_rhom * P.grav;
+  else red_grav = (rho_m - P.rho_a_amb) / rho_m * P.grav;
   R u2 = sq(r_u) + sq(r_v);
   m.Ri = (u2 > R(0)) ? rmin(cst<R>(1.0e15), red_grav * r_h / u2) : R(0);
   m.rho_m = rho_m;
@@ -281,8 +295,12 @@ __device__ __forceinline__ Mixt<R> mixt_var(const Phys<R>& P, const R* qpj, bool
     for (int i = 0; i < ns; ++i) { xs[i] = al[i] * P.rho_s[i] * inv_rhom; sxs += xs[i]; }
     R xc = R(1) - sxs;
     R cp_c;
-    if (P.gas) cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
-    else cp_c = P.sp_heat_l;
+    if (P.gas) {
+      if constexpr (sizeof(R) == 4) cp_c = P.sp_heat_a;   // (x_c c_a) / x_c
+      else cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
+    } else {
+      cp_c = P.sp_heat_l;
+    }
     R dcp = R(0);
     for (int i = 0; i < ns; ++i) dcp += xs[i] * P.sp_heat_s[i];
     m.cp_c = cp_c;
@@ -319,7 +337,9 @@ __device__ __forceinline__ Mixt<R> qp_to_qc_mixt(const Phys<R>& P, const R* qp, 
   R rho_c;
   if (P.gas) {
     R rho_a = P.pres / (P.sp_gas_const_a * r_T);
-    rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
+    // carrier of air alone: ((1 - at) rho_a) / (1 - at) is rho_a
+    if constexpr (sizeof(R) == 4) rho_c = rho_a;
+    else rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
   } else {
     rho_c = P.rho_l;
   }
@@ -330,8 +350,12 @@ __device__ __forceinline__ Mixt<R> qp_to_qc_mixt(const Phys<R>& P, const R* qp, 
   R inv_rhom = R(1) / rho_m;
   R xc = alphac * rho_c * inv_rhom;
   R cp_c;
-  if (P.gas) cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
-  else cp_c = P.sp_heat_l;
+  if (P.gas) {
+    if constexpr (sizeof(R) == 4) cp_c = P.sp_heat_a;   // (x_c c_a) / x_c
+    else cp_c = (xc > P.thr_eps) ? ((xc - R(0)) * P.sp_heat_a + R(0)) / xc : P.sp_heat_a;
+  } else {
+    cp_c = P.sp_heat_l;
+  }
   R dcp = R(0);
   for (int i = 0; i < ns; ++i) dcp += (arhos[i] * inv_rhom) * P.sp_heat_s[i];
   R cmix = dcp + xc * cp_c;
@@ -346,7 +370,8 @@ __device__ __forceinline__ Mixt<R> qp_to_qc_mixt(const Phys<R>& P, const R* qp, 
   for (int i = 0; i < ns; ++i) qc[4 + i] = (arhos[i] * inv_rhom) * qc[0];
   m.rho_m = rho_m;
   m.rho_c = rho_c;
-  m.red_grav = (rho_m - P.rho_a_amb) / rho_m * P.grav;
+  if constexpr (sizeof(R) == 4) m.red_grav = (rho_m - P.rho_a_amb) * inv_rhom * P.grav;
+  else m.red_grav = (rho_m - P.rho_a_amb) / rho_m * P.grav;
   return m;
 }
 
@@ -388,7 +413,8 @@ __device__ __forceinline__ void eval_fluxes(const Phys<R>& P, const R* qcj, cons
     if (ns > 0 && flux[0] > R(0)) {
       R s = R(0);
       for (int i = 0; i < ns; ++i) s += flux[4 + i];
-      if (s / flux[0] > R(1))
+      // flux[0] > 0 here: the FP32 form compares without the division
+      if (sizeof(R) == 4 ? s > flux[0] : s / flux[0] > R(1))
         for (int i = 0; i < ns; ++i) flux[4 + i] = flux[4 + i] / s * flux[0];
     }
   } else {
