@@ -388,6 +388,12 @@ __device__ __forceinline__ float minmod_f(float a, float b) {
   if (m <= 0.0f) return 0.0f;
   return 0.5f * (copysignf(1.0f, a) + copysignf(1.0f, b)) * m;
 }
+// minmod of two differences by their sign bits: min(|a|, |b|) with a's
+// sign when the signs agree, else 0 (a zero gives a zero of either sign)
+__device__ __forceinline__ float minmod_sign_f(float a, float b) {
+  const float m = fminf(fabsf(a), fabsf(b));
+  return ((__float_as_uint(a) ^ __float_as_uint(b)) & 0x80000000u) ? 0.0f : copysignf(m, a);
+}
 __device__ __forceinline__ float maxmod_f(float a, float b) {
   if (fabsf(a * b) <= 0.0f) return 0.0f;
   return 0.5f * (copysignf(1.0f, a) + copysignf(1.0f, b)) * fmaxf(fabsf(a), fabsf(b));
@@ -569,6 +575,18 @@ __device__ __forceinline__ void recon_side(const KArgs<R>& a, const R* sqp, cons
   auto comp = [&](int m) -> R { return (DIR == 1) ? xcomp(g, m) : ycomp(g, m); };
   const R inv_d = (DIR == 1) ? g.one_by_dx : g.one_by_dy;
   const R d2 = (DIR == 1) ? g.dx2 : g.dy2;
+  if constexpr (sizeof(R) == 4 && LIM == 1) {
+    // FP32 form, minmod on every variable, uniform spacing: the limited
+    // slope times rc dx/2 is (rc dx/2)(1/dx) minmod of the two differences
+    const R kd = g.rc * d2 * inv_d;
+#pragma unroll
+    for (int i = 0; i < np; ++i) {
+      const R v1 = QP(i, 0);
+      const R dq = kd * minmod_sign_f(QP(i, 1) - v1, v1 - QP(i, -1));
+      out[i] = plus ? v1 + dq : v1 - dq;
+    }
+    return;
+  }
   const Spacing<R> sp = spacing<R>(comp(c - 1), comp(c), comp(c + 1), true, inv_d);
 #pragma unroll
   for (int i = 0; i < np; ++i) {
@@ -644,13 +662,15 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
     for (int i = 0; i < nv; ++i) H[i] = R(0);
   } else {
     const R den = a2 - a1;
-    const R fac = (a2 * a1) / den;
+    if constexpr (sizeof(R) == 8) {
+      const R fac = (a2 * a1) / den;
 #pragma unroll
-    for (int i = 0; i < nv; ++i) {
-      R avg;
-      if constexpr (sizeof(R) == 8) avg = (a2 * L.f[i] - a1 * Rt.f[i]) / den;
-      else avg = (a2 * L.f[i] - a1 * Rt.f[i]) * (1.0f / den);
-      H[i] = avg + fac * (Rt.q[i] - L.q[i]);
+      for (int i = 0; i < nv; ++i) H[i] = (a2 * L.f[i] - a1 * Rt.f[i]) / den + fac * (Rt.q[i] - L.q[i]);
+    } else {
+      const R inv_den = 1.0f / den;
+      const R fac = (a2 * a1) * inv_den;
+#pragma unroll
+      for (int i = 0; i < nv; ++i) H[i] = (a2 * L.f[i] - a1 * Rt.f[i]) * inv_den + fac * (Rt.q[i] - L.q[i]);
     }
   }
   if (ns > 0) {
