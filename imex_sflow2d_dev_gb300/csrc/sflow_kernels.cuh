@@ -667,7 +667,7 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = (a2 * L.f[i] - a1 * Rt.f[i]) / den + fac * (Rt.q[i] - L.q[i]);
     } else {
-      const R inv_den = 1.0f / den;
+      const R inv_den = fdiv(R(1), den);
       const R fac = (a2 * a1) * inv_den;
 #pragma unroll
       for (int i = 0; i < nv; ++i) H[i] = (a2 * L.f[i] - a1 * Rt.f[i]) * inv_den + fac * (Rt.q[i] - L.q[i]);
@@ -678,7 +678,7 @@ __device__ __forceinline__ R kt_flux(const Side<R, NS>& L, const Side<R, NS>& Rt
       R s = R(0), s2 = R(0);
       if constexpr (sizeof(R) == 4) {
         // one reciprocal of the mass flux for the FP32 form
-        const R inv0 = R(1) / H[0];
+        const R inv0 = fdiv(R(1), H[0]);
 #pragma unroll
         for (int i = 0; i < ns; ++i) { s += H[4 + i] * inv0; s2 += H[4 + i]; }
         s2 = s2 * inv0;
@@ -995,8 +995,8 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
           double dty = (ay > 0.0) ? g.cfl * g.dy / ay : 1.0e300;
           dtloc = rmin(dtx, dty);
         } else {
-          float dtx = (ax > 0.0f) ? g.cfl_dx / ax : 3.0e38f;
-          float dty = (ay > 0.0f) ? g.cfl_dy / ay : 3.0e38f;
+          float dtx = (ax > 0.0f) ? fdiv(g.cfl_dx, ax) : 3.0e38f;
+          float dty = (ay > 0.0f) ? fdiv(g.cfl_dy, ay) : 3.0e38f;
           dtloc = fminf(dtx, dty);
         }
       }

@@ -29,6 +29,15 @@ template <class R>
 __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
 template <class R>
 __device__ __forceinline__ R sq(R a) { return a * a; }
+// Division of the FP32 form's per-face and per-cell closures: approximate
+// (2 ulp for divisors of magnitude 2^-126 .. 2^126, far outside the
+// densities, depths, temperatures and speeds divided by here); the FP64
+// form divides exactly.
+template <class R>
+__device__ __forceinline__ R fdiv(R a, R b) {
+  if constexpr (sizeof(R) == 4) return __fdividef(a, b);
+  else return a / b;
+}
 
 // ---------------------------------------------------------------------------
 // float <-> double conversions on the integer pipe.  GB300 executes FP64
@@ -115,7 +124,7 @@ __device__ __forceinline__ R qc_to_qp(const Phys<R>& P, const R* q, R* qp) {
   R xs[kMaxSolid];
   R inv_qj1;
   if (q[0] > P.thr_eps) {
-    inv_qj1 = R(1) / q[0];
+    inv_qj1 = fdiv(R(1), q[0]);
     R sq_ = R(0);
     for (int i = 0; i < ns; ++i) { xs[i] = q[4 + i] * inv_qj1; sq_ += q[4 + i]; }
     if (sq_ == q[0]) {
@@ -137,8 +146,8 @@ __device__ __forceinline__ R qc_to_qp(const Phys<R>& P, const R* q, R* qp) {
   R cmix = dcp + cbyxc;
   R T;
   if (q[0] > P.thr_eps_sing) {
-    if (P.energy) T = (q[3] - cst<R>(0.5) * (sq(q[1]) + sq(q[2])) * inv_qj1) / (q[0] * cmix);
-    else T = q[3] / (q[0] * cmix);
+    if (P.energy) T = fdiv(q[3] - cst<R>(0.5) * (sq(q[1]) + sq(q[2])) * inv_qj1, q[0] * cmix);
+    else T = fdiv(q[3], q[0] * cmix);
     if (T <= R(0)) T = P.T_ambient;
   } else {
     T = P.T_ambient;
@@ -157,7 +166,7 @@ __device__ __forceinline__ R qc_to_qp(const Phys<R>& P, const R* q, R* qp) {
   R dinv = R(0);
   for (int i = 0; i < ns; ++i) dinv += xs[i] * P.inv_rho_s[i];
   R inv_rhom = dinv + xc * inv_rho_c;
-  R rho_m = R(1) / inv_rhom;
+  R rho_m = fdiv(R(1), inv_rhom);
   R h = q[0] * inv_rhom;
   R u, v;
   if (q[0] > P.thr_eps_sing) {
@@ -204,13 +213,13 @@ __device__ __forceinline__ void qp_to_qc(const Phys<R>& P, const R* qp, R* qc) {
   R arhos[kMaxSolid];
   R at = R(0);
   for (int i = 0; i < ns; ++i) {
-    R al = P.alpha ? qp[4 + i] : qp[4 + i] / qp[0];
+    R al = P.alpha ? qp[4 + i] : fdiv(qp[4 + i], qp[0]);
     at += al;
     arhos[i] = al * P.rho_s[i];
   }
   R rho_c;
   if (P.gas) {
-    R rho_a = P.pres / (P.sp_gas_const_a * r_T);
+    R rho_a = fdiv(P.pres, P.sp_gas_const_a * r_T);
     // carrier of air alone: ((1 - at) rho_a) / (1 - at) is rho_a
     if constexpr (sizeof(R) == 4) rho_c = rho_a;
     else rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
@@ -221,7 +230,7 @@ __device__ __forceinline__ void qp_to_qc(const Phys<R>& P, const R* qp, R* qc) {
   R sa = R(0);
   for (int i = 0; i < ns; ++i) sa += arhos[i];
   R rho_m = alphac * rho_c + sa;
-  R inv_rhom = R(1) / rho_m;
+  R inv_rhom = fdiv(R(1), rho_m);
   R xc = alphac * rho_c * inv_rhom;
   R cp_c;
   if (P.gas) {
@@ -265,10 +274,10 @@ __device__ __forceinline__ Mixt<R> mixt_var(const Phys<R>& P, const R* qpj, bool
   R r_u = qpj[nv], r_v = qpj[nv + 1], r_T = qpj[3];
   R al[kMaxSolid];
   R at = R(0);
-  for (int i = 0; i < ns; ++i) { al[i] = P.alpha ? qpj[4 + i] : qpj[4 + i] / qpj[0]; at += al[i]; }
+  for (int i = 0; i < ns; ++i) { al[i] = P.alpha ? qpj[4 + i] : fdiv(qpj[4 + i], qpj[0]); at += al[i]; }
   R rho_c;
   if (P.gas) {
-    R rho_a = P.pres / (P.sp_gas_const_a * r_T);
+    R rho_a = fdiv(P.pres, P.sp_gas_const_a * r_T);
     // carrier of air alone: ((1 - at) rho_a) / (1 - at) is rho_a
     if constexpr (sizeof(R) == 4) rho_c = rho_a;
     else rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
@@ -278,12 +287,12 @@ __device__ __forceinline__ Mixt<R> mixt_var(const Phys<R>& P, const R* qpj, bool
   R d = R(0);
   for (int i = 0; i < ns; ++i) d += al[i] * P.rho_s[i];
   R rho_m = (R(1) - at) * rho_c + d;
-  R inv_rhom = R(1) / rho_m;
+  R inv_rhom = fdiv(R(1), rho_m);
   R red_grav;
   if constexpr (sizeof(R) == 4) red_grav = (rho_m - P.rho_a_amb) * inv_rhom * P.grav;
   else red_grav = (rho_m - P.rho_a_amb) / rho_m * P.grav;
   R u2 = sq(r_u) + sq(r_v);
-  m.Ri = (u2 > R(0)) ? rmin(cst<R>(1.0e15), red_grav * r_h / u2) : R(0);
+  m.Ri = (u2 > R(0)) ? rmin(cst<R>(1.0e15), fdiv(red_grav * r_h, u2)) : R(0);
   m.rho_m = rho_m;
   m.rho_c = rho_c;
   m.red_grav = red_grav;
@@ -330,13 +339,13 @@ __device__ __forceinline__ Mixt<R> qp_to_qc_mixt(const Phys<R>& P, const R* qp, 
   R arhos[kMaxSolid];
   R at = R(0);
   for (int i = 0; i < ns; ++i) {
-    R al = P.alpha ? qp[4 + i] : qp[4 + i] / qp[0];
+    R al = P.alpha ? qp[4 + i] : fdiv(qp[4 + i], qp[0]);
     at += al;
     arhos[i] = al * P.rho_s[i];
   }
   R rho_c;
   if (P.gas) {
-    R rho_a = P.pres / (P.sp_gas_const_a * r_T);
+    R rho_a = fdiv(P.pres, P.sp_gas_const_a * r_T);
     // carrier of air alone: ((1 - at) rho_a) / (1 - at) is rho_a
     if constexpr (sizeof(R) == 4) rho_c = rho_a;
     else rho_c = ((R(1) - R(0) - at - R(0)) * rho_a + R(0)) / (R(1) - R(0) - at);
@@ -347,7 +356,7 @@ __device__ __forceinline__ Mixt<R> qp_to_qc_mixt(const Phys<R>& P, const R* qp, 
   R sa = R(0);
   for (int i = 0; i < ns; ++i) sa += arhos[i];
   R rho_m = alphac * rho_c + sa;
-  R inv_rhom = R(1) / rho_m;
+  R inv_rhom = fdiv(R(1), rho_m);
   R xc = alphac * rho_c * inv_rhom;
   R cp_c;
   if (P.gas) {
