@@ -462,7 +462,9 @@ def run_gb300(args, d):
     # tile height of the FP32 form: autotuned on the workload before the
     # timed region (the plain FP64 form has one compiled height)
     tune = None
-    if args.tune_steps > 0:
+    if args.tile_h:
+        tune = {"tile_h": args.tile_h, "tuner": "fixed by --tile-h"}
+    elif args.tune_steps > 0:
         st = lib.Solver(p32, B)
         tune = autotune_run(st, W.to_aos(q), args.warmup, args.tune_steps)
         st.close()
@@ -646,6 +648,9 @@ def main():
     ap.add_argument("--large-steps", type=int, default=10)
     ap.add_argument("--tune-steps", type=int, default=64,
                     help="steps per tile height of the autotuner (0: default 32x8 tiles)")
+    ap.add_argument("--tile-h", type=int, default=0, choices=[0, 8, 16],
+                    help="FP32 tile height of the main leg without the autotuner (0: autotune); "
+                         "a profiler run uses it to keep the height of the plain run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
