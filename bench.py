@@ -614,7 +614,7 @@ def run_gb300(args, d):
                          "traffic": traffic, "alg_bytes_per_active_cell": alg[dom],
                          "kernel_ms_per_step": {k: v / max(pk_steps, 1) for k, v in kms.items()},
                          "limiter": ("SM instruction issue, not HBM: ncu on the 2048^2 case shows "
-                                     "k_flux issuing on 74 % of cycles at 7.6 % of DRAM throughput "
+                                     "k_flux issuing on 70 % of cycles at 8.6 % of DRAM throughput "
                                      "(profiles/k_flux_k_stage2_pyroclastic_2048.md)")},
             "cpu_baseline": ({k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
                              if cb else None),
