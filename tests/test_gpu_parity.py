@@ -346,3 +346,40 @@ def test_upwind_scheme_matches_oracle():
     assert max(err) <= FP64_TOL, err
     o, s = run_pair(p, B, q, 50, precision=PREC_FP32)
     assert l1_err(s.download_q(), o.q(), p.n_vars, p.comp_cells_x, p.comp_cells_y) <= FP32_L1_TOL
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32])
+def test_domain_without_mass_stays_empty(precision):
+    """No mass and no inlet: check_solve finds only the border seeds, every
+    face is dry, no wave speed bounds the step (only the driver's clamps
+    set dt), and the state stays exactly zero; step count, time and active
+    cells as the oracle's."""
+    p, B, _ = W.dam_break(nx=70, ny=45, t_end=100.0)
+    q = W.rest_state_q(p, np.zeros((45, 70)), 300.0, [0.0])
+    o, s = run_pair(p, B, q, 10, precision=precision)
+    sg, so = s.stats(), o.stats()
+    assert sg.status == 0 and so.status == 0
+    assert sg.steps == so.steps == 10
+    assert sg.t == pytest.approx(so.t, rel=1e-12)
+    assert sg.solve_cells == so.solve_cells
+    assert not np.any(o.q())
+    assert not np.any(s.download_q())
+
+
+@pytest.mark.parametrize("shape", [(5, 5), (7, 5), (5, 9)])
+def test_smallest_domains_match_oracle(shape):
+    """The smallest two-dimensional domains the kernels take (nx, ny >= 5):
+    every cell is within two cells of an edge, so every face takes the
+    boundary reconstruction; FP64 bit for bit against the oracle (no
+    Newton on the liquid dam break), FP32 within its L1 bar."""
+    nx, ny = shape
+    p, B, _ = W.dam_break(nx=nx, ny=ny, t_end=100.0)
+    x = (np.arange(nx) + 0.5) * p.cell_size
+    h = np.where(x[None, :] < 0.5 * nx * p.cell_size, 1.0, 0.1) * np.ones((ny, 1))
+    q = W.rest_state_q(p, h, 300.0, [0.0])
+    o, s = run_pair(p, B, q, 30)
+    assert s.stats().status == 0 and s.stats().steps == 30
+    np.testing.assert_array_equal(s.download_q(), o.q())
+    o, s = run_pair(p, B, q, 30, precision=PREC_FP32)
+    assert s.stats().status == 0
+    assert l1_err(s.download_q(), o.q(), p.n_vars, nx, ny) <= FP32_L1_TOL
