@@ -124,6 +124,35 @@ def test_batch_runs_equal_their_single_run_result(precision):
     b.close()
 
 
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32])
+def test_batch_with_empty_and_smallest_runs(precision):
+    """Edge runs in one batch: a domain without mass or inlet (stays exactly
+    zero, counts its border cells), the smallest domain (5 x 5: one tile,
+    every cell on the boundary reconstruction) and a normal current; each
+    as the run alone."""
+    p0, B0, _ = W.dam_break(nx=70, ny=45, t_end=100.0)
+    q0 = W.rest_state_q(p0, np.zeros((45, 70)), 300.0, [0.0])
+    p1, B1, _ = W.dam_break(nx=5, ny=5, t_end=100.0)
+    x = (np.arange(5) + 0.5) * p1.cell_size
+    q1 = W.rest_state_q(p1, np.where(x[None, :] < 2.5, 1.0, 0.1) * np.ones((5, 1)), 300.0, [0.0])
+    runs = [(p0, B0, q0), (p1, B1, q1), _pyro(80, 80, 20.0, settling=False)]
+    b = L.Batch(precision, max_runs=4, max_cells=1 << 20)
+    ids = [b.submit(p, B, W.to_aos(q)) for p, B, q in runs]
+    b.advance(25)
+    for (p, B, q), rid in zip(runs, ids):
+        ref, st_ref = _alone(p, B, q, 25, precision)
+        got, refc = b.counters(rid)["cell_updates"], _alone_cells(p, B, q, 25, precision)
+        if precision == PREC_FP64:
+            assert got == refc
+        else:
+            assert abs(got - refc) <= 1e-3 * max(refc, 1)
+        st, _ = b.poll(rid)
+        assert st.status == 0 and st.steps == 25
+        same_run(b.collect(rid), ref, precision, p.n_vars)
+    assert not np.any(_alone(p0, B0, q0, 25, precision)[0])
+    b.close()
+
+
 def test_runs_admitted_in_flight_equal_alone():
     """Continuous batching: B joins after A has run 10 steps, C after 25;
     each result equals the run alone with its own step count."""
