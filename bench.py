@@ -340,6 +340,15 @@ def ensemble_leg(lib, n_runs, steps, tune=True):
             "autotune": tuned}
 
 
+def step_bytes(n_vars, word=4, n_geo=5, deposit_classes=0):
+    """Algorithmic bytes of one cell update of the whole N_RK = 2 step in one
+    pass: read q and write q, read and write the stage increment once
+    (3 n words), the topography terms and g_c (n_geo + 1 words), the three
+    maxima maps read and written (24 B) and, with settling, the FP64
+    deposit of each class read and written (16 B a class)."""
+    return 3 * n_vars * word + (n_geo + 1) * 4 + 24 + 16 * deposit_classes
+
+
 def form_errors(lib, p, B, q, steps):
     """L1 and Linf relative errors of h, hu, hv, alpha_s and T of the FP32
     bulk form against the plain FP64 form after `steps` steps from the same
@@ -574,6 +583,10 @@ def run_gb300(args, d):
     if d.rank == 0 and args.ensemble_runs > 0:
         ens = ensemble_leg(lib, args.ensemble_runs, args.ensemble_steps, tune=args.tune_steps > 0)
         ens["speedup_vs_fp64_plain"] = ens["value"] / value64 if value64 else None
+        sb = step_bytes(6, deposit_classes=2)   # every member: 2 settling classes, FP32 state
+        ens["hbm_roofline"] = {"bytes_per_cell_update": sb, "achieved_GBs": ens["value"] * sb / 1e9,
+                               "peak_GBs": peak, "frac": ens["value"] * sb / 1e9 / peak,
+                               "peak_kind": peak_kind}
         pe, Be, qe, _ = W.ensemble_params(0, PREC_FP32, 300)
         ens["error_vs_fp64"] = {"member": 0, "side": pe.comp_cells_x, "steps": 300,
                                 **form_errors(lib, pe, Be, qe, 300)}
