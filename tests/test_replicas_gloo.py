@@ -46,7 +46,9 @@ def _rank(rank, world, port, out):
 def test_two_replicas_aggregate_over_gloo():
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
+    # a spawned manager process: no fork of a process that may already hold
+    # a CUDA context (when the GPU tests ran first in the same session)
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
