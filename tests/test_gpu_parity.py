@@ -383,3 +383,39 @@ def test_smallest_domains_match_oracle(shape):
     o, s = run_pair(p, B, q, 30, precision=PREC_FP32)
     assert s.stats().status == 0
     assert l1_err(s.download_q(), o.q(), p.n_vars, nx, ny) <= FP32_L1_TOL
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32])
+def test_launches_without_programmatic_dependency_give_the_same_bits(precision, monkeypatch):
+    """SFLOW_PDL=0 (read when a handle or batch is created) launches the
+    step kernels without programmatic dependent launch: the same kernels in
+    the same order, so the same bits, for a handle and for a batch."""
+    p, B, q = _pyro(settling=True, entrainment=True)
+    p.precision = precision
+    qa = W.to_aos(q)
+
+    def handle():
+        s = L.Solver(p, B)
+        s.upload_q(qa)
+        s.advance(max_steps=40)
+        out, st = s.download_q(), s.stats()
+        s.close()
+        return out, st
+
+    def batch():
+        b = L.Batch(precision, max_runs=2, max_cells=1 << 20)
+        rid = b.submit(p, B, qa)
+        b.advance(40)
+        out = b.collect(rid)
+        b.close()
+        return out
+
+    a, sa = handle()
+    ab = batch()
+    monkeypatch.setenv("SFLOW_PDL", "0")
+    n, sn = handle()
+    nb = batch()
+    assert sa.status == 0 and sa.steps == sn.steps == 40
+    assert sa.t == sn.t
+    np.testing.assert_array_equal(a, n)
+    np.testing.assert_array_equal(ab, nb)
