@@ -158,6 +158,14 @@ int sflow_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
   return SFLOW_OK;
 }
 
+int sflow_eval_math(int32_t which, int64_t n, const double* x, const double* y, double* out) {
+  if (which < 0 || which > 5 || n < 0 || (n > 0 && (!x || !out)) || ((which == 0 || which == 3) && n > 0 && !y))
+    return fail(SFLOW_EINVAL, "bad argument");
+  const int rc = sflow::eval_math(which, (long long)n, x, y, out);
+  if (rc != SFLOW_OK) return fail(rc, "device evaluation failed");
+  return SFLOW_OK;
+}
+
 int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count) {
   if (!count) return fail(SFLOW_EINVAL, "count is NULL");
   if (precision != SFLOW_PREC_FP32 && precision != SFLOW_PREC_FP64) return fail(SFLOW_EINVAL, "unknown precision");

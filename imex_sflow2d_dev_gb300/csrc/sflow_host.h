@@ -100,5 +100,7 @@ BatchBase* make_batch_fp64(int max_runs, int64_t max_tiles, std::string& err);
 BatchBase* make_batch_fp32(int max_runs, int64_t max_tiles, std::string& err);
 // self-check of the integer-pipe float <-> double conversions (sflow_fp32.cu)
 int check_conversions(long long n, unsigned long long seed, long long* mismatches);
+// the FP64 pow / log / cos of sflow_math.h (and CUDA's) on the device (sflow_fp64.cu)
+int eval_math(int which, long long n, const double* x, const double* y, double* out);
 
 }  // namespace sflow

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include "sflow_physics.cuh"
+#include "sflow_sum.cuh"
 
 namespace sflow {
 

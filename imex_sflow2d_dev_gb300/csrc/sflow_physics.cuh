@@ -14,6 +14,7 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "sflow_math.h"
 #include "sflow_types.cuh"
 
 namespace sflow {
@@ -29,6 +30,18 @@ template <class R>
 __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
 template <class R>
 __device__ __forceinline__ R sq(R a) { return a * a; }
+// x^y and log x: in the FP64 form the library's own functions (sflow_math.h),
+// which give the oracle's bits; in the FP32 form CUDA's powf and logf.
+template <class R>
+__device__ __forceinline__ R rpow(R x, R y) {
+  if constexpr (sizeof(R) == 8) return sfm_pow(x, y);
+  else return powf(x, y);
+}
+template <class R>
+__device__ __forceinline__ R rlog(R x) {
+  if constexpr (sizeof(R) == 8) return sfm_log(x);
+  else return logf(x);
+}
 // Division of the FP32 form's per-face and per-cell closures: approximate
 // (2 ulp for divisors of magnitude 2^-126 .. 2^126, far outside the
 // densities, depths, temperatures and speeds divided by here); the FP64
@@ -465,11 +478,12 @@ __device__ __forceinline__ void expl_terms(const Phys<R>& P, const Geo<R>& g, co
   }
 }
 
-// time factor of the ring inlet (constitutive_2d.f90:3320-3349), FP64
+// time factor of the ring inlet (constitutive_2d.f90:3320-3349), FP64; the
+// cosine is the library's own (sflow_math.h), the same bits as the oracle's
 __device__ __forceinline__ double source_time_coeff(const double* tp, double pi_g, double time) {
   double t_coeff;
   if (time >= tp[3]) {
-    if (tp[2] > 0.0 && time < tp[3] + tp[2]) t_coeff = 0.5 * (1.0 + cos(pi_g * (time - tp[3]) / tp[2]));
+    if (tp[2] > 0.0 && time < tp[3] + tp[2]) t_coeff = 0.5 * (1.0 + sfm_cos(pi_g * (time - tp[3]) / tp[2]));
     else t_coeff = 0.0;
   } else {
     double t_rem = fmod(time, tp[0]);
@@ -477,9 +491,9 @@ __device__ __forceinline__ double source_time_coeff(const double* tp, double pi_
     if (tp[2] == 0.0) {
       if (t_rem <= tp[1]) t_coeff = 1.0;
     } else {
-      if (t_rem < tp[2]) t_coeff = 0.5 * (1.0 - cos(pi_g * t_rem / tp[2]));
+      if (t_rem < tp[2]) t_coeff = 0.5 * (1.0 - sfm_cos(pi_g * t_rem / tp[2]));
       else if (t_rem <= tp[1] - tp[2]) t_coeff = 1.0;
-      else if (t_rem <= tp[1]) t_coeff = 0.5 * (1.0 + cos(pi_g * ((t_rem - tp[1]) / tp[2] + 1.0)));
+      else if (t_rem <= tp[1]) t_coeff = 0.5 * (1.0 + sfm_cos(pi_g * ((t_rem - tp[1]) / tp[2] + 1.0)));
     }
   }
   return t_coeff;
@@ -510,36 +524,52 @@ __device__ __forceinline__ void semi_impl_terms(const Phys<R>& P, const Geo<R>& 
 // ---------------------------------------------------------------------------
 // Implicit friction (constitutive_2d.f90:3513-4009, rheology 1 and 6) with
 // the gas-density / temperature closure of c_phys_var (1154-1322), written
-// once over a number type N: double for the residual, Dual2 for the two
-// Jacobian columns d/d(hu), d/d(hv).  This replaces the complex-step
-// derivative of solver_2d.f90:2302-2367: forward-mode derivatives are exact
-// for these rational/sqrt expressions, as the complex step is.
+// once over a number type N: double for the residual, Cplx for the
+// complex-step Jacobian of the plain FP64 form (solver_2d.f90:2302-2367,
+// the derivative the reference takes).
 // ---------------------------------------------------------------------------
-struct Dual2 {
-  double v, d0, d1;
-  __device__ Dual2() {}
-  __device__ Dual2(double x) : v(x), d0(0.0), d1(0.0) {}
-  __device__ Dual2(double x, double a, double b) : v(x), d0(a), d1(b) {}
-};
-__device__ __forceinline__ Dual2 operator+(Dual2 a, Dual2 b) { return Dual2(a.v + b.v, a.d0 + b.d0, a.d1 + b.d1); }
-__device__ __forceinline__ Dual2 operator-(Dual2 a, Dual2 b) { return Dual2(a.v - b.v, a.d0 - b.d0, a.d1 - b.d1); }
-__device__ __forceinline__ Dual2 operator-(Dual2 a) { return Dual2(-a.v, -a.d0, -a.d1); }
-__device__ __forceinline__ Dual2 operator*(Dual2 a, Dual2 b) {
-  return Dual2(a.v * b.v, a.d0 * b.v + a.v * b.d0, a.d1 * b.v + a.v * b.d1);
-}
-__device__ __forceinline__ Dual2 operator/(Dual2 a, Dual2 b) {
-  double r = a.v / b.v;
-  double ib = 1.0 / b.v;
-  return Dual2(r, (a.d0 - r * b.d0) * ib, (a.d1 - r * b.d1) * ib);
-}
-__device__ __forceinline__ Dual2 dsqrt(Dual2 a) {
-  double s = sqrt(a.v);
-  double h = (s > 0.0) ? 0.5 / s : 0.0;
-  return Dual2(s, a.d0 * h, a.d1 * h);
-}
 __device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ double val(double a) { return a; }
-__device__ __forceinline__ double val(Dual2 a) { return a.v; }
+
+// Complex numbers of the complex-step Jacobian with the arithmetic written
+// out: textbook product, Smith's quotient (R. L. Smith, CACM 5(8), 1962),
+// principal square root sqrt((|z| + |x|)/2).  The oracle spells the same
+// formulas in C; compiled without contraction (--fmad=false), the two give
+// the same Jacobian bits, and so the same Newton iterates.  A real operand
+// is a complex number with zero imaginary part, for which each operation
+// returns the real result exactly.
+struct Cplx {
+  double re, im;
+  __device__ Cplx() {}
+  __device__ Cplx(double r) : re(r), im(0.0) {}
+  __device__ Cplx(double r, double i) : re(r), im(i) {}
+};
+__device__ __forceinline__ Cplx operator+(Cplx a, Cplx b) { return Cplx(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ Cplx operator-(Cplx a, Cplx b) { return Cplx(a.re - b.re, a.im - b.im); }
+__device__ __forceinline__ Cplx operator*(Cplx a, Cplx b) {
+  return Cplx(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+__device__ __forceinline__ Cplx operator/(Cplx a, Cplx b) {
+  if (fabs(b.re) >= fabs(b.im)) {
+    const double r = b.im / b.re, den = b.re + b.im * r;
+    return Cplx((a.re + a.im * r) / den, (a.im - a.re * r) / den);
+  }
+  const double r = b.re / b.im, den = b.re * r + b.im;
+  return Cplx((a.re * r + a.im) / den, (a.im * r - a.re) / den);
+}
+__device__ __forceinline__ Cplx dsqrt(Cplx z) {
+  const double ar = fabs(z.re), ai = fabs(z.im);
+  if (ar == 0.0 && ai == 0.0) return Cplx(0.0, z.im);
+  double m;
+  if (ai == 0.0) m = ar;
+  else if (ar == 0.0) m = ai;
+  else if (ar >= ai) { const double t = ai / ar; m = ar * sqrt(1.0 + t * t); }
+  else { const double t = ar / ai; m = ai * sqrt(1.0 + t * t); }
+  const double t = sqrt((ar + m) * 0.5);
+  if (z.re >= 0.0) return Cplx(t, z.im / (2.0 * t));
+  return Cplx(ai / (2.0 * t), copysign(t, z.im));
+}
+__device__ __forceinline__ double val(Cplx a) { return a.re; }
 
 template <class N, int NS>
 __device__ __forceinline__ void implicit_terms(const Phys<double>& P, double Bx, double By,
@@ -639,24 +669,30 @@ __device__ __forceinline__ void newton_eval_f(const NewtonCtx& c, const double* 
   scal_f = 0.5 * s;
 }
 
-// Jacobian of f with respect to qj_rel for the implicit columns 1, 2:
-// J(k,i) = d f_k / d qrel_i = qj_org_i * (delta_ki - dt a_diag dNH_k/dq_i)
+// Jacobian of f with respect to qj_rel for the implicit columns 1, 2
+// (solver_2d.f90:2302-2367): J(k,i) = qj_org_i delta_ki - dt a_diag
+// Im(NH_k(qj_rel qj_org + i h e_i qj_org)) / h with h = n_vars EPSILON, the
+// complex step of the reference, evaluated at qj_rel * qj_org.
 template <int NS>
-__device__ __forceinline__ void newton_jacobian(const NewtonCtx& c, const double* qj,
+__device__ __forceinline__ void newton_jacobian(const NewtonCtx& c, const double* qj_rel,
                                                 const double* qj_org, double& s11, double& s12,
                                                 double& s21, double& s22) {
   constexpr int nv = 4 + NS;
-  Dual2 qd[kMaxVars];
-  for (int i = 0; i < nv; ++i) qd[i] = Dual2(qj[i]);
-  qd[1].d0 = 1.0;
-  qd[2].d1 = 1.0;
-  Dual2 n1, n2;
-  implicit_terms<Dual2, NS>(*c.P, c.Bx, c.By, qd, n1, n2);
-  const double k = c.dt * c.a_diag;
-  s11 = qj_org[1] - k * (n1.d0 * qj_org[1]);
-  s12 = -k * (n1.d1 * qj_org[2]);
-  s21 = -k * (n2.d0 * qj_org[1]);
-  s22 = qj_org[2] - k * (n2.d1 * qj_org[2]);
+  const double h = nv * kEps, one_by_h = 1.0 / h;
+  double jc[2][2];
+  for (int col = 1; col <= 2; ++col) {
+    Cplx qc[kMaxVars];
+    for (int k = 0; k < nv; ++k) qc[k] = Cplx(qj_rel[k] * qj_org[k]);
+    qc[col] = Cplx(qj_rel[col], h) * Cplx(qj_org[col]);
+    Cplx n1, n2;
+    implicit_terms<Cplx, NS>(*c.P, c.Bx, c.By, qc, n1, n2);
+    jc[0][col - 1] = 1.0 * n1.im * one_by_h;
+    jc[1][col - 1] = 1.0 * n2.im * one_by_h;
+  }
+  s11 = 1.0 * qj_org[1] - c.dt * c.a_diag * jc[0][0];
+  s12 = 0.0 - c.dt * c.a_diag * jc[0][1];
+  s21 = 0.0 - c.dt * c.a_diag * jc[1][0];
+  s22 = 1.0 * qj_org[2] - c.dt * c.a_diag * jc[1][1];
 }
 
 // returns iterations used (kMaxNewton+1 when the limit was reached)
@@ -680,7 +716,7 @@ __device__ int solve_rk_step(const NewtonCtx& c, double* qj) {
     if (mf < TOLF) return it;
     if (!isfinite(scal_f)) return kMaxNewton + 1;   // NaN/Inf state: give up at once
     double s11, s12, s21, s22;
-    newton_jacobian<NS>(c, qj, qj_org, s11, s12, s21, s22);
+    newton_jacobian<NS>(c, qj_rel, qj_org, s11, s12, s21, s22);
     // explicit rows: diagonal qj_org (mask11); coupling mask21 is zero
     for (int i = 0; i < nv; ++i) p[i] = (i == 1 || i == 2) ? 0.0 : -(f[i] / qj_org[i]) + 0.0;
     double d2a = f[1], d2b = f[2];
@@ -796,10 +832,10 @@ __device__ __forceinline__ R settling_velocity(const Phys<R>& P, R diam, R rhos,
     for (int i = 1; i <= 20; ++i) {
       R sv_old = sv;
       if (P.collective)
-        inv_sqrt_C_D = sqrt(R(1) / (cst<R>(24.0) * (R(1) + cst<R>(0.15) * pow(Rey, cst<R>(0.687))) / Rey +
-                                    P.A_drag * (log(Rey) - P.B_drag)));
+        inv_sqrt_C_D = sqrt(R(1) / (cst<R>(24.0) * (R(1) + cst<R>(0.15) * rpow<R>(Rey, cst<R>(0.687))) / Rey +
+                                    P.A_drag * (rlog<R>(Rey) - P.B_drag)));
       else
-        inv_sqrt_C_D = sqrt(Rey / (cst<R>(24.0) * (R(1) + cst<R>(0.15) * pow(Rey, cst<R>(0.687)))));
+        inv_sqrt_C_D = sqrt(Rey / (cst<R>(24.0) * (R(1) + cst<R>(0.15) * rpow<R>(Rey, cst<R>(0.687)))));
       sv = const_part * inv_sqrt_C_D;
       if (fabs(sv_old - sv) / sv_old < cst<R>(1.0e-6)) return sv;
       Rey = diam * sv * inv_kin_visc;
@@ -833,7 +869,7 @@ __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R 
     if (al[i] > R(0) && P.settling) {
       R sv = settling_velocity<R>(P, P.diam_s[i], P.rho_s[i], m.rho_c, inv_kin_visc);
       dep[i] = al[i] * sv * R(1);
-      dep[i] = dep[i] * pow(R(1) - rmin(R(1), at / alpha_max), hind_exp);
+      dep[i] = dep[i] * rpow<R>(R(1) - rmin(R(1), at / alpha_max), hind_exp);
       dep[i] = rmin(dep[i], r_h * al[i] / dt);
     }
   }
@@ -846,7 +882,7 @@ __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R 
   cpl = rmin(cpl, (r_h * (R(1) - sal) - P.coeff_porosity * (r_h * sal - dt * sdep)) / dt);
   R air_entr = R(0);
   if (P.entrain && r_h > R(0) && m.Ri > R(0)) {
-    R entr_coeff = cst<R>(0.075) / sqrt(R(1) + cst<R>(718.0) * pow(m.Ri, cst<R>(2.4)));
+    R entr_coeff = cst<R>(0.075) / sqrt(R(1) + cst<R>(718.0) * rpow<R>(m.Ri, cst<R>(2.4)));
     air_entr = entr_coeff * sqrt(mod_vel2);
   }
   R rho_dep_tot = R(0), rho_ers_tot = R(0), s_dep = R(0), s_ers = R(0);

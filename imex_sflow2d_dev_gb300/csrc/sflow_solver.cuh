@@ -87,24 +87,12 @@ __global__ void k_map_to_host(const R* __restrict__ m, double* __restrict__ out,
 
 static __global__ void k_stats_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
   // block m reduces value m: Neumaier-compensated strided sums per thread,
-  // then a fixed-order tree (deterministic)
+  // then a fixed-order compensated tree (deterministic)
   const int m = blockIdx.x;
-  double s = 0.0, cmp = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-    double x = part[b * 4 + m];
-    double t = s + x;
-    if (fabs(s) >= fabs(x)) cmp += (s - t) + x;
-    else cmp += (x - t) + s;
-    s = t;
-  }
-  __shared__ double sh[256];
-  sh[threadIdx.x] = s + cmp;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[m] = sh[0];
+  double s[1] = {0.0}, cmp[1] = {0.0};
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) csum_add(s[0], cmp[0], part[b * 4 + m]);
+  __shared__ double sh_s[256], sh_c[256];
+  csum_block<1, 256>(s, cmp, sh_s, sh_c, out + m);
 }
 
 // ---------------------------------------------------------------------------

@@ -88,7 +88,7 @@ template <class R, int NS>
 __global__ void k_stats_partial(KArgs<R> a, double* __restrict__ part) {
   constexpr int nv = 4 + NS, np = nv + 2;
   const Grid<R>& g = a.g;
-  double v[4] = {0, 0, 0, 0};
+  double v[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0};
   const int64_t N = (int64_t)g.nx * g.ny;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
        c += (int64_t)gridDim.x * blockDim.x) {
@@ -96,25 +96,17 @@ __global__ void k_stats_partial(KArgs<R> a, double* __restrict__ part) {
     int64_t d = cidx(g, j, k);
     R q[nv];
     for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + d];
-    v[0] += (double)q[0];
+    csum_add(v[0], cv[0], (double)q[0]);
     if (q[0] > R(0)) {
       R qp[np];
       qc_to_qp<R, NS>(a.pr, q, qp);
-      v[1] += (double)qp[0];
+      csum_add(v[1], cv[1], (double)qp[0]);
     }
     if ((double)q[0] > 1.0e-7) v[2] += 1.0;
-    for (int i = 0; i < NS; ++i) v[3] += (double)q[4 + i];
+    for (int i = 0; i < NS; ++i) csum_add(v[3], cv[3], (double)q[4 + i]);
   }
-  __shared__ double sh[4][256];
-  for (int m = 0; m < 4; ++m) sh[m][threadIdx.x] = v[m];
-  __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s)
-      for (int m = 0; m < 4; ++m) sh[m][threadIdx.x] += sh[m][threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0)
-    for (int m = 0; m < 4; ++m) part[blockIdx.x * 4 + m] = sh[m][0];
+  __shared__ double sh_s[4 * 256], sh_c[4 * 256];
+  csum_block<4, 256>(v, cv, sh_s, sh_c, part + blockIdx.x * 4);
 }
 
 

@@ -95,6 +95,7 @@ def load(build_if_missing=True):
         "sflow_batch_launch_count": (i64, [vp]),
         "sflow_tile_shapes": (C.c_int, [i32, C.POINTER(i32), i32, C.POINTER(i32)]),
         "sflow_check_conversions": (C.c_int, [i64, C.c_uint64, C.POINTER(i64)]),
+        "sflow_eval_math": (C.c_int, [i32, i64, dp, dp, dp]),
         "sflow_set_tile_shape": (C.c_int, [vp, i32]),
         "sflow_get_tile_shape": (C.c_int, [vp, C.POINTER(i32)]),
         "sflow_autotune": (C.c_int, [vp, i64, C.POINTER(i32), dp, i32]),
@@ -126,7 +127,8 @@ def exported_symbols():
             "sflow_download_phys", "sflow_download_deposit", "sflow_upload_deposit",
             "sflow_upload_maps", "sflow_set_output_time", "sflow_tile_shapes",
             "sflow_set_tile_shape", "sflow_get_tile_shape", "sflow_autotune",
-            "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape", "sflow_check_conversions"]
+            "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape", "sflow_check_conversions",
+            "sflow_eval_math"]
 
 
 TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
@@ -139,6 +141,23 @@ def check_conversions(n=1 << 22, seed=12345):
     m = C.c_int64(-1)
     _check(lib.sflow_check_conversions(int(n), int(seed), C.byref(m)))
     return m.value
+
+
+MATH_FUNCS = {"pow": 0, "log": 1, "cos": 2, "cuda_pow": 3, "cuda_log": 4, "cuda_cos": 5}
+
+
+def eval_math(name, x, y=None):
+    """The library's FP64 pow / log / cos (or CUDA's, 'cuda_*') evaluated on
+    the device over the arrays x (and y for pow)."""
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+    out = np.empty_like(x)
+    yp = None
+    if y is not None:
+        y = np.ascontiguousarray(np.broadcast_to(np.asarray(y, dtype=np.float64), x.shape))
+        yp = _dp(y)
+    _check(lib.sflow_eval_math(MATH_FUNCS[name], x.size, _dp(x), yp, _dp(out)))
+    return out
 
 
 def tile_shapes(precision):

@@ -5,8 +5,8 @@
  * (src/IMEX_SfloW2D.f90) calls argument-less module procedures that act on
  * module globals.  Each entry point below replaces one of those call sites;
  * the citation next to it names the reference routine it stands in for.
- * A Fortran host binds them with ISO_C_BINDING, a C,
- * C++ or Python host binds them directly.
+ * A Fortran host binds them with ISO_C_BINDING interfaces, a C, C++ or
+ * Python host binds them directly.
  *
  * Conventions
  *  - All entry points return 0 on success, a negative SFLOW_E* code on a
@@ -260,6 +260,13 @@ int64_t sflow_device_bytes(const sflow_handle* h);
  * hardware conversions on n seeded bit patterns; *mismatches must be 0. */
 int sflow_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 
+/* The FP64 pow (which 0), log (1) and cos (2) that the FP64 kernels use for
+ * the settling, entrainment and inlet-ramp closures -- functions of this
+ * library that give the same bits on the device as on the host -- and
+ * CUDA's pow, log, cos (3, 4, 5), evaluated on the device for n host
+ * arguments (y only for pow).  For tests of those functions. */
+int sflow_eval_math(int32_t which, int64_t n, const double* x, const double* y, double* out);
+
 #define SFLOW_TILE_CANDIDATES 2
 int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count);
 int sflow_set_tile_shape(sflow_handle* h, int32_t tile_h);
@@ -290,22 +297,26 @@ int sflow_host_scalars(const SflowParams* p, const double* B_cent, double* out4)
  * SflowStepStats, IMEX_SfloW2D.f90:535-542) of a state that the caller
  * already holds in device memory, computed without allocating anything.
  * No counterpart in the reference: it exists for callers that cannot call
- * cudaMalloc when they need the sums (inside a CUDA graph capture, in a
- * stream callback or host node, or under a host framework that owns all
- * device memory).
- *   p        parameters of the domain (only grid size, n_solid and the
- *            carrier/energy constants are read)
+ * cudaMalloc where they need the sums, such as a host framework that owns
+ * all device memory through its own pool and forbids raw allocations by
+ * the libraries it loads.  Call it from ordinary host code.
+ *   p        parameters of the domain (grid size, n_solid and the carrier /
+ *            energy constants are read; rejected like sflow_create rejects
+ *            them, SFLOW_EINVAL)
  *   q_dev    device pointer, q(1:n_vars,1:nx,1:ny) doubles, reference layout
  *   sums_dev device pointer to 4 doubles, written asynchronously
  *   stream   cudaStream_t to launch on (NULL = default stream)
  * Scratch: one fixed 128 KiB device array inside the library, held by every
  * GPU that loads the library until the process exits.  Domains above
  * 67,108,864 cells (8192 x 8192) are rejected with SFLOW_ERANGE.  The first
- * call on a device looks up the array's address; make that first call
- * before any stream capture.  All calls share the array: calls whose kernels
- * may overlap on the GPU (different streams without ordering) race and can
- * return wrong sums; calls on one stream are safe.  Errors:
- * sflow_log_sums_noalloc_error().
+ * call on a device looks up the array's address with that device current;
+ * make that first call before any stream capture.  All calls share the
+ * array: calls whose kernels may overlap on the GPU (different streams
+ * without ordering) race and can return wrong sums; calls on one stream are
+ * safe.  The sums are compensated (Neumaier) within each thread, block and
+ * across blocks.  Argument errors: sflow_log_sums_noalloc_error() (cleared
+ * at every call); an error of the kernels themselves shows up at the
+ * caller's next synchronisation of the stream.
  */
 int sflow_log_sums_noalloc(const SflowParams* p, const double* q_dev, double* sums_dev, void* stream);
 const char* sflow_log_sums_noalloc_error(void);

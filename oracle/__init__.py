@@ -58,6 +58,7 @@ def _load():
     lib.oracle_minmod.argtypes = [C.c_double, C.c_double]
     lib.oracle_limit.restype = C.c_double
     lib.oracle_limit.argtypes = [dp, dp, ip, C.c_double]
+    lib.sflow_oracle_eval_math.argtypes = [ip, C.c_int64, dp, dp, dp]
     _lib = lib
     return lib
 
@@ -74,6 +75,16 @@ def limit(v, z, limiter, theta=1.0):
     v = np.ascontiguousarray(v, dtype=np.float64)
     z = np.ascontiguousarray(z, dtype=np.float64)
     return _load().oracle_limit(_dp(v), _dp(z), limiter, theta)
+
+
+def eval_math(name, x, y=None):
+    """The shared FP64 pow / log / cos (sflow_math.h) as the host computes
+    them, over the arrays x (and y for pow)."""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+    out = np.empty_like(x)
+    yy = np.ascontiguousarray(np.broadcast_to(np.asarray(0.0 if y is None else y, dtype=np.float64), x.shape))
+    _load().sflow_oracle_eval_math({"pow": 0, "log": 1, "cos": 2}[name], x.size, _dp(x), _dp(yy), _dp(out))
+    return out
 
 
 def set_threads(n):

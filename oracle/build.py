@@ -14,10 +14,10 @@ LIB = os.path.join(HERE, "libsflow_oracle.so")
 
 
 def build_oracle(force=False, verbose=False):
+    deps = [SRC, os.path.join(HERE, "..", "include", "sflow.h"),
+            os.path.join(HERE, "..", "imex_sflow2d_dev_gb300", "csrc", "sflow_math.h")]
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)
-            and os.path.getmtime(LIB) >= os.path.getmtime(
-                os.path.join(HERE, "..", "include", "sflow.h"))):
+            and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps)):
         return LIB
     cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp",
            "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",

@@ -39,7 +39,6 @@
  *  terms, no bottom radial source, no erosion (EROSION_COEFF = 0),
  *  rheology models 1 (Voellmy-Salm) and 6, SOLVER_SCHEME KT or UP.
  */
-#include <complex.h>
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
@@ -47,6 +46,9 @@
 #include <string.h>
 
 #include "../include/sflow.h"
+/* pow, log and cos of the FP64 closures: the same functions, and so the
+ * same bits, as the GPU kernels (double-double evaluation, see the header) */
+#include "../imex_sflow2d_dev_gb300/csrc/sflow_math.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -56,7 +58,47 @@
 #define MAXV (SFLOW_MAX_VARS + 2)
 #define MAXS SFLOW_MAX_SOLID
 
-typedef double complex cplx;
+/* Complex numbers of the complex-step Jacobian, with the arithmetic written
+ * out (the GPU's plain FP64 form uses the same formulas, so both compute
+ * the same Jacobian bits): products by the textbook formula, quotients by
+ * Smith's algorithm (R. L. Smith, CACM 5(8), 1962), the square root by the
+ * principal-branch formula sqrt((|z| + |x|)/2).  A real operand is a complex
+ * number with zero imaginary part; for such operands every operation gives
+ * the real result exactly, so the real calls of the closure (eval_f) equal
+ * real arithmetic. */
+typedef struct {
+  double re, im;
+} cplx;
+static cplx cx(double re, double im) {
+  cplx z;
+  z.re = re;
+  z.im = im;
+  return z;
+}
+static cplx cr(double re) { return cx(re, 0.0); }
+static cplx c_add(cplx a, cplx b) { return cx(a.re + b.re, a.im + b.im); }
+static cplx c_sub(cplx a, cplx b) { return cx(a.re - b.re, a.im - b.im); }
+static cplx c_mul(cplx a, cplx b) { return cx(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+static cplx c_div(cplx a, cplx b) {
+  if (fabs(b.re) >= fabs(b.im)) {
+    const double r = b.im / b.re, den = b.re + b.im * r;
+    return cx((a.re + a.im * r) / den, (a.im - a.re * r) / den);
+  }
+  const double r = b.re / b.im, den = b.re * r + b.im;
+  return cx((a.re * r + a.im) / den, (a.im * r - a.re) / den);
+}
+static cplx c_sqrt(cplx z) {
+  const double ar = fabs(z.re), ai = fabs(z.im);
+  if (ar == 0.0 && ai == 0.0) return cx(0.0, z.im);
+  double m;
+  if (ai == 0.0) m = ar;
+  else if (ar == 0.0) m = ai;
+  else if (ar >= ai) { const double t = ai / ar; m = ar * sqrt(1.0 + t * t); }
+  else { const double t = ar / ai; m = ai * sqrt(1.0 + t * t); }
+  const double t = sqrt((ar + m) * 0.5);
+  if (z.re >= 0.0) return cx(t, z.im / (2.0 * t));
+  return cx(ai / (2.0 * t), copysign(t, z.im));
+}
 
 /* ------------------------------------------------------------------------ */
 /* physical constants and flags (constitutive_2d.f90:25-275 module data)     */
@@ -370,80 +412,85 @@ void oracle_eval_fluxes_p(const phys_t* P, const double* qcj, const double* qpj,
 
 /* ------------------------------------------------------------------------ */
 /* constitutive_2d.f90:1154-1322 c_phys_var and 3513-4009                    */
-/* eval_implicit_terms (rheology 1 and 6), complex arithmetic, as called by  */
-/* the complex-step Jacobian.  DOT_PRODUCT conjugates its first argument.   */
+/* eval_implicit_terms (rheology 1 and 6), complex arithmetic: the reference */
+/* evaluates the implicit terms in complex variables for the real residual   */
+/* as well as for the complex-step Jacobian.  DOT_PRODUCT conjugates its     */
+/* first (complex) argument; the implicit columns hu, hv leave the solid     */
+/* mass fractions real, so the conjugation changes no digit and is omitted.  */
 /* ------------------------------------------------------------------------ */
 static void c_phys_var(const phys_t* P, const cplx* q, cplx* h, cplx* u, cplx* v,
                        cplx* T, cplx* rho_m) {
   const int ns = P->ns;
-  cplx xs[MAXS], inv_cqj1;
-  if (creal(q[0]) > EPS) {
-    inv_cqj1 = 1.0 / q[0];
-    for (int i = 0; i < ns; ++i) xs[i] = q[4 + i] * inv_cqj1;
+  cplx inv_cqj1;
+  if (q[0].re > EPS) {
+    inv_cqj1 = c_div(cr(1.0), q[0]);
   } else {
-    *h = 0.0; *u = 0.0; *v = 0.0; *T = P->T_ambient; *rho_m = P->rho_a_amb;
+    *h = cr(0.0); *u = cr(0.0); *v = cr(0.0); *T = cr(P->T_ambient); *rho_m = cr(P->rho_a_amb);
     return;
   }
-  cplx xs_tot = 0.0;
-  for (int i = 0; i < ns; ++i) xs_tot += xs[i];
-  cplx xc = 1.0 - xs_tot;
+  cplx xs_tot = cr(0.0), dcp = cr(0.0), dinv = cr(0.0);
+  for (int i = 0; i < ns; ++i) xs_tot = c_add(xs_tot, c_mul(q[4 + i], inv_cqj1));
+  for (int i = 0; i < ns; ++i) {
+    const cplx xs = c_mul(q[4 + i], inv_cqj1);
+    dcp = c_add(dcp, c_mul(xs, cr(P->sp_heat_s[i])));
+    dinv = c_add(dinv, c_mul(xs, cr(P->inv_rho_s[i])));
+  }
+  const cplx xc = c_sub(cr(1.0), xs_tot);
   cplx cp_c;
-  if (P->gas) cp_c = ((xc - 0.0) * P->sp_heat_a + 0.0) / xc;
-  else cp_c = P->sp_heat_l;
-  cplx dcp = 0.0;
-  for (int i = 0; i < ns; ++i) dcp += conj(xs[i]) * P->sp_heat_s[i];
-  cplx cmix = dcp + xc * cp_c;
-  if (creal(q[0]) > P->eps_sing) {
-    if (P->energy) *T = (q[3] - 0.5 * (q[1] * q[1] + q[2] * q[2]) * inv_cqj1) / (q[0] * cmix);
-    else *T = q[3] / (q[0] * cmix);
-    if (creal(*T) <= 0.0) *T = P->T_ambient;
+  if (P->gas) cp_c = c_div(c_add(c_mul(c_sub(xc, cr(0.0)), cr(P->sp_heat_a)), cr(0.0)), xc);
+  else cp_c = cr(P->sp_heat_l);
+  const cplx cmix = c_add(dcp, c_mul(xc, cp_c));
+  if (q[0].re > P->eps_sing) {
+    if (P->energy)
+      *T = c_div(c_sub(q[3], c_mul(c_mul(cr(0.5), c_add(c_mul(q[1], q[1]), c_mul(q[2], q[2]))), inv_cqj1)),
+                 c_mul(q[0], cmix));
+    else
+      *T = c_div(q[3], c_mul(q[0], cmix));
+    if (T->re <= 0.0) *T = cr(P->T_ambient);
   } else {
-    *T = P->T_ambient;
+    *T = cr(P->T_ambient);
   }
   cplx inv_rho_c;
   if (P->gas) {
-    cplx Rc = ((xc - 0.0) * P->sp_gas_const_a + 0.0) / xc;
-    inv_rho_c = Rc * *T * P->inv_pres;
+    const cplx Rc = c_div(c_add(c_mul(c_sub(xc, cr(0.0)), cr(P->sp_gas_const_a)), cr(0.0)), xc);
+    inv_rho_c = c_mul(c_mul(Rc, *T), cr(P->inv_pres));
   } else {
-    inv_rho_c = P->inv_rho_l;
+    inv_rho_c = cr(P->inv_rho_l);
   }
-  cplx dinv = 0.0;
-  for (int i = 0; i < ns; ++i) dinv += conj(xs[i]) * P->inv_rho_s[i];
-  cplx inv_rhom = dinv + xc * inv_rho_c;
-  *rho_m = 1.0 / inv_rhom;
-  *h = q[0] * inv_rhom;
-  if (creal(q[0]) > P->eps_sing) {
-    *u = q[1] * inv_cqj1;
-    *v = q[2] * inv_cqj1;
+  const cplx inv_rhom = c_add(dinv, c_mul(xc, inv_rho_c));
+  *rho_m = c_div(cr(1.0), inv_rhom);
+  *h = c_mul(q[0], inv_rhom);
+  if (q[0].re > P->eps_sing) {
+    *u = c_mul(q[1], inv_cqj1);
+    *v = c_mul(q[2], inv_cqj1);
   } else {
-    cplx q4 = q[0] * q[0];
-    q4 = q4 * q4;
-    cplx den = csqrt(q4 + P->eps_sing4);
-    *u = sqrt(2.0) * q[0] * q[1] / den;
-    *v = sqrt(2.0) * q[0] * q[2] / den;
+    cplx q4 = c_mul(q[0], q[0]);
+    q4 = c_mul(q4, q4);
+    const cplx den = c_sqrt(c_add(q4, cr(P->eps_sing4)));
+    *u = c_div(c_mul(c_mul(cr(sqrt(2.0)), q[0]), q[1]), den);
+    *v = c_div(c_mul(c_mul(cr(sqrt(2.0)), q[0]), q[2]), den);
   }
 }
 
 static void c_implicit_terms(const phys_t* P, double Bx, double By, const cplx* q, cplx* nh) {
-  for (int i = 0; i < P->nv; ++i) nh[i] = 0.0;
+  for (int i = 0; i < P->nv; ++i) nh[i] = cr(0.0);
   if (!P->rheo) return;
   cplx h, u, v, T, rho_m;
   c_phys_var(P, q, &h, &u, &v, &T, &rho_m);
-  cplx red_grav = (rho_m - P->rho_a_amb) / rho_m * P->grav;
-  cplx w = P->slope_corr ? (u * Bx + v * By) : 0.0;
-  cplx mod_vel2 = u * u + v * v + w * w;
-  cplx mod_vel = csqrt(mod_vel2);
-  cplx mod_vel_hor = csqrt(u * u + v * v);
-  if (P->rheo_model == 1) {
-    if (creal(mod_vel) != 0.0) {
-      cplx turb = rho_m * red_grav / P->xi * mod_vel2;
-      nh[1] = nh[1] - turb * (u / mod_vel);
-      nh[2] = nh[2] - turb * (v / mod_vel);
-    }
-  } else if (P->rheo_model == 6) {
-    if (creal(mod_vel) != 0.0) {
-      nh[1] = nh[1] - rho_m * (u / mod_vel_hor) * P->friction_factor * mod_vel2;
-      nh[2] = nh[2] - rho_m * (v / mod_vel_hor) * P->friction_factor * mod_vel2;
+  if (!(q[0].re > EPS)) return;   /* h = u = v = 0: no friction */
+  const cplx red_grav = c_mul(c_div(c_sub(rho_m, cr(P->rho_a_amb)), rho_m), cr(P->grav));
+  const cplx w = P->slope_corr ? c_add(c_mul(u, cr(Bx)), c_mul(v, cr(By))) : cr(0.0);
+  const cplx mod_vel2 = c_add(c_add(c_mul(u, u), c_mul(v, v)), c_mul(w, w));
+  const cplx mod_vel = c_sqrt(mod_vel2);
+  if (mod_vel.re != 0.0) {
+    if (P->rheo_model == 1) {
+      const cplx turb = c_mul(c_div(c_mul(rho_m, red_grav), cr(P->xi)), mod_vel2);
+      nh[1] = c_sub(nh[1], c_mul(turb, c_div(u, mod_vel)));
+      nh[2] = c_sub(nh[2], c_mul(turb, c_div(v, mod_vel)));
+    } else if (P->rheo_model == 6) {
+      const cplx mod_vel_hor = c_sqrt(c_add(c_mul(u, u), c_mul(v, v)));
+      nh[1] = c_sub(nh[1], c_mul(c_mul(c_mul(rho_m, c_div(u, mod_vel_hor)), cr(P->friction_factor)), mod_vel2));
+      nh[2] = c_sub(nh[2], c_mul(c_mul(c_mul(rho_m, c_div(v, mod_vel_hor)), cr(P->friction_factor)), mod_vel2));
     }
   }
 }
@@ -451,9 +498,9 @@ static void c_implicit_terms(const phys_t* P, double Bx, double By, const cplx* 
 /* real call of eval_implicit_terms (r_qj path): complex with zero imag */
 static void r_implicit_terms(const phys_t* P, double Bx, double By, const double* q, double* nh) {
   cplx cq[SFLOW_MAX_VARS], cn[SFLOW_MAX_VARS];
-  for (int i = 0; i < SFLOW_MAX_VARS; ++i) cq[i] = (i < P->nv) ? q[i] : 0.0;
+  for (int i = 0; i < SFLOW_MAX_VARS; ++i) cq[i] = cr((i < P->nv) ? q[i] : 0.0);
   c_implicit_terms(P, Bx, By, cq, cn);
-  for (int i = 0; i < P->nv; ++i) nh[i] = creal(cn[i]);
+  for (int i = 0; i < P->nv; ++i) nh[i] = cn[i].re;
 }
 
 /* constitutive_2d.f90:4027-4547 eval_nh_semi_impl_terms (rheology 1) */
@@ -504,22 +551,22 @@ static void eval_f(const newton_ctx* c, const double* qj, double* f, double* sca
   *scal_f = 0.5 * s;
 }
 
-/* left_matrix(i,j) stored row-major L[i*nv+j] */
+/* left_matrix(i,j) stored row-major L[i*nv+j]; columns 1, 2 (hu, hv) by
+ * complex step with h = n_vars EPSILON on the normalised unknowns */
 static void eval_jacobian(const newton_ctx* c, const double* qj_rel, const double* qj_org,
                           double* L) {
   const int nv = c->P->nv;
   const double h = nv * EPS, one_by_h = 1.0 / h;
   for (int i = 0; i < nv * nv; ++i) L[i] = 0.0;
-  cplx qr[SFLOW_MAX_VARS], qc[SFLOW_MAX_VARS], nh[SFLOW_MAX_VARS];
+  cplx qc[SFLOW_MAX_VARS], nh[SFLOW_MAX_VARS];
   for (int i = 0; i < nv; ++i) {
     L[i * nv + i] = 1.0 * qj_org[i];
     if (i == 1 || i == 2) {
-      for (int k = 0; k < nv; ++k) qr[k] = qj_rel[k];
-      qr[i] = CMPLX(qj_rel[i], h);
-      for (int k = 0; k < nv; ++k) qc[k] = qr[k] * qj_org[k];
+      for (int k = 0; k < nv; ++k) qc[k] = cr(qj_rel[k] * qj_org[k]);
+      qc[i] = c_mul(cx(qj_rel[i], h), cr(qj_org[i]));
       c_implicit_terms(c->P, c->Bx, c->By, qc, nh);
       for (int k = 0; k < nv; ++k) {
-        double jr = 1.0 * cimag(nh[k]) * one_by_h;
+        double jr = 1.0 * nh[k].im * one_by_h;
         L[k * nv + i] = L[k * nv + i] - c->dt * c->a_diag * jr;
       }
     }
@@ -695,7 +742,7 @@ static void expl_terms(const phys_t* P, double Bx, double By, double Bxx, double
     double t_coeff;
     if (time >= tp[3]) {
       if (tp[2] > 0.0 && time < tp[3] + tp[2])
-        t_coeff = 0.5 * (1.0 + cos(P->pi_g * (time - tp[3]) / tp[2]));
+        t_coeff = 0.5 * (1.0 + sfm_cos(P->pi_g * (time - tp[3]) / tp[2]));
       else
         t_coeff = 0.0;
     } else {
@@ -704,10 +751,10 @@ static void expl_terms(const phys_t* P, double Bx, double By, double Bxx, double
       if (tp[2] == 0.0) {
         if (t_rem <= tp[1]) t_coeff = 1.0;
       } else {
-        if (t_rem < tp[2]) t_coeff = 0.5 * (1.0 - cos(P->pi_g * t_rem / tp[2]));
+        if (t_rem < tp[2]) t_coeff = 0.5 * (1.0 - sfm_cos(P->pi_g * t_rem / tp[2]));
         else if (t_rem <= tp[1] - tp[2]) t_coeff = 1.0;
         else if (t_rem <= tp[1])
-          t_coeff = 0.5 * (1.0 + cos(P->pi_g * ((t_rem - tp[1]) / tp[2] + 1.0)));
+          t_coeff = 0.5 * (1.0 + sfm_cos(P->pi_g * ((t_rem - tp[1]) / tp[2] + 1.0)));
       }
     }
     if (t_coeff > 0.0) {
@@ -744,10 +791,10 @@ static double settling_velocity(const phys_t* P, double diam, double rhos, doubl
     for (int i = 1; i <= 20; ++i) {
       sv_old = sv;
       if (P->collective)
-        inv_sqrt_C_D = sqrt(1.0 / (24.0 * (1.0 + 0.15 * pow(Rey, 0.687)) / Rey +
-                                   P->A_drag * (log(Rey) - P->B_drag)));
+        inv_sqrt_C_D = sqrt(1.0 / (24.0 * (1.0 + 0.15 * sfm_pow(Rey, 0.687)) / Rey +
+                                   P->A_drag * (sfm_log(Rey) - P->B_drag)));
       else
-        inv_sqrt_C_D = sqrt(Rey / (24.0 * (1.0 + 0.15 * pow(Rey, 0.687))));
+        inv_sqrt_C_D = sqrt(Rey / (24.0 * (1.0 + 0.15 * sfm_pow(Rey, 0.687))));
       sv = const_part * inv_sqrt_C_D;
       if (fabs(sv_old - sv) / sv_old < 1.0e-6) return sv;
       Rey = diam * sv * inv_kin_visc;
@@ -787,7 +834,7 @@ static void mass_exchange(const phys_t* P, const double* qpj, double Bx, double 
     if (alphas[i] > 0.0 && P->settling) {
       double sv = settling_velocity(P, P->diam_s[i], P->rho_s[i], rhoc, inv_kin_visc);
       dep[i] = alphas[i] * sv * 1.0;
-      dep[i] = dep[i] * pow(1.0 - dmin(1.0, at / alpha_max), hind_exp);
+      dep[i] = dep[i] * sfm_pow(1.0 - dmin(1.0, at / alpha_max), hind_exp);
       dep[i] = dmin(dep[i], r_h * alphas[i] / dt);
     }
   }
@@ -798,7 +845,7 @@ static void mass_exchange(const phys_t* P, const double* qpj, double Bx, double 
                    P->coeff_porosity * (r_h * sumv(alphas, ns) - dt * sumv(dep, ns))) / dt);
   double air_entr = 0.0;
   if (P->entrain && r_h > 0.0 && m.Ri > 0.0) {
-    double entr_coeff = 0.075 / sqrt(1.0 + 718.0 * pow(m.Ri, 2.4));
+    double entr_coeff = 0.075 / sqrt(1.0 + 718.0 * sfm_pow(m.Ri, 2.4));
     air_entr = entr_coeff * sqrt(mod_vel2);
   }
   double rho_dep_tot = dotv(P->rho_s, dep, ns);
@@ -2176,4 +2223,14 @@ int sflow_oracle_newton(const oracle_t* o, double dt, double a_diag, double Bx, 
                         const double* q_old, const double* Rj, double* q_inout) {
   newton_ctx nc = {&o->P, dt, a_diag, Bx, By, q_old, Rj};
   return solve_rk_step(&nc, q_inout);
+}
+
+/* the shared FP64 functions as the host computes them (tests compare them
+ * with correctly rounded values and with the device's bits) */
+double sflow_oracle_pow(double x, double y) { return sfm_pow(x, y); }
+double sflow_oracle_log(double x) { return sfm_log(x); }
+double sflow_oracle_cos(double x) { return sfm_cos(x); }
+void sflow_oracle_eval_math(int which, int64_t n, const double* x, const double* y, double* out) {
+  for (int64_t i = 0; i < n; ++i)
+    out[i] = which == 0 ? sfm_pow(x[i], y[i]) : which == 1 ? sfm_log(x[i]) : sfm_cos(x[i]);
 }

@@ -1,7 +1,8 @@
-"""A short run of the pyroclastic workload for profilers (ncu).
+"""A short run of the benchmark workloads for profilers (ncu), beside
+bench.py: the commands recorded under profiles/ run it.
 
-    python -m imex_sflow2d_dev_gb300.profile_case --n 2048 --steps 6 --precision fp32
-    python -m imex_sflow2d_dev_gb300.profile_case --ensemble 256 --steps 64
+    python profile_case.py --n 2048 --steps 6 --precision fp32
+    python profile_case.py --ensemble 256 --steps 64
 
 --ensemble N: the first N members of the batched ensemble (side
 log-uniform in [128, 1024], own DEM and parameters) submitted to one batch
@@ -15,10 +16,14 @@ separate launch).  With n = 2048 the FP32 working set (~400 MB) exceeds the
 126 MB L2, so DRAM counters of a single launch are meaningful.
 """
 import argparse
+import os
+import sys
 
-from . import lib
-from . import workloads as W
-from .params import PREC_FP32, PREC_FP64
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from imex_sflow2d_dev_gb300 import lib  # noqa: E402
+from imex_sflow2d_dev_gb300 import workloads as W  # noqa: E402
+from imex_sflow2d_dev_gb300.params import PREC_FP32, PREC_FP64  # noqa: E402
 
 
 def main():

@@ -4,6 +4,7 @@ restart state that this library's readers make of them, so that the GPU
 tests can run those cases without the reference tree.
 
     python tests/golden/make_reference_fixtures.py /path/to/reference
+    SFLOW_REFERENCE_DIR=/path/to/reference python tests/golden/make_reference_fixtures.py
 
 Writes tests/golden/reference_tests.npz (compressed).
 """
@@ -39,4 +40,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SFLOW_REFERENCE_DIR", "")
+    if not ref:
+        sys.exit("usage: make_reference_fixtures.py /path/to/reference (or set SFLOW_REFERENCE_DIR)")
+    main(ref)

@@ -68,3 +68,43 @@ def test_log_sums_noalloc_rejects_domains_beyond_its_scratch():
     with pytest.raises(L.SflowError) as e:
         L.log_sums_noalloc(p, 1, 1)
     assert e.value.code == -5 and "67,108,864" in str(e.value)
+
+
+@pytest.mark.parametrize("change", ["n_solid=0", "n_solid=4", "gas_and_liquid", "no_carrier", "cell_size",
+                                    "pres", "rho_s", "narrow"])
+def test_log_sums_noalloc_rejects_what_create_rejects(change):
+    """Bad parameters come back as SFLOW_EINVAL with a message before any
+    device work (the pointers are never touched)."""
+    p, B, q = W.dam_break(nx=16, ny=16)
+    if change.startswith("n_solid"):
+        p.n_solid = int(change.split("=")[1])
+    elif change == "gas_and_liquid":
+        p.gas_flag = p.liquid_flag = 1
+    elif change == "no_carrier":
+        p.gas_flag = p.liquid_flag = 0
+    elif change == "cell_size":
+        p.cell_size = 0.0
+    elif change == "pres":
+        p.pres = -1.0
+    elif change == "rho_s":
+        p.rho_s[0] = 0.0
+    else:
+        p.comp_cells_y = 3
+    with pytest.raises(L.SflowError) as e:
+        L.log_sums_noalloc(p, 1, 1)
+    assert e.value.code == -1 and str(e.value).strip()
+
+
+def test_log_sums_noalloc_error_message_is_cleared_by_the_next_call():
+    p, B, q = W.dam_break(nx=16, ny=16)
+    p.cell_size = 0.0
+    with pytest.raises(L.SflowError):
+        L.log_sums_noalloc(p, 1, 1)
+    lib = L.load()
+    assert lib.sflow_log_sums_noalloc_error().decode() != ""
+    p.cell_size = 1.0
+    p.comp_cells_x = p.comp_cells_y = 8193
+    with pytest.raises(L.SflowError) as e:
+        L.log_sums_noalloc(p, 1, 1)
+    assert "67,108,864" in lib.sflow_log_sums_noalloc_error().decode()
+    assert e.value.code == -5

@@ -1,0 +1,171 @@
+"""The benchmark configurations at their full size on the GPU against the
+oracle (the C restatement of the reference time step):
+
+  dam break   200 x 200, dx = 1 m, flat bed, liquid carrier, h = 1 / 0.1 m,
+              transmissive boundaries, minmod, CFL 0.24, to t = 10 s, with
+              the reference's default tableau (N_RK = 2) and the second-order
+              IMEX-SSP(3,3,2) (N_RK = 3)
+  current     1024 x 1024, dx = 10 m, cone + fBm DEM, ring inlet 1e6 kg/s,
+              2 particle classes, hot gas with the energy equation, Voellmy
+              friction, slope correction, settling; 20 steps from a seeded
+              developed current
+  ensemble    members of the 256-run ensemble (own DEM, friction, inlet and
+              particle draws) over their 2000 steps from the empty state
+
+Tolerances, written in each test:
+  plain FP64 form  max |q_gpu - q_oracle| / max |q_oracle| <= 1e-10 for
+                   every conserved variable (and the same step count, time
+                   and active-cell count)
+  FP32 bulk form   relative L1 error of h, hu, hv, T and each alpha_s
+                   <= 1e-4 against the oracle; relative Linf <= 1e-3
+A solid class that has settled out of the flow (its mass at round-off
+level) is scaled by at least 1e-6 of the largest total mass (FP64) or of h
+(FP32), so its residue is not divided by itself.
+                   (thin cells at the front, where T = (E - |hu|^2/2rh)/(rh c)
+                   cancels, carry the largest pointwise error)
+"""
+import numpy as np
+import pytest
+
+import oracle
+from imex_sflow2d_dev_gb300 import lib as L
+from imex_sflow2d_dev_gb300 import workloads as W
+from imex_sflow2d_dev_gb300.params import PREC_FP32, PREC_FP64
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+FP32_L1_TOL = 1e-4
+FP32_LINF_TOL = 1e-3
+
+_ORACLE_CACHE = {}
+
+
+def _oracle_result(key, p, B, q, steps=None):
+    """Oracle run (cached per configuration: both forms compare with it)."""
+    if key not in _ORACLE_CACHE:
+        pp = p.copy()
+        pp.precision = PREC_FP64
+        o = oracle.Oracle(pp, B)
+        o.set_q(W.to_aos(q))
+        if steps is None:
+            o.run()
+        else:
+            o.run(max_steps=steps)
+        _ORACLE_CACHE[key] = (o.q(), o.qp(), o.stats())
+        o.close()
+    return _ORACLE_CACHE[key]
+
+
+def _gpu_result(p, B, q, precision, steps=None):
+    pp = p.copy()
+    pp.precision = precision
+    s = L.Solver(pp, B)
+    s.upload_q(W.to_aos(q))
+    st = s.advance() if steps is None else s.advance(max_steps=steps)
+    out = (s.download_q(), s.download_qp(), st)
+    s.close()
+    return out
+
+
+def _maxrel(a, b, nv, nx, ny):
+    """max |a - b| / max |b| per conserved variable; a solid class whose
+    mass has left the flow (settled out) is scaled by at least 1e-6 of the
+    largest total mass, so its round-off residue (~1e-15) is not divided by
+    itself."""
+    A, R = W.from_aos(a, nv, nx, ny), W.from_aos(b, nv, nx, ny)
+    floor = 1e-6 * np.abs(R[0]).max()
+    out = []
+    for i in range(nv):
+        scale = np.abs(R[i]).max()
+        if i >= 4:
+            scale = max(scale, floor)
+        out.append(float(np.abs(A[i] - R[i]).max() / max(scale, 1e-300)))
+    return out
+
+
+def _field_errors(p, qp_g, qp_o):
+    """Relative L1 and Linf errors of h, hu, hv, T (wet cells) and alpha_s."""
+    nv, nx, ny = p.n_vars, p.comp_cells_x, p.comp_cells_y
+    G, O = W.from_aos(qp_g, nv + 2, nx, ny), W.from_aos(qp_o, nv + 2, nx, ny)
+    wet = O[0] > 0
+    out = {}
+    names = ["h", "hu", "hv", "T"] + [f"alpha_s{i + 1}" for i in range(p.n_solid)]
+    for i, n in enumerate(names):
+        a, r = (G[i][wet], O[i][wet]) if n == "T" else (G[i], O[i])
+        ref1, refi = np.abs(r).sum(), np.abs(r).max() if r.size else 0.0
+        if i >= 4:   # a class that has settled out: scale by 1e-6 of the flow's h
+            ref1, refi = max(ref1, 1e-6 * np.abs(O[0]).sum()), max(refi, 1e-6 * np.abs(O[0]).max())
+        d = np.abs(a - r)
+        out[n] = (float(d.sum() / ref1) if ref1 > 0 else float(d.sum()),
+                  float(d.max() / refi) if refi > 0 else (float(d.max()) if d.size else 0.0))
+    return out
+
+
+def _check_fp64(p, B, q, key, steps=None):
+    qo, qpo, so = _oracle_result(key, p, B, q, steps)
+    qg, qpg, sg = _gpu_result(p, B, q, PREC_FP64, steps)
+    assert sg.status == so.status == 0
+    assert sg.steps == so.steps
+    assert sg.t == so.t
+    assert sg.solve_cells == so.solve_cells
+    err = _maxrel(qg, qo, p.n_vars, p.comp_cells_x, p.comp_cells_y)
+    assert max(err) <= FP64_TOL, err
+    return sg
+
+
+def _check_fp32(p, B, q, key, steps=None):
+    qo, qpo, so = _oracle_result(key, p, B, q, steps)
+    qg, qpg, sg = _gpu_result(p, B, q, PREC_FP32, steps)
+    assert sg.status == 0
+    if steps is not None:
+        assert sg.steps == so.steps
+    errs = _field_errors(p, qpg, qpo)
+    for n, (l1, linf) in errs.items():
+        assert l1 <= FP32_L1_TOL, (n, l1, linf)
+        assert linf <= FP32_LINF_TOL, (n, l1, linf)
+    return errs
+
+
+@pytest.mark.parametrize("n_rk", [2, 3])
+def test_dam_break_200_to_10s_fp64_matches_oracle(n_rk):
+    p, B, q = W.dam_break(nx=200, ny=200, dx=1.0, n_rk=n_rk, t_end=10.0)
+    sg = _check_fp64(p, B, q, ("dam", n_rk))
+    assert sg.t == 10.0 and sg.steps > 100
+
+
+@pytest.mark.parametrize("n_rk", [2, 3])
+def test_dam_break_200_to_10s_fp32_error_against_oracle(n_rk):
+    p, B, q = W.dam_break(nx=200, ny=200, dx=1.0, n_rk=n_rk, t_end=10.0)
+    _check_fp32(p, B, q, ("dam", n_rk))
+
+
+def _current_1024():
+    p, B, _ = W.pyroclastic(nx=1024, ny=1024, dx=10.0, settling=True, t_end=1.0e9)
+    return p, B, W.developed_current_state(p, B)
+
+
+def test_current_1024_fp64_matches_oracle():
+    p, B, q = _current_1024()
+    sg = _check_fp64(p, B, q, ("cur1024",), steps=20)
+    assert sg.solve_cells > 300000
+
+
+def test_current_1024_fp32_error_against_oracle():
+    p, B, q = _current_1024()
+    _check_fp32(p, B, q, ("cur1024",), steps=20)
+
+
+ENSEMBLE_MEMBERS = [1, 36]    # the two smallest members (131^2 and 132^2)
+
+
+@pytest.mark.parametrize("member", ENSEMBLE_MEMBERS)
+def test_ensemble_member_2000_steps_fp64_matches_oracle(member):
+    p, B, q, steps = W.ensemble_params(member, PREC_FP64, 2000)
+    _check_fp64(p, B, q, ("ens", member), steps=steps)
+
+
+@pytest.mark.parametrize("member", ENSEMBLE_MEMBERS)
+def test_ensemble_member_2000_steps_fp32_error_against_oracle(member):
+    p, B, q, steps = W.ensemble_params(member, PREC_FP32, 2000)
+    _check_fp32(p, B, q, ("ens", member), steps=steps)
