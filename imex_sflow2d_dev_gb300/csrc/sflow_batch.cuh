@@ -32,10 +32,19 @@ class Batch : public BatchBase {
   ~Batch() override {
     for (auto& g : groups_)
       if (g) g->release();
+    if (tstream_) {
+      cudaStreamSynchronize(tstream_);
+      cudaEventDestroy(ev0_);
+      cudaEventDestroy(ev1_);
+      for (auto& e : evg_)
+        if (e) cudaEventDestroy(e);
+      cudaStreamDestroy(tstream_);
+    }
   }
   std::string err_;
 
   int submit(const HostSetup& hs, const double* q_aos, int64_t max_steps, int* id) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     if (hs.nrk != 2) { err_ = "batched runs use the N_RK = 2 tableau"; return SFLOW_EINVAL; }
     if (hs.ns < kMinSolidBuilt || hs.ns > kMaxSolidBuilt) { err_ = "n_solid out of range"; return SFLOW_EINVAL; }
     Group* g = group(hs.ns);
@@ -129,8 +138,78 @@ class Batch : public BatchBase {
     return SFLOW_OK;
   }
 
-  int advance(int64_t steps, int* finished) override {
-    int nfin = 0;
+  int advance(int64_t steps, int* finished) override { return advance_impl(steps, finished, nullptr); }
+
+  // Device time of `steps` batch steps: an event on a timing stream that
+  // every group's stream waits for, the groups' steps, one event per group
+  // that the timing stream waits for, and a last event there.
+  int advance_timed(int64_t steps, int* finished, double* ms) override {
+    if (!ms) { err_ = "ms is NULL"; return SFLOW_EINVAL; }
+    *ms = 0.0;
+    if (!tstream_) {
+      cudaError_t e = cudaStreamCreateWithFlags(&tstream_, cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreate(&ev0_);
+      if (e == cudaSuccess) e = cudaEventCreate(&ev1_);
+      for (int i = 0; e == cudaSuccess && i <= kMaxSolidBuilt; ++i)
+        e = cudaEventCreateWithFlags(&evg_[i], cudaEventDisableTiming);
+      if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+    }
+    return advance_impl(steps, finished, ms);
+  }
+
+  // `steps` batch steps launched one by one without programmatic dependent
+  // launch, with events between the five kernels; ms5 gets the summed
+  // device time of k_b_cand, k_b_mask, k_b_flux, k_b_dt, k_b_stage2 over
+  // the steps and the groups
+  int profile_kernels(int64_t steps, int* finished, double* ms5) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
+    for (int i = 0; i < 5; ++i) ms5[i] = 0.0;
+    cudaEvent_t ev[6];
+    for (int i = 0; i < 6; ++i)
+      if (cudaEventCreate(&ev[i]) != cudaSuccess) { err_ = "cudaEventCreate failed"; return SFLOW_ECUDA; }
+    int rc = SFLOW_OK;
+    for (auto& gp : groups_) {
+      Group* g = gp.get();
+      if (!g || g->live == 0) continue;
+      for (int64_t st = 0; st < steps && rc == SFLOW_OK; ++st) {
+        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux, g->lim, 0, ev);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
+        for (int i = 0; i < 5 && e == cudaSuccess; ++i) {
+          float f = 0.0f;
+          e = cudaEventElapsedTime(&f, ev[i], ev[i + 1]);
+          ms5[i] += f;
+        }
+        if (e != cudaSuccess) { err_ = cudaGetErrorString(e); rc = SFLOW_ECUDA; }
+        g->launches += 5;
+      }
+    }
+    for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+    if (rc != SFLOW_OK) return rc;
+    return advance_impl(0, finished, nullptr);
+  }
+
+  int advance_impl(int64_t steps, int* finished, double* ms) {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
+    int rc = launch_impl(steps, ms != nullptr);
+    if (rc != SFLOW_OK) return rc;
+    return wait_impl(finished, ms);
+  }
+
+  // Enqueue `steps` batch steps on the groups' streams and return at once.
+  int launch(int64_t steps) override {
+    if (launched_) { err_ = "steps already launched: wait first"; return SFLOW_ESTATE; }
+    return launch_impl(steps, false);
+  }
+  // Wait for the launched steps, read the runs' summaries.
+  int wait(int* finished) override { return wait_impl(finished, nullptr); }
+
+  int launch_impl(int64_t steps, bool timed) {
+    if (timed) {
+      cudaError_t e = cudaEventRecord(ev0_, tstream_);
+      for (auto& gp : groups_)
+        if (e == cudaSuccess && gp && gp->live > 0) e = cudaStreamWaitEvent(gp->stream, ev0_, 0);
+      if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+    }
     for (auto& gp : groups_) {
       Group* g = gp.get();
       if (!g || g->live == 0) continue;
@@ -146,10 +225,32 @@ class Batch : public BatchBase {
         left -= kChunk;
       }
       for (; left > 0; --left) {
-        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux, g->lim, g->pdl);
+        cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux, g->lim, g->pdl, nullptr);
         if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
         g->launches += 5;
       }
+    }
+    launched_ = true;
+    return SFLOW_OK;
+  }
+
+  int wait_impl(int* finished, double* ms) {
+    int nfin = 0;
+    launched_ = false;
+    if (ms) {
+      cudaError_t e = cudaSuccess;
+      for (int i = 0; i <= kMaxSolidBuilt; ++i) {
+        Group* g = groups_[i].get();
+        if (!g || g->live == 0) continue;
+        if (e == cudaSuccess) e = cudaEventRecord(evg_[i], g->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(tstream_, evg_[i], 0);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev1_, tstream_);
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev1_);
+      float f = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&f, ev0_, ev1_);
+      if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+      *ms = (double)f;
     }
     // groups run concurrently on their streams; wait for all, then read the
     // per-slot summaries
@@ -176,6 +277,7 @@ class Batch : public BatchBase {
   }
 
   int poll(int id, SflowStepStats* st, int* done) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     Slot* s = lookup(id);
     if (!s) return SFLOW_EINVAL;
     if (st) {
@@ -187,6 +289,7 @@ class Batch : public BatchBase {
   }
 
   int counters(int id, int64_t* cells, int64_t* steps) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     Slot* s = lookup(id);
     if (!s) return SFLOW_EINVAL;
     SflowStepStats st;
@@ -197,7 +300,16 @@ class Batch : public BatchBase {
     return SFLOW_OK;
   }
 
+  int border_updates(int id, int64_t* n) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
+    Slot* s = lookup(id);
+    if (!s) return SFLOW_EINVAL;
+    *n = s->solver->border_total();
+    return SFLOW_OK;
+  }
+
   int collect(int id, double* q_aos) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     Slot* s = lookup(id);
     if (!s) return SFLOW_EINVAL;
     Group* g = group(recs_[id].ns);
@@ -235,6 +347,7 @@ class Batch : public BatchBase {
   }
 
   int download(int id, double* q_aos) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     Slot* s = lookup(id);
     if (!s) return SFLOW_EINVAL;
     int rc = s->solver->download(q_aos);
@@ -248,7 +361,7 @@ class Batch : public BatchBase {
   int set_tile_shape(int th) override {
     if (th == tile_h_) return SFLOW_OK;
     if (!tile_h_built<R>(th)) { err_ = "no kernels built for this tile height"; return SFLOW_EINVAL; }
-    if (live() > 0) { err_ = "the tile height changes only while the batch holds no run"; return SFLOW_ESTATE; }
+    if (live() > 0 || launched_) { err_ = "the tile height changes only while the batch holds no run"; return SFLOW_ESTATE; }
     for (auto& g : groups_)
       if (g) {
         g->release();
@@ -314,7 +427,7 @@ class Batch : public BatchBase {
       cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
       for (int i = 0; i < kChunk; ++i) {
-        e = tab.b_step(args, stream, grids, smem_flux, lim, pdl);
+        e = tab.b_step(args, stream, grids, smem_flux, lim, pdl, nullptr);
         if (e != cudaSuccess) {
           cudaGraph_t g0 = nullptr;
           cudaStreamEndCapture(stream, &g0);
@@ -406,6 +519,9 @@ class Batch : public BatchBase {
   int max_runs_;
   int64_t max_tiles_;
   int tile_h_ = kTileHDefault;
+  cudaStream_t tstream_ = nullptr;   // timing stream of advance_timed
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evg_[kMaxSolidBuilt + 1] = {};
+  bool launched_ = false;            // launch() called, wait() not yet
   std::unique_ptr<Group> groups_[kMaxSolidBuilt + 1];
   std::vector<Rec> recs_;
 };

@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
       const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
       Ldout[pos] = e;
       atomicAdd((unsigned long long*)&br.st->cells_acc[br.st->steps & 1], (unsigned long long)br.tile_count[tile]);
+      atomicAdd(&br.st->border_acc[br.st->steps & 1], (unsigned long long)br.tile_count[tile]);
       continue;
     }
     if (br.tile_seed[tile]) {

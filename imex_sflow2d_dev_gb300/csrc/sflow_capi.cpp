@@ -16,6 +16,10 @@ struct sflow_batch {
   int precision = 0;
 };
 
+struct sflow_setup {
+  HostSetup hs;
+};
+
 struct sflow_handle {
   SolverBase* solver = nullptr;
   int nx = 0, ny = 0, nv = 0;
@@ -96,6 +100,78 @@ int sflow_batch_submit(sflow_batch* b, const SflowParams* p, const double* B_cen
   if (rc < 0) return fail(rc, b->impl->error());
   *run_id = id;
   return SFLOW_OK;
+}
+
+int sflow_setup_create(const SflowParams* p, const double* B_cent, sflow_setup** out) {
+  if (!p || !out) return fail(SFLOW_EINVAL, "NULL argument");
+  *out = nullptr;
+  sflow_setup* s = new (std::nothrow) sflow_setup();
+  if (!s) return fail(SFLOW_ENOMEM, "host allocation failed");
+  std::string err;
+  const int rc = sflow::host_setup(p, B_cent, s->hs, err);
+  if (rc != SFLOW_OK) {
+    delete s;
+    return fail(rc, err);
+  }
+  *out = s;
+  return SFLOW_OK;
+}
+
+void sflow_setup_destroy(sflow_setup* s) { delete s; }
+
+int sflow_batch_submit_setup(sflow_batch* b, const sflow_setup* s, const double* q_aos, int64_t max_steps,
+                             int32_t* run_id) {
+  BATCH_CHECK(b);
+  if (!s || !q_aos || !run_id) return fail(SFLOW_EINVAL, "NULL argument");
+  if (s->hs.p.precision != b->precision) return fail(SFLOW_EINVAL, "run precision differs from the batch precision");
+  int id = -1;
+  const int rc = b->impl->submit(s->hs, q_aos, max_steps, &id);
+  if (rc < 0) return fail(rc, b->impl->error());
+  *run_id = id;
+  return SFLOW_OK;
+}
+
+int sflow_batch_launch(sflow_batch* b, int64_t steps) {
+  BATCH_CHECK(b);
+  if (steps < 0) return fail(SFLOW_EINVAL, "steps must be >= 0");
+  BATCH_FORWARD(b, b->impl->launch(steps));
+}
+
+int sflow_batch_wait(sflow_batch* b, int32_t* finished) {
+  BATCH_CHECK(b);
+  int nf = 0;
+  const int rc = b->impl->wait(&nf);
+  if (rc < 0) return fail(rc, b->impl->error());
+  if (finished) *finished = nf;
+  return SFLOW_OK;
+}
+
+int sflow_batch_advance_timed(sflow_batch* b, int64_t steps, int32_t* finished, double* device_ms) {
+  BATCH_CHECK(b);
+  if (steps < 0) return fail(SFLOW_EINVAL, "steps must be >= 0");
+  if (!device_ms) return fail(SFLOW_EINVAL, "device_ms is NULL");
+  int nf = 0;
+  int rc = b->impl->advance_timed(steps, &nf, device_ms);
+  if (rc < 0) return fail(rc, b->impl->error());
+  if (finished) *finished = nf;
+  return SFLOW_OK;
+}
+
+int sflow_batch_profile_kernels(sflow_batch* b, int64_t steps, int32_t* finished, double* ms5) {
+  BATCH_CHECK(b);
+  if (steps < 0) return fail(SFLOW_EINVAL, "steps must be >= 0");
+  if (!ms5) return fail(SFLOW_EINVAL, "ms5 is NULL");
+  int nf = 0;
+  int rc = b->impl->profile_kernels(steps, &nf, ms5);
+  if (rc < 0) return fail(rc, b->impl->error());
+  if (finished) *finished = nf;
+  return SFLOW_OK;
+}
+
+int sflow_batch_dry_border_updates(sflow_batch* b, int32_t run_id, int64_t* n) {
+  BATCH_CHECK(b);
+  if (!n) return fail(SFLOW_EINVAL, "n is NULL");
+  BATCH_FORWARD(b, b->impl->border_updates(run_id, n));
 }
 
 int sflow_batch_advance(sflow_batch* b, int64_t steps, int32_t* finished) {
@@ -444,6 +520,15 @@ int sflow_host_scalars(const SflowParams* p, const double* B_cent, double* out4)
   out4[1] = s.src_rho_m;
   out4[2] = s.src_cp_mix;
   out4[3] = s.eps_sing;
+  return SFLOW_OK;
+}
+
+int sflow_dry_border_updates(sflow_handle* h, int64_t* n) {
+  CHECK_HANDLE(h);
+  if (!n) return fail(SFLOW_EINVAL, "n is NULL");
+  const int64_t v = h->solver->border_total();
+  if (v < 0) return fail(SFLOW_ECUDA, "could not read the run state");
+  *n = v;
   return SFLOW_OK;
 }
 

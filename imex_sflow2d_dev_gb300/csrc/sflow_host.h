@@ -70,6 +70,8 @@ class SolverBase {
   virtual int64_t device_bytes() const = 0;
   virtual int newton_stats(int64_t* total, int* maxit) = 0;
   virtual int64_t cells_total() = 0;
+  // active-cell updates of dry border tiles (counted, skipped by the kernels)
+  virtual int64_t border_total() = 0;
   virtual int tile_shape() const = 0;
   virtual int set_tile_shape(int tile_h) = 0;
   virtual int autotune(int64_t steps, int* best, double* ms_per_mcu) = 0;
@@ -85,8 +87,17 @@ class BatchBase {
   virtual ~BatchBase() {}
   virtual int submit(const HostSetup& hs, const double* q_aos, int64_t max_steps, int* id) = 0;
   virtual int advance(int64_t steps, int* finished) = 0;
+  // the same with the device time of the steps (CUDA events across the
+  // groups' streams) in *ms
+  virtual int advance_timed(int64_t steps, int* finished, double* ms) = 0;
+  // steps one by one with the device time of each of the five kernels
+  virtual int profile_kernels(int64_t steps, int* finished, double* ms5) = 0;
+  // asynchronous form of advance: launch returns at once, wait synchronises
+  virtual int launch(int64_t steps) = 0;
+  virtual int wait(int* finished) = 0;
   virtual int poll(int id, SflowStepStats* s, int* done) = 0;
   virtual int counters(int id, int64_t* cells, int64_t* steps) = 0;
+  virtual int border_updates(int id, int64_t* n) = 0;
   virtual int download(int id, double* q_aos) = 0;
   virtual int collect(int id, double* q_aos) = 0;
   virtual int live() const = 0;

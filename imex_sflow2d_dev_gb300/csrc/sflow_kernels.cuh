@@ -298,7 +298,10 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
   }
   if (threadIdx.x == 0) {
     a.tile_active[ty * tiles_x + tx] = (uint8_t)code;
-    if (code == TILE_DRY_BORDER) a.tile_count[ty * tiles_x + tx] = (uint16_t)cnt;
+    if (code == TILE_DRY_BORDER) {
+      a.tile_count[ty * tiles_x + tx] = (uint16_t)cnt;
+      atomicAdd(&st->border_acc[st->steps & 1], (unsigned long long)cnt);
+    }
     if (cnt) atomicAdd((unsigned long long*)&st->cells_acc[st->steps & 1], (unsigned long long)cnt);
   }
   return code;
@@ -335,8 +338,10 @@ __device__ __forceinline__ bool mask_tile_skippable(const KArgs<R>& a, int tx, i
             break;
           }
         }
-      if (skip && ta == TILE_DRY_BORDER)
+      if (skip && ta == TILE_DRY_BORDER) {
         atomicAdd((unsigned long long*)&a.st->cells_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
+        atomicAdd(&a.st->border_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
+      }
     }
   }
   return __syncthreads_or(skip) != 0;
@@ -1058,6 +1063,7 @@ __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   const unsigned long long cells = atomicExch(&st->cells_acc[p], 0ull);
   st->last_cells = (long long)cells;
   st->cells_total += (long long)cells;
+  st->border_total += (long long)atomicExch(&st->border_acc[p], 0ull);
   st->steps += 1;
 }
 

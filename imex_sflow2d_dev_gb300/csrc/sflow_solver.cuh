@@ -511,6 +511,8 @@ class Solver : public SolverBase {
     h.last_cells = (long long)h.cells_acc[p];
     h.cells_total += (long long)h.cells_acc[p];
     h.cells_acc[p] = 0;
+    h.border_total += (long long)h.border_acc[p];
+    h.border_acc[p] = 0;
     h.dtmin_bits = bits_of(1.0e300);
     limits_known_ = false;
     SFLOW_CU(cudaMemcpyAsync(st_, &h, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
@@ -703,6 +705,11 @@ class Solver : public SolverBase {
     RunState h;
     if (cudaMemcpy(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
     return h.cells_total;
+  }
+  int64_t border_total() override {
+    RunState h;
+    if (cudaMemcpy(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return h.border_total;
   }
 
  private:

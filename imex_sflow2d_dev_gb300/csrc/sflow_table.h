@@ -35,9 +35,10 @@ struct KernelTable {
   // of k_b_cand / k_b_mask / k_b_flux / k_b_stage2 for this device
   cudaError_t (*b_setup)(size_t smem_flux, int* grids) = nullptr;
   // lim = 1: every run of the group uses minmod for every variable
-  // pdl: launch with programmatic dependent launch
+  // pdl: launch with programmatic dependent launch; ev: NULL, or 6 events
+  // recorded before, between and after the five kernels
   cudaError_t (*b_step)(const BatchArgs<R>&, cudaStream_t, const int* grids, size_t smem_flux, int lim,
-                        int pdl) = nullptr;
+                        int pdl, cudaEvent_t* ev) = nullptr;
   cudaError_t (*b_admit)(const BatchArgs<R>&, cudaStream_t, int slot, unsigned gen, unsigned ntiles) = nullptr;
   cudaError_t (*b_summary)(const BatchArgs<R>&, cudaStream_t) = nullptr;
 };

@@ -175,18 +175,25 @@ static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
 }
 template <class R, int NS, int TH>
 static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* grids, size_t smem_flux, int lim,
-                              int pdl) {
+                              int pdl, cudaEvent_t* ev) {
   const dim3 T(TileShape<TH>::FLUX_THREADS);
-  cudaError_t e = launch_step_kernel(k_b_cand<R>, dim3(grids[0]), dim3(kBatchCandThreads), 0, s, pdl, b);
+  auto rec = [&](int i) -> cudaError_t { return ev ? cudaEventRecord(ev[i], s) : cudaSuccess; };
+  cudaError_t e = rec(0);
+  if (e == cudaSuccess) e = launch_step_kernel(k_b_cand<R>, dim3(grids[0]), dim3(kBatchCandThreads), 0, s, pdl, b);
+  if (e == cudaSuccess) e = rec(1);
   if (e == cudaSuccess)
     e = launch_step_kernel(k_b_mask<R, TH>, dim3(grids[1]), dim3(TileShape<TH>::MASK_THREADS), 0, s, pdl, b);
+  if (e == cudaSuccess) e = rec(2);
   if (e == cudaSuccess) {
     if (lim == 1) e = launch_step_kernel(k_b_flux<R, NS, 1, TH>, dim3(grids[2]), T, smem_flux, s, pdl, b);
     else e = launch_step_kernel(k_b_flux<R, NS, -1, TH>, dim3(grids[2]), T, smem_flux, s, pdl, b);
   }
+  if (e == cudaSuccess) e = rec(3);
   if (e == cudaSuccess) e = launch_step_kernel(k_b_dt<R>, dim3(1), dim3(kBatchCandThreads), 0, s, pdl, b);
+  if (e == cudaSuccess) e = rec(4);
   if (e == cudaSuccess)
     e = launch_step_kernel(k_b_stage2<R, NS, TH>, dim3(grids[3]), dim3(TileShape<TH>::STAGE_THREADS), 0, s, pdl, b);
+  if (e == cudaSuccess) e = rec(5);
   return e;
 }
 

@@ -85,6 +85,9 @@ struct RunState {
   int pad2;
   double tp[4];                    // time_param
   double pi_g;
+  // active cells of dry border tiles (tile code 3: counted, not computed)
+  unsigned long long border_acc[2];
+  long long border_total;
 };
 
 }  // namespace sflow

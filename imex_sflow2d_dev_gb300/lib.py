@@ -87,6 +87,15 @@ def load(build_if_missing=True):
         "sflow_batch_destroy": (None, [vp]),
         "sflow_batch_submit": (C.c_int, [vp, P, dp, dp, i64, C.POINTER(i32)]),
         "sflow_batch_advance": (C.c_int, [vp, i64, C.POINTER(i32)]),
+        "sflow_batch_advance_timed": (C.c_int, [vp, i64, C.POINTER(i32), dp]),
+        "sflow_batch_profile_kernels": (C.c_int, [vp, i64, C.POINTER(i32), dp]),
+        "sflow_setup_create": (C.c_int, [P, dp, C.POINTER(vp)]),
+        "sflow_setup_destroy": (None, [vp]),
+        "sflow_batch_submit_setup": (C.c_int, [vp, vp, dp, i64, C.POINTER(i32)]),
+        "sflow_batch_launch": (C.c_int, [vp, i64]),
+        "sflow_batch_wait": (C.c_int, [vp, C.POINTER(i32)]),
+        "sflow_batch_dry_border_updates": (C.c_int, [vp, i32, C.POINTER(i64)]),
+        "sflow_dry_border_updates": (C.c_int, [vp, C.POINTER(i64)]),
         "sflow_batch_poll": (C.c_int, [vp, i32, S, C.POINTER(i32)]),
         "sflow_batch_counters": (C.c_int, [vp, i32, C.POINTER(i64), C.POINTER(i64)]),
         "sflow_batch_download": (C.c_int, [vp, i32, dp]),
@@ -128,7 +137,10 @@ def exported_symbols():
             "sflow_upload_maps", "sflow_set_output_time", "sflow_tile_shapes",
             "sflow_set_tile_shape", "sflow_get_tile_shape", "sflow_autotune",
             "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape", "sflow_check_conversions",
-            "sflow_eval_math"]
+            "sflow_eval_math", "sflow_batch_advance_timed", "sflow_batch_profile_kernels",
+            "sflow_setup_create", "sflow_setup_destroy", "sflow_batch_submit_setup",
+            "sflow_batch_launch", "sflow_batch_wait", "sflow_batch_dry_border_updates",
+            "sflow_dry_border_updates"]
 
 
 TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
@@ -423,8 +435,10 @@ class Solver:
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
         d = C.c_int32()
         _check(self.lib.sflow_counters(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        e = C.c_int64(0)
+        _check(self.lib.sflow_dry_border_updates(self.h, C.byref(e)))
         return {"cell_updates": a.value, "steps": b.value, "newton_iters": c.value,
-                "newton_max": d.value}
+                "newton_max": d.value, "dry_border_updates": e.value}
 
     def launch_count(self):
         return self.lib.sflow_launch_count(self.h)
@@ -477,6 +491,35 @@ class Solver:
 EBUSY = -6
 
 
+class Setup:
+    """The host part of a batch submission (validation, topography terms,
+    ring-inlet geometry) of one run, made without touching the GPU
+    (sflow_setup_create); safe to build on worker threads."""
+
+    def __init__(self, params, B_cent, precision=None):
+        self.lib = load()
+        p = params.copy()
+        if precision is not None:
+            p.precision = precision
+        self.p = p
+        B = np.ascontiguousarray(B_cent, dtype=np.float64).reshape(-1)
+        if B.size != p.comp_cells_x * p.comp_cells_y:
+            raise ValueError("B_cent must have nx*ny values")
+        self.h = C.c_void_p()
+        _check(self.lib.sflow_setup_create(C.byref(p), _dp(B), C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.lib.sflow_setup_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Batch:
     """Many independent runs resident on the GPU and advanced together
     (sflow_batch_* of include/sflow.h).  submit() returns a run id, or None
@@ -518,10 +561,52 @@ class Batch:
         self._shape[rid.value] = p.n_vars * p.comp_cells_x * p.comp_cells_y
         return rid.value
 
+    def submit_setup(self, setup, q_aos, max_steps=0):
+        """submit() of a run prepared as a Setup (the GPU part only)."""
+        p = setup.p
+        q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
+        if q.size != p.n_vars * p.comp_cells_x * p.comp_cells_y:
+            raise ValueError("q must have n_vars*nx*ny values")
+        rid = C.c_int32(-1)
+        rc = self.lib.sflow_batch_submit_setup(self.h, setup.h, _dp(q), int(max_steps), C.byref(rid))
+        if rc == EBUSY:
+            return None
+        _check(rc)
+        self._shape[rid.value] = p.n_vars * p.comp_cells_x * p.comp_cells_y
+        return rid.value
+
     def advance(self, steps):
         f = C.c_int32(0)
         _check(self.lib.sflow_batch_advance(self.h, int(steps), C.byref(f)))
         return f.value
+
+    def advance_timed(self, steps):
+        """advance() with the device time of the steps: (finished, ms)."""
+        f = C.c_int32(0)
+        ms = C.c_double(0.0)
+        _check(self.lib.sflow_batch_advance_timed(self.h, int(steps), C.byref(f), C.byref(ms)))
+        return f.value, ms.value
+
+    def profile_kernels(self, steps):
+        """steps batch steps one at a time; summed device ms per kernel."""
+        f = C.c_int32(0)
+        out = np.zeros(5)
+        _check(self.lib.sflow_batch_profile_kernels(self.h, int(steps), C.byref(f), _dp(out)))
+        return dict(zip(("cand", "mask", "flux", "dt", "stage"), out.tolist()))
+
+    def launch(self, steps):
+        """Enqueue steps and return at once (wait() before any other call)."""
+        _check(self.lib.sflow_batch_launch(self.h, int(steps)))
+
+    def wait(self):
+        f = C.c_int32(0)
+        _check(self.lib.sflow_batch_wait(self.h, C.byref(f)))
+        return f.value
+
+    def dry_border_updates(self, rid):
+        n = C.c_int64(0)
+        _check(self.lib.sflow_batch_dry_border_updates(self.h, rid, C.byref(n)))
+        return n.value
 
     def poll(self, rid):
         s = SflowStepStats()

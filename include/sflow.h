@@ -277,6 +277,8 @@ int sflow_autotune(sflow_handle* h, int64_t steps_per_shape, int32_t* best, doub
  * active cells), steps, Newton iterations and the largest per-cell count. */
 int sflow_counters(sflow_handle* h, int64_t* cell_updates, int64_t* steps,
                    int64_t* newton_iters, int32_t* newton_max);
+/* dry-border part of the cell updates (see sflow_batch_dry_border_updates) */
+int sflow_dry_border_updates(sflow_handle* h, int64_t* n);
 
 /*
  * Host-side set-up of a domain without touching the GPU (for tests and
@@ -351,9 +353,39 @@ int sflow_batch_create(int32_t precision, int32_t max_runs, int64_t max_cells, s
 void sflow_batch_destroy(sflow_batch* b);
 int sflow_batch_submit(sflow_batch* b, const SflowParams* p, const double* B_cent, const double* q_aos,
                        int64_t max_steps, int32_t* run_id);
+/* The host part of sflow_batch_submit on its own: validation, topography
+ * terms and ring-inlet geometry of a run (no GPU work, no batch), so that a
+ * request loop can prepare arriving runs on other threads while the batch
+ * advances; sflow_batch_submit_setup then allocates and uploads the run.
+ * A setup is read-only after creation and can be submitted to any batch of
+ * its precision, any number of times. */
+typedef struct sflow_setup sflow_setup;
+int sflow_setup_create(const SflowParams* p, const double* B_cent, sflow_setup** out);
+void sflow_setup_destroy(sflow_setup* s);
+int sflow_batch_submit_setup(sflow_batch* b, const sflow_setup* s, const double* q_aos, int64_t max_steps,
+                             int32_t* run_id);
+/* Asynchronous sflow_batch_advance: sflow_batch_launch enqueues `steps`
+ * batch steps and returns at once; sflow_batch_wait waits for them and
+ * reports finished runs.  Between the two only host work is allowed: every
+ * other batch call answers SFLOW_ESTATE until the wait. */
+int sflow_batch_launch(sflow_batch* b, int64_t steps);
+int sflow_batch_wait(sflow_batch* b, int32_t* finished);
 int sflow_batch_advance(sflow_batch* b, int64_t steps, int32_t* finished);
+/* sflow_batch_advance with the device time of the steps (CUDA events on the
+ * batch's streams) in *device_ms */
+int sflow_batch_advance_timed(sflow_batch* b, int64_t steps, int32_t* finished, double* device_ms);
+/* `steps` batch steps launched one at a time with CUDA events between the
+ * five kernels of a step; ms5 = summed device ms of k_b_cand, k_b_mask,
+ * k_b_flux, k_b_dt, k_b_stage2 (for the benchmark's per-kernel roofline) */
+int sflow_batch_profile_kernels(sflow_batch* b, int64_t steps, int32_t* finished, double* ms5);
 int sflow_batch_poll(sflow_batch* b, int32_t run_id, SflowStepStats* stats, int32_t* done);
 int sflow_batch_counters(sflow_batch* b, int32_t run_id, int64_t* cell_updates, int64_t* steps);
+/* The part of the cell updates that falls in dry border tiles: tiles active
+ * only through the domain's border cells (always in check_solve's mask,
+ * solver_2d.f90:351-354) whose 4-cell frame holds no mass and no ring cell.
+ * They count as active cells, as in the reference, but the flux and stage
+ * kernels skip them (their result is no change). */
+int sflow_batch_dry_border_updates(sflow_batch* b, int32_t run_id, int64_t* n);
 int sflow_batch_download(sflow_batch* b, int32_t run_id, double* q_aos);
 int sflow_batch_collect(sflow_batch* b, int32_t run_id, double* q_aos);
 int32_t sflow_batch_live(const sflow_batch* b);

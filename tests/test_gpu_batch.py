@@ -243,3 +243,39 @@ def test_tile_list_capacity_is_enforced():
     ref, _ = _alone(ps, Bs, qs, 6, PREC_FP32)
     same_run(b.collect(small), ref, PREC_FP32, ps.n_vars)
     b.close()
+
+
+def test_setups_launch_wait_and_timed_advance_give_the_same_runs():
+    """Runs prepared on the host with sflow_setup_create and submitted with
+    sflow_batch_submit_setup, advanced by sflow_batch_launch/_wait and by
+    sflow_batch_advance_timed, equal the same runs submitted and advanced
+    the plain way, bit for bit (FP64 form); the device time is positive,
+    the per-kernel profile covers the five kernels, and the dry-border part
+    of the cell updates is counted within them."""
+    runs = _mix()
+    steps = 40
+    ref = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 20)
+    ids = [ref.submit(p, B, W.to_aos(q), max_steps=steps) for p, B, q in runs]
+    ref.advance(steps)
+    want = [ref.download(i) for i in ids]
+    cu_want = [ref.counters(i)["cell_updates"] for i in ids]
+    ref.close()
+    b = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 20)
+    setups = [L.Setup(p, B, precision=PREC_FP64) for p, B, q in runs]
+    ids = [b.submit_setup(st, W.to_aos(q), max_steps=steps) for st, (p, B, q) in zip(setups, runs)]
+    for st in setups:
+        st.close()
+    b.launch(16)
+    with pytest.raises(L.SflowError):
+        b.download(ids[0])          # steps in flight: refused
+    b.wait()
+    _, ms = b.advance_timed(16)
+    assert ms > 0.0
+    prof = b.profile_kernels(steps - 32)
+    assert set(prof) == {"cand", "mask", "flux", "dt", "stage"} and all(v > 0.0 for v in prof.values())
+    for i, w, cu in zip(ids, want, cu_want):
+        np.testing.assert_array_equal(b.download(i), w)
+        c = b.counters(i)
+        assert c["cell_updates"] == cu and c["steps"] == steps
+        assert 0 <= b.dry_border_updates(i) <= cu
+    b.close()
