@@ -1,44 +1,52 @@
 """Benchmark of the IMEX_SfloW2D time step on GB300.
 
-Workload (one step = one driver iteration of the time loop): the single
-pyroclastic-style current of the benchmark configurations -- 1024x1024 cells,
-dx = 10 m, Gaussian cone (1500 m, sigma 2 km) + fBm DEM (Hurst 0.8, 20 m RMS,
-seed 1), ring inlet of radius 50 m at the summit with 1e6 kg/s at 20 m/s,
-2 particle classes (1e-4 / 1e-3 m, 2500 / 1500 kg/m^3, 1 % / 2 %), gas at
-1000 K with temperature-dependent density (total-energy equation), Voellmy
-friction (mu = 0.1, xi = 1000), slope correction, N_RK = 2, KT fluxes,
-minmod.  The state is a seeded developed current (37 % of the cells wet,
-see workloads.developed_current_state) shared by every arm.
+Headline workload (the configuration the metric is quoted on): the batched
+ensemble -- 256 independent ring-inlet currents, grid sides log-uniform in
+[128, 1024] (dx 5-20 m), each on its own seeded Gaussian-cone + fBm DEM,
+per-run Voellmy mu in [0.05, 0.3] and xi in [200, 2000], inlet radius
+20-200 m, inlet temperature 600-1200 K, particle volume fractions
+0.005-0.05 of 2 classes, settling on (workloads.ensemble_params), each run
+2000 steps from the empty state with N_RK = 2, KT fluxes, minmod.  All runs
+are resident together and advanced by the batch engine (persistent kernels
+over a device-built tile queue, CUDA graphs of 16 steps).
 
-Metric: cell-updates/s = sum over steps of the active cells (solve_cells of
-the reference's check_solve) / time.  `value` is the FP32 bulk form (FP32
-state and fluxes, FP64 implicit Newton solve, FP64 mass sums, FP64-exact
-wet/dry tests) timed on the device with CUDA events on the solver's stream,
-one step per timed interval with a 512 MB write between steps to flush L2
-(the working set, ~100 MB, would otherwise stay in the 126 MB L2).  The
-plain FP64 form is timed the same way and reported beside it, with the L1
-error of h between the two forms.  `e2e` is the same metric through the C
-ABI with the state in pinned host memory copied in and out every step;
-its `transfers` split times the two copies alone and, for the host link's
-rate, copy-engine copies of the same pinned buffer.
+One bench step is one chunk of 2000 / K batch steps (every run advances
+that many time steps), so the K timed steps cover the runs' 2000 steps.
 
-Further legs on rank 0, each a key of the same JSON line:
-  ensemble      the 256-run mixed ensemble (sides 128-1024, own DEMs and
-                draws) in one batch of persistent kernels, FP32 bulk form;
-                its speed-up is taken against the plain FP64 form's
-                cell-updates/s of the main leg, and the L1/Linf errors of
-                h, hu, hv, T and alpha_s of the two forms on member 0;
-  served        Poisson arrivals of short jobs through the request loop
-                (admission by free HBM), p50/p99 submit-to-done latency;
-  large_domain  one 8192x8192 domain (3 classes, entrainment), FP32 bulk
-                against FP64 on a few steps, with the same error norms.
-Each leg is switched off by a zero size (--ensemble-runs 0,
---served-requests 0, --large-n 0).
+Metric: cell-updates/s = sum over runs and steps of the active cells
+(solve_cells of the reference's check_solve) / time.
+  value        FP32 bulk form with FP64 Newton, device time (CUDA events on
+               the batch's streams) of the K steps, inputs resident in HBM
+  fp64_plain   the same ensemble in the plain FP64 form (same batch
+               engine), the same K steps: the same-workload comparator
+  e2e          the same ensemble through the C ABI from host buffers:
+               sflow_batch_submit of every run (host set-up, upload),
+               the K steps, sflow_batch_collect with the download of every
+               run's q, host wall clock
+  cpu_baseline the oracle (C restatement of the reference time step) built
+               with the reference's compiler flags (-fopenmp -Ofast
+               -funroll-all-loops) on a bounded sample of the ensemble, one
+               single-threaded process per member on the host cores, as the
+               reference runs ensembles (one job per process)
+The working set (every run's state, increments, topography and maps,
+~6 GB) and the per-step traffic of the active tiles (~1.4 M cells x ~150 B)
+exceed the 129 MB L2, so no flush is needed between steps.
+
+Further legs (keys of the same JSON line; a zero size switches each off):
+  current_1024  the single 1024^2 current from a seeded developed state,
+                FP32 vs FP64, per-kernel times and the k_flux roofline
+  served        Poisson arrivals (20/s) of 200 dam-break and ring-inlet
+                jobs through the request loop, p50/p99 time to solution,
+                beside the stream served one job at a time by the plain
+                FP64 form (service times measured per job)
+  large_domain  one 8192^2 domain (3 classes, entrainment)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
 import argparse
 import json
+import math
+import multiprocessing as mp
 import os
 import statistics
 import subprocess
@@ -57,14 +65,11 @@ from imex_sflow2d_dev_gb300.params import PREC_FP32, PREC_FP64  # noqa: E402
 METRIC = ("cell-updates/s (batched FP32 vs plain FP64 GPU, ≤1e-4 L1 err) ; "
           "p50/p99 solve latency")
 UNIT = "cell-updates/s"
-WORKLOAD = "pyroclastic current 1024x1024 dx=10m, ring inlet 1e6 kg/s, 2 classes, Voellmy, N_RK=2"
-
-
-def build_workload(precision):
-    p, B, _ = W.pyroclastic(nx=1024, ny=1024, dx=10.0, settling=False, precision=precision,
-                            t_end=1.0e9)
-    q = W.developed_current_state(p, B)
-    return p, B, q
+ENS_RUNS, ENS_STEPS = 256, 2000
+WORKLOAD = (f"batched ensemble: {ENS_RUNS} ring-inlet runs x {ENS_STEPS} steps, sides 128-1024 "
+            "log-uniform, dx 5-20 m, own cone+fBm DEMs, per-run mu/xi/inlet draws, 2 classes, N_RK=2")
+CPU_SAMPLE_EVERY = 16          # cpu sample: members 0, 16, 32, ...
+CPU_SAMPLE_STEPS = 200         # time steps per sampled member across the K bench steps
 
 
 def dist_env():
@@ -133,12 +138,10 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
-def read_traffic():
-    """DRAM bytes per active cell of the dominant kernel from the committed
-    ncu summary (profiles/), or None."""
-    path = os.path.join(ROOT, "profiles", "k_flux_pyroclastic_traffic.json")
+def read_profile(name):
+    """A committed ncu summary (profiles/<name>.json), or None."""
     try:
-        with open(path) as fh:
+        with open(os.path.join(ROOT, "profiles", name + ".json")) as fh:
             return json.load(fh)
     except Exception:
         return None
@@ -200,57 +203,249 @@ class ClockSampler:
         return out
 
 
-def l1_rel(a, b):
-    return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+# ---------------------------------------------------------------------------
+# errors of the FP32 form
+# ---------------------------------------------------------------------------
+
+def field_errors(p, qp_test, qp_ref):
+    """Relative L1 / Linf of h, hu, hv, T and each alpha_s of qp_test
+    against qp_ref (physical variables, reference layout).  T over the cells
+    thicker than 1e-3 of the deepest (a film whose energy is almost all
+    kinetic carries the rounding of its fluxes a thousandfold); a solid class
+    that has settled out is scaled by at least 1e-6 of h."""
+    nv, nx, ny = p.n_vars, p.comp_cells_x, p.comp_cells_y
+    G, O = W.from_aos(qp_test, nv + 2, nx, ny), W.from_aos(qp_ref, nv + 2, nx, ny)
+    thick = O[0] > 1e-3 * max(O[0].max(), 1e-300)
+    out = {}
+    names = ["h", "hu", "hv", "T"] + [f"alpha_s{i + 1}" for i in range(p.n_solid)]
+    for i, n in enumerate(names):
+        a, r = (G[i][thick], O[i][thick]) if n == "T" else (G[i], O[i])
+        ref1 = np.abs(r).sum()
+        refi = np.abs(r).max() if r.size else 0.0
+        if i >= 4:
+            ref1 = max(ref1, 1e-6 * np.abs(O[0]).sum())
+            refi = max(refi, 1e-6 * np.abs(O[0]).max())
+        d = np.abs(a - r)
+        out[n] = {"l1_rel": float(d.sum() / ref1) if ref1 > 0 else float(d.sum()),
+                  "linf_rel": (float(d.max() / refi) if refi > 0 else float(d.max())) if d.size else 0.0}
+    return out
 
 
-def cpu_baseline(p, B, q, max_seconds=20.0, max_steps=40):
-    """The oracle (C restatement of the reference time step, OpenMP on all
-    host cores) on a bounded sample of the same workload."""
+def worst(errs_list):
+    """Largest L1 and Linf of each field over several results."""
+    out = {}
+    for e in errs_list:
+        for n, v in e.items():
+            o = out.setdefault(n, {"l1_rel": 0.0, "linf_rel": 0.0})
+            o["l1_rel"] = max(o["l1_rel"], v["l1_rel"])
+            o["linf_rel"] = max(o["linf_rel"], v["linf_rel"])
+    return out
+
+
+def qp_of_state(p, B, q_aos):
+    """Physical variables (h, hu, hv, T, alpha_s..., u, v) of a state by the
+    oracle's FP64 closure (qc_to_qp), for the error norms."""
     import oracle
-    threads = os.cpu_count() or 1
-    oracle.set_threads(threads)
-    o = oracle.Oracle(p, B)
+    pp = p.copy()
+    pp.precision = PREC_FP64
+    o = oracle.Oracle(pp, B)
+    o.set_q(q_aos)
+    qp = o.qp()
+    o.close()
+    return qp
+
+
+# ---------------------------------------------------------------------------
+# CPU side (spawned processes: no fork after a CUDA context)
+# ---------------------------------------------------------------------------
+
+def _cpu_member_worker(args):
+    """One ensemble member on one host core with the oracle's timing build:
+    `warm` untimed steps, then (after the barrier) `chunks` x `chunk` steps.
+    Returns (cell updates of the timed steps, seconds)."""
+    index, warm, chunks, chunk, barrier = args
+    import oracle
+    oracle.set_threads(1, timing=True)
+    p, B, q, _ = W.ensemble_params(index, PREC_FP64, ENS_STEPS)
+    o = oracle.Oracle(p, B, timing=True)
     o.set_q(W.to_aos(q))
-    o.step()  # first step outside the sample (page faults, thread start)
+    for _ in range(warm):
+        o.step()
+    barrier.wait()
     cells = 0
-    n = 0
     t0 = time.perf_counter()
-    while n < max_steps:
+    for _ in range(chunks * chunk):
         o.step()
         cells += o.stats().solve_cells
-        n += 1
-        if time.perf_counter() - t0 > max_seconds:
-            break
     dt = time.perf_counter() - t0
     o.close()
-    return {"value": cells / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} steps of the 1024x1024 workload from the same initial state, "
-                      f"{cells} cell updates in {dt:.2f} s (oracle C restatement, OpenMP)",
-            "steps": n, "seconds": dt}
+    return cells, dt
 
 
-def run_reference(args, d):
-    if d.rank != 0:
-        return 0
-    p, B, q = build_workload(PREC_FP64)
-    steps = max(args.steps // 10, 3)
-    cb = cpu_baseline(p, B, q, max_seconds=25.0, max_steps=steps + args.warmup)
-    line = {
-        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
-        "n_gpus": args.gpus, "steps": cb["steps"], "warmup": 1,
-        "ms_per_step": 1e3 * cb["seconds"] / max(cb["steps"], 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded DEM and developed-current state)",
-        "config": {"workload": WORKLOAD, "cells": 1024 * 1024, "precision": "FP64 CPU",
-                   "implementation": "oracle/sflow_oracle.c (C restatement of the Fortran "
-                                     "reference, which has no compiler on this box)"},
-        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
-    return 0
+def cpu_ensemble_sample(K, warmup_steps):
+    """The reference's CPU path on a bounded sample of the ensemble: members
+    0, 16, ..., 240, one single-threaded process each (the reference runs an
+    ensemble as one job per process, EXAMPLES/EXAMPLE_ENSEMBLE_ETNA/
+    launch_jobs.py), all started together after `warmup_steps` untimed steps;
+    the K bench steps cover CPU_SAMPLE_STEPS time steps of each member.
+    Rate = cell updates of all members / wall time of the slowest."""
+    members = list(range(0, ENS_RUNS, CPU_SAMPLE_EVERY))
+    chunk = max(1, CPU_SAMPLE_STEPS // K)
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as mgr:
+        barrier = mgr.Barrier(len(members) + 1)
+        with ctx.Pool(processes=len(members)) as pool:
+            res = pool.map_async(_cpu_member_worker,
+                                 [(m, warmup_steps, K, chunk, barrier) for m in members])
+            barrier.wait()
+            t0 = time.perf_counter()
+            out = res.get()
+            wall = time.perf_counter() - t0
+    cells = sum(c for c, _ in out)
+    return {"value": cells / wall, "unit": UNIT, "cores": min(cores, len(members)), "kind": "port",
+            "sample": (f"members {members[0]}..{members[-1]} every {CPU_SAMPLE_EVERY} ({len(members)} runs, "
+                       f"one single-threaded process each) x {K * chunk} steps after {warmup_steps} "
+                       f"untimed steps: {cells} cell updates in {wall:.2f} s; oracle C restatement "
+                       f"built -Ofast -funroll-all-loops -fopenmp (the reference's flags)"),
+            "steps": K, "chunk_steps": chunk, "seconds": wall, "cell_updates": cells}
+
+
+def _oracle_member_worker(index):
+    """One member over its 2000 steps with the oracle's parity build (one
+    host core); returns (index, q)."""
+    import oracle
+    oracle.set_threads(1)
+    p, B, q, steps = W.ensemble_params(index, PREC_FP64, ENS_STEPS)
+    o = oracle.Oracle(p, B)
+    o.set_q(W.to_aos(q))
+    o.run(max_steps=steps)
+    qo = o.q()
+    o.close()
+    return index, qo
+
+
+# ---------------------------------------------------------------------------
+# GPU ensemble legs
+# ---------------------------------------------------------------------------
+
+def ensemble_members(precision, n_runs):
+    return [W.ensemble_params(i, precision, ENS_STEPS) for i in range(n_runs)]
+
+
+def ensemble_batch(lib, precision, members, tile_h):
+    cells = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members)
+    b = lib.Batch(precision, max_runs=len(members), max_cells=int(cells * 1.2) + 4096)
+    if tile_h:
+        b.set_tile_shape(tile_h)
+    return b
+
+
+def ensemble_submit(b, members):
+    ids = []
+    for p, B, q, st in members:
+        rid = b.submit(p, B, W.to_aos(q), max_steps=st)
+        if rid is None:
+            raise RuntimeError("ensemble member not admitted")
+        ids.append(rid)
+    return ids
+
+
+def ensemble_timed(lib, precision, members, K, chunk, tile_h, keep=()):
+    """Submit every member (untimed), then the K bench steps of `chunk`
+    batch steps each, device-timed.  Returns the record and the final q of
+    the members in `keep`."""
+    b = ensemble_batch(lib, precision, members, tile_h)
+    ids = ensemble_submit(b, members)
+    l0 = b.launch_count()
+    ms = []
+    for _ in range(K):
+        _, m = b.advance_timed(chunk)
+        ms.append(m)
+    launches = b.launch_count() - l0
+    cu = sum(b.counters(i)["cell_updates"] for i in ids)
+    border = sum(b.dry_border_updates(i) for i in ids)
+    steps = [b.counters(i)["steps"] for i in ids]
+    status = 0
+    for i in ids:
+        st, _ = b.poll(i)
+        status |= int(st.status)
+    kept = {k: b.download(ids[k]) for k in keep}
+    b.close()
+    dense = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members) * ENS_STEPS
+    tot_ms = float(sum(ms))
+    return {"runs": len(members), "steps_per_run": ENS_STEPS, "bench_steps": K,
+            "batch_steps_per_bench_step": chunk,
+            "cell_updates": cu, "dry_border_updates": border, "computed_cell_updates": cu - border,
+            "dense_cell_steps": dense, "active_fraction": cu / dense,
+            "device_ms": tot_ms, "ms_per_bench_step": tot_ms / K, "value": cu / (tot_ms / 1e3),
+            "computed_value": (cu - border) / (tot_ms / 1e3), "unit": UNIT,
+            "gpu_launches": launches, "min_steps_done": min(steps), "status_bits": status}, kept
+
+
+def ensemble_profile(lib, members, tile_h, at_step, steps):
+    """Per-kernel device time of `steps` batch steps of the FP32 ensemble
+    from batch step `at_step` (events between the five kernels)."""
+    b = ensemble_batch(lib, PREC_FP32, members, tile_h)
+    ids = ensemble_submit(b, members)
+    b.advance(at_step)
+    c0 = sum(b.counters(i)["cell_updates"] for i in ids)
+    d0 = sum(b.dry_border_updates(i) for i in ids)
+    ms = b.profile_kernels(steps)
+    c1 = sum(b.counters(i)["cell_updates"] for i in ids)
+    d1 = sum(b.dry_border_updates(i) for i in ids)
+    b.close()
+    return ms, (c1 - c0) / steps, ((c1 - c0) - (d1 - d0)) / steps
+
+
+def ensemble_e2e(lib, members, K, chunk, tile_h):
+    """The ensemble through the C ABI from host buffers: submit (host set-up
+    and upload), K bench steps, collect with the download of q; wall clock."""
+    b = ensemble_batch(lib, PREC_FP32, members, tile_h)
+    qs = [W.to_aos(q) for _, _, q, _ in members]
+    t0 = time.perf_counter()
+    ids = []
+    for (p, B, _, st), qa in zip(members, qs):
+        rid = b.submit(p, B, qa, max_steps=st)
+        if rid is None:
+            raise RuntimeError("ensemble member not admitted")
+        ids.append(rid)
+    for _ in range(K):
+        b.advance(chunk)
+    cu = 0
+    out_bytes = 0
+    for rid in ids:
+        cu += b.counters(rid)["cell_updates"]
+        q = b.collect(rid, want_q=True)
+        out_bytes += q.nbytes
+    wall = time.perf_counter() - t0
+    b.close()
+    in_bytes = sum(qa.nbytes + B.size * 8 for (p, B, _, _), qa in zip(members, qs))
+    return {"value": cu / wall, "unit": UNIT, "h2d_bytes_per_step": in_bytes / K,
+            "d2h_bytes_per_step": out_bytes / K, "seconds": wall, "steps": K,
+            "path": "sflow_batch_submit (host set-up + upload) of every run, sflow_batch_advance, "
+                    "sflow_batch_collect with q download; host buffers, wall clock"}
+
+
+def warm_up(lib, precision, members, tile_h, steps):
+    """Untimed: a scratch batch of every 8th member advanced `steps` batch
+    steps (graph capture, module loading, allocator and cache warm-up)."""
+    sample = members[::8]
+    b = ensemble_batch(lib, precision, sample, tile_h)
+    ensemble_submit(b, sample)
+    b.advance(steps)
+    b.close()
+
+
+# ---------------------------------------------------------------------------
+# single 1024^2 current
+# ---------------------------------------------------------------------------
+
+def current_workload(precision):
+    p, B, _ = W.pyroclastic(nx=1024, ny=1024, dx=10.0, settling=False, precision=precision,
+                            t_end=1.0e9)
+    q = W.developed_current_state(p, B)
+    return p, B, q
 
 
 def autotune_run(s, qa, warmup, steps):
@@ -267,15 +462,11 @@ def autotune_run(s, qa, warmup, steps):
             "tuner": "sflow_autotune (CUDA events over graph-replayed steps of this run)"}
 
 
-def timed_form(lib, p, B, q, steps, warmup, flush=True, tune_steps=0, tile_h=None):
+def timed_form(lib, p, B, q, steps, warmup, flush=True, tile_h=None):
     s = lib.Solver(p, B)
-    qa = W.to_aos(q)
-    tune = None
-    if tune_steps > 0:
-        tune = autotune_run(s, qa, warmup, tune_steps)
-    elif tile_h:
+    if tile_h:
         s.set_tile_shape(tile_h)
-    s.upload_q(qa)
+    s.upload_q(W.to_aos(q))
     s.advance(max_steps=warmup)
     c0 = s.counters()
     l0 = s.launch_count()
@@ -285,117 +476,103 @@ def timed_form(lib, p, B, q, steps, warmup, flush=True, tune_steps=0, tile_h=Non
     cells = c1["cell_updates"] - c0["cell_updates"]
     return s, {"ms": ms, "cells": cells, "steps": c1["steps"] - c0["steps"],
                "launches": l1 - l0, "newton_iters": c1["newton_iters"] - c0["newton_iters"],
-               "newton_max": c1["newton_max"], "autotune": tune, "tile_h": s.tile_shape()}
+               "newton_max": c1["newton_max"], "tile_h": s.tile_shape()}
 
 
-def ensemble_leg(lib, n_runs, steps, tune=True):
-    """Batched ensemble: n_runs independent ring-inlet runs (side log-uniform
-    in [128, 1024], dx U[5, 20] m, own DEM seed, mu, xi, source radius and
-    temperature, particle fractions; workloads.ensemble_params) resident
-    together and advanced `steps` steps each by the batched engine (FP32
-    bulk form, FP64 Newton).  Inputs are uploaded before the timed region;
-    the timed region is the batch advance until every run has stopped."""
-    ts = time.perf_counter()
-    members = [W.ensemble_params(i, PREC_FP32, steps) for i in range(n_runs)]
-    cells = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members)
-    print(f"[bench] ensemble inputs: {n_runs} runs, {cells} cells, {time.perf_counter() - ts:.1f} s",
-          file=sys.stderr, flush=True)
-    tuned = None
-    if tune:
-        # every 8th member, 128 batch steps per tile height, in a scratch batch
-        from imex_sflow2d_dev_gb300 import autotune as A
+def current_leg(lib, steps, warmup, tune_steps, peak, peak_kind):
+    """The single 1024^2 current (the benchmark configurations' second case)
+    from a seeded developed state: FP32 and FP64 forms, event-timed single
+    steps with L2 flushed between them, per-kernel times, k_flux roofline,
+    and e2e through sflow_put_q / sflow_step / sflow_download_q from pinned
+    host memory."""
+    p32, B, q = current_workload(PREC_FP32)
+    p64 = p32.copy()
+    p64.precision = PREC_FP64
+    nx, ny, nv = p32.comp_cells_x, p32.comp_cells_y, p32.n_vars
+    tune = None
+    if tune_steps > 0:
+        st = lib.Solver(p32, B)
+        tune = autotune_run(st, W.to_aos(q), warmup, tune_steps)
+        st.close()
+    th = tune["tile_h"] if tune else None
+    s32, r32 = timed_form(lib, p32, B, q, steps, warmup, tile_h=th)
+    s32.close()
+    s64, r64 = timed_form(lib, p64, B, q, max(steps // 5, 3), warmup)
+    s64.close()
+    v32 = r32["cells"] / (r32["ms"] / 1e3)
+    v64 = r64["cells"] / (r64["ms"] / 1e3)
+    pk = lib.Solver(p32, B)
+    pk.set_tile_shape(r32["tile_h"])
+    pk.upload_q(W.to_aos(q))
+    pk.advance(max_steps=warmup)
+    c0 = pk.counters()
+    kms = pk.profile_kernels(max(steps // 2, 3), flush_l2=True)
+    c1 = pk.counters()
+    pk.close()
+    pk_steps = max(c1["steps"] - c0["steps"], 1)
+    pk_cells = (c1["cell_updates"] - c0["cell_updates"]) / pk_steps
+    alg = (2 * nv + 5) * 4 + 2       # q, 5 topography terms, flag + mask bytes, write divFlux - expl
+    dur_s = kms["flux"] / 1e3 / pk_steps
+    achieved = alg * pk_cells / dur_s / 1e9
+    prof = read_profile("k_flux_pyroclastic_traffic")
+    traffic = prof["bytes_per_active_cell"] * pk_cells if prof and prof.get("bytes_per_active_cell") else None
+    out = {"workload": "pyroclastic current 1024x1024 dx=10m, ring inlet 1e6 kg/s, 2 classes, Voellmy, "
+                       "N_RK=2, seeded developed state, L2 flushed between event-timed steps",
+           "fp32": {"value": v32, "ms_per_step": r32["ms"] / max(r32["steps"], 1), "steps": r32["steps"],
+                    "active_cells_per_step": r32["cells"] / max(r32["steps"], 1), "tile_h": r32["tile_h"],
+                    "newton_iters_per_cell": r32["newton_iters"] / max(r32["cells"], 1)},
+           "fp64_plain": {"value": v64, "ms_per_step": r64["ms"] / max(r64["steps"], 1), "steps": r64["steps"]},
+           "speedup_fp32_over_fp64": v32 / v64 if v64 else None, "autotune": tune,
+           "kernel_ms_per_step": {k: v / pk_steps for k, v in kms.items()},
+           "roofline_k_flux": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                               "alg_bytes_per_active_cell": alg}}
+    try:
+        import torch
+        pinned = torch.empty(nx * ny * nv, dtype=torch.float64, pin_memory=True)
+        pinned.numpy()[:] = W.to_aos(q)
+        se = lib.Solver(p32, B)
+        se.set_tile_shape(r32["tile_h"])
+        se.upload_q(W.to_aos(q))
+        se.advance(max_steps=warmup)
+        ptr = pinned.data_ptr()
+        ne = max(steps // 5, 3)
+        c0 = se.counters()
+        se.download_q_ptr(ptr)
         t0 = time.perf_counter()
-        sample = [(p, B, W.to_aos(q)) for p, B, q, _ in members[::8]]
-        best, rates = A.tune_batch(PREC_FP32, sample, steps=128)
-        tuned = {"tile_h": best, "cell_updates_per_s": {str(k): v for k, v in rates.items()},
-                 "sample": f"{len(sample)} runs (every 8th member), 16 + 128 batch steps per height",
-                 "seconds": time.perf_counter() - t0, "tuner": "autotune.tune_batch"}
-        print(f"[bench] ensemble autotune: {tuned}", file=sys.stderr, flush=True)
-    b = lib.Batch(PREC_FP32, max_runs=n_runs, max_cells=int(cells * 1.2) + 4096)
-    if tuned:
-        b.set_tile_shape(tuned["tile_h"])
-    ids = []
-    for p, B, q, st in members:
-        rid = b.submit(p, B, W.to_aos(q), max_steps=st)
-        if rid is None:
-            raise RuntimeError("ensemble member not admitted")
-        ids.append(rid)
-    print(f"[bench] ensemble submitted: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
-    l0 = b.launch_count()
-    t0 = time.perf_counter()
-    while True:
-        fin = b.advance(64)
-        if fin == len(ids):
-            break
-    dt = time.perf_counter() - t0
-    print(f"[bench] ensemble advanced: {dt:.1f} s", file=sys.stderr, flush=True)
-    launches = b.launch_count() - l0
-    cu = sum(b.counters(i)["cell_updates"] for i in ids)
-    dense = sum(m[0].comp_cells_x * m[0].comp_cells_y for m in members) * steps
-    b.close()
-    return {"runs": n_runs, "steps_per_run": steps, "cells_total": cells,
-            "cell_updates": cu, "dense_cell_steps": dense, "seconds": dt,
-            "value": cu / dt, "unit": UNIT, "gpu_launches": launches,
-            "timing": "host clock around the batch advance calls (each ends synchronised)",
-            "autotune": tuned}
-
-
-def step_bytes(n_vars, word=4, n_geo=5, deposit_classes=0):
-    """Algorithmic bytes of one cell update of the whole N_RK = 2 step in one
-    pass: read q and write q, read and write the stage increment once
-    (3 n words), the topography terms and g_c (n_geo + 1 words), the three
-    maxima maps read and written (24 B) and, with settling, the FP64
-    deposit of each class read and written (16 B a class)."""
-    return 3 * n_vars * word + (n_geo + 1) * 4 + 24 + 16 * deposit_classes
-
-
-def form_errors(lib, p, B, q, steps):
-    """L1 and Linf relative errors of h, hu, hv, alpha_s and T of the FP32
-    bulk form against the plain FP64 form after `steps` steps from the same
-    state (the FP64 form matches the CPU oracle to 1e-10 in the parity
-    tests, so it stands in for the oracle at sizes the oracle cannot run in
-    seconds)."""
-    nx, ny, nv = p.comp_cells_x, p.comp_cells_y, p.n_vars
-    out = {}
-    res = {}
-    for prec in (PREC_FP32, PREC_FP64):
-        pp = p.copy()
-        pp.precision = prec
-        s = lib.Solver(pp, B)
-        s.upload_q(W.to_aos(q))
-        s.advance(max_steps=steps)
-        res[prec] = (W.from_aos(s.download_q(), nv, nx, ny), W.from_aos(s.download_qp(), nv + 2, nx, ny))
-        s.close()
-    (q32, qp32), (q64, qp64) = res[PREC_FP32], res[PREC_FP64]
-    fields = {"h": (qp32[0], qp64[0]), "hu": (q32[1], q64[1]), "hv": (q32[2], q64[2]),
-              "T": (qp32[3], qp64[3])}
-    for i in range(p.n_solid):
-        fields[f"alpha_s{i + 1}"] = (qp32[4 + i], qp64[4 + i])
-    for n, (a, r) in fields.items():
-        if n == "T":   # temperature of wet cells only (dry cells carry T_ambient)
-            wet = qp64[0] > 0
-            a, r = a[wet], r[wet]
-        out[n] = {"l1_rel": float(np.abs(a - r).sum() / max(np.abs(r).sum(), 1e-300)),
-                  "linf_rel": float(np.abs(a - r).max() / max(np.abs(r).max(), 1e-300)) if r.size else 0.0}
+        for _ in range(ne):
+            se.put_q_ptr(ptr)
+            se.step()
+            se.download_q_ptr(ptr)
+        te = time.perf_counter() - t0
+        c1 = se.counters()
+        se.close()
+        nbytes = nx * ny * nv * 8
+        out["e2e"] = {"value": (c1["cell_updates"] - c0["cell_updates"]) / te, "unit": UNIT,
+                      "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": ne,
+                      "path": "sflow_put_q + sflow_step + sflow_download_q, pinned host buffers"}
+    except Exception as exc:  # pragma: no cover - reported, not hidden
+        out["e2e"] = {"value": None, "error": str(exc)}
     return out
 
 
+# ---------------------------------------------------------------------------
+# large domain and served legs
+# ---------------------------------------------------------------------------
+
 def large_leg(lib, n, steps, warmup, tune_steps=16):
-    """Large single domain: n x n cells, dx = 2 m, diamond-square DEM
-    (Hurst 0.8, relief 2000 m, seed 5), 3 particle classes (1e-5, 1e-4,
-    1e-3 m), entrainment and settling on, one ring inlet, from a seeded
-    developed current of radius 3.5 km (workloads.large_domain).  The
-    working set (~12 GB in FP32) is far larger than L2, so steps are timed
-    back to back; the plain FP64 form is timed beside it on fewer steps and
-    the FP32-vs-FP64 errors are taken after `steps` steps."""
+    """One n x n domain, dx = 2 m, diamond-square DEM (Hurst 0.8, relief
+    2000 m, seed 5), 3 particle classes, entrainment and settling, one ring
+    inlet, from a seeded developed current; timed back to back (the ~12 GB
+    working set is far larger than L2)."""
     ts = time.perf_counter()
     p32, B, _ = W.large_domain(n=n, precision=PREC_FP32)
     q = W.developed_current_state(p32, B, radius=min(3500.0, 0.2 * n * p32.cell_size))
     qa = W.to_aos(q)
     del q
-    print(f"[bench] large inputs {n}x{n}: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
-    out = {"cells": n * n, "steps": steps, "workload":
-           f"{n}x{n} dx=2m diamond-square DEM, 3 classes, entrainment + settling, ring inlet, developed current"}
+    out = {"cells": n * n, "workload": f"{n}x{n} dx=2m diamond-square DEM, 3 classes, entrainment + "
+                                       f"settling, ring inlet, developed current"}
+    res = {}
     for name, prec, nst in (("fp32", PREC_FP32, steps), ("fp64_plain", PREC_FP64, max(steps // 5, 2))):
         pp = p32.copy()
         pp.precision = prec
@@ -412,258 +589,285 @@ def large_leg(lib, n, steps, warmup, tune_steps=16):
                      "active_cells_per_step": cu / nst, "tile_h": s.tile_shape()}
         s.close()
     out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64_plain"]["value"]
-    out["error_vs_fp64"] = {"steps": steps, **form_errors(lib, p32, B, W.from_aos(qa, p32.n_vars, n, n), steps)}
-    print(f"[bench] large done: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
+    # FP32 against FP64 after `steps` steps from the same state
+    for prec in (PREC_FP32, PREC_FP64):
+        pp = p32.copy()
+        pp.precision = prec
+        s = lib.Solver(pp, B)
+        s.upload_q(qa)
+        s.advance(max_steps=steps)
+        res[prec] = s.download_qp()
+        s.close()
+    out["error_vs_fp64"] = {"steps": steps, **field_errors(p32, res[PREC_FP32], res[PREC_FP64])}
+    out["seconds"] = time.perf_counter() - ts
     return out
 
 
-def served_leg(lib, n_requests, rate, tile_h=None):
+def served_leg(lib, n_requests, rate, probe_steps, tile_h=None):
     """Served solves: Poisson arrivals (mean `rate` per s) of dam-break and
     ring-inlet jobs (side log-uniform in [64, 2048], 1-3 classes, 500-5000
     steps; workloads.served_job) through the request loop (continuous
-    batching).  Job inputs are prepared before the clock starts; time to
-    solution = finish - arrival."""
+    batching, host preparation on worker threads).  Job inputs are built
+    before the clock starts; time to solution = finish - arrival.
+
+    Beside it, the same stream served one job at a time by the plain FP64
+    form through a handle: every job's FP64 service time is measured on its
+    own first `probe_steps` steps (set-up, upload and graph-replayed steps,
+    wall clock) and scaled to its step count, and the stream is queued first
+    come first served on those times.  Running the stream itself one job at
+    a time would take ~20 minutes; a few jobs small enough to run whole in a
+    few seconds are run whole, and their measured and scaled service times
+    are reported together as a check of the scaling."""
     from imex_sflow2d_dev_gb300 import serve as S
-    ts = time.perf_counter()
     jobs = [W.served_job(i, PREC_FP32) for i in range(n_requests)]
-    print(f"[bench] served inputs: {time.perf_counter() - ts:.1f} s", file=sys.stderr, flush=True)
     arr = W.poisson_arrivals(n_requests, rate)
     reqs = [S.Request(i, arr[i], p, B, q, st, kind) for i, (p, B, q, st, kind) in enumerate(jobs)]
     cells = sum(p.comp_cells_x * p.comp_cells_y for p, *_ in jobs)
     loop = S.RequestLoop(PREC_FP32, max_runs=64, max_cells=int(cells * 1.2) + 4096, chunk=16,
                          tile_h=tile_h)
     recs = loop.run(reqs)
-    print(f"[bench] served: {max(r['finished_s'] for r in recs):.1f} s", file=sys.stderr, flush=True)
     launches = loop.batch.launch_count()
     loop.close()
     out = S.summarize(recs)
-    out.update({"rate_per_s": rate, "gpu_launches": launches, "tile_h": tile_h or 8,
-                "jobs": [{k: r[k] for k in ("kind", "cells", "n_solid", "steps", "tts_s")} for r in recs]})
-    return out, recs
-
-
-def fp64_one_at_a_time(recs, fp64_rate):
-    """Time to solution of the same request stream served one job at a time
-    by the plain FP64 form, modelled from the measured FP64 cell-update rate
-    (each job's service time = its cell updates / rate; first come, first
-    served)."""
-    order = sorted(recs, key=lambda r: r["arrival_s"])
-    t = 0.0
+    out.update({"rate_per_s": rate, "gpu_launches": launches, "tile_h": tile_h or 8})
+    # one job at a time, plain FP64 form
+    t0 = time.perf_counter()
+    service = []
+    check = []
+    for i, (p, B, q, st, kind) in enumerate(jobs):
+        p64 = p.copy()
+        p64.precision = PREC_FP64
+        n = min(probe_steps, st)
+        ts = time.perf_counter()
+        s = lib.Solver(p64, B)
+        s.upload_q(W.to_aos(q))
+        s.advance(max_steps=n)
+        probe = time.perf_counter() - ts
+        est = probe * st / n
+        if p.comp_cells_x <= 128 and len(check) < 6:
+            s.advance(max_steps=st - n)
+            whole = time.perf_counter() - ts
+            check.append({"request": i, "steps": st, "measured_s": whole, "scaled_s": est})
+        s.close()
+        service.append(est)
+    clock = 0.0
     tts = []
-    for r in order:
-        t = max(t, r["arrival_s"]) + r["cell_updates"] / fp64_rate
-        tts.append(t - r["arrival_s"])
+    for i in np.argsort(arr, kind="stable"):
+        clock = max(clock, arr[i]) + service[i]
+        tts.append(clock - arr[i])
     tts = np.array(tts)
-    total = sum(r["cell_updates"] for r in order)
-    return {"p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
-            "cell_updates_per_s": total / (t - order[0]["arrival_s"]),
-            "basis": "modelled from the measured plain-FP64 cell-update rate of the main workload"}
+    total_cu = sum(r["cell_updates"] for r in recs)
+    span = clock - float(arr.min())
+    out["fp64_one_at_a_time"] = {
+        "requests": n_requests, "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
+        "makespan_s": span, "cell_updates_per_s": total_cu / max(span, 1e-12),
+        "probe_steps": probe_steps, "probe_seconds": time.perf_counter() - t0,
+        "whole_job_check": check,
+        "basis": ("each job's plain-FP64 service time measured over its first steps (set-up, upload, "
+                  "graph-replayed steps) and scaled to its step count; FCFS queue on the stream's "
+                  "arrival times")}
+    out["jobs"] = [{k: r[k] for k in ("kind", "cells", "n_solid", "steps", "tts_s")} for r in recs]
+    return out
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_reference(args, d):
+    """The reference arm: the reference's CPU path (the oracle, built with
+    the reference's compiler flags) on a bounded sample of the same
+    ensemble, same K and W."""
+    if d.rank != 0:
+        return 0
+    cb = cpu_ensemble_sample(args.steps, args.warmup * max(1, CPU_SAMPLE_STEPS // args.steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * cb["seconds"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded DEMs and per-run draws)",
+        "config": {"workload": WORKLOAD, "precision": "FP64 CPU",
+                   "bench_step": f"{cb['chunk_steps']} time steps of every sampled member",
+                   "implementation": "oracle/sflow_oracle.c (C restatement of the Fortran reference, "
+                                     "which has no compiler on this box), reference compiler flags"},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def log(msg):
+    print(f"[bench] {msg}", file=sys.stderr, flush=True)
 
 
 def run_gb300(args, d):
     from imex_sflow2d_dev_gb300 import lib
     lib.load()
-    p32, B, q = build_workload(PREC_FP32)
-    p64 = p32.copy()
-    p64.precision = PREC_FP64
-    nx, ny, nv = p32.comp_cells_x, p32.comp_cells_y, p32.n_vars
+    K, Wm = args.steps, args.warmup
+    chunk = int(math.ceil(ENS_STEPS / K))
+    peak, peak_kind = read_peaks()
+    n_runs = args.ensemble_runs
 
-    # tile height of the FP32 form: autotuned on the workload before the
-    # timed region (the plain FP64 form has one compiled height)
-    tune = None
-    if args.tile_h:
-        tune = {"tile_h": args.tile_h, "tuner": "fixed by --tile-h"}
-    elif args.tune_steps > 0:
-        st = lib.Solver(p32, B)
-        tune = autotune_run(st, W.to_aos(q), args.warmup, args.tune_steps)
-        st.close()
+    cb = None
+    if d.rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_ensemble_sample(K, Wm * max(1, CPU_SAMPLE_STEPS // K))
+        log(f"cpu baseline {cb['value']:.3e}")
+
+    members32 = ensemble_members(PREC_FP32, n_runs)
+    members64 = ensemble_members(PREC_FP64, n_runs)
+    tuned = None
+    th = args.tile_h or None
+    if not th and args.tune_steps > 0:
+        from imex_sflow2d_dev_gb300 import autotune as A
+        t0 = time.perf_counter()
+        sample = [(p, B, W.to_aos(q)) for p, B, q, _ in members32[::8]]
+        best, rates = A.tune_batch(PREC_FP32, sample, steps=128)
+        tuned = {"tile_h": best, "cell_updates_per_s": {str(k): v for k, v in rates.items()},
+                 "sample": f"{len(sample)} runs (every 8th member), 16 + 128 batch steps per height",
+                 "seconds": time.perf_counter() - t0, "tuner": "autotune.tune_batch"}
+        th = best
+    warm_up(lib, PREC_FP32, members32, th, Wm * chunk)
+
+    # timed region: the FP32 ensemble, K bench steps
+    err_members = sorted(range(n_runs), key=lambda i: members32[i][0].comp_cells_x)[:args.oracle_members]
     clocks = ClockSampler(d.local)
     d.barrier()
     clocks.start()
     t_wall0 = time.perf_counter()
-    s32, r32 = timed_form(lib, p32, B, q, args.steps, args.warmup, tile_h=tune["tile_h"] if tune else None)
+    r32, q32 = ensemble_timed(lib, PREC_FP32, members32, K, chunk, th, keep=err_members)
     t_wall1 = time.perf_counter()
     clk = clocks.stop()
     d.barrier()
-    value, ms_max = aggregate(d, r32["cells"], r32["ms"])
+    value, ms_max = aggregate(d, r32["cell_updates"], r32["device_ms"])
+    log(f"ensemble fp32 {value:.3e} ({r32['device_ms']:.1f} ms)")
 
-    # plain FP64 form, same start state and step count
-    s64, r64 = timed_form(lib, p64, B, q, max(args.steps // 5, 3), args.warmup)
-    value64 = r64["cells"] / (r64["ms"] / 1e3)
-    # FP32 vs FP64 after the same number of steps from the same state
-    nerr = 20
-    errs = form_errors(lib, p32, B, q, nerr)
+    # the oracle on the smallest members (host cores) while the GPU runs FP64
+    pool = res_or = None
+    if d.rank == 0 and args.oracle_members > 0:
+        ctx = mp.get_context("spawn")
+        pool = ctx.Pool(processes=len(err_members))
+        res_or = pool.map_async(_oracle_member_worker, err_members)
+    warm_up(lib, PREC_FP64, members64, None, 16)
+    r64, q64 = ensemble_timed(lib, PREC_FP64, members64, K, chunk, None, keep=err_members)
+    value64 = r64["value"]
+    log(f"ensemble fp64 {value64:.3e} ({r64['device_ms']:.1f} ms)")
+    err_fp64, err_oracle = [], []
+    if res_or is not None:
+        orc = dict(res_or.get())
+        pool.close()
+        pool.join()
+        for k in err_members:
+            p, B = members64[k][0], members64[k][1]
+            err_oracle.append(field_errors(p, qp_of_state(p, B, q32[k]), qp_of_state(p, B, orc[k])))
+            err_fp64.append(float(np.abs(q64[k] - orc[k]).max() / max(np.abs(orc[k]).max(), 1e-300)))
 
-    # per-kernel device time (events between the kernels of each step)
-    pk = lib.Solver(p32, B)
-    pk.set_tile_shape(r32["tile_h"])
-    pk.upload_q(W.to_aos(q))
-    pk.advance(max_steps=args.warmup)
-    c0 = pk.counters()
-    kms = pk.profile_kernels(max(args.steps // 2, 3), flush_l2=True)
-    c1 = pk.counters()
-    pk_steps = c1["steps"] - c0["steps"]
-    pk_cells = (c1["cell_updates"] - c0["cell_updates"]) / max(pk_steps, 1)
-    pk.close()
-    dom = max(("flux", "stage"), key=lambda k: kms[k])
-    s4 = 4  # FP32 bytes
-    n = nv
-    # algorithmic bytes per active cell (reads + writes a launch must do):
-    #  flux : q (n) + topography terms for the explicit sources (5) + flag and
-    #         mask bytes, write divFlux - expl (n)
-    #  stage: q (n) + divFlux - expl (n) + 3 topography terms + mask byte,
-    #         write q (n), read+write 3 maxima maps
-    alg = {"flux": (2 * n + 5) * s4 + 2, "stage": (3 * n + 3 + 6) * s4 + 1}
-    bytes_launch = alg[dom] * pk_cells
-    dur_s = kms[dom] / 1e3 / max(pk_steps, 1)
-    achieved = bytes_launch / dur_s / 1e9
-    peak, peak_kind = read_peaks()
-    tr = read_traffic()
-    traffic = None
-    if tr and tr.get("kernel") == dom and tr.get("bytes_per_active_cell"):
-        traffic = tr["bytes_per_active_cell"] * pk_cells
+    # e2e through the C ABI from host buffers
+    e2e = ensemble_e2e(lib, members32, K, chunk, th)
+    log(f"ensemble e2e {e2e['value']:.3e}")
 
-    # end to end through the C ABI, state in pinned host memory every step
-    e2e = None
-    try:
-        import torch
-        pinned = torch.empty(nx * ny * nv, dtype=torch.float64, pin_memory=True)
-        pinned.numpy()[:] = W.to_aos(q)
-        se = lib.Solver(p32, B)
-        se.set_tile_shape(r32["tile_h"])
-        se.upload_q(W.to_aos(q))
-        se.advance(max_steps=args.warmup)
-        ptr = pinned.data_ptr()
-        ne = max(args.steps // 5, 3)
-        c0 = se.counters()
-        se.download_q_ptr(ptr)
-        t0 = time.perf_counter()
-        for _ in range(ne):
-            se.put_q_ptr(ptr)
-            se.step()
-            se.download_q_ptr(ptr)
-        te = time.perf_counter() - t0
-        c1 = se.counters()
-        nbytes = nx * ny * nv * 8
-        e2e = {"value": d.sum((c1["cell_updates"] - c0["cell_updates"])) / d.max(te),
-               "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "steps": ne,
-               "path": "sflow_put_q + sflow_step + sflow_download_q, pinned host buffers",
-               "ms_per_step": te / ne * 1e3}
-        # where the time goes: the two host transfers alone, and plain
-        # copy-engine copies of the same pinned buffer (the host link's rate)
-        dev = torch.empty(nx * ny * nv, dtype=torch.float64, device="cuda")
+    # per-kernel device times of the developed ensemble and the roofline of
+    # its dominant kernel (algorithmic bytes per computed cell: the dry
+    # border tiles are counted but not touched)
+    kms, cells_launch, computed_launch = ensemble_profile(lib, members32, th, ENS_STEPS // 2, 16)
+    dom = max(kms, key=lambda k: kms[k])
+    nv = 6
+    alg_bytes = {"flux": (2 * nv + 5) * 4 + 2,           # q, 5 topography terms, flags, write divFlux - expl
+                 "stage": (3 * nv + 3 + 6) * 4 + 1 + 32,  # q, increment, 3 topography, maps rw, mask, deposit rw
+                 "mask": 4 + 1 + 1, "cand": 0, "dt": 0}
+    launch_s = kms[dom] / 1e3 / 16
+    achieved = alg_bytes[dom] * computed_launch / launch_s / 1e9
+    prof = read_profile("k_b_flux_ensemble_256") if dom == "flux" else None
+    traffic = (prof["dram_bytes_per_computed_cell"] * computed_launch
+               if prof and prof.get("dram_bytes_per_computed_cell") else None)
+    roofline = {"bound": "hbm", "kernel": "k_b_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "alg_bytes_per_computed_cell": alg_bytes[dom],
+                "computed_cells_per_launch": computed_launch, "active_cells_per_launch": cells_launch,
+                "kernel_ms_per_step": {k: v / 16 for k, v in kms.items()},
+                "kernel_share": {k: v / sum(kms.values()) for k, v in kms.items()},
+                "profile_window": f"16 batch steps from step {ENS_STEPS // 2}, events between kernels"}
+    if prof and prof.get("warp_inst_per_computed_cell") and prof.get("issue_peak_warp_inst_per_s"):
+        roofline["issue_frac"] = (prof["warp_inst_per_computed_cell"] * computed_launch / launch_s
+                                  / prof["issue_peak_warp_inst_per_s"])
+    log(f"profile {roofline['kernel_ms_per_step']}")
 
-        def wall_ms(fn, n=8):
-            fn()
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            for _ in range(n):
-                fn()
-            torch.cuda.synchronize()
-            return (time.perf_counter() - t) / n * 1e3
-
-        split = {"put_ms": wall_ms(lambda: se.put_q_ptr(ptr)),
-                 "download_ms": wall_ms(lambda: se.download_q_ptr(ptr)),
-                 "dma_h2d_ms": wall_ms(lambda: dev.copy_(pinned, non_blocking=True)),
-                 "dma_d2h_ms": wall_ms(lambda: pinned.copy_(dev, non_blocking=True))}
-        for k in list(split):
-            split[k.replace("_ms", "_GBs")] = nbytes / (split[k] * 1e-3) / 1e9
-        e2e["transfers"] = split
-        del dev
-        se.close()
-    except Exception as exc:  # pragma: no cover - reported, not hidden
-        e2e = {"value": None, "unit": UNIT, "error": str(exc)}
-
-    cb = None
-    if d.rank == 0 and not args.no_cpu_baseline:
-        cb = cpu_baseline(p64, B, q, max_seconds=args.cpu_seconds, max_steps=40)
-
-    ens = None
-    if d.rank == 0 and args.ensemble_runs > 0:
-        ens = ensemble_leg(lib, args.ensemble_runs, args.ensemble_steps, tune=args.tune_steps > 0)
-        ens["speedup_vs_fp64_plain"] = ens["value"] / value64 if value64 else None
-        sb = step_bytes(6, deposit_classes=2)   # every member: 2 settling classes, FP32 state
-        ens["hbm_roofline"] = {"bytes_per_cell_update": sb, "achieved_GBs": ens["value"] * sb / 1e9,
-                               "peak_GBs": peak, "frac": ens["value"] * sb / 1e9 / peak,
-                               "peak_kind": peak_kind}
-        pe, Be, qe, _ = W.ensemble_params(0, PREC_FP32, 300)
-        ens["error_vs_fp64"] = {"member": 0, "side": pe.comp_cells_x, "steps": 300,
-                                **form_errors(lib, pe, Be, qe, 300)}
+    cur = None
+    if d.rank == 0 and args.current_steps > 0:
+        cur = current_leg(lib, args.current_steps, Wm, args.tune_steps, peak, peak_kind)
+        log(f"current 1024 {cur['fp32']['value']:.3e}")
     large = None
     if d.rank == 0 and args.large_n > 0:
-        large = large_leg(lib, args.large_n, args.large_steps, args.warmup,
-                          tune_steps=16 if args.tune_steps > 0 else 0)
+        large = large_leg(lib, args.large_n, args.large_steps, Wm, tune_steps=16 if args.tune_steps > 0 else 0)
+        log(f"large {large['fp32']['value']:.3e}")
     srv = None
     if d.rank == 0 and args.served_requests > 0:
-        srv, recs = served_leg(lib, args.served_requests, args.served_rate,
-                               tile_h=ens["autotune"]["tile_h"] if ens and ens.get("autotune") else None)
-        srv["fp64_one_at_a_time"] = fp64_one_at_a_time(recs, value64)
+        srv = served_leg(lib, args.served_requests, args.served_rate, args.served_probe_steps, tile_h=th)
+        log(f"served p50 {srv['p50_s']:.2f} p99 {srv['p99_s']:.2f}")
 
     if d.rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_max / max(r32["steps"], 1),
+            "steps": K, "warmup": Wm, "ms_per_step": ms_max / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded cone+fBm DEM, seeded developed-current state)",
-            "config": {"workload": WORKLOAD, "cells": nx * ny,
-                       "active_cells_per_step": r32["cells"] / max(r32["steps"], 1),
-                       "form": "FP32 bulk + FP64 implicit solve",
-                       "l2": "flushed between timed steps (512 MB write), one step per "
-                             "event-timed interval",
-                       "parallelism": f"replicas x{args.gpus}",
-                       "tile": f"32x{r32['tile_h']} cells"},
-            "autotune": tune,
-            "fp64_plain": {"value": value64, "ms_per_step": r64["ms"] / max(r64["steps"], 1),
-                           "steps": r64["steps"], "newton_iters_per_cell":
-                           r64["newton_iters"] / max(r64["cells"], 1)},
+            "data": "synthetic (seeded cone+fBm DEMs, per-run draws; empty initial states)",
+            "config": {"workload": WORKLOAD, "runs": n_runs, "steps_per_run": ENS_STEPS,
+                       "bench_step": f"{chunk} batch steps of all runs",
+                       "form": "FP32 bulk + FP64 implicit Newton, FP64 log sums and wet/dry tests",
+                       "l2": "inputs larger than L2 (~6 GB resident; ~200 MB of active tiles per step)",
+                       "parallelism": f"replicas x{args.gpus}", "tile": f"32x{th or 8} cells",
+                       "dense_cell_steps": r32["dense_cell_steps"],
+                       "active_fraction": r32["active_fraction"],
+                       "computed_cell_updates_per_s": aggregate(d, r32["computed_cell_updates"],
+                                                                r32["device_ms"])[0],
+                       "computed_note": "active cells minus the dry border tiles the kernels skip "
+                                        "(counted as active, as in the reference)"},
+            "ensemble_fp32": r32,
+            "fp64_plain": {"value": value64, "same_workload": True, **{k: r64[k] for k in (
+                "device_ms", "ms_per_bench_step", "cell_updates", "gpu_launches", "min_steps_done")}},
             "speedup_fp32_over_fp64": value / value64 if value64 else None,
-            "error_vs_fp64": {"l1_rel_h": errs["h"]["l1_rel"], "steps": nerr, **errs},
-            "newton_iters_per_cell": r32["newton_iters"] / max(r32["cells"], 1),
-            "roofline": {"bound": "hbm", "kernel": "k_flux" if dom == "flux" else "k_stage2",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": traffic, "alg_bytes_per_active_cell": alg[dom],
-                         "kernel_ms_per_step": {k: v / max(pk_steps, 1) for k, v in kms.items()},
-                         "limiter": ("SM instruction issue, not HBM: ncu on the 2048^2 case shows "
-                                     "k_flux issuing on 70 % of cycles at 8.6 % of DRAM throughput "
-                                     "(profiles/k_flux_k_stage2_pyroclastic_2048.md)")},
+            "error_vs_oracle": ({"members": err_members, "steps": ENS_STEPS,
+                                 "fp32_worst": worst(err_oracle),
+                                 "fp64_max_rel_q": max(err_fp64) if err_fp64 else None}
+                                if err_oracle else None),
+            "autotune": tuned,
+            "roofline": roofline,
             "cpu_baseline": ({k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
                              if cb else None),
             "e2e": e2e,
-            "gpu_launches": r32["launches"],
-            "ensemble": ens,
+            "gpu_launches": r32["gpu_launches"],
+            "current_1024": cur,
             "served": srv,
             "large_domain": large,
             "clocks": clk,
             "wall_s_timed_region": t_wall1 - t_wall0,
         }
         print(json.dumps(line), flush=True)
-    for x in (s32, s64):
-        x.close()
     return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ensemble-runs", type=int, default=256)
-    ap.add_argument("--ensemble-steps", type=int, default=2000)
-    ap.add_argument("--served-requests", type=int, default=24)
+    ap.add_argument("--ensemble-runs", type=int, default=ENS_RUNS)
+    ap.add_argument("--oracle-members", type=int, default=8,
+                    help="smallest members checked against the oracle over their 2000 steps")
+    ap.add_argument("--current-steps", type=int, default=20)
+    ap.add_argument("--served-requests", type=int, default=200)
     ap.add_argument("--served-rate", type=float, default=20.0)
+    ap.add_argument("--served-probe-steps", type=int, default=16,
+                    help="steps of each job run by the plain FP64 form to measure its service time")
     ap.add_argument("--large-n", type=int, default=8192)
     ap.add_argument("--large-steps", type=int, default=10)
     ap.add_argument("--tune-steps", type=int, default=64,
-                    help="steps per tile height of the autotuner (0: default 32x8 tiles)")
+                    help="steps per tile height of the autotuners (0: default 32x8 tiles)")
     ap.add_argument("--tile-h", type=int, default=0, choices=[0, 8, 16],
-                    help="FP32 tile height of the main leg without the autotuner (0: autotune); "
-                         "a profiler run uses it to keep the height of the plain run")
+                    help="FP32 tile height of the ensemble without the autotuner (0: autotune)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -9,17 +9,22 @@ import os
 
 import numpy as np
 
-from .build import LIB, build_oracle
+from .build import LIB, LIB_FAST, build_oracle
 
 _lib = None
+_lib_fast = None
 
 
-def _load():
-    global _lib
-    if _lib is not None:
+def _load(timing=False):
+    """The parity build, or with timing=True the build with the reference's
+    compiler flags (used only to time the CPU baseline)."""
+    global _lib, _lib_fast
+    if timing and _lib_fast is not None:
+        return _lib_fast
+    if not timing and _lib is not None:
         return _lib
     build_oracle()
-    lib = C.CDLL(LIB)
+    lib = C.CDLL(LIB_FAST if timing else LIB)
     vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.c_int
     lib.sflow_oracle_create.restype = vp
     lib.sflow_oracle_create.argtypes = [vp, dp]
@@ -59,7 +64,10 @@ def _load():
     lib.oracle_limit.restype = C.c_double
     lib.oracle_limit.argtypes = [dp, dp, ip, C.c_double]
     lib.sflow_oracle_eval_math.argtypes = [ip, C.c_int64, dp, dp, dp]
-    _lib = lib
+    if timing:
+        _lib_fast = lib
+    else:
+        _lib = lib
     return lib
 
 
@@ -87,19 +95,19 @@ def eval_math(name, x, y=None):
     return out
 
 
-def set_threads(n):
-    _load().sflow_oracle_set_threads(int(n))
+def set_threads(n, timing=False):
+    _load(timing).sflow_oracle_set_threads(int(n))
 
 
-def threads():
-    return _load().sflow_oracle_threads()
+def threads(timing=False):
+    return _load(timing).sflow_oracle_threads()
 
 
 class Oracle:
     """One oracle solver over (params, B_cent)."""
 
-    def __init__(self, params, B):
-        self.lib = _load()
+    def __init__(self, params, B, timing=False):
+        self.lib = _load(timing)
         self.p = params.copy()
         self.nx, self.ny = params.comp_cells_x, params.comp_cells_y
         self.nv = params.n_vars
