@@ -47,6 +47,12 @@ class Batch : public BatchBase {
     if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     if (hs.nrk != 2) { err_ = "batched runs use the N_RK = 2 tableau"; return SFLOW_EINVAL; }
     if (hs.ns < kMinSolidBuilt || hs.ns > kMaxSolidBuilt) { err_ = "n_solid out of range"; return SFLOW_EINVAL; }
+    if (hs.p.erosion_coeff != 0.0 || hs.p.bottom_radial_source_flag || hs.n_thk * hs.n_dyn > 0) {
+      // their per-step work (source factors, topography) and results
+      // (erosion, vulnerability table) belong to the single-run solver
+      err_ = "erosion, the bottom radial source and the vulnerability table run on the single-run solver";
+      return SFLOW_EINVAL;
+    }
     Group* g = group(hs.ns);
     if (!g) return SFLOW_ECUDA;
     int slot = -1;

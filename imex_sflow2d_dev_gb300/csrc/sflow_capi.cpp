@@ -290,6 +290,10 @@ void sflow_default_params(SflowParams* p) {
   for (int i = 0; i < 4; ++i) p->time_param[i] = -1.0;
   p->t_end = 5.0e-2;
   p->dt_output = 5.0e-3;
+  for (int i = 0; i < SFLOW_MAX_LEVELS; ++i) p->thickness_levels[i] = p->dyn_pres_levels[i] = -1.0;
+  p->erodible_porosity = p->T_erodible = p->initial_erodible_thickness = -1.0;
+  for (int i = 0; i < SFLOW_MAX_SOLID; ++i) p->erodible_fract[i] = -1.0;
+  for (int i = 0; i < SFLOW_MAX_INTERVALS; ++i) p->t_intervals[i] = p->vel_intervals[i] = -1.0;
 }
 
 int sflow_create(const SflowParams* p, const double* B_cent, sflow_handle** out) {
@@ -389,6 +393,44 @@ int sflow_upload_deposit(sflow_handle* h, const double* in) {
   CHECK_HANDLE(h);
   if (!in) return fail(SFLOW_EINVAL, "in is NULL");
   FORWARD(h->solver->upload_deposit(in));
+}
+
+int sflow_download_erosion(sflow_handle* h, double* out) {
+  CHECK_HANDLE(h);
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  FORWARD(h->solver->download_erosion(0, out));
+}
+int sflow_download_erodible(sflow_handle* h, double* out) {
+  CHECK_HANDLE(h);
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  FORWARD(h->solver->download_erosion(1, out));
+}
+int sflow_set_erodible(sflow_handle* h, const double* thickness) {
+  CHECK_HANDLE(h);
+  if (!thickness) return fail(SFLOW_EINVAL, "thickness is NULL");
+  FORWARD(h->solver->set_erodible(thickness));
+}
+int sflow_download_topography(sflow_handle* h, double* B_cent) {
+  CHECK_HANDLE(h);
+  if (!B_cent) return fail(SFLOW_EINVAL, "B_cent is NULL");
+  FORWARD(h->solver->download_topography(B_cent));
+}
+int sflow_set_nodata(sflow_handle* h, const uint8_t* nodata) {
+  CHECK_HANDLE(h);
+  FORWARD(h->solver->set_nodata(nodata));
+}
+int sflow_vuln_table_size(sflow_handle* h, int32_t* n_thk, int32_t* n_dyn) {
+  CHECK_HANDLE(h);
+  int a = 0, b = 0;
+  int rc = h->solver->vuln_table(&a, &b, nullptr);
+  if (n_thk) *n_thk = a;
+  if (n_dyn) *n_dyn = b;
+  return rc;
+}
+int sflow_download_vuln_table(sflow_handle* h, uint8_t* out) {
+  CHECK_HANDLE(h);
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  FORWARD(h->solver->vuln_table(nullptr, nullptr, out));
 }
 
 int sflow_upload_maps(sflow_handle* h, const double* hmax, const double* pdynmax, const double* mod_vel_max) {
@@ -504,8 +546,10 @@ int sflow_host_geometry(const SflowParams* p, const double* B_cent, int32_t whic
       uint8_t c = s.cflags[i];
       out[i] = (double)(((c >> 2) & 1) | (((c >> 3) & 1) << 1) | (((c >> 4) & 1) << 2) | (((c >> 5) & 1) << 3));
     }
+  } else if (which == 13) {
+    for (size_t i = 0; i < N; ++i) out[i] = s.cell_fract.empty() ? 0.0 : s.cell_fract[i];
   } else {
-    return fail(SFLOW_EINVAL, "which must be in 0..12");
+    return fail(SFLOW_EINVAL, "which must be in 0..13");
   }
   return SFLOW_OK;
 }

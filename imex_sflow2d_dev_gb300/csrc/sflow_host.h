@@ -24,10 +24,28 @@ struct HostSetup {
   int take_last = 0;
   // per-cell fields, row-major [k][j] (k = y index)
   std::vector<double> Bx, By, Bxx, Bxy, Byy, gc, dgcx, dgcy;
-  std::vector<uint8_t> cflags;                 // source_cell | E<<2 | W<<3 | N<<4 | S<<5
+  std::vector<uint8_t> cflags;                 // source_cell | E<<2 | W<<3 | N<<4 | S<<5 | BSRC<<7
   std::vector<double> arc_perim, arc_nx, arc_ny;
   int64_t ring_cells = 0;
+  // update_erosion_deposition_cell runs (settling, entrainment or erosion)
+  int exchange = 0;
+  // erosion of the erodible layer (inpout_2d.f90:1818-1990)
+  double erodible_porosity = 0, coeff_porosity = 0;
+  double erodible_fract[SFLOW_MAX_SOLID] = {0, 0, 0, 0};
+  double erodible_init = 0;            // uniform initial erodible thickness
+  // bottom radial source: fraction of each cell inside the source ellipse
+  // (compute_cell_fract, geometry_2d.f90:1899-1994), 0 outside
+  std::vector<double> cell_fract;
+  int64_t bottom_cells = 0;
+  // vulnerability table levels (inpout_2d.f90:3792-3870)
+  int n_thk = 0, n_dyn = 0;
+  double thk_levels[SFLOW_MAX_LEVELS] = {0}, dyn_levels[SFLOW_MAX_LEVELS] = {0};
+  // topography (B_cent), row-major
+  std::vector<double> B;
 };
+
+constexpr uint8_t kFlagNodata = 0x40;   // B_nodata cell
+constexpr uint8_t kFlagBottom = 0x80;   // cell fraction of the bottom source > 0
 
 // Validates p and fills s; returns 0 or SFLOW_EINVAL with a message in err.
 int host_setup(const SflowParams* p, const double* B_cent, HostSetup& s, std::string& err);
@@ -54,6 +72,12 @@ class SolverBase {
   virtual int download_deposit(double* out) = 0;
   virtual int download_phys(double* out) = 0;
   virtual int upload_deposit(const double* in) = 0;
+  // which 0: accumulated erosion, 1: erodible layer (n_solid planes)
+  virtual int download_erosion(int which, double* out) = 0;
+  virtual int download_topography(double* out) = 0;
+  virtual int set_erodible(const double* thickness) = 0;
+  virtual int set_nodata(const uint8_t* nodata) = 0;
+  virtual int vuln_table(int* n_thk, int* n_dyn, uint8_t* out) = 0;
   virtual int upload_maps(const double* h, const double* p, const double* v) = 0;
   virtual int set_output_time(double t_output) = 0;
   virtual int check_solve(int solve_all) = 0;

@@ -309,7 +309,7 @@ namespace io {
 // ---------------------------------------------------------------------------
 // namelist keys -> SflowParams / SflowRunInfo
 // ---------------------------------------------------------------------------
-enum Kind { K_INT, K_REAL, K_BOOL, K_STR, K_IARR, K_RARR, K_OFF, K_ZERO, K_ACCEPT };
+enum Kind { K_INT, K_REAL, K_BOOL, K_STR, K_IARR, K_RARR, K_OFF, K_ZERO, K_ACCEPT, K_NOFILE };
 
 struct Key {
   const char* group;
@@ -368,9 +368,9 @@ static const Key kKeys[] = {
     PK("NEWRUN_PARAMETERS", "CURVATURE_TERM_FLAG", K_BOOL, curvature_term_flag),
     XK("NEWRUN_PARAMETERS", "N_ADD_GAS", K_ZERO),
     XK("NEWRUN_PARAMETERS", "COLLAPSING_VOLUME_FLAG", K_OFF),
-    XK("NEWRUN_PARAMETERS", "TOPO_CHANGE_FLAG", K_OFF),
+    PK("NEWRUN_PARAMETERS", "TOPO_CHANGE_FLAG", K_BOOL, topo_change_flag),
     XK("NEWRUN_PARAMETERS", "SUBTRACT_INIT_FLAG", K_OFF),
-    XK("NEWRUN_PARAMETERS", "BOTTOM_RADIAL_SOURCE_FLAG", K_OFF),
+    PK("NEWRUN_PARAMETERS", "BOTTOM_RADIAL_SOURCE_FLAG", K_BOOL, bottom_radial_source_flag),
     XK("NEWRUN_PARAMETERS", "VERTICAL_PROFILES_FLAG", K_OFF),
     XK("NEWRUN_PARAMETERS", "LATERAL_SOURCE_FLAG", K_OFF),
     XK("NEWRUN_PARAMETERS", "STOCHASTIC_FLAG", K_OFF),
@@ -392,7 +392,7 @@ static const Key kKeys[] = {
     PK("RADIAL_SOURCE_PARAMETERS", "Y_SOURCE", K_REAL, y_source),
     PK("RADIAL_SOURCE_PARAMETERS", "R_SOURCE", K_REAL, r_source),
     PK("RADIAL_SOURCE_PARAMETERS", "R2_SOURCE", K_REAL, r2_source),
-    XK("RADIAL_SOURCE_PARAMETERS", "ANGLE_SOURCE", K_ACCEPT),
+    PK("RADIAL_SOURCE_PARAMETERS", "ANGLE_SOURCE", K_REAL, angle_source),
     PK("RADIAL_SOURCE_PARAMETERS", "VEL_SOURCE", K_REAL, vel_source),
     PK("RADIAL_SOURCE_PARAMETERS", "T_SOURCE", K_REAL, T_source),
     PK("RADIAL_SOURCE_PARAMETERS", "H_SOURCE", K_REAL, h_source),
@@ -407,9 +407,9 @@ static const Key kKeys[] = {
     XK("RADIAL_SOURCE_PARAMETERS", "XG_SOURCE", K_ACCEPT),
     PK("RADIAL_SOURCE_PARAMETERS", "AZIMUTH_SOURCE", K_REAL, azimuth_source),
     PK("RADIAL_SOURCE_PARAMETERS", "ARC_WIDTH_SOURCE", K_REAL, arc_width_source),
-    XK("RADIAL_SOURCE_PARAMETERS", "N_INTERVALS", K_ZERO),
-    XK("RADIAL_SOURCE_PARAMETERS", "T_INTERVALS", K_ACCEPT),
-    XK("RADIAL_SOURCE_PARAMETERS", "VEL_INTERVALS", K_ACCEPT),
+    PK("RADIAL_SOURCE_PARAMETERS", "N_INTERVALS", K_INT, n_intervals),
+    PA("RADIAL_SOURCE_PARAMETERS", "T_INTERVALS", K_RARR, t_intervals, SFLOW_MAX_INTERVALS),
+    PA("RADIAL_SOURCE_PARAMETERS", "VEL_INTERVALS", K_RARR, vel_intervals, SFLOW_MAX_INTERVALS),
     // TEMPERATURE_PARAMETERS (:368-370): cooling terms, off at their defaults
     XK("TEMPERATURE_PARAMETERS", "EMISSIVITY", K_ZERO),
     XK("TEMPERATURE_PARAMETERS", "ATM_HEAT_TRANSF_COEFF", K_ZERO),
@@ -441,14 +441,15 @@ static const Key kKeys[] = {
     PA("SOLID_TRANSPORT_PARAMETERS", "SP_HEAT_S", K_RARR, sp_heat_s, SFLOW_MAX_SOLID),
     XK("SOLID_TRANSPORT_PARAMETERS", "SPHERICITY_S", K_ACCEPT),
     PK("SOLID_TRANSPORT_PARAMETERS", "EROSION_COEFF", K_REAL, erosion_coeff),
-    XK("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_POROSITY", K_ACCEPT),
+    PK("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_POROSITY", K_REAL, erodible_porosity),
     PK("SOLID_TRANSPORT_PARAMETERS", "SETTLING_FLAG", K_BOOL, settling_flag),
-    XK("SOLID_TRANSPORT_PARAMETERS", "T_ERODIBLE", K_ACCEPT),
-    XK("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_FILE", K_ACCEPT),
-    XK("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_FRACT", K_ACCEPT),
+    PK("SOLID_TRANSPORT_PARAMETERS", "T_ERODIBLE", K_REAL, T_erodible),
+    // the erodible layer per cell comes through sflow_set_erodible
+    XK("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_FILE", K_NOFILE),
+    PA("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_FRACT", K_RARR, erodible_fract, SFLOW_MAX_SOLID),
     PK("SOLID_TRANSPORT_PARAMETERS", "ALPHASTOT_MIN", K_REAL, alphastot_min),
-    XK("SOLID_TRANSPORT_PARAMETERS", "INITIAL_ERODIBLE_THICKNESS", K_ACCEPT),
-    XK("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_DEPOSIT_FLAG", K_OFF),
+    PK("SOLID_TRANSPORT_PARAMETERS", "INITIAL_ERODIBLE_THICKNESS", K_REAL, initial_erodible_thickness),
+    PK("SOLID_TRANSPORT_PARAMETERS", "ERODIBLE_DEPOSIT_FLAG", K_BOOL, erodible_deposit_flag),
     PK("SOLID_TRANSPORT_PARAMETERS", "MAXIMUM_SOLID_PACKING", K_REAL, maximum_solid_packing),
     PK("SOLID_TRANSPORT_PARAMETERS", "A_DRAG", K_REAL, A_drag),
     PK("SOLID_TRANSPORT_PARAMETERS", "B_DRAG", K_REAL, B_drag),
@@ -474,9 +475,10 @@ static const Key kKeys[] = {
     PK("LIQUID_TRANSPORT_PARAMETERS", "RHO_L", K_REAL, rho_l),
     PK("LIQUID_TRANSPORT_PARAMETERS", "KIN_VISC_L", K_REAL, kin_visc_l),
     PK("LIQUID_TRANSPORT_PARAMETERS", "LOSS_RATE", K_REAL, loss_rate),
+    // VULNERABILITY_TABLE_PARAMETERS (:380)
+    PA("VULNERABILITY_TABLE_PARAMETERS", "THICKNESS_LEVELS0", K_RARR, thickness_levels, SFLOW_MAX_LEVELS),
+    PA("VULNERABILITY_TABLE_PARAMETERS", "DYN_PRES_LEVELS0", K_RARR, dyn_pres_levels, SFLOW_MAX_LEVELS),
     // output-only groups: accepted, not used by the solver
-    XK("VULNERABILITY_TABLE_PARAMETERS", "THICKNESS_LEVELS0", K_ACCEPT),
-    XK("VULNERABILITY_TABLE_PARAMETERS", "DYN_PRES_LEVELS0", K_ACCEPT),
     XK("RUNOUT_PARAMETERS", "X0_RUNOUT", K_ACCEPT), XK("RUNOUT_PARAMETERS", "Y0_RUNOUT", K_ACCEPT),
     XK("RUNOUT_PARAMETERS", "DT_RUNOUT", K_ACCEPT), XK("RUNOUT_PARAMETERS", "EPS_STOP", K_ACCEPT),
     XK("RUNOUT_PARAMETERS", "ALPHAS_THRESHOLD", K_ACCEPT),
@@ -643,6 +645,17 @@ static int apply_group(NGroup& g, SflowParams* p, SflowRunInfo* run, SflowBC bcs
         }
         break;
       case K_ACCEPT:
+        break;
+      case K_NOFILE:
+        for (const NValue& v : it.values) {
+          if (v.null) continue;
+          std::string t = v.text;
+          while (!t.empty() && t.back() == ' ') t.pop_back();
+          if (!t.empty()) {
+            err = where(g, it) + ": not read by this driver (give the field with sflow_set_erodible)";
+            return SFLOW_EINVAL;
+          }
+        }
         break;
     }
   }

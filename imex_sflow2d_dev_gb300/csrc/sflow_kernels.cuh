@@ -51,8 +51,13 @@ constexpr int kTileHDefault = 8;
 // flag byte bits
 constexpr uint8_t F_SC_MASK = 0x3;  // source_cell (0, 1 ring interior, 2 ring boundary)
 constexpr uint8_t F_E = 0x4, F_W = 0x8, F_N = 0x10, F_S = 0x20;
-constexpr uint8_t F_WET = 0x40;     // set in shared memory only: active and q1 > 0
-constexpr uint8_t F_ACTIVE = 0x80;  // set in shared memory only
+constexpr uint8_t F_STATIC = 0x3f;  // the bits above: copied to the flux kernel's shared flags
+// in the flag plane only
+constexpr uint8_t F_NODATA = 0x40;  // B_nodata: the assembly empties the cell (solver_2d.f90:1626)
+constexpr uint8_t F_BSRC = 0x80;    // inside the bottom radial source (cell fraction > 0)
+// in the flux kernel's shared flags only
+constexpr uint8_t F_WET = 0x40;     // active and q1 > 0
+constexpr uint8_t F_ACTIVE = 0x80;
 
 template <class R>
 struct KArgs {
@@ -80,6 +85,13 @@ struct KArgs {
   R* pdynmax;
   R* mvmax;
   double* deposit;   // n_solid planes (settling only): accumulated dt * deposition
+  double* erosion;   // n_solid planes (erosion only): accumulated dt * erosion
+  double* erodible;  // n_solid planes (erosion only): erodible solid thickness
+  double* Bc;        // topography (topography change only), FP64
+  const R* bfrac;    // bottom radial source: cell fraction inside the source
+  const double* bsrc_tab;   // bottom radial source: n_intervals, t_intervals, vel_intervals
+  uint32_t* vuln;    // vulnerability table: words planes of 32 entries
+  int vuln_words;
   RunState* st;
   double tableau_at[16], tableau_ad[16], omega_t[4], omega[4];
   int take_last;
@@ -201,6 +213,12 @@ static_assert(MRX <= 64, "a frame row must fit one 64-bit mask");
 // skip it.
 constexpr uint8_t TILE_DRY_BORDER = 3;
 
+// One warp evaluates one tile: lane x owns frame columns x and 32 + x
+// (x < 8) of every frame row, the seeds of a row become one 64-bit mask by
+// two ballots, and lane x then tests the cells of tile column x row by
+// row.  A tile needs no barrier and no other warp, so a block of 8 warps
+// keeps 8 tiles (their load latencies) in flight.  Returns the tile code
+// (warp-uniform).  srow: the warp's MRY masks in shared memory.
 // Returns the tile code (block-uniform).
 template <class R, int TH>
 __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x,
@@ -249,7 +267,9 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
           if (jj == 0 || jj == g.nx - 1 || kk == 0 || kk == g.ny - 1) sd = 1;
           else if (qv[r][h] > R(0)) sd = 1;
           else if (a.pd.radial_source && (fv[r][h] & F_SC_MASK) == 2) sd = 1;
-          sp = (qv[r][h] > R(0)) || (a.pd.radial_source && (fv[r][h] & F_SC_MASK) != 0);
+          else if (a.pd.bottom_source && (fv[r][h] & F_BSRC)) sd = 1;
+          sp = (qv[r][h] > R(0)) || (a.pd.radial_source && (fv[r][h] & F_SC_MASK) != 0) ||
+               (a.pd.bottom_source && (fv[r][h] & F_BSRC));
         }
         bits[h] = __ballot_sync(0xffffffffu, sd);
         wspec |= __ballot_sync(0xffffffffu, sp);
@@ -318,33 +338,70 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
 // code, mask and active count while no tile of its 3 x 3 neighbourhood
 // holds mass: its 4-cell frame then stays dry, and its seeds are static.
 // Only its count is added.
-// The test is made by thread 0 and shared with one barrier (block-uniform).
+// Threads 0-8 read the nine wet flags together; one barrier shares the
+// result (block-uniform).
 template <class R>
 __device__ __forceinline__ bool mask_tile_skippable(const KArgs<R>& a, int tx, int ty, int tiles_x, int tiles_y) {
-  int skip = 0;
-  if (threadIdx.x == 0) {
-    const int nt = tiles_x * tiles_y, t = ty * tiles_x + tx;
-    const unsigned par = (unsigned)(a.st->steps & 1);
-    a.tile_wet_step[(par ^ 1u) * nt + t] = 0;
-    const uint8_t ta = a.tile_active[t];
-    if (ta == TILE_DRY_BORDER || (ta == 0 && !a.tile_static[t])) {
-      const uint8_t* w = a.tile_wet_step + par * nt;
-      skip = 1;
-      for (int dy = -1; dy <= 1 && skip; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-          const int x = tx + dx, y = ty + dy;
-          if (x >= 0 && x < tiles_x && y >= 0 && y < tiles_y && w[y * tiles_x + x]) {
-            skip = 0;
-            break;
-          }
-        }
-      if (skip && ta == TILE_DRY_BORDER) {
-        atomicAdd((unsigned long long*)&a.st->cells_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
-        atomicAdd(&a.st->border_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
-      }
-    }
+  const int nt = tiles_x * tiles_y, t = ty * tiles_x + tx;
+  const unsigned par = (unsigned)(a.st->steps & 1);
+  int wet = 0;
+  if (threadIdx.x < 9) {
+    const int x = tx + (int)threadIdx.x % 3 - 1, y = ty + (int)threadIdx.x / 3 - 1;
+    if (x >= 0 && x < tiles_x && y >= 0 && y < tiles_y) wet = a.tile_wet_step[par * nt + y * tiles_x + x] != 0;
   }
-  return __syncthreads_or(skip) != 0;
+  const uint8_t ta = a.tile_active[t];
+  const bool any_wet = __syncthreads_or(wet) != 0;
+  if (threadIdx.x == 0) a.tile_wet_step[(par ^ 1u) * nt + t] = 0;
+  const bool skip = (ta == TILE_DRY_BORDER || (ta == 0 && !a.tile_static[t])) && !any_wet;
+  if (skip && ta == TILE_DRY_BORDER && threadIdx.x == 0) {
+    atomicAdd((unsigned long long*)&a.st->cells_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
+    atomicAdd(&a.st->border_acc[a.st->steps & 1], (unsigned long long)a.tile_count[t]);
+  }
+  return skip;
+}
+
+// Time factor and inflow velocity of the bottom radial source at `time`
+// (constitutive_2d.f90:3151-3187): the piecewise-constant velocity of the
+// last interval started (factor 1 while it is positive), or vel_source
+// with the linear ramps of time_param.
+__device__ __forceinline__ void bottom_source_coeff(const double* tab, const double* tp, double vel_source,
+                                                    double time, double& t_coeff, double& vel) {
+  const int n = tab ? (int)tab[0] : 0;
+  if (n > 0) {
+    vel = 0.0;
+    for (int i = n - 1; i >= 0; --i)
+      if (time >= tab[1 + i]) { vel = tab[1 + n + i]; break; }
+    t_coeff = (vel > 0.0) ? 1.0 : 0.0;
+    return;
+  }
+  vel = vel_source;
+  const double t_rem = fmod(time + tp[3], tp[0]);
+  if (tp[2] == 0.0) {
+    t_coeff = (t_rem <= tp[1]) ? 1.0 : 0.0;
+  } else if (t_rem <= tp[2]) {
+    t_coeff = t_rem / tp[2];
+  } else if (t_rem <= tp[1] - tp[2]) {
+    t_coeff = 1.0;
+  } else if (t_rem <= tp[1]) {
+    t_coeff = 1.0 - (t_rem - tp[1] + tp[2]) / tp[2];
+  } else {
+    t_coeff = 0.0;
+  }
+}
+
+// start-of-step source factors of a run (ring inlet, bottom source)
+template <class R>
+__device__ __forceinline__ void source_factors(const KArgs<R>& a, RunState* st, double t) {
+  st->src_t_coeff = source_time_coeff(st->tp, st->pi_g, t);
+  st->src_t_coeff_f = (float)st->src_t_coeff;
+  if (a.pd.bottom_source) {
+    double tc, vel;
+    bottom_source_coeff(a.bsrc_tab, st->tp, a.pd.vel_source, t, tc, vel);
+    st->bsrc_t_coeff = tc;
+    st->bsrc_vel = vel;
+    st->bsrc_t_coeff_f = (float)tc;
+    st->bsrc_vel_f = (float)vel;
+  }
 }
 
 // mode 0: check_solve(.FALSE.); 1: check_solve(.TRUE.) (solve_all); 2: as 0
@@ -356,10 +413,7 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_mask(KArgs<R> a
   RunState* st = a.st;
   const double t = st->t;
   if (!running(st)) return;
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
-    st->src_t_coeff = source_time_coeff(st->tp, st->pi_g, t);
-    st->src_t_coeff_f = (float)st->src_t_coeff;
-  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) source_factors(a, st, t);
   if (mode == 2 && mask_tile_skippable(a, blockIdx.x, blockIdx.y, gridDim.x, gridDim.y)) return;
   mask_tile<R, TH>(a, mode == 1, blockIdx.x, blockIdx.y, gridDim.x, mode == 2);
 }
@@ -844,12 +898,14 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
       for (int i = 0; i < nv; ++i) qv[it][i] = qin[i * g.plane + c];
     }
   }
+  int any_bsrc = 0;
 #pragma unroll
   for (int it = 0; it < NIT; ++it) {
     const int idx = tid + it * FLUX_THREADS;
     if (idx >= RX * RY) break;
     R qp[np];
-    uint8_t fl = flv[it];
+    any_bsrc |= (flv[it] & F_BSRC) != 0;
+    uint8_t fl = flv[it] & F_STATIC;
     bool wet = false;
     if (mv[it]) {
       fl |= F_ACTIVE;
@@ -872,14 +928,16 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   // beyond the domain edge are dry too when every boundary condition is
   // (Neumann, 0).  A tile with no wet cell in its halo skips the faces.
   const bool some_wet = __syncthreads_or(any_wet);
+  const bool any_bsrc_tile = P.bottom_source ? __syncthreads_or(any_bsrc) != 0 : false;
   const bool inside = j0 - HALO >= 0 && k0 - HALO >= 0 && j0 + TX + HALO <= g.nx && k0 + TY + HALO <= g.ny;
   const bool tile_dry = !some_wet && (g.dry_bc || inside);
   // every halo cell wet: no face can have a dry stencil
   const bool face_checks = !__syncthreads_and(all_wet);
   if (tile_dry) {
-    // a dry tile without ring cells is left unchanged by the stage kernel
-    // (q stays 0, divFlux - expl = 0, the maxima keep their values)
-    int ring = 0;
+    // a dry tile without ring or bottom-source cells is left unchanged by
+    // the stage kernel (q stays 0, divFlux - expl = 0, the maxima keep
+    // their values)
+    int ring = any_bsrc;
     for (int idx = tid; idx < TX * TY; idx += FLUX_THREADS) {
       const int rx = idx % TX + HALO, ry = idx / TX + HALO;
       ring |= (sfl[ry * RX + rx] & F_SC_MASK) != 0;
@@ -982,7 +1040,13 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
         if constexpr (sizeof(R) == 8) tcoef = st->src_t_coeff;
         else tcoef = st->src_t_coeff_f;
       }
-      expl_terms<R, NS>(P, geo, qp, tcoef, ap, anx, any_, e);
+      R bf = R(0), btc = R(0), bvel = R(0);   // bottom source cells only
+      if (P.bottom_source && any_bsrc_tile && (__ldg(a.cflags + c) & F_BSRC)) {
+        bf = __ldg(a.bfrac + c);
+        if constexpr (sizeof(R) == 8) { btc = st->bsrc_t_coeff; bvel = st->bsrc_vel; }
+        else { btc = st->bsrc_t_coeff_f; bvel = st->bsrc_vel_f; }
+      }
+      expl_terms<R, NS>(P, geo, qp, tcoef, ap, anx, any_, bf, btc, bvel, e);
 #pragma unroll
       for (int i = 0; i < nv; ++i) {
         R d = R(0);
@@ -1067,17 +1131,91 @@ __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   st->steps += 1;
 }
 
+// ---------------------------------------------------------------------------
+// k_topography: topography_reconstruction (geometry_2d.f90:555-895) after
+// the topography changed (TOPO_CHANGE_FLAG, IMEX_SfloW2D.f90:445): 5-point
+// centred slopes and curvatures of B on cells 3 .. n-2, the two-cell frame
+// copied from the nearest computed row / column (a clamped index), then the
+// slope factor and its derivatives.  FP64 with every product and sum
+// rounded on its own (the host's order), written to the topography planes
+// in R.  One thread per cell.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(256) k_topography(KArgs<R> a) {
+  step_kernel_entry();
+  const Grid<R>& g = a.g;
+  if (!a.st->run_step) return;
+  const int64_t n = (int64_t)g.nx * g.ny;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j = (int)(i % g.nx), k = (int)(i / g.nx);
+  const int jj = j < 2 ? 2 : (j > g.nx - 3 ? g.nx - 3 : j);
+  const int kk = g.ny == 1 ? 0 : (k < 2 ? 2 : (k > g.ny - 3 ? g.ny - 3 : k));
+  const double c1[5] = {-2.0, -1.0, 0.0, 1.0, 2.0};
+  const double c2[5] = {2.0, -1.0, -2.0, -1.0, 2.0};
+  const double dx = g.dx, dy = g.dy;
+  const double* B = a.Bc;
+  auto Bat = [&](int x, int y) { return B[cidx(g, x, y)]; };
+  double px = 0.0, py = 0.0, sxx = 0.0, syy = 0.0, ws = 0.0;
+  for (int m = 0; m < 5; ++m) {
+    px = __dadd_rn(px, __dmul_rn(c1[m], Bat(jj + m - 2, kk)));
+    sxx = __dadd_rn(sxx, __dmul_rn(c2[m], Bat(jj + m - 2, kk)));
+  }
+  double bx, by, bxx, byy, bxy;
+  bx = __ddiv_rn(px, __dmul_rn(10.0, dx));
+  bxx = __ddiv_rn(sxx, __dmul_rn(7.0, __dmul_rn(dx, dx)));
+  if (g.ny == 1) {
+    by = __ddiv_rn(0.0, __dmul_rn(10.0, dy));
+    byy = __ddiv_rn(0.0, __dmul_rn(7.0, __dmul_rn(dy, dy)));
+    bxy = 0.0;
+  } else {
+    for (int m = 0; m < 5; ++m) {
+      py = __dadd_rn(py, __dmul_rn(c1[m], Bat(jj, kk + m - 2)));
+      syy = __dadd_rn(syy, __dmul_rn(c2[m], Bat(jj, kk + m - 2)));
+    }
+    for (int mm = 0; mm < 5; ++mm)
+      for (int m = 0; m < 5; ++m) ws = __dadd_rn(ws, __dmul_rn(__dmul_rn(c1[m], c1[mm]), Bat(jj + m - 2, kk + mm - 2)));
+    by = __ddiv_rn(py, __dmul_rn(10.0, dy));
+    byy = __ddiv_rn(syy, __dmul_rn(7.0, __dmul_rn(dy, dy)));
+    bxy = __ddiv_rn(ws, __dmul_rn(__dmul_rn(10.0, dx), __dmul_rn(10.0, dy)));
+  }
+  const int64_t c = cidx(g, j, k);
+  R* const* geo = const_cast<R* const*>(a.geo);
+  geo[0][c] = (R)bx;
+  geo[1][c] = (R)by;
+  if (geo[2]) { geo[2][c] = (R)bxx; geo[3][c] = (R)bxy; geo[4][c] = (R)byy; }
+  if (a.pd.slope_corr) {
+    const double gc = __ddiv_rn(1.0, __dadd_rn(__dadd_rn(1.0, __dmul_rn(bx, bx)), __dmul_rn(by, by)));
+    const double gc2 = __dmul_rn(-2.0, __dmul_rn(gc, gc));
+    geo[5][c] = (R)gc;
+    geo[6][c] = (R)__dmul_rn(gc2, __dadd_rn(__dmul_rn(bx, bxx), __dmul_rn(by, bxy)));
+    geo[7][c] = (R)__dmul_rn(gc2, __dadd_rn(__dmul_rn(bx, bxy), __dmul_rn(by, byy)));
+  }
+}
+
 static __global__ void k_dt(RunState* st, double max_dt) {
   step_kernel_entry();
   dt_update(st, max_dt);
 }
 
+// The physical variables of a cell's current state, kept between the
+// assembly fixes, the erosion/deposition step and the post-step maxima of
+// one step so that qc_to_qp of an unchanged state is not evaluated again
+// (the same function of the same state: the same values).
+template <class R, int NS>
+struct CellQp {
+  R qp[4 + NS + 2];
+  R pdyn;
+  bool valid;
+};
+
 // ---------------------------------------------------------------------------
 // Positivity fixes of assemble_sol (solver_2d.f90:1381-1628) on an FP64 or
-// FP32 state; returns status bits.
+// FP32 state; returns status bits.  cq (may be null) receives qc_to_qp of
+// the state when the fixes leave it unchanged after that evaluation.
 // ---------------------------------------------------------------------------
 template <class R, int NS>
-__device__ __forceinline__ unsigned assemble_fixes(const Phys<R>& P, R* q) {
+__device__ __forceinline__ unsigned assemble_fixes(const Phys<R>& P, R* q, CellQp<R, NS>* cq = nullptr) {
   constexpr int nv = 4 + NS, ns = NS;
   unsigned st = 0;
 #pragma unroll
@@ -1105,14 +1243,17 @@ __device__ __forceinline__ unsigned assemble_fixes(const Phys<R>& P, R* q) {
         if (q[4 + i] > P.thr_neg1e7) q[4 + i] = R(0);
     }
   }
-  R qp[nv + 2];
-  qc_to_qp<R, NS>(P, q, qp);
+  R qp_local[nv + 2];
+  R* qp = cq ? cq->qp : qp_local;
+  const R pdyn = qc_to_qp<R, NS>(P, q, qp);
+  if (cq) { cq->pdyn = pdyn; cq->valid = true; }
   if (qp[3] < P.thr_273) st |= SFLOW_S_LOW_T;
   if (ns > 0) {
     R ssum = R(0);
 #pragma unroll
     for (int i = 0; i < ns; ++i) ssum += q[4 + i];
     if (ssum > q[0]) {
+      if (cq) cq->valid = false;
       bool small;
       if constexpr (sizeof(R) == 8) small = ((ssum - q[0]) / q[0] < 1.0e-10) || (q[0] < P.thr_eps);
       else small = !((ssum - q[0]) / q[0] > P.thr_1em10) || (q[0] < P.thr_eps);
@@ -1127,26 +1268,65 @@ __device__ __forceinline__ unsigned assemble_fixes(const Phys<R>& P, R* q) {
   return st;
 }
 
-// update_erosion_deposition_cell (solver_2d.f90:2382-2597) for one cell
+// Per-cell inputs and results of the mass exchange.
+template <class R, int NS>
+struct CellExch {
+  R erodible[NS];   // erodible solid thicknesses (erosion only, else 0)
+  R bf;             // bottom radial source: cell fraction inside the source
+  R dep[NS], ers[NS], topo;   // deposition / erosion rates, topography rate
+};
+
+// update_erosion_deposition_cell (solver_2d.f90:2382-2597) for one cell: the
+// state part.  cq (may be null): on entry the qc_to_qp of q if valid, on
+// return that of the final state (invalid when the cell was emptied).
 template <class R, int NS>
 __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const Geo<R>& geo, R dt,
-                                                       R* q, R* dep_out) {
+                                                       R* q, CellExch<R, NS>& ex, CellQp<R, NS>* cq = nullptr) {
   constexpr int nv = 4 + NS, ns = NS;
   unsigned st = 0;
-  R qp[nv + 2], dep[kMaxSolid], eqn[nv];
-  if (q[0] > R(0)) qc_to_qp<R, NS>(P, q, qp);
-  else {
+  R qp[nv + 2], eqn[nv];
+  R* dep = ex.dep;
+  if (cq && cq->valid) {
+    // qc_to_qp of a state with q(1) <= eps is the dry state, as below
+#pragma unroll
+    for (int i = 0; i < nv + 2; ++i) qp[i] = cq->qp[i];
+  } else if (q[0] > R(0)) {
+    qc_to_qp<R, NS>(P, q, qp);
+  } else {
 #pragma unroll
     for (int i = 0; i < nv + 2; ++i) qp[i] = R(0);
     qp[3] = P.T_ambient;
   }
-  mass_exchange<R, NS>(P, qp, geo.Bx, geo.By, dt, dep, eqn);
+  if (cq) cq->valid = false;
+  mass_exchange<R, NS>(P, qp, geo.Bx, geo.By, dt, P.erosion_coeff > R(0) ? ex.erodible : nullptr, dep, ex.ers,
+                       eqn, ex.topo);
+  if (P.bottom_source && ex.bf > R(0)) {
+    // the part of the cell inside the bottom source exchanges nothing
+    const R out_frac = R(1) - ex.bf;
 #pragma unroll
-  for (int i = 0; i < ns; ++i) dep_out[i] = dep[i];
+    for (int i = 0; i < ns; ++i) { dep[i] = dep[i] * out_frac; ex.ers[i] = ex.ers[i] * out_frac; }
+#pragma unroll
+    for (int i = 0; i < nv; ++i) eqn[i] = eqn[i] * out_frac;
+    ex.topo = ex.topo * out_frac;
+  }
+  const R q0_before = q[0];
 #pragma unroll
   for (int i = 0; i < nv; ++i) q[i] = q[i] + dt * eqn[i];
 #pragma unroll
   for (int i = 0; i < ns; ++i) q[4 + i] = rmax(R(0), q[4 + i]);
+  if constexpr (sizeof(R) == 4) {
+    // FP32 form: when the limited deposition and carrier loss remove the
+    // whole mass (exactly zero in exact arithmetic), the sum leaves a
+    // rounding residual of a few ulp of the old mass, with a momentum
+    // residual of its own: a film with an arbitrary velocity.  A cell left
+    // with less than 2^-16 of its mass is emptied (the FP64 form empties
+    // residuals down to -1e-10 and keeps positive ones, which are 2^-52
+    // relative there).
+    if (fabsf(q[0]) <= q0_before * 0x1p-16f) {
+#pragma unroll
+      for (int i = 0; i < nv; ++i) q[i] = R(0);
+    }
+  }
   if (!(q[0] > R(0))) {
     if (q[0] > P.thr_neg1e10) {
 #pragma unroll
@@ -1176,9 +1356,15 @@ __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const G
   }
   R red_grav = R(0);
   if (q[0] > R(0)) {
-    qc_to_qp<R, NS>(P, q, qp);
+    const R pdyn = qc_to_qp<R, NS>(P, q, qp);
     Mixt<R> m = mixt_var<R, NS>(P, qp, false);
     red_grav = m.red_grav;
+    if (cq && red_grav > R(0)) {
+#pragma unroll
+      for (int i = 0; i < nv + 2; ++i) cq->qp[i] = qp[i];
+      cq->pdyn = pdyn;
+      cq->valid = true;
+    }
   }
   if (red_grav <= R(0)) {
 #pragma unroll
@@ -1187,26 +1373,94 @@ __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const G
   return st;
 }
 
-// deposit(j,k,:) += dt * deposition_term (solver_2d.f90:2476-2477), FP64
+template <class R>
+__device__ __forceinline__ double to_d(R x) {
+  if constexpr (sizeof(R) == 4) return f2d_exact(x);
+  else return x;
+}
+
+// The accumulated fields of update_erosion_deposition_cell
+// (solver_2d.f90:2476-2494), in FP64: deposit += dt*deposition, erosion +=
+// dt*erosion, erodible -= dt*erosion (+ dt*deposition with
+// ERODIBLE_DEPOSIT_FLAG), B += dt*topo_term with TOPO_CHANGE_FLAG.
 template <class R, int NS>
-__device__ __forceinline__ void add_deposit(const KArgs<R>& a, int64_t c, double dt, const R* dep) {
-  if (!a.deposit) return;
+__device__ __forceinline__ void add_deposit(const KArgs<R>& a, int64_t c, double dt, const CellExch<R, NS>& ex) {
+  const int64_t pl = a.g.plane;
+  if (a.deposit) {
 #pragma unroll
-  for (int i = 0; i < NS; ++i) {
-    double d;
-    if constexpr (sizeof(R) == 4) d = f2d_exact(dep[i]);
-    else d = dep[i];
-    a.deposit[i * a.g.plane + c] += dt * d;
+    for (int i = 0; i < NS; ++i) a.deposit[i * pl + c] += dt * to_d(ex.dep[i]);
+  }
+  if (a.erosion) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) a.erosion[i * pl + c] += dt * to_d(ex.ers[i]);
+#pragma unroll
+    for (int i = 0; i < NS; ++i) a.erodible[i * pl + c] = a.erodible[i * pl + c] - dt * to_d(ex.ers[i]);
+    if (a.pd.erodible_deposit) {
+#pragma unroll
+      for (int i = 0; i < NS; ++i) a.erodible[i * pl + c] = a.erodible[i * pl + c] + dt * to_d(ex.dep[i]);
+    }
+  }
+  if (a.Bc) a.Bc[c] = a.Bc[c] + dt * to_d(ex.topo);
+}
+
+// nodata emptying of assemble_sol (solver_2d.f90:1626) and
+// update_erosion_deposition_cell for one cell after the assembly
+template <class R, int NS>
+__device__ __forceinline__ unsigned cell_exchange(const KArgs<R>& a, int64_t c, double dt, R* q,
+                                                  CellQp<R, NS>* cq) {
+  constexpr int nv = 4 + NS;
+  if (a.pd.nodata && (__ldg(a.cflags + c) & F_NODATA)) {
+#pragma unroll
+    for (int i = 0; i < nv; ++i) q[i] = R(0);
+    if (cq) cq->valid = false;
+  }
+  if (!a.pd.exchange) return 0;
+  const Geo<R> geo = load_geo(a, c);
+  CellExch<R, NS> ex;
+#pragma unroll
+  for (int i = 0; i < NS; ++i) ex.erodible[i] = a.erodible ? (R)a.erodible[i * a.g.plane + c] : R(0);
+  ex.bf = (a.pd.bottom_source && (__ldg(a.cflags + c) & F_BSRC)) ? __ldg(a.bfrac + c) : R(0);
+  const unsigned st = erosion_deposition<R, NS>(a.pr, geo, from_double<R>(dt), q, ex, cq);
+  add_deposit<R, NS>(a, c, dt, ex);
+  return st;
+}
+
+// vulnerability table (IMEX_SfloW2D.f90:339-353, 477-491): entry
+// i_thk * n_dyn + i_dyn of a cell holding mass is h >= thickness level i_thk
+// and p_dyn >= dynamic-pressure level i_dyn; OR-ed over the steps (set at
+// the start).  Entry e is bit e % 32 of the cell's word plane e / 32.
+template <class R>
+__device__ __forceinline__ void vuln_update(const KArgs<R>& a, int64_t c, R h, R p_dyn, bool accumulate) {
+  const Phys<R>& P = a.pr;
+  unsigned w[(SFLOW_MAX_LEVELS * SFLOW_MAX_LEVELS + 31) / 32];
+  for (int i = 0; i < a.vuln_words; ++i) w[i] = 0u;
+  int e = 0;
+  for (int it = 0; it < P.n_thk; ++it) {
+    const bool th = h >= P.thk_levels[it];
+    for (int id = 0; id < P.n_dyn; ++id, ++e)
+      if (th && p_dyn >= P.dyn_levels[id]) w[e >> 5] |= 1u << (e & 31);
+  }
+  for (int i = 0; i < a.vuln_words; ++i) {
+    uint32_t* p = a.vuln + (int64_t)i * a.g.plane + c;
+    *p = accumulate ? (*p | w[i]) : w[i];
   }
 }
 
 // post-step maxima (IMEX_SfloW2D.f90:449-505)
 template <class R, int NS>
-__device__ __forceinline__ void post_step_maps(const KArgs<R>& a, int64_t c, const R* q) {
+__device__ __forceinline__ void post_step_maps(const KArgs<R>& a, int64_t c, const R* q,
+                                               const CellQp<R, NS>* cq = nullptr) {
   constexpr int nv = 4 + NS;
   if (q[0] > R(0)) {
     R qp[nv + 2];
-    R p_dyn = qc_to_qp<R, NS>(a.pr, q, qp);
+    R p_dyn;
+    if (cq && cq->valid) {
+#pragma unroll
+      for (int i = 0; i < nv + 2; ++i) qp[i] = cq->qp[i];
+      p_dyn = cq->pdyn;
+    } else {
+      p_dyn = qc_to_qp<R, NS>(a.pr, q, qp);
+    }
     R hm = a.hmax[c];
     a.hmax[c] = rmax(hm, qp[0]);
     if (qp[0] > a.pr.thr_1em3) {
@@ -1214,6 +1468,7 @@ __device__ __forceinline__ void post_step_maps(const KArgs<R>& a, int64_t c, con
       a.pdynmax[c] = rmax(a.pdynmax[c], p_dyn);
       a.mvmax[c] = rmax(a.mvmax[c], mv);
     }
+    if (a.vuln) vuln_update<R>(a, c, qp[0], p_dyn, true);
   }
 }
 
@@ -1370,10 +1625,7 @@ __device__ __forceinline__ int stage2_cell(const KArgs<R>& a, int mode, int j, i
   for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + c];
   if (mode > 0) {
     if (mode == 1) {
-      const Geo<R> geo = load_geo(a, c);
-      R dep[NS];
-      status |= erosion_deposition<R, NS>(a.pr, geo, from_double<R>(dt), q, dep);
-      add_deposit<R, NS>(a, c, dt, dep);
+      status |= cell_exchange<R, NS>(a, c, dt, q, nullptr);
 #pragma unroll
       for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
     } else {
@@ -1388,15 +1640,16 @@ __device__ __forceinline__ int stage2_cell(const KArgs<R>& a, int mode, int j, i
       s2[i] = R(0);
     }
     status |= stage_cell<R, NS>(a, geo, q, s1, s2, dt, 1.0, q, rn, nit);
-    status |= assemble_fixes<R, NS>(a.pr, q);
-    if (mode < 0 && (a.pd.settling || a.pd.entrain)) {
-      R dep[NS];
-      status |= erosion_deposition<R, NS>(a.pr, geo, from_double<R>(dt), q, dep);
-      add_deposit<R, NS>(a, c, dt, dep);
+    CellQp<R, NS> cq;
+    status |= assemble_fixes<R, NS>(a.pr, q, &cq);
+    if (mode < 0) status |= cell_exchange<R, NS>(a, c, dt, q, &cq);
+    else if (a.pd.nodata && (__ldg(a.cflags + c) & F_NODATA)) {
+#pragma unroll
+      for (int i = 0; i < nv; ++i) q[i] = R(0);
     }
 #pragma unroll
     for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
-    if (mode < 0) post_step_maps<R, NS>(a, c, q);
+    if (mode < 0) post_step_maps<R, NS>(a, c, q, &cq);
   }
   return q[0] > R(0);
 }
@@ -1557,16 +1810,12 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_assemble(KArgs
 #pragma unroll
         for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + c] - dtr * (s1[i] - s2[i]);
       }
-      status |= assemble_fixes<R, NS>(a.pr, q);
-      if (a.pd.settling || a.pd.entrain) {
-        const Geo<R> geo = load_geo(a, c);
-        R dep[NS];
-        status |= erosion_deposition<R, NS>(a.pr, geo, from_double<R>(dt), q, dep);
-        add_deposit<R, NS>(a, c, dt, dep);
-      }
+      CellQp<R, NS> cq;
+      status |= assemble_fixes<R, NS>(a.pr, q, &cq);
+      status |= cell_exchange<R, NS>(a, c, dt, q, &cq);
 #pragma unroll
       for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
-      post_step_maps<R, NS>(a, c, q);
+      post_step_maps<R, NS>(a, c, q, &cq);
     }
   }
   if (status) atomicOr(&st->status, status);

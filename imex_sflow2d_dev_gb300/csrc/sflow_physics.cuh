@@ -445,16 +445,17 @@ __device__ __forceinline__ void eval_fluxes(const Phys<R>& P, const R* qcj, cons
 }
 
 // ---------------------------------------------------------------------------
-// constitutive_2d.f90:3024-3431 eval_expl_terms (gravity/slope terms and the
-// lateral ring inlet; no bottom radial source)
+// constitutive_2d.f90:3024-3431 eval_expl_terms: gravity/slope terms, the
+// bottom radial source (cell fraction bf inside the source, time factor
+// b_coeff, inflow velocity b_vel) and the lateral ring inlet
 // ---------------------------------------------------------------------------
 template <class R, int NS>
 __device__ __forceinline__ void expl_terms(const Phys<R>& P, const Geo<R>& g, const R* qpj,
                                            R t_coeff_src, R arc_perim, R arc_nx, R arc_ny,
-                                           R* e) {
+                                           R bf, R b_coeff, R b_vel, R* e) {
   constexpr int ns = NS, nv = 4 + NS;
   for (int i = 0; i < nv; ++i) e[i] = R(0);
-  if (!(qpj[0] > P.thr_eps) && arc_perim == R(0)) return;
+  if (!(qpj[0] > P.thr_eps) && bf == R(0) && arc_perim == R(0)) return;
   if (qpj[0] > P.thr_eps) {
     R r_h = qpj[0], r_u = qpj[nv], r_v = qpj[nv + 1];
     Mixt<R> m = mixt_var<R, NS>(P, qpj, true);
@@ -463,6 +464,16 @@ __device__ __forceinline__ void expl_terms(const Phys<R>& P, const Geo<R>& g, co
     e[1] = -g.gc * m.rho_m * tg * r_h * g.Bx + cst<R>(0.5) * m.rho_m * m.red_grav * sq(r_h) * g.dgcx;
     e[2] = -g.gc * m.rho_m * tg * r_h * g.By + cst<R>(0.5) * m.rho_m * m.red_grav * sq(r_h) * g.dgcy;
     e[3] = P.energy ? (e[1] * r_u + e[2] * r_v) : R(0);
+  }
+  if (P.bottom_source && bf > R(0)) {
+    // inflow state: h = 1, T = T_source, alphas_source (its mixt_var is
+    // src_rho_m, src_cp_mix); the momentum terms add zero
+    const R h_dot = bf * b_vel;
+    e[0] = e[0] + b_coeff * h_dot * P.src_rho_m;
+    e[1] = e[1] + R(0);
+    e[2] = e[2] + R(0);
+    e[3] = e[3] + b_coeff * h_dot * P.src_rho_m * P.src_cp_mix * P.T_source;
+    for (int i = 0; i < ns; ++i) e[4 + i] = e[4 + i] + b_coeff * h_dot * P.alphas_source[i] * P.rho_s[i];
   }
   if (P.radial_source && arc_perim > R(0) && P.h_source > R(0)) {
     R t_coeff = t_coeff_src;
@@ -818,7 +829,8 @@ __device__ int solve_rk_step(const NewtonCtx& c, double* qj) {
 
 // ---------------------------------------------------------------------------
 // constitutive_2d.f90:5326-5404 settling_velocity and 4574-5153
-// eval_mass_exchange_terms (no erosion / pore pressure / vaporisation); FP64
+// eval_mass_exchange_terms (settling, erosion of the erodible layer, air
+// entrainment; no pore pressure / vaporisation)
 // ---------------------------------------------------------------------------
 template <class R>
 __device__ __forceinline__ R settling_velocity(const Phys<R>& P, R diam, R rhos, R rhoc,
@@ -844,12 +856,20 @@ __device__ __forceinline__ R settling_velocity(const Phys<R>& P, R diam, R rhos,
   return sv;
 }
 
+// erodible: the cell's erodible solid thicknesses (null: none, as with
+// EROSION_COEFF = 0).  Returns the deposition and erosion rates (dep, ers),
+// the equation terms and the topography rate topo.  As in the reference the
+// erosion rates are set before the ALPHASTOT_MIN return, which leaves the
+// equation terms at zero.  With ERODIBLE_DEPOSIT_FLAG the erodible layer
+// takes the cell's temperature (the reference sets its module-wide
+// T_erodible to the cell's T just before this use).
 template <class R, int NS>
 __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R Bx, R By, R dt,
-                                              R* dep, R* eqn) {
+                                              const R* erodible, R* dep, R* ers, R* eqn, R& topo) {
   constexpr int ns = NS, nv = 4 + NS;
-  for (int i = 0; i < ns; ++i) dep[i] = R(0);
+  for (int i = 0; i < ns; ++i) { dep[i] = R(0); ers[i] = R(0); }
   for (int i = 0; i < nv; ++i) eqn[i] = R(0);
+  topo = R(0);
   if (!(qpj[0] > P.thr_eps)) return;
   const R alpha_max = cst<R>(0.6), hind_exp = cst<R>(4.65);
   R r_h = qpj[0], r_u = qpj[nv], r_v = qpj[nv + 1];
@@ -858,7 +878,17 @@ __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R 
   for (int i = 0; i < ns; ++i) { al[i] = P.alpha ? qpj[4 + i] : qpj[4 + i] / qpj[0]; at += al[i]; }
   R r_w = P.slope_corr ? (r_u * Bx + r_v * By) : R(0);
   R mod_vel2 = sq(r_u) + sq(r_v) + sq(r_w);
-  R tot_erosion = R(0) / (R(1) - P.erodible_porosity);
+  if (P.erosion_coeff > R(0)) {
+    // Fagents & Baloga (2006) eq. 5 with the solid volume fraction
+    const R mod_vel = sqrt(mod_vel2);
+    const R tot = P.erosion_coeff * mod_vel * r_h * (R(1) - at);
+    const R tot_solid = tot * (R(1) - P.erodible_porosity);
+    for (int i = 0; i < ns; ++i) ers[i] = P.erodible_fract[i] * tot_solid;
+  }
+  for (int i = 0; i < ns; ++i) ers[i] = rmax(R(0), rmin(ers[i], (erodible ? erodible[i] : R(0)) / dt));
+  R tot_solid_erosion = R(0);
+  for (int i = 0; i < ns; ++i) tot_solid_erosion += ers[i];
+  R tot_erosion = tot_solid_erosion / (R(1) - P.erodible_porosity);
   R cont_erosion = tot_erosion * P.erodible_porosity;
   if (at <= P.alphastot_min) return;
   R r_T = qpj[3];
@@ -885,24 +915,28 @@ __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R 
     R entr_coeff = cst<R>(0.075) / sqrt(R(1) + cst<R>(718.0) * rpow<R>(m.Ri, cst<R>(2.4)));
     air_entr = entr_coeff * sqrt(mod_vel2);
   }
-  R rho_dep_tot = R(0), rho_ers_tot = R(0), s_dep = R(0), s_ers = R(0);
+  const R T_ers = P.erodible_deposit ? r_T : P.T_erodible;
+  R rho_dep_tot = R(0), rho_ers_tot = R(0), s_dep = R(0), s_ers = R(0), dep_tot = R(0), ers_tot = R(0);
+  for (int i = 0; i < ns; ++i) dep_tot += dep[i];
+  for (int i = 0; i < ns; ++i) ers_tot += ers[i];
   for (int i = 0; i < ns; ++i) rho_dep_tot += P.rho_s[i] * dep[i];
-  for (int i = 0; i < ns; ++i) rho_ers_tot += P.rho_s[i] * R(0);
+  for (int i = 0; i < ns; ++i) rho_ers_tot += P.rho_s[i] * ers[i];
   for (int i = 0; i < ns; ++i) s_dep += P.rho_s[i] * P.sp_heat_s[i] * dep[i];
-  for (int i = 0; i < ns; ++i) s_ers += P.rho_s[i] * P.sp_heat_s[i] * R(0);
+  for (int i = 0; i < ns; ++i) s_ers += P.rho_s[i] * P.sp_heat_s[i] * ers[i];
   eqn[0] = P.rho_a_amb * air_entr + rho_ers_tot - rho_dep_tot + P.rho_c_sub * cont_erosion -
            m.rho_c * cpl;
   eqn[1] = -r_u * (rho_dep_tot + m.rho_c * cpl);
   eqn[2] = -r_v * (rho_dep_tot + m.rho_c * cpl);
   if (P.energy)
     eqn[3] = -r_T * (s_dep + m.rho_c * m.cp_c * cpl) - cst<R>(0.5) * mod_vel2 * (rho_dep_tot + m.rho_c * cpl) +
-             P.T_erodible * (s_ers + P.rho_c_sub * m.cp_c * cont_erosion) +
+             T_ers * (s_ers + P.rho_c_sub * m.cp_c * cont_erosion) +
              P.T_ambient * P.sp_heat_a * P.rho_a_amb * air_entr;
   else
     eqn[3] = -r_T * (s_dep + m.rho_c * m.cp_c * cpl) +
-             P.T_erodible * (s_ers + P.rho_c_sub * m.cp_c * cont_erosion) +
+             T_ers * (s_ers + P.rho_c_sub * m.cp_c * cont_erosion) +
              P.T_ambient * P.sp_heat_a * P.rho_a_amb * air_entr;
-  for (int i = 0; i < ns; ++i) eqn[4 + i] = P.rho_s[i] * (R(0) - dep[i]);
+  for (int i = 0; i < ns; ++i) eqn[4 + i] = P.rho_s[i] * (ers[i] - dep[i]);
+  topo = (dep_tot - ers_tot) / (R(1) - P.erodible_porosity);
 }
 
 // ---------------------------------------------------------------------------

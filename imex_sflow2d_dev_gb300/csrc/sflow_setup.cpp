@@ -247,6 +247,54 @@ static void ring_source(HostSetup& s) {
     if (s.cflags[c] & 0x3) ++s.ring_cells;
 }
 
+// compute_cell_fract (geometry_2d.f90:1899-1994): the fraction of 200 x 200
+// sub-cell points of each cell inside the source ellipse (semi-axes
+// r_source along the rotated x axis and r2_source, rotation angle_source
+// degrees); cells outside the ellipse's bounding box are 0.  The quotient
+// is taken in single precision, as the reference's REAL(SUM(...))/n2.
+static void cell_fractions(HostSetup& s) {
+  const SflowParams& p = s.p;
+  const int nx = s.nx, ny = s.ny;
+  const size_t N = (size_t)nx * ny;
+  s.cell_fract.assign(N, 0.0);
+  const int n = 200, n2 = n * n;
+  const double ang = p.angle_source / 180.0 * std::atan(1.0) * 4.0;
+  const double ca = std::cos(ang), sa = std::sin(ang);
+  std::vector<double> xsub(n), ysub(n);   // the offsets take n distinct values
+  for (int h = 1; h <= n; ++h) {
+    double v = (2.0 * (double)h - 1.0) / (2.0 * (double)n);
+    xsub[h - 1] = (v - 0.5) * s.dx;
+    ysub[h - 1] = (v - 0.5) * s.dy;
+  }
+  auto xst = [&](int j) { return p.x0 + (double)j * s.dx; };
+  auto yst = [&](int k) { return p.y0 + (double)k * s.dy; };
+  const double xs = p.x_source, ys = p.y_source, rs = p.r_source, r2s = p.r2_source;
+  const double rmx = std::fmax(rs, r2s);
+  const double rs2 = rs * rs, r2s2 = r2s * r2s;
+  for (int k = 0; k < ny; ++k) {
+    for (int j = 0; j < nx; ++j) {
+      if (xst(j + 1) < xs - rmx || xst(j) > xs + rmx || yst(k + 1) < ys - rmx || yst(k) > ys + rmx) continue;
+      const double xc = 0.5 * (xst(j) + xst(j + 1)), yc = 0.5 * (yst(k) + yst(k + 1));
+      int cnt = 0;
+      for (int iy = 0; iy < n; ++iy) {
+        const double dyv = yc + ysub[iy] - ys;
+        for (int ix = 0; ix < n; ++ix) {
+          const double dxv = xc + xsub[ix] - xs;
+          const double a1 = dxv * ca + dyv * sa;
+          const double a2 = -(dxv * sa) + dyv * ca;
+          if (a1 * a1 / rs2 + a2 * a2 / r2s2 <= 1.0) ++cnt;
+        }
+      }
+      const double f = (double)((float)cnt / (float)n2);
+      s.cell_fract[(size_t)k * nx + j] = f;
+      if (f > 0.0) {
+        s.cflags[(size_t)k * nx + j] |= kFlagBottom;
+        ++s.bottom_cells;
+      }
+    }
+  }
+}
+
 int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::string& err) {
   if (!pin) { err = "params is NULL"; return SFLOW_EINVAL; }
   s.p = *pin;
@@ -257,14 +305,19 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
     err = "comp_cells_x must be >= 5 and comp_cells_y 1 or >= 5";
     return SFLOW_EINVAL;
   }
-  if (p.comp_cells_y == 1 && p.radial_source_flag) { err = "a radial source needs comp_cells_y > 1"; return SFLOW_EINVAL; }
+  if (p.comp_cells_y == 1 && (p.radial_source_flag || p.bottom_radial_source_flag)) { err = "a radial source needs comp_cells_y > 1"; return SFLOW_EINVAL; }
+  if (p.radial_source_flag && p.bottom_radial_source_flag) {
+    // the lateral ring needs H_SOURCE or MFR_SOURCE, which the bottom source forbids
+    err = "radial_source_flag and bottom_radial_source_flag exclude each other";
+    return SFLOW_EINVAL;
+  }
   if ((int64_t)p.comp_cells_x * p.comp_cells_y > (int64_t)1 << 31) { err = "domain larger than 2^31 cells"; return SFLOW_ERANGE; }
   if (p.n_solid < 1 || p.n_solid > 3) { err = "the GPU kernels are built for n_solid = 1, 2 or 3"; return SFLOW_EINVAL; }
   if (p.n_rk < 1 || p.n_rk > 4) { err = "N_RK must be 1, 2, 3 or 4"; return SFLOW_EINVAL; }
   if (p.gas_flag && p.liquid_flag) { err = "gas carrier with a liquid phase is not supported"; return SFLOW_EINVAL; }
   if (!p.gas_flag && !p.liquid_flag) { err = "one of gas_flag / liquid_flag must be set"; return SFLOW_EINVAL; }
   if (p.rheology_flag && p.rheology_model != 1 && p.rheology_model != 6) { err = "rheology_model must be 1 or 6"; return SFLOW_EINVAL; }
-  if (p.erosion_coeff != 0.0) { err = "erosion_coeff must be 0"; return SFLOW_EINVAL; }
+  if (p.erosion_coeff < 0.0) { err = "erosion_coeff must be >= 0"; return SFLOW_EINVAL; }
   if (p.solver_scheme != SFLOW_SCHEME_KT && p.solver_scheme != SFLOW_SCHEME_UP) {
     err = "SOLVER_SCHEME must be KT or UP";
     return SFLOW_EINVAL;
@@ -297,8 +350,56 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   s.pi_g = 4.0 * std::atan(1.0);
   s.rho_a_amb = p.pres / (p.sp_gas_const_a * p.T_ambient);
   s.kin_visc_c = p.gas_flag ? p.kin_visc_a : p.kin_visc_l;
-  s.T_erodible = 300.0;
+  // erodible layer (inpout_2d.f90:1818-1990)
+  if (p.erosion_coeff == 0.0) {
+    s.erodible_porosity = 0.0;
+    for (int i = 0; i < p.n_solid; ++i) s.erodible_fract[i] = 1.0 / p.n_solid;
+    s.T_erodible = 300.0;
+    s.coeff_porosity = 0.0;
+    s.erodible_init = 0.0;
+  } else {
+    if (p.erodible_porosity < 0.0 || p.erodible_porosity > 1.0) { err = "erodible_porosity must be in [0, 1]"; return SFLOW_EINVAL; }
+    s.erodible_porosity = p.erodible_porosity;
+    s.coeff_porosity = p.erodible_porosity / (1.0 - p.erodible_porosity);
+    if (p.n_solid == 1) {
+      s.erodible_fract[0] = 1.0;
+    } else {
+      double sum = 0.0;
+      for (int i = 0; i < p.n_solid; ++i) {
+        if (p.erodible_fract[i] < 0.0) { err = "erodible_fract must be >= 0"; return SFLOW_EINVAL; }
+        s.erodible_fract[i] = p.erodible_fract[i];
+        sum += p.erodible_fract[i];
+      }
+      if (sum != 1.0) {
+        if (!(sum > 0.0)) { err = "erodible_fract sums to 0"; return SFLOW_EINVAL; }
+        for (int i = 0; i < p.n_solid; ++i) s.erodible_fract[i] = s.erodible_fract[i] / sum;
+      }
+    }
+    if (p.T_erodible < 0.0) { err = "T_erodible must be given (>= 0) with erosion"; return SFLOW_EINVAL; }
+    s.T_erodible = p.T_erodible;
+    s.erodible_init = p.initial_erodible_thickness >= 0.0 ? p.initial_erodible_thickness : 0.0;
+  }
   s.rho_c_sub = p.gas_flag ? p.pres / (p.sp_gas_const_a * s.T_erodible) : p.rho_l;
+  s.exchange = (p.erosion_coeff != 0.0 || p.settling_flag || p.entrainment_flag) ? 1 : 0;
+
+  // vulnerability table levels (inpout_2d.f90:3808-3866)
+  {
+    int nt = 0, nd = 0;
+    for (int i = 0; i < SFLOW_MAX_LEVELS; ++i) {
+      if (p.thickness_levels[i] >= 0.0) ++nt;
+      if (p.dyn_pres_levels[i] >= 0.0) ++nd;
+    }
+    for (int i = 0; i < nt; ++i)
+      if (p.thickness_levels[i] < 0.0) { err = "thickness_levels: the levels >= 0 must come first"; return SFLOW_EINVAL; }
+    for (int i = 0; i < nd; ++i)
+      if (p.dyn_pres_levels[i] < 0.0) { err = "dyn_pres_levels: the levels >= 0 must come first"; return SFLOW_EINVAL; }
+    for (int i = 0; i < nt; ++i) s.thk_levels[i] = p.thickness_levels[i];
+    for (int i = 0; i < nd; ++i) s.dyn_levels[i] = p.dyn_pres_levels[i];
+    if (nt > 0 && nd == 0) { nd = 1; s.dyn_levels[0] = 0.0; }
+    if (nd > 0 && nt == 0) { nt = 1; s.thk_levels[0] = 0.0; }
+    s.n_thk = nt;
+    s.n_dyn = nd;
+  }
 
   // IMEX tableaux (solver_2d.f90:421-487)
   {
@@ -335,13 +436,32 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
 
   if (!B) { err = "B_cent is NULL"; return SFLOW_EINVAL; }
   topography(s, B);
+  s.B.assign(B, B + (size_t)s.nx * s.ny);
 
-  // inlet (radial ring) constants
+  // inlet (radial ring / bottom source) constants
   s.h_source = p.h_source;
   for (int i = 0; i < 4; ++i) s.time_param[i] = p.time_param[i];
-  if (p.radial_source_flag) {
+  if (p.n_intervals != 0) {
+    // inpout_2d.f90:4451-4512
+    if (!p.bottom_radial_source_flag) { err = "n_intervals needs bottom_radial_source_flag"; return SFLOW_EINVAL; }
+    if (p.n_intervals < 0 || p.n_intervals > SFLOW_MAX_INTERVALS) { err = "n_intervals must be in 0..100"; return SFLOW_EINVAL; }
+    for (int i = 0; i < p.n_intervals; ++i) {
+      if (p.t_intervals[i] < 0.0) { err = "t_intervals must be >= 0"; return SFLOW_EINVAL; }
+      if (p.vel_intervals[i] < 0.0) { err = "vel_intervals must be >= 0"; return SFLOW_EINVAL; }
+      if (i > 0 && p.t_intervals[i] <= p.t_intervals[i - 1]) { err = "t_intervals must increase"; return SFLOW_EINVAL; }
+    }
+  }
+  if (p.bottom_radial_source_flag) {
+    // inpout_2d.f90:4029-4075: the inflow is vel_source over the ellipse
+    if (p.h_source >= 0.0 || p.mfr_source >= 0.0) {
+      err = "h_source / mfr_source must not be given with bottom_radial_source_flag";
+      return SFLOW_EINVAL;
+    }
+    if (p.vel_source == -1.0) { err = "vel_source must be given with bottom_radial_source_flag"; return SFLOW_EINVAL; }
+  }
+  if (p.radial_source_flag || p.bottom_radial_source_flag) {
     if (!(p.r_source > 0.0)) { err = "r_source must be > 0"; return SFLOW_EINVAL; }
-    if (p.r2_source <= 0.0) p.r2_source = p.r_source;
+    if (p.r2_source <= 0.0) { p.r2_source = p.r_source; p.angle_source = 0.0; }
     // inpout_2d.f90:4140-4175: the ring must stay a cell away from the edges
     const double rmax_ = std::fmax(p.r_source, p.r2_source);
     if (p.x_source - rmax_ <= p.x0 + p.cell_size || p.x_source + rmax_ >= p.x0 + (p.comp_cells_x - 1) * p.cell_size ||
@@ -353,13 +473,14 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
       s.time_param[0] = p.t_end; s.time_param[1] = p.t_end; s.time_param[2] = 0.0; s.time_param[3] = p.t_end;
     }
     double qs[SFLOW_MAX_VARS + 2] = {0};
-    const double r1 = p.r_source, r2 = p.r2_source;
-    const double he = sqd(r1 - r2) / sqd(r1 + r2);
-    double len = s.pi_g * (r1 + r2) *
-                 (1.0 + 0.25 * he + sqd(he) / 64.0 + he * he * he / 256.0 + sqd(sqd(he)) * 25.0 / 16384.0 +
-                  sqd(sqd(he)) * he * 49.0 / 65536.0);
-    if (p.arc_width_source < 360.0) len = len * (p.arc_width_source / 360.0);
-    if (p.mfr_source >= 0.0) {
+    if (p.radial_source_flag && p.mfr_source >= 0.0) {
+      // inlet thickness from the mass flow rate over the ring's length
+      const double r1 = p.r_source, r2 = p.r2_source;
+      const double he = sqd(r1 - r2) / sqd(r1 + r2);
+      double len = s.pi_g * (r1 + r2) *
+                   (1.0 + 0.25 * he + sqd(he) / 64.0 + he * he * he / 256.0 + sqd(sqd(he)) * 25.0 / 16384.0 +
+                    sqd(sqd(he)) * he * 49.0 / 65536.0);
+      if (p.arc_width_source < 360.0) len = len * (p.arc_width_source / 360.0);
       if (!(p.vel_source > 0.0)) { err = "vel_source must be > 0 with mfr_source"; return SFLOW_EINVAL; }
       const double hs = 1.0;
       qs[0] = hs; qs[1] = hs * p.vel_source; qs[2] = 0.0; qs[3] = p.T_source;
@@ -370,7 +491,8 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
       s.h_source = p.mfr_source / (len * rho_m * p.vel_source * 1.0);
       s.time_param[1] = 1.0e14 / p.mfr_source;
     }
-    // inlet state of eval_expl_terms (constitutive_2d.f90:3351-3384)
+    // inflow state of eval_expl_terms (constitutive_2d.f90:3192-3225,
+    // 3351-3384): h = 1, T_source, alphas_source, at rest
     for (int i = 0; i < SFLOW_MAX_VARS + 2; ++i) qs[i] = 0.0;
     qs[0] = 1.0;
     qs[3] = p.T_source;
@@ -378,6 +500,7 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
     host_mixt_var(s, qs, &s.src_rho_m, &s.src_cp_mix);
   }
   ring_source(s);
+  if (p.bottom_radial_source_flag) cell_fractions(s);
   return SFLOW_OK;
 }
 

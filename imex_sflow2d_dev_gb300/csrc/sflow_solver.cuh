@@ -143,12 +143,7 @@ class Solver : public SolverBase {
       SFLOW_CU(put_plane(geo_[i], *gsrc[i]));
     }
     SFLOW_CU(alloc((void**)&cflags_, plane_));
-    {
-      std::vector<uint8_t> f((size_t)plane_, 0);
-      for (int k = 0; k < ny; ++k)
-        for (int j = 0; j < nx; ++j) f[(size_t)k * pitch_ + j] = hs_.cflags[(size_t)k * nx + j];
-      SFLOW_CU(cudaMemcpy(cflags_, f.data(), plane_, cudaMemcpyHostToDevice));
-    }
+    SFLOW_CU(put_flags());
     SFLOW_CU(alloc((void**)&arc_, sizeof(R) * plane_ * 3));
     SFLOW_CU(put_plane(arc_, hs_.arc_perim));
     SFLOW_CU(put_plane(arc_ + plane_, hs_.arc_nx));
@@ -159,9 +154,36 @@ class Solver : public SolverBase {
     SFLOW_CU(alloc((void**)&hmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&pdynmax_, sizeof(R) * plane_));
     SFLOW_CU(alloc((void**)&mvmax_, sizeof(R) * plane_));
-    if (hs_.p.settling_flag || hs_.p.entrainment_flag) {
+    if (hs_.exchange) {
       SFLOW_CU(alloc((void**)&deposit_, sizeof(double) * plane_ * hs_.ns));
       SFLOW_CU(cudaMemset(deposit_, 0, sizeof(double) * plane_ * hs_.ns));
+    }
+    if (hs_.p.erosion_coeff > 0.0 || (hs_.p.erodible_deposit_flag && hs_.exchange)) {
+      // erosion, or deposits that build the erodible layer
+      SFLOW_CU(alloc((void**)&erosion_, sizeof(double) * plane_ * hs_.ns));
+      SFLOW_CU(alloc((void**)&erodible_, sizeof(double) * plane_ * hs_.ns));
+      SFLOW_CU(reset_erosion());
+    }
+    if (hs_.p.topo_change_flag && hs_.exchange) {
+      SFLOW_CU(alloc((void**)&Bc_, sizeof(double) * plane_));
+      SFLOW_CU(put_plane_d(Bc_, hs_.B));
+    }
+    if (hs_.p.bottom_radial_source_flag) {
+      SFLOW_CU(alloc((void**)&bfrac_, sizeof(R) * plane_));
+      SFLOW_CU(put_plane(bfrac_, hs_.cell_fract));
+      std::vector<double> tab(1 + 2 * (size_t)SFLOW_MAX_INTERVALS, 0.0);
+      tab[0] = (double)hs_.p.n_intervals;
+      for (int i = 0; i < hs_.p.n_intervals; ++i) {
+        tab[1 + i] = hs_.p.t_intervals[i];
+        tab[1 + hs_.p.n_intervals + i] = hs_.p.vel_intervals[i];
+      }
+      SFLOW_CU(alloc((void**)&bsrc_tab_, sizeof(double) * tab.size()));
+      SFLOW_CU(cudaMemcpy(bsrc_tab_, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+    }
+    if (hs_.n_thk * hs_.n_dyn > 0) {
+      vuln_words_ = (hs_.n_thk * hs_.n_dyn + 31) / 32;
+      SFLOW_CU(alloc((void**)&vuln_, sizeof(uint32_t) * plane_ * vuln_words_));
+      SFLOW_CU(cudaMemset(vuln_, 0, sizeof(uint32_t) * plane_ * vuln_words_));
     }
     SFLOW_CU(alloc((void**)&st_, sizeof(RunState)));
     nstat_blocks_ = 1024;
@@ -255,6 +277,8 @@ class Solver : public SolverBase {
     SFLOW_CU(cudaMemcpyAsync(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice, stream_));
     SFLOW_CU(dispatch_init_maps((unsigned)((N + 255) / 256)));
     if (deposit_) SFLOW_CU(cudaMemsetAsync(deposit_, 0, sizeof(double) * plane_ * hs_.ns, stream_));
+    if (erosion_) SFLOW_CU(reset_erosion());
+    if (Bc_) SFLOW_CU(reset_topography());
     SFLOW_CU(cudaMemsetAsync(tile_wet_, 0xff, 3 * (size_t)tiles_x_ * tiles_y_, stream_));
     SFLOW_CU(cudaStreamSynchronize(stream_));
     uploaded_ = true;
@@ -449,6 +473,74 @@ class Solver : public SolverBase {
     }
     return SFLOW_OK;
   }
+  // erosion (accumulated dt * erosion_term) or the erodible layer, n_solid
+  // planes of nx*ny (class slowest)
+  int download_erosion(int which, double* out) override {
+    const double* src = which == 0 ? erosion_ : erodible_;
+    if (!src) {
+      std::memset(out, 0, sizeof(double) * (size_t)hs_.nx * hs_.ny * hs_.ns);
+      return SFLOW_OK;
+    }
+    for (int i = 0; i < hs_.ns; ++i) SFLOW_CU(get_plane_d(out + (size_t)i * hs_.nx * hs_.ny, src + (size_t)i * plane_));
+    return SFLOW_OK;
+  }
+  // B_cent (changes with TOPO_CHANGE_FLAG)
+  int download_topography(double* out) override {
+    if (!Bc_) {
+      std::memcpy(out, hs_.B.data(), sizeof(double) * hs_.B.size());
+      return SFLOW_OK;
+    }
+    return get_plane_d(out, Bc_) == cudaSuccess ? SFLOW_OK : SFLOW_ECUDA;
+  }
+  // erodible layer thickness per cell (the reference's erodible_init: each
+  // class gets erodible_fract * (1 - erodible_porosity) of it)
+  int set_erodible(const double* thickness) override {
+    if (!erodible_) { err_ = "the run has no erodible layer (erosion_coeff = 0)"; return SFLOW_EINVAL; }
+    const size_t N = (size_t)hs_.nx * hs_.ny;
+    std::vector<double> pl(N);
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    for (int i = 0; i < hs_.ns; ++i) {
+      for (size_t c = 0; c < N; ++c) pl[c] = hs_.erodible_fract[i] * (1.0 - hs_.erodible_porosity) * thickness[c];
+      SFLOW_CU(put_plane_d(erodible_ + (size_t)i * plane_, pl));
+    }
+    erodible_user_.assign(thickness, thickness + N);
+    return SFLOW_OK;
+  }
+  // B_nodata cells (nonzero): the assembly empties them
+  int set_nodata(const uint8_t* nodata) override {
+    const int nx = hs_.nx, ny = hs_.ny;
+    bool any = false;
+    for (int k = 0; k < ny; ++k)
+      for (int j = 0; j < nx; ++j) {
+        uint8_t& f = hs_.cflags[(size_t)k * nx + j];
+        f = (uint8_t)((f & ~kFlagNodata) | (nodata && nodata[(size_t)k * nx + j] ? kFlagNodata : 0));
+        any |= (f & kFlagNodata) != 0;
+      }
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    SFLOW_CU(put_flags());
+    ka_.pr.nodata = ka_.pd.nodata = any ? 1 : 0;
+    drop_graphs();
+    return SFLOW_OK;
+  }
+  // vulnerability table: n_thk * n_dyn planes of nx*ny bytes (0/1)
+  int vuln_table(int* n_thk, int* n_dyn, uint8_t* out) override {
+    if (n_thk) *n_thk = hs_.n_thk;
+    if (n_dyn) *n_dyn = hs_.n_dyn;
+    if (!out || !vuln_) return SFLOW_OK;
+    const int nx = hs_.nx, ny = hs_.ny;
+    std::vector<uint32_t> buf((size_t)plane_);
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    const int ne = hs_.n_thk * hs_.n_dyn;
+    for (int w = 0; w < vuln_words_; ++w) {
+      SFLOW_CU(cudaMemcpy(buf.data(), vuln_ + (size_t)w * plane_, sizeof(uint32_t) * plane_, cudaMemcpyDeviceToHost));
+      for (int e = 32 * w; e < std::min(ne, 32 * w + 32); ++e)
+        for (int k = 0; k < ny; ++k)
+          for (int j = 0; j < nx; ++j)
+            out[(size_t)e * nx * ny + (size_t)k * nx + j] = (uint8_t)((buf[(size_t)k * pitch_ + j] >> (e & 31)) & 1u);
+    }
+    return SFLOW_OK;
+  }
+
   int set_output_time(double t_output) override {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
     SFLOW_CU(cudaMemcpyAsync(&st_->t_output, &t_output, sizeof(double), cudaMemcpyHostToDevice, stream_));
@@ -524,7 +616,8 @@ class Solver : public SolverBase {
   int erosion_deposition(double dt) override {
     SFLOW_CU(reset_wet_flags());
     if (dt != pending_dt_) { err_ = "dt differs from the last sflow_imex_rk"; return SFLOW_ESTATE; }
-    if (hs_.p.settling_flag || hs_.p.entrainment_flag) SFLOW_CU(launch_stage2(1));
+    if (hs_.exchange) SFLOW_CU(launch_stage2(1));
+    if (Bc_) SFLOW_CU(launch_topography());
     return SFLOW_OK;
   }
   int post_step(SflowStepStats* s) override {
@@ -722,6 +815,11 @@ class Solver : public SolverBase {
   cudaStream_t stream_ = nullptr;
   R *q_ = nullptr, *rd_ = nullptr, *rn_ = nullptr, *qs_ = nullptr, *arc_ = nullptr, *hmax_ = nullptr, *pdynmax_ = nullptr, *mvmax_ = nullptr;
   double* deposit_ = nullptr;
+  double *erosion_ = nullptr, *erodible_ = nullptr, *Bc_ = nullptr, *bsrc_tab_ = nullptr;
+  R* bfrac_ = nullptr;
+  uint32_t* vuln_ = nullptr;
+  int vuln_words_ = 0;
+  std::vector<double> erodible_user_;   // thickness set by set_erodible (else uniform)
   R* geo_[8];
   uint8_t *cflags_ = nullptr, *mask_ = nullptr, *tile_active_ = nullptr, *tile_wet_ = nullptr,
           *tile_static_ = nullptr;
@@ -782,8 +880,9 @@ class Solver : public SolverBase {
   }
 
   int steps_launches() const {
-    if (hs_.nrk == 2) return 4;
-    int n = 3 + hs_.nrk + 1;
+    const int topo = Bc_ ? 1 : 0;
+    if (hs_.nrk == 2) return 4 + topo;
+    int n = 3 + hs_.nrk + 1 + topo;
     const bool fused0 = hs_.a_dirk[0] == 0.0 && hs_.omega_tilde[0] > 0.0;
     for (int i = 0; i < hs_.nrk; ++i)
       if (hs_.omega_tilde[i] > 0.0 && !(i == 0 && fused0)) ++n;
@@ -823,8 +922,8 @@ class Solver : public SolverBase {
     }
     return e;
   }
-  // tiles with a border cell or a ring-boundary cell (seeds of every
-  // check_solve) within n_RK cells
+  // tiles with a border cell, a ring-boundary cell or a bottom-source cell
+  // (seeds of every check_solve) within n_RK cells
   std::vector<uint8_t> tile_static_host() const {
     const int nx = hs_.nx, ny = hs_.ny, r = hs_.nrk, th = tile_h_;
     std::vector<uint8_t> ts((size_t)tiles_x_ * tiles_y_, 0);
@@ -833,10 +932,12 @@ class Solver : public SolverBase {
         const int j0 = tx * TX - r, j1 = std::min(nx, (tx + 1) * TX) - 1 + r;
         const int k0 = ty * th - r, k1 = std::min(ny, (ty + 1) * th) - 1 + r;
         uint8_t v = (j0 <= 0 || j1 >= nx - 1 || k0 <= 0 || k1 >= ny - 1) ? 1 : 0;
-        if (!v && hs_.p.radial_source_flag)
+        if (!v && (hs_.p.radial_source_flag || hs_.p.bottom_radial_source_flag))
           for (int k = std::max(k0, 0); k <= std::min(k1, ny - 1) && !v; ++k)
-            for (int j = std::max(j0, 0); j <= std::min(j1, nx - 1); ++j)
-              if ((hs_.cflags[(size_t)k * nx + j] & 3) == 2) { v = 1; break; }
+            for (int j = std::max(j0, 0); j <= std::min(j1, nx - 1); ++j) {
+              const uint8_t f = hs_.cflags[(size_t)k * nx + j];
+              if ((f & 3) == 2 || (f & kFlagBottom)) { v = 1; break; }
+            }
         ts[(size_t)ty * tiles_x_ + tx] = v;
       }
     return ts;
@@ -898,6 +999,57 @@ class Solver : public SolverBase {
     return cudaMemcpy(dst, buf.data(), sizeof(R) * plane_, cudaMemcpyHostToDevice);
   }
 
+  cudaError_t put_flags() {
+    const int nx = hs_.nx, ny = hs_.ny;
+    std::vector<uint8_t> f((size_t)plane_, 0);
+    for (int k = 0; k < ny; ++k)
+      for (int j = 0; j < nx; ++j) f[(size_t)k * pitch_ + j] = hs_.cflags[(size_t)k * nx + j];
+    return cudaMemcpy(cflags_, f.data(), plane_, cudaMemcpyHostToDevice);
+  }
+  cudaError_t put_plane_d(double* dst, const std::vector<double>& src) {
+    std::vector<double> buf((size_t)plane_, 0.0);
+    for (int k = 0; k < hs_.ny; ++k)
+      for (int j = 0; j < hs_.nx; ++j) buf[(size_t)k * pitch_ + j] = src[(size_t)k * hs_.nx + j];
+    return cudaMemcpy(dst, buf.data(), sizeof(double) * plane_, cudaMemcpyHostToDevice);
+  }
+  cudaError_t get_plane_d(double* out, const double* src) {
+    std::vector<double> buf((size_t)plane_);
+    cudaError_t e = cudaStreamSynchronize(stream_);
+    if (e == cudaSuccess) e = cudaMemcpy(buf.data(), src, sizeof(double) * plane_, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    for (int k = 0; k < hs_.ny; ++k)
+      for (int j = 0; j < hs_.nx; ++j) out[(size_t)k * hs_.nx + j] = buf[(size_t)k * pitch_ + j];
+    return cudaSuccess;
+  }
+  // erosion 0; erodible layer = erodible_fract * (1 - porosity) * thickness
+  // (inpout_2d.f90:1983-1986), the thickness uniform or set by set_erodible
+  cudaError_t reset_erosion() {
+    const size_t N = (size_t)hs_.nx * hs_.ny;
+    cudaError_t e = cudaStreamSynchronize(stream_);
+    if (e == cudaSuccess) e = cudaMemset(erosion_, 0, sizeof(double) * plane_ * hs_.ns);
+    std::vector<double> pl(N);
+    for (int i = 0; i < hs_.ns && e == cudaSuccess; ++i) {
+      const double f = hs_.erodible_fract[i] * (1.0 - hs_.erodible_porosity);
+      for (size_t c = 0; c < N; ++c) pl[c] = f * (erodible_user_.empty() ? hs_.erodible_init : erodible_user_[c]);
+      e = put_plane_d(erodible_ + (size_t)i * plane_, pl);
+    }
+    return e;
+  }
+  // B_cent and its topography terms as set up
+  cudaError_t reset_topography() {
+    cudaError_t e = cudaStreamSynchronize(stream_);
+    if (e == cudaSuccess) e = put_plane_d(Bc_, hs_.B);
+    const std::vector<double>* gsrc[8] = {&hs_.Bx, &hs_.By, &hs_.Bxx, &hs_.Bxy, &hs_.Byy, &hs_.gc, &hs_.dgcx, &hs_.dgcy};
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i)
+      if (geo_[i]) e = put_plane(geo_[i], *gsrc[i]);
+    return e;
+  }
+  cudaError_t launch_topography() {
+    ++launches_;
+    const int64_t n = (int64_t)hs_.nx * hs_.ny;
+    return launch_step_kernel(k_topography<R>, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, stream_, ka_.g.pdl, ka_);
+  }
+
   static R thr(double x) {
     if constexpr (sizeof(R) == 8) return x;
     else return float_below(x);
@@ -947,8 +1099,33 @@ class Solver : public SolverBase {
     P.kin_visc_c = (T)hs_.kin_visc_c; P.loss_rate = (T)p.loss_rate;
     P.alphastot_min = (T)p.alphastot_min; P.max_packing = (T)p.maximum_solid_packing;
     P.A_drag = (T)p.A_drag; P.B_drag = (T)p.B_drag;
-    P.coeff_porosity = (T)0.0; P.rho_c_sub = (T)hs_.rho_c_sub; P.T_erodible = (T)hs_.T_erodible;
-    P.erodible_porosity = (T)0.0;
+    P.coeff_porosity = (T)hs_.coeff_porosity; P.rho_c_sub = (T)hs_.rho_c_sub; P.T_erodible = (T)hs_.T_erodible;
+    P.erodible_porosity = (T)hs_.erodible_porosity;
+    P.erosion_coeff = (T)p.erosion_coeff;
+    for (int i = 0; i < kMaxSolid; ++i) P.erodible_fract[i] = (T)hs_.erodible_fract[i];
+    P.erodible_deposit = p.erodible_deposit_flag ? 1 : 0;
+    P.topo_change = p.topo_change_flag ? 1 : 0;
+    P.bottom_source = p.bottom_radial_source_flag ? 1 : 0;
+    P.exchange = hs_.exchange;
+    P.nodata = 0;
+    for (size_t c = 0; c < hs_.cflags.size(); ++c)
+      if (hs_.cflags[c] & kFlagNodata) { P.nodata = 1; break; }
+    // levels: a float h satisfies h >= level exactly when (double)h does,
+    // with level rounded up to the next float
+    auto up = [&](double x) -> T {
+      if constexpr (sizeof(T) == 8) return x;
+      else {
+        float f = (float)x;
+        if ((double)f < x) f = std::nextafterf(f, INFINITY);
+        return f;
+      }
+    };
+    P.n_thk = hs_.n_thk;
+    P.n_dyn = hs_.n_dyn;
+    for (int i = 0; i < SFLOW_MAX_LEVELS; ++i) {
+      P.thk_levels[i] = up(hs_.thk_levels[i]);
+      P.dyn_levels[i] = up(hs_.dyn_levels[i]);
+    }
   }
 
   void fill_args() {
@@ -998,6 +1175,13 @@ class Solver : public SolverBase {
     ka_.tile_count = tile_count_;
     ka_.hmax = hmax_; ka_.pdynmax = pdynmax_; ka_.mvmax = mvmax_; ka_.st = st_;
     ka_.deposit = deposit_;
+    ka_.erosion = erosion_;
+    ka_.erodible = erodible_;
+    ka_.Bc = Bc_;
+    ka_.bfrac = bfrac_;
+    ka_.bsrc_tab = bsrc_tab_;
+    ka_.vuln = vuln_;
+    ka_.vuln_words = vuln_words_;
     ka_.take_last = hs_.take_last;
   }
 
@@ -1052,18 +1236,22 @@ class Solver : public SolverBase {
     return tab_.stage2(ka_, dim3(tiles_x_, tiles_y_), stream_, mode);
   }
 
+  // one step; with a changing topography its terms are recomputed after it
   cudaError_t launch_step() {
+    cudaError_t e;
     if (hs_.nrk == 2) {
-      cudaError_t e = launch_mask(2);
-      if (e != cudaSuccess) return e;
-      e = launch_flux(1);
-      if (e != cudaSuccess) return e;
-      e = launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt);
-      ++launches_;
-      if (e != cudaSuccess) return e;
-      return launch_stage2(-1);
+      e = launch_mask(2);
+      if (e == cudaSuccess) e = launch_flux(1);
+      if (e == cudaSuccess) {
+        e = launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt);
+        ++launches_;
+      }
+      if (e == cudaSuccess) e = launch_stage2(-1);
+    } else {
+      e = launch_step_general();
     }
-    return launch_step_general();
+    if (e == cudaSuccess && Bc_) e = launch_topography();
+    return e;
   }
 
   // N_RK = 1, 3, 4: the timestep pass at q0 (fused with the stage-1 flux

@@ -80,6 +80,14 @@ __global__ void k_init_maps(KArgs<R> a) {
   a.hmax[d] = h;
   a.pdynmax[d] = pd;
   a.mvmax[d] = mv;
+  if (a.vuln) {
+    if (q[0] > R(0)) {
+      const R p_dyn = qc_to_qp<R, NS>(a.pr, q, qp);
+      vuln_update<R>(a, d, qp[0], p_dyn, false);
+    } else {
+      for (int w = 0; w < a.vuln_words; ++w) a.vuln[(int64_t)w * g.plane + d] = 0u;
+    }
+  }
 }
 
 // log-line sums over all cells (IMEX_SfloW2D.f90:535-542) in FP64 with a

@@ -33,6 +33,18 @@ struct Phys {
   R diam_s[kMaxSolid];
   R alphastot_min, max_packing, A_drag, B_drag, coeff_porosity, rho_c_sub, T_erodible,
       erodible_porosity;
+  // erosion of the erodible layer (constitutive_2d.f90:4732-4760)
+  R erosion_coeff, erodible_fract[kMaxSolid];
+  int erodible_deposit, topo_change;
+  // bottom radial source (constitutive_2d.f90:3149-3307)
+  int bottom_source;
+  int nodata;     // some cell is B_nodata (emptied by the assembly)
+  int exchange;   // update_erosion_deposition_cell runs: settling, entrainment or erosion
+  // vulnerability table (IMEX_SfloW2D.f90:351, 489): levels as R (for the
+  // FP32 form the smallest float not below the FP64 level, so that a float
+  // compares with it as its FP64 value would)
+  int n_thk, n_dyn;
+  R thk_levels[SFLOW_MAX_LEVELS], dyn_levels[SFLOW_MAX_LEVELS];
 };
 
 // Topography terms of one cell.
@@ -85,6 +97,10 @@ struct RunState {
   int pad2;
   double tp[4];                    // time_param
   double pi_g;
+  // bottom radial source at this step's t: time factor and inflow velocity
+  // (constitutive_2d.f90:3151-3187)
+  double bsrc_t_coeff, bsrc_vel;
+  float bsrc_t_coeff_f, bsrc_vel_f;
   // active cells of dry border tiles (tile code 3: counted, not computed)
   unsigned long long border_acc[2];
   long long border_total;

@@ -39,8 +39,6 @@ class Run:
         self.p, self.run = p, run
         nx, ny = p.comp_cells_x, p.comp_cells_y
         B, nodata = L.read_dem(self._path(run["topography_file"]), p)
-        if nodata.any():
-            raise L.SflowError(-1, "the DEM has NODATA cells inside the domain (B_nodata is not supported)")
         rf = run["restart_file"]
         self.t = p.t_start
         state = None
@@ -56,9 +54,11 @@ class Run:
             raise L.SflowError(-1, f"restart file {rf}: only .q_2d and restart.bin are supported")
         self.B = np.ascontiguousarray(B, dtype=np.float64)
         self.solver = L.Solver(p, self.B)
+        if nodata.any():
+            self.solver.set_nodata(nodata)   # emptied by every assembly (solver_2d.f90:1626)
         self.solver.upload_q(q)
         if state is not None:
-            if p.settling_flag or p.entrainment_flag:
+            if p.settling_flag or p.entrainment_flag or p.erosion_coeff != 0.0:
                 self.solver.upload_deposit(state["deposit"])
             self.solver.upload_maps(state["hmax"], state["pdynmax"], state["mod_vel_max"])
             self.solver.set_clock(state["t"], state["dt"], state["dt"])
@@ -81,6 +81,8 @@ class Run:
             L.write_q2d(name, p, q)
             self.solver.put_q(q)   # the reference zeroes tiny values in its state
             self.written.append(name)
+        if p.topo_change_flag:
+            self.B = self.solver.download_topography()
         if run["output_phys_flag"]:
             phys = self.solver.download_phys()
             dep = self.solver.download_deposit()
@@ -93,6 +95,8 @@ class Run:
 
     def write_restart(self):
         st = self.solver.stats()
+        if self.p.topo_change_flag:
+            self.B = self.solver.download_topography()
         h, pd, v = self.solver.maps()
         name = self._path("restart.bin")
         L.write_restart(name, self.p, st.t, st.dt, self.solver.download_q(), self.B,

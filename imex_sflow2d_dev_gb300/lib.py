@@ -83,6 +83,13 @@ def load(build_if_missing=True):
         "sflow_upload_deposit": (C.c_int, [vp, dp]),
         "sflow_upload_maps": (C.c_int, [vp, dp, dp, dp]),
         "sflow_set_output_time": (C.c_int, [vp, C.c_double]),
+        "sflow_download_erosion": (C.c_int, [vp, dp]),
+        "sflow_download_erodible": (C.c_int, [vp, dp]),
+        "sflow_set_erodible": (C.c_int, [vp, dp]),
+        "sflow_download_topography": (C.c_int, [vp, dp]),
+        "sflow_set_nodata": (C.c_int, [vp, C.POINTER(C.c_uint8)]),
+        "sflow_vuln_table_size": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32)]),
+        "sflow_download_vuln_table": (C.c_int, [vp, C.POINTER(C.c_uint8)]),
         "sflow_batch_create": (C.c_int, [i32, i32, i64, C.POINTER(vp)]),
         "sflow_batch_destroy": (None, [vp]),
         "sflow_batch_submit": (C.c_int, [vp, P, dp, dp, i64, C.POINTER(i32)]),
@@ -140,7 +147,9 @@ def exported_symbols():
             "sflow_eval_math", "sflow_batch_advance_timed", "sflow_batch_profile_kernels",
             "sflow_setup_create", "sflow_setup_destroy", "sflow_batch_submit_setup",
             "sflow_batch_launch", "sflow_batch_wait", "sflow_batch_dry_border_updates",
-            "sflow_dry_border_updates"]
+            "sflow_dry_border_updates", "sflow_download_erosion", "sflow_download_erodible",
+            "sflow_set_erodible", "sflow_download_topography", "sflow_set_nodata",
+            "sflow_vuln_table_size", "sflow_download_vuln_table"]
 
 
 TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
@@ -458,6 +467,50 @@ class Solver:
     def upload_deposit(self, dep):
         d = np.ascontiguousarray(dep, dtype=np.float64).reshape(-1)
         _check(self.lib.sflow_upload_deposit(self.h, _dp(d)))
+
+    def _cells(self):
+        return self.p.comp_cells_x * self.p.comp_cells_y
+
+    def download_erosion(self):
+        """Accumulated erosion per class (class slowest, nx*ny each)."""
+        out = np.empty(self._cells() * self.p.n_solid)
+        _check(self.lib.sflow_download_erosion(self.h, _dp(out)))
+        return out
+
+    def download_erodible(self):
+        """Erodible solid thickness left per class."""
+        out = np.empty(self._cells() * self.p.n_solid)
+        _check(self.lib.sflow_download_erodible(self.h, _dp(out)))
+        return out
+
+    def set_erodible(self, thickness):
+        """Erodible layer thickness per cell (ERODIBLE_FILE's field)."""
+        t = np.ascontiguousarray(thickness, dtype=np.float64).reshape(-1)
+        _check(self.lib.sflow_set_erodible(self.h, _dp(t)))
+
+    def download_topography(self):
+        out = np.empty(self._cells())
+        _check(self.lib.sflow_download_topography(self.h, _dp(out)))
+        return out
+
+    def set_nodata(self, nodata):
+        """B_nodata per cell (None clears)."""
+        if nodata is None:
+            _check(self.lib.sflow_set_nodata(self.h, None))
+            return
+        m = np.ascontiguousarray(nodata, dtype=np.uint8).reshape(-1)
+        _check(self.lib.sflow_set_nodata(self.h, m.ctypes.data_as(C.POINTER(C.c_uint8))))
+
+    def vuln_table(self):
+        """(n_thk, n_dyn, table as uint8 [n_thk*n_dyn, ny, nx]) or None."""
+        a, b = C.c_int32(0), C.c_int32(0)
+        _check(self.lib.sflow_vuln_table_size(self.h, C.byref(a), C.byref(b)))
+        n = a.value * b.value
+        if n == 0:
+            return None
+        out = np.empty(n * self._cells(), dtype=np.uint8)
+        _check(self.lib.sflow_download_vuln_table(self.h, out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return a.value, b.value, out.reshape(n, self.p.comp_cells_y, self.p.comp_cells_x)
 
     def upload_maps(self, hmax=None, pdynmax=None, mod_vel_max=None):
         arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) if a is not None else None

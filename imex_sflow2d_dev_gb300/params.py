@@ -6,9 +6,11 @@ onto SflowParams one to one.
 """
 import ctypes as C
 
-SFLOW_ABI_VERSION = 1
+SFLOW_ABI_VERSION = 2
 MAX_SOLID = 4
 MAX_VARS = 4 + MAX_SOLID
+MAX_LEVELS = 10
+MAX_INTERVALS = 100
 
 PREC_FP64 = 0
 PREC_FP32 = 1
@@ -72,6 +74,14 @@ class SflowParams(C.Structure):
         ("time_param", C.c_double * 4),
         ("azimuth_source", C.c_double), ("arc_width_source", C.c_double),
         ("t_start", C.c_double), ("t_end", C.c_double), ("dt_output", C.c_double),
+        # ABI version 2
+        ("thickness_levels", C.c_double * MAX_LEVELS), ("dyn_pres_levels", C.c_double * MAX_LEVELS),
+        ("erodible_porosity", C.c_double), ("T_erodible", C.c_double),
+        ("initial_erodible_thickness", C.c_double), ("erodible_fract", C.c_double * MAX_SOLID),
+        ("erodible_deposit_flag", C.c_int32), ("topo_change_flag", C.c_int32),
+        ("bottom_radial_source_flag", C.c_int32), ("n_intervals", C.c_int32),
+        ("angle_source", C.c_double),
+        ("t_intervals", C.c_double * MAX_INTERVALS), ("vel_intervals", C.c_double * MAX_INTERVALS),
     ]
 
     @property
@@ -106,8 +116,12 @@ def params_to_dict(p):
 
 
 def params_from_dict(d):
-    p = SflowParams()
+    """SflowParams from params_to_dict output; keys the dict does not hold
+    (fields added after it was made) keep the defaults."""
+    p = default_params()
     for name, _ in SflowParams._fields_:
+        if name not in d:
+            continue
         v = d[name]
         if name == "bc":
             for s in range(4):
@@ -163,6 +177,13 @@ def default_params():
     for i in range(4):
         p.time_param[i] = -1.0
     p.t_end, p.dt_output = 5.0e-2, 5.0e-3
+    for i in range(MAX_LEVELS):
+        p.thickness_levels[i] = p.dyn_pres_levels[i] = -1.0
+    p.erodible_porosity = p.T_erodible = p.initial_erodible_thickness = -1.0
+    for i in range(MAX_SOLID):
+        p.erodible_fract[i] = -1.0
+    for i in range(MAX_INTERVALS):
+        p.t_intervals[i] = p.vel_intervals[i] = -1.0
     return p
 
 

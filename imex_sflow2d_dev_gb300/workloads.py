@@ -257,6 +257,101 @@ def pyroclastic(nx=1024, ny=1024, dx=10.0, precision=PREC_FP64, t_end=600.0, see
     return p, B, q
 
 
+def bottom_source_flow(nx=96, ny=80, dx=10.0, precision=PREC_FP64, t_end=60.0, intervals=False,
+                       angle=30.0, erosion=False, topo_change=False, vuln=False, seed=3):
+    """Hot particle-laden gas rising from a bottom radial source (an
+    ellipse of semi-axes 60 m x 40 m turned by `angle` degrees, vertical
+    inflow 4 m/s ramped by time_param, or piecewise-constant intervals) on
+    a cone + fBm DEM, with Voellmy friction, slope correction, settling and
+    optionally erosion of a 0.5 m erodible layer with topography change and
+    a vulnerability table."""
+    p = default_params()
+    p.precision = precision
+    p.comp_cells_x, p.comp_cells_y, p.cell_size = nx, ny, dx
+    p.x0 = p.y0 = 0.0
+    p.n_solid = 2
+    p.gas_flag, p.liquid_flag, p.energy_flag = 1, 0, 1
+    p.rheology_flag, p.rheology_model = 1, 1
+    p.mu, p.xi = 0.15, 800.0
+    p.slope_correction_flag = 1
+    _gas_common(p)
+    for i, (rho, d, a) in enumerate([(2500.0, 2.0e-4, 0.04), (1500.0, 1.0e-3, 0.02)]):
+        p.rho_s[i], p.diam_s[i], p.sp_heat_s[i] = rho, d, 1100.0
+        p.alphas_source[i] = a
+    p.settling_flag = 1
+    p.bottom_radial_source_flag = 1
+    p.x_source, p.y_source = 0.45 * nx * dx, 0.5 * ny * dx
+    p.r_source, p.r2_source, p.angle_source = 60.0, 40.0, angle
+    p.vel_source, p.T_source = 4.0, 900.0
+    p.h_source = p.mfr_source = -1.0
+    if intervals:
+        p.n_intervals = 3
+        for i, (t, v) in enumerate([(0.0, 4.0), (8.0, 0.0), (14.0, 6.0)]):
+            p.t_intervals[i], p.vel_intervals[i] = t, v
+    else:
+        p.time_param[0], p.time_param[1], p.time_param[2], p.time_param[3] = 40.0, 30.0, 5.0, 0.0
+    if erosion:
+        p.erosion_coeff = 2.0e-4
+        p.erodible_porosity = 0.35
+        p.T_erodible = 320.0
+        p.initial_erodible_thickness = 0.5
+        p.erodible_fract[0], p.erodible_fract[1] = 0.75, 0.5    # normalised to 0.6 / 0.4
+        p.topo_change_flag = 1 if topo_change else 0
+    if vuln:
+        for i, v in enumerate([0.05, 0.5, 2.0]):
+            p.thickness_levels[i] = v
+        for i, v in enumerate([10.0, 500.0]):
+            p.dyn_pres_levels[i] = v
+    p.n_rk = 2
+    p.cfl, p.dt0, p.max_dt = 0.24, 1.0e-2, 10.0
+    p.set_bc_all(1, 0.0)
+    p.t_start, p.t_end = 0.0, t_end
+    p.dt_output = 2.0 * (p.t_end - p.t_start)
+    B = cone_fbm_dem(nx, ny, dx, height=120.0, sigma=600.0, rms=2.0, seed=seed)
+    q = np.zeros((p.n_vars, ny, nx))
+    return p, B, q
+
+
+def eroding_dam_break(nx=120, ny=60, dx=2.0, precision=PREC_FP64, t_end=12.0, deposit_flag=False,
+                      topo_change=True):
+    """A 2 m high column of sediment-laden water released on a 6 % slope
+    over a 0.3 m erodible bed (liquid carrier, two particle classes,
+    settling, erosion, topography change)."""
+    p = default_params()
+    p.precision = precision
+    p.comp_cells_x, p.comp_cells_y, p.cell_size = nx, ny, dx
+    p.x0 = p.y0 = 0.0
+    p.n_solid = 2
+    p.gas_flag, p.liquid_flag, p.energy_flag = 0, 1, 0
+    p.rheology_flag, p.rheology_model = 1, 1
+    p.mu, p.xi = 0.05, 500.0
+    p.slope_correction_flag = 1
+    _gas_common(p)
+    p.rho_l, p.sp_heat_l, p.kin_visc_l, p.loss_rate = 1000.0, 4186.0, 1.0e-6, 0.0
+    for i, (rho, d) in enumerate([(2600.0, 3.0e-4), (2000.0, 1.0e-4)]):
+        p.rho_s[i], p.diam_s[i], p.sp_heat_s[i] = rho, d, 900.0
+    p.settling_flag = 1
+    p.erosion_coeff = 1.0e-3
+    p.erodible_porosity = 0.4
+    p.T_erodible = 290.0
+    p.initial_erodible_thickness = 0.3
+    p.erodible_fract[0], p.erodible_fract[1] = 0.5, 0.5
+    p.erodible_deposit_flag = 1 if deposit_flag else 0
+    p.topo_change_flag = 1 if topo_change else 0
+    p.n_rk = 2
+    p.cfl, p.dt0, p.max_dt = 0.24, 1.0e-3, 1.0
+    p.set_bc_all(1, 0.0)
+    p.t_start, p.t_end = 0.0, t_end
+    p.dt_output = 2.0 * (p.t_end - p.t_start)
+    x = (np.arange(nx) + 0.5) * dx
+    y = (np.arange(ny) + 0.5) * dx
+    B = np.broadcast_to(0.06 * (nx * dx - x)[None, :], (ny, nx)).copy()
+    r2 = (x[None, :] - 0.2 * nx * dx) ** 2 + (y[:, None] - 0.5 * ny * dx) ** 2
+    h = np.where(r2 <= (0.15 * ny * dx) ** 2, 2.0, 0.0)
+    q = rest_state_q(p, h, 290.0, [0.15, 0.1])
+    return p, B, q
+
+
 def developed_current_state(p, B, radius=3500.0, h_max=3.0, u_max=15.0, T=950.0, seed=11):
     """A spread gas-particle current over the cone, as a seeded stand-in for
     the state of the pyroclastic run a few minutes after the inlet opened:

@@ -29,12 +29,17 @@
 extern "C" {
 #endif
 
-#define SFLOW_ABI_VERSION 1
+#define SFLOW_ABI_VERSION 2
 
 #define SFLOW_MAX_SOLID 4
 /* n_vars = 4 + n_solid (src/inpout_2d.f90:2045-2046 with n_add_gas = 0,
  * no stochastic, no pore pressure, no gas+liquid mixture). */
 #define SFLOW_MAX_VARS (4 + SFLOW_MAX_SOLID)
+/* vulnerability-table levels of each kind (thickness_levels0 and
+ * dyn_pres_levels0 of the reference, inpout_2d.f90:293-294) */
+#define SFLOW_MAX_LEVELS 10
+/* velocity intervals of a bottom radial source (inpout_2d.f90:900-902) */
+#define SFLOW_MAX_INTERVALS 100
 
 /* ---- error codes (negative) ---------------------------------------------- */
 #define SFLOW_OK 0
@@ -136,6 +141,33 @@ typedef struct {
 
   /* RUN_PARAMETERS */
   double t_start, t_end, dt_output;
+
+  /* ---- fields of ABI version 2 ---- */
+  /* VULNERABILITY_TABLE_PARAMETERS (inpout_2d.f90:3792-3870): the levels
+   * >= 0 are used, in order (default -1: no table); when only one kind is
+   * given the other is a single level 0.  Cell (j,k) sets table entry
+   * (i_thk-1)*n_dyn + i_dyn once h >= thickness_levels[i_thk] and
+   * p_dyn >= dyn_pres_levels[i_dyn] (IMEX_SfloW2D.f90:351, 489) */
+  double thickness_levels[SFLOW_MAX_LEVELS], dyn_pres_levels[SFLOW_MAX_LEVELS];
+  /* SOLID_TRANSPORT_PARAMETERS: erosion of an erodible layer
+   * (constitutive_2d.f90:4732-4760; inpout_2d.f90:1818-1990).  With
+   * erosion_coeff = 0 the reference sets porosity 0, fractions 1/n_solid
+   * and T_erodible 300 K; -1 means "not given". */
+  double erodible_porosity, T_erodible, initial_erodible_thickness;
+  double erodible_fract[SFLOW_MAX_SOLID];
+  int32_t erodible_deposit_flag;
+  /* NEWRUN_PARAMETERS: the topography follows erosion and deposition,
+   * with the topography terms recomputed every step (IMEX_SfloW2D.f90:445) */
+  int32_t topo_change_flag;
+  /* bottom radial source (NEWRUN bottom_radial_source_flag; cell fractions
+   * of the source ellipse, geometry_2d.f90:1899-1994; inflow rate
+   * constitutive_2d.f90:3149-3307): vertical inflow velocity vel_source,
+   * ellipse semi-axes r_source / r2_source rotated by angle_source
+   * (degrees), and optionally n_intervals piecewise-constant velocities
+   * vel_intervals from the times t_intervals (else the time_param ramp) */
+  int32_t bottom_radial_source_flag, n_intervals;
+  double angle_source;
+  double t_intervals[SFLOW_MAX_INTERVALS], vel_intervals[SFLOW_MAX_INTERVALS];
 } SflowParams;
 
 /* Fill p with the defaults of init_param (src/inpout_2d.f90:408-985). */
@@ -287,7 +319,8 @@ int sflow_dry_border_updates(sflow_handle* h, int64_t* n);
  * geometry_2d.f90:555-895), 5 grav_coeff  6 d grav_coeff/dx
  * 7 d grav_coeff/dy, 8 ring inlet perimeter  9 its normal x  10 normal y
  * (init_source, geometry_2d.f90:907-1323), 11 source_cell (0, 1, 2),
- * 12 ring face flags (E | W<<1 | N<<2 | S<<3).
+ * 12 ring face flags (E | W<<1 | N<<2 | S<<3), 13 bottom radial source
+ * cell fraction (compute_cell_fract, geometry_2d.f90:1899-1994).
  */
 int sflow_host_geometry(const SflowParams* p, const double* B_cent, int32_t which, double* out);
 /* out[0] = h_source (inpout_2d.f90:4745), out[1] = rho_m and out[2] = c_p of
@@ -471,6 +504,40 @@ int sflow_download_deposit(sflow_handle* h, double* out);
 int sflow_upload_deposit(sflow_handle* h, const double* in);
 int sflow_upload_maps(sflow_handle* h, const double* hmax, const double* pdynmax, const double* mod_vel_max);
 int sflow_set_output_time(sflow_handle* h, double t_output);
+
+/*
+ * Erosion, topography change, B_nodata and the vulnerability table (ABI 2).
+ * Planes are nx*ny doubles or bytes with j fastest (the reference's (j,k)
+ * order), classes / table entries slowest.
+ *   sflow_download_erosion     erosion(:,:,1:n_solid), the accumulated
+ *                              dt * erosion_term (solver_2d.f90:2479);
+ *                              zeros when EROSION_COEFF = 0
+ *   sflow_download_erodible    erodible(1:n_solid,:,:), the erodible solid
+ *                              thicknesses left (solver_2d.f90:2482-2488)
+ *   sflow_set_erodible         the erodible layer thickness per cell (the
+ *                              reference's erodible_init, read from
+ *                              ERODIBLE_FILE): class i gets
+ *                              erodible_fract(i) * (1 - erodible_porosity)
+ *                              of it (inpout_2d.f90:1983-1986).  Kept for
+ *                              later sflow_upload_q calls, which otherwise
+ *                              reset the layer to INITIAL_ERODIBLE_THICKNESS
+ *   sflow_download_topography  B_cent; it changes with TOPO_CHANGE_FLAG
+ *                              (B += dt * topo_term, solver_2d.f90:2490)
+ *   sflow_set_nodata           B_nodata per cell (nonzero: no data); the
+ *                              assembly empties those cells
+ *                              (solver_2d.f90:1626).  NULL clears it
+ *   sflow_vuln_table_size      n_thk, n_dyn of the table (0, 0: none)
+ *   sflow_download_vuln_table  n_thk*n_dyn planes of 0/1 bytes: entry
+ *                              (i_thk-1)*n_dyn + i_dyn-1 is vuln_table
+ *                              (IMEX_SfloW2D.f90:351, 489)
+ */
+int sflow_download_erosion(sflow_handle* h, double* out);
+int sflow_download_erodible(sflow_handle* h, double* out);
+int sflow_set_erodible(sflow_handle* h, const double* thickness);
+int sflow_download_topography(sflow_handle* h, double* B_cent);
+int sflow_set_nodata(sflow_handle* h, const uint8_t* nodata);
+int sflow_vuln_table_size(sflow_handle* h, int32_t* n_thk, int32_t* n_dyn);
+int sflow_download_vuln_table(sflow_handle* h, uint8_t* out);
 
 /* Build information ("fp64+fp32 sm_103a ..."). */
 const char* sflow_build_info(void);

@@ -64,6 +64,14 @@ def _load(timing=False):
     lib.oracle_limit.restype = C.c_double
     lib.oracle_limit.argtypes = [dp, dp, ip, C.c_double]
     lib.sflow_oracle_eval_math.argtypes = [ip, C.c_int64, dp, dp, dp]
+    u8p = C.POINTER(C.c_uint8)
+    lib.sflow_oracle_get_erosion.argtypes = [vp, ip, dp]
+    lib.sflow_oracle_get_topography.argtypes = [vp, dp]
+    lib.sflow_oracle_get_cell_fract.argtypes = [vp, dp]
+    lib.sflow_oracle_set_erodible.argtypes = [vp, dp]
+    lib.sflow_oracle_set_nodata.argtypes = [vp, u8p]
+    lib.sflow_oracle_vuln_size.argtypes = [vp, C.POINTER(ip), C.POINTER(ip)]
+    lib.sflow_oracle_get_vuln.argtypes = [vp, u8p]
     if timing:
         _lib_fast = lib
     else:
@@ -161,6 +169,48 @@ class Oracle:
         out = np.empty(self.nx * self.ny * (self.nv - 4))
         self.lib.sflow_oracle_get_deposit(self.h, _dp(out))
         return out
+
+    def erosion(self):
+        """Accumulated erosion per class (class slowest)."""
+        out = np.empty(self.nx * self.ny * (self.nv - 4))
+        self.lib.sflow_oracle_get_erosion(self.h, 0, _dp(out))
+        return out
+
+    def erodible(self):
+        out = np.empty(self.nx * self.ny * (self.nv - 4))
+        self.lib.sflow_oracle_get_erosion(self.h, 1, _dp(out))
+        return out
+
+    def topography(self):
+        out = np.empty(self.nx * self.ny)
+        self.lib.sflow_oracle_get_topography(self.h, _dp(out))
+        return out
+
+    def cell_fract(self):
+        out = np.empty(self.nx * self.ny)
+        self.lib.sflow_oracle_get_cell_fract(self.h, _dp(out))
+        return out
+
+    def set_erodible(self, thickness):
+        t = np.ascontiguousarray(thickness, dtype=np.float64).reshape(-1)
+        self.lib.sflow_oracle_set_erodible(self.h, _dp(t))
+
+    def set_nodata(self, nodata):
+        if nodata is None:
+            self.lib.sflow_oracle_set_nodata(self.h, None)
+            return
+        m = np.ascontiguousarray(nodata, dtype=np.uint8).reshape(-1)
+        self.lib.sflow_oracle_set_nodata(self.h, m.ctypes.data_as(C.POINTER(C.c_uint8)))
+
+    def vuln_table(self):
+        a, b = C.c_int(0), C.c_int(0)
+        self.lib.sflow_oracle_vuln_size(self.h, C.byref(a), C.byref(b))
+        n = a.value * b.value
+        if n == 0:
+            return None
+        out = np.empty(n * self.nx * self.ny, dtype=np.uint8)
+        self.lib.sflow_oracle_get_vuln(self.h, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return a.value, b.value, out.reshape(n, self.ny, self.nx)
 
     def mask(self):
         m = np.empty(self.nx * self.ny, dtype=np.uint8)

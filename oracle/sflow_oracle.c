@@ -11,12 +11,12 @@
  * reference's own tests (TESTS/run_tests.sh) only check that an output file
  * is written, so there are no golden vectors to pin against.  The oracle
  * is therefore pinned by (a) known-answer tests derived by hand from the
- * reference formulas (tests/golden/), (b) physical invariants (mass
+ * reference formulas (tests/golden/) and (b) physical invariants (mass
  * conservation, lake at rest, x/y mirror symmetry, the Ritter dam-break
- * solution) and (c) an independent Jacobian: this file differentiates the
- * implicit friction term by complex step exactly as the reference does
- * (solver_2d.f90:2302-2367 with complexify.f90), while the GPU path uses an
- * analytic (dual-number) Jacobian.
+ * solution).  The implicit friction term is differentiated by complex step
+ * as the reference does (solver_2d.f90:2302-2367 with complexify.f90), with
+ * the complex arithmetic written out (the GPU's plain FP64 form spells the
+ * same formulas, so both compute the same Jacobian).
  *
  * Every routine names the reference routine it restates (path:line inside
  * the reference project).  The arithmetic follows the reference operation
@@ -35,9 +35,15 @@
  *      T < 273 K; here a status bit is raised and the step continues.
  *  D4  A non-finite Newton residual ends the Newton solve at once (the
  *      reference iterates to its iteration limits on such a cell).
+ *  D5  With ERODIBLE_DEPOSIT_FLAG the erodible layer's temperature in the
+ *      energy exchange is the cell's own temperature.  The reference
+ *      assigns its module-wide T_erodible = r_T just before that use in
+ *      eval_mass_exchange_terms (constitutive_2d.f90:5044), so each cell
+ *      sees its own value there too; only the stored global differs.
  *  Scope: n_add_gas = 0, no stochastic / pore-pressure / vertical-profile
- *  terms, no bottom radial source, no erosion (EROSION_COEFF = 0),
- *  rheology models 1 (Voellmy-Salm) and 6, SOLVER_SCHEME KT or UP.
+ *  terms, rheology models 1 (Voellmy-Salm) and 6, SOLVER_SCHEME KT or UP;
+ *  erosion with a uniform or user-given erodible layer, topography change,
+ *  the bottom radial source, B_nodata cells and the vulnerability table.
  */
 #include <float.h>
 #include <math.h>
@@ -119,6 +125,15 @@ typedef struct {
   int limiter[MAXV];
   double x_source, y_source, r_source, r2_source, vel_source, T_source, h_source;
   double alphas_source[MAXS], time_param[4], pi_g;
+  /* erosion (constitutive_2d.f90:225-232; inpout_2d.f90:1818-1990) */
+  double erodible_fract[MAXS], erodible_init;
+  int erodible_deposit, topo_change, exchange;
+  /* bottom radial source (constitutive_2d.f90:3149-3307) */
+  int bottom_source, n_intervals;
+  double angle_source, t_intervals[SFLOW_MAX_INTERVALS], vel_intervals[SFLOW_MAX_INTERVALS];
+  /* vulnerability table (inpout_2d.f90:3808-3866) */
+  int n_thk, n_dyn;
+  double thk_levels[SFLOW_MAX_LEVELS], dyn_levels[SFLOW_MAX_LEVELS];
 } phys_t;
 
 /* ------------------------------------------------------------------------ */
@@ -719,14 +734,15 @@ static int solve_rk_step(const newton_ctx* c, double* qj) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* constitutive_2d.f90:3024-3431 eval_expl_terms (no bottom radial source)   */
+/* constitutive_2d.f90:3024-3431 eval_expl_terms                             */
 /* ------------------------------------------------------------------------ */
 static void expl_terms(const phys_t* P, double Bx, double By, double Bxx, double Bxy, double Byy,
                        double gc, double dgcx, double dgcy, const double* qpj, double time,
-                       double arc_perim, double arc_nx, double arc_ny, double area, double* e) {
+                       double cell_fract, double arc_perim, double arc_nx, double arc_ny, double area,
+                       double* e) {
   const int nv = P->nv, ns = P->ns;
   for (int i = 0; i < nv; ++i) e[i] = 0.0;
-  if (qpj[0] <= EPS && arc_perim == 0.0) return;
+  if (qpj[0] <= EPS && cell_fract == 0.0 && arc_perim == 0.0) return;
   if (qpj[0] > EPS) {
     double r_h = qpj[0], r_u = qpj[nv], r_v = qpj[nv + 1];
     mixt_t m;
@@ -736,6 +752,41 @@ static void expl_terms(const phys_t* P, double Bx, double By, double Bxx, double
     e[1] = -gc * m.rho_m * tg * r_h * Bx + 0.5 * m.rho_m * m.red_grav * sq(r_h) * dgcx;
     e[2] = -gc * m.rho_m * tg * r_h * By + 0.5 * m.rho_m * m.red_grav * sq(r_h) * dgcy;
     e[3] = P->energy ? (e[1] * r_u + e[2] * r_v) : 0.0;
+  }
+  /* bottom radial source (constitutive_2d.f90:3149-3307) */
+  if (P->bottom_source && cell_fract > 0.0) {
+    const double* tp = P->time_param;
+    double t_coeff, h_dot;
+    if (P->n_intervals > 0) {
+      double vel_local = 0.0;
+      for (int i = P->n_intervals - 1; i >= 0; --i)
+        if (time >= P->t_intervals[i]) { vel_local = P->vel_intervals[i]; break; }
+      t_coeff = vel_local > 0.0 ? 1.0 : 0.0;
+      h_dot = cell_fract * vel_local;
+    } else {
+      double t_rem = fmod(time + tp[3], tp[0]);
+      if (tp[2] == 0.0) {
+        t_coeff = t_rem <= tp[1] ? 1.0 : 0.0;
+      } else {
+        if (t_rem <= tp[2]) t_coeff = t_rem / tp[2];
+        else if (t_rem <= tp[1] - tp[2]) t_coeff = 1.0;
+        else if (t_rem <= tp[1]) t_coeff = 1.0 - (t_rem - tp[1] + tp[2]) / tp[2];
+        else t_coeff = 0.0;
+      }
+      h_dot = cell_fract * P->vel_source;
+    }
+    double qs[MAXV];
+    for (int i = 0; i < nv + 2; ++i) qs[i] = 0.0;
+    qs[0] = 1.0;
+    qs[3] = P->T_source;
+    for (int i = 0; i < ns; ++i) qs[4 + i] = P->alpha ? P->alphas_source[i] : P->alphas_source[i] * qs[0];
+    mixt_t m;
+    mixt_var(P, qs, 1, &m);
+    e[0] = e[0] + t_coeff * h_dot * m.rho_m;
+    e[1] = e[1] + 0.0;
+    e[2] = e[2] + 0.0;
+    e[3] = e[3] + t_coeff * h_dot * m.rho_m * m.cp_mix * P->T_source;
+    for (int i = 0; i < ns; ++i) e[4 + i] = e[4 + i] + t_coeff * h_dot * P->alphas_source[i] * P->rho_s[i];
   }
   if (P->radial_source && arc_perim > 0.0 && P->h_source > 0.0) {
     const double* tp = P->time_param;
@@ -803,13 +854,17 @@ static double settling_velocity(const phys_t* P, double diam, double rhos, doubl
   return sv;
 }
 
-/* constitutive_2d.f90:4574-5153 eval_mass_exchange_terms (no erosion,
- * no pore pressure, no vaporisation, no vertical profiles) */
-static void mass_exchange(const phys_t* P, const double* qpj, double Bx, double By, double dt,
-                          double* dep, double* eqn) {
+/* constitutive_2d.f90:4574-5153 eval_mass_exchange_terms (no pore
+ * pressure, no vaporisation, no vertical profiles): settling, erosion of the
+ * erodible layer, air entrainment; returns deposition / erosion rates, the
+ * equation terms and the topography rate */
+static void mass_exchange(const phys_t* P, const double* qpj, double Bx, double By,
+                          const double* erodible, double dt, double* dep, double* ers, double* eqn,
+                          double* topo) {
   const int nv = P->nv, ns = P->ns;
-  for (int i = 0; i < ns; ++i) dep[i] = 0.0;
+  for (int i = 0; i < ns; ++i) { dep[i] = 0.0; ers[i] = 0.0; }
   for (int i = 0; i < nv; ++i) eqn[i] = 0.0;
+  *topo = 0.0;
   if (qpj[0] <= EPS) return;
   const double alpha_max = 0.6, hind_exp = 4.65;
   double r_h = qpj[0], r_u = qpj[nv], r_v = qpj[nv + 1];
@@ -818,14 +873,24 @@ static void mass_exchange(const phys_t* P, const double* qpj, double Bx, double 
   double at = sumv(alphas, ns);
   double r_w = P->slope_corr ? (r_u * Bx + r_v * By) : 0.0;
   double mod_vel2 = sq(r_u) + sq(r_v) + sq(r_w);
-  /* erosion_coeff = 0: erosion_term = MAX(0,MIN(0,erodible/dt)) = 0 */
-  double ers[MAXS];
-  for (int i = 0; i < ns; ++i) ers[i] = 0.0;
-  double tot_solid_erosion = 0.0;
-  double tot_erosion = tot_solid_erosion / (1.0 - P->erodible_porosity);
+  double mod_vel = sqrt(mod_vel2);
+  double tot_erosion, tot_solid_erosion;
+  if (P->erosion_coeff > 0.0) {
+    /* Fagents & Baloga (2006), eq. 5, with the solid volume fraction */
+    tot_erosion = P->erosion_coeff * mod_vel * r_h * (1.0 - at);
+    tot_solid_erosion = tot_erosion * (1.0 - P->erodible_porosity);
+    for (int i = 0; i < ns; ++i) ers[i] = P->erodible_fract[i] * tot_solid_erosion;
+  } else {
+    for (int i = 0; i < ns; ++i) ers[i] = 0.0;
+  }
+  for (int i = 0; i < ns; ++i) ers[i] = dmax(0.0, dmin(ers[i], erodible[i] / dt));
+  tot_solid_erosion = sumv(ers, ns);
+  tot_erosion = tot_solid_erosion / (1.0 - P->erodible_porosity);
   double cont_erosion = tot_erosion * P->erodible_porosity;
   if (at <= P->alphastot_min) return;
   double r_T = qpj[3];
+  /* ERODIBLE_DEPOSIT_FLAG: T_erodible = r_T (constitutive_2d.f90:5044) */
+  const double T_ers = P->erodible_deposit ? r_T : P->T_erodible;
   mixt_t m;
   mixt_var(P, qpj, 1, &m);
   double inv_kin_visc = 1.0 / P->kin_visc_c;
@@ -860,13 +925,14 @@ static void mass_exchange(const phys_t* P, const double* qpj, double Bx, double 
   if (P->energy)
     eqn[3] = -r_T * (s_dep + m.rho_c * m.cp_c * cpl) -
              0.5 * mod_vel2 * (rho_dep_tot + m.rho_c * cpl) +
-             P->T_erodible * (s_ers + P->rho_c_sub * m.cp_c * cont_erosion) +
+             T_ers * (s_ers + P->rho_c_sub * m.cp_c * cont_erosion) +
              P->T_ambient * P->sp_heat_a * P->rho_a_amb * air_entr;
   else
     eqn[3] = -r_T * (s_dep + m.rho_c * m.cp_c * cpl) +
-             P->T_erodible * (s_ers + P->rho_c_sub * m.cp_c * cont_erosion) +
+             T_ers * (s_ers + P->rho_c_sub * m.cp_c * cont_erosion) +
              P->T_ambient * P->sp_heat_a * P->rho_a_amb * air_entr;
   for (int i = 0; i < ns; ++i) eqn[4 + i] = P->rho_s[i] * (ers[i] - dep[i]);
+  *topo = (sumv(dep, ns) - sumv(ers, ns)) / (1.0 - P->erodible_porosity);
 }
 
 /* ======================================================================== */
@@ -892,6 +958,10 @@ typedef struct oracle {
   double t, dt, dt_old, dt_old_old, t_output;
   double a_tilde_ij[16], a_dirk_ij[16], omega_tilde[4], omega[4];
   double *hmax, *pdynmax, *mod_vel_max, *deposit;
+  /* erosion, bottom source, nodata, vulnerability table */
+  double *erosion, *erodible, *erodible_thk, *B_init, *cell_fract;
+  unsigned char *nodata, *vuln;
+  int have_erodible_thk;
   uint32_t status;
   int64_t steps;
   int max_newton_iter_seen;
@@ -1130,13 +1200,14 @@ static void init_source(oracle_t* o) {
  * MFR_SOURCE and VEL_SOURCE; time_param(2) from MFR (4435-4437) */
 static void derive_source(oracle_t* o) {
   phys_t* P = &o->P;
-  if (!P->radial_source) return;
+  if (!P->radial_source && !P->bottom_source) return;
   if (P->time_param[0] < 0.0 || P->time_param[1] < 0.0 || P->time_param[2] < 0.0 ||
       P->time_param[3] < 0.0) {
     P->time_param[0] = o->prm.t_end; P->time_param[1] = o->prm.t_end;
     P->time_param[2] = 0.0; P->time_param[3] = o->prm.t_end;
   }
-  if (P->r2_source <= 0.0) P->r2_source = P->r_source;
+  if (P->r2_source <= 0.0) { P->r2_source = P->r_source; P->angle_source = 0.0; }
+  if (!P->radial_source) return;
   double r1 = P->r_source, r2 = P->r2_source;
   double h_ell = sq(r1 - r2) / sq(r1 + r2);
   double len = P->pi_g * (r1 + r2) *
@@ -1158,6 +1229,47 @@ static void derive_source(oracle_t* o) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* geometry_2d.f90:1899-1994 compute_cell_fract: 200 x 200 sub-cell points   */
+/* per cell inside the rotated ellipse; REAL(count)/n2 in single precision   */
+/* ------------------------------------------------------------------------ */
+static void compute_cell_fract(oracle_t* o) {
+  const phys_t* P = &o->P;
+  const int n_points = 200, n_points2 = n_points * n_points;
+  const double ang_rad = P->angle_source / 180.0 * atan(1.0) * 4.0;
+  const double xs = P->x_source, ys = P->y_source, rs = P->r_source, r2s = P->r2_source;
+  const double rmx = dmax(rs, r2s);
+  double* xsub = xcalloc(n_points2, 8);
+  double* ysub = xcalloc(n_points2, 8);
+  for (int h = 1; h <= n_points; ++h) {
+    for (int i = h; i <= n_points2; i += n_points) xsub[i - 1] = (double)h;
+    for (int i = (h - 1) * n_points + 1; i <= h * n_points; ++i) ysub[i - 1] = (double)h;
+  }
+  for (int i = 0; i < n_points2; ++i) {
+    xsub[i] = (2.0 * xsub[i] - 1.0) / (2.0 * (double)n_points);
+    ysub[i] = (2.0 * ysub[i] - 1.0) / (2.0 * (double)n_points);
+    xsub[i] = (xsub[i] - 0.5) * o->dx;
+    ysub[i] = (ysub[i] - 0.5) * o->dy;
+  }
+  for (int j = 0; j < o->nx; ++j)
+    for (int k = 0; k < o->ny; ++k) {
+      double f = 0.0;
+      if (!(o->x_stag[j + 1] < xs - rmx || o->x_stag[j] > xs + rmx || o->y_stag[k + 1] < ys - rmx ||
+            o->y_stag[k] > ys + rmx)) {
+        int cnt = 0;
+        for (int i = 0; i < n_points2; ++i) {
+          double a = (o->x_comp[j] + xsub[i] - xs) * cos(ang_rad) + (o->y_comp[k] + ysub[i] - ys) * sin(ang_rad);
+          double b = -((o->x_comp[j] + xsub[i] - xs) * sin(ang_rad)) + (o->y_comp[k] + ysub[i] - ys) * cos(ang_rad);
+          if (sq(a) / sq(rs) + sq(b) / sq(r2s) <= 1.0) ++cnt;
+        }
+        f = (double)((float)cnt / (float)n_points2);
+      }
+      o->cell_fract[IDX(j, k)] = f;
+    }
+  free(xsub);
+  free(ysub);
+}
+
+/* ------------------------------------------------------------------------ */
 /* solver_2d.f90:667-858 check_solve                                         */
 /* ------------------------------------------------------------------------ */
 static void check_solve(oracle_t* o, int solve_all) {
@@ -1170,6 +1282,9 @@ static void check_solve(oracle_t* o, int solve_all) {
   for (int k = 1; k < ny - 1; ++k)
     for (int j = 1; j < nx - 1; ++j)
       if (o->q[IDX(j, k) * nv + 0] > 0.0) m[IDX(j, k)] = 1;
+  if (o->P.bottom_source)
+    for (int i = 0; i < o->N; ++i)
+      if (o->cell_fract[i] > 0.0) m[i] = 1;
   if (o->P.radial_source)
     for (int k = 1; k < ny - 1; ++k)
       for (int j = 1; j < nx - 1; ++j)
@@ -1772,7 +1887,7 @@ static void imex_RK_solver(oracle_t* o) {
         if (qrk[0] > 0.0) oracle_qc_to_qp_p(P, qrk, qprk, NULL);
         else dry_qp(P, qprk);
         expl_terms(P, o->Bx[c], o->By[c], o->Bxx[c], o->Bxy[c], o->Byy[c], o->gc[c], o->dgcx[c],
-                   o->dgcy[c], qprk, o->t, o->arc_perim[c], o->arc_nx[c], o->arc_ny[c],
+                   o->dgcy[c], qprk, o->t, o->cell_fract[c], o->arc_perim[c], o->arc_nx[c], o->arc_ny[c],
                    o->dx * o->dy, &o->expl[((size_t)irk * N + c) * nv]);
       }
     }
@@ -1844,12 +1959,14 @@ static void imex_RK_solver(oracle_t* o) {
         for (int i = 0; i < ns; ++i) q[4 + i] = q[4 + i] / s * q[0];
       }
     }
+    /* solver_2d.f90:1626 */
+    if (o->nodata[c])
+      for (int i = 0; i < nv; ++i) q[i] = 0.0;
   }
   o->status |= st;
 }
 
-/* solver_2d.f90:2382-2597 update_erosion_deposition_cell (no erosion,
- * topo_change off) */
+/* solver_2d.f90:2382-2597 update_erosion_deposition_cell */
 static void update_erosion_deposition(oracle_t* o) {
   const phys_t* P = &o->P;
   const int nv = P->nv, np = nv + 2, ns = P->ns;
@@ -1861,13 +1978,26 @@ static void update_erosion_deposition(oracle_t* o) {
     const size_t c = IDX(o->j_cent[l], o->k_cent[l]);
     double* q = &o->q[c * nv];
     double* qp = &o->qp[c * np];
-    double dep[MAXS], eqn[SFLOW_MAX_VARS];
+    double dep[MAXS], ers[MAXS], eqn[SFLOW_MAX_VARS], topo, erod[MAXS];
     if (q[0] > 0.0) oracle_qc_to_qp_p(P, q, qp, NULL);
     else dry_qp(P, qp);
-    mass_exchange(P, qp, o->Bx[c], o->By[c], dt, dep, eqn);
+    for (int i = 0; i < ns; ++i) erod[i] = o->erodible[c * MAXS + i];
+    mass_exchange(P, qp, o->Bx[c], o->By[c], erod, dt, dep, ers, eqn, &topo);
+    if (P->bottom_source) {
+      const double out_of_source_fraction = 1.0 - o->cell_fract[c];
+      for (int i = 0; i < ns; ++i) dep[i] = dep[i] * out_of_source_fraction;
+      for (int i = 0; i < ns; ++i) ers[i] = ers[i] * out_of_source_fraction;
+      for (int i = 0; i < nv; ++i) eqn[i] = eqn[i] * out_of_source_fraction;
+      topo = topo * out_of_source_fraction;
+    }
     for (int i = 0; i < nv; ++i) q[i] = q[i] + dt * eqn[i];
     for (int i = 0; i < ns; ++i) q[4 + i] = dmax(0.0, q[4 + i]);
     for (int i = 0; i < ns; ++i) o->deposit[c * MAXS + i] += dt * dep[i];
+    for (int i = 0; i < ns; ++i) o->erosion[c * MAXS + i] += dt * ers[i];
+    for (int i = 0; i < ns; ++i) o->erodible[c * MAXS + i] = o->erodible[c * MAXS + i] - dt * ers[i];
+    if (P->erodible_deposit)
+      for (int i = 0; i < ns; ++i) o->erodible[c * MAXS + i] = o->erodible[c * MAXS + i] + dt * dep[i];
+    if (P->topo_change) o->B_cent[c] = o->B_cent[c] + dt * topo;
     if (q[0] <= 0.0) {
       if (q[0] > -1.0e-10) {
         for (int i = 0; i < nv; ++i) q[i] = 0.0;
@@ -1900,6 +2030,23 @@ static void update_erosion_deposition(oracle_t* o) {
   o->status |= st;
 }
 
+/* IMEX_SfloW2D.f90:339-353, 477-491: entry it*n_dyn + id of the table is
+ * h >= thickness level it and p_dyn >= dynamic-pressure level id */
+static void vuln_cell(oracle_t* o, size_t c, double h, double p_dyn, int accumulate) {
+  const phys_t* P = &o->P;
+  const int ne = P->n_thk * P->n_dyn;
+  unsigned char* v = &o->vuln[c * SFLOW_MAX_LEVELS * SFLOW_MAX_LEVELS];
+  int e = 0;
+  for (int it = 0; it < P->n_thk; ++it) {
+    int thck = h >= P->thk_levels[it];
+    for (int id = 0; id < P->n_dyn; ++id, ++e) {
+      int pdyn = p_dyn >= P->dyn_levels[id];
+      v[e] = accumulate ? (v[e] || (thck && pdyn)) : (thck && pdyn);
+    }
+  }
+  (void)ne;
+}
+
 /* IMEX_SfloW2D.f90:449-505 post-step qc_to_qp and maxima */
 static void post_step(oracle_t* o) {
   const phys_t* P = &o->P;
@@ -1917,6 +2064,7 @@ static void post_step(oracle_t* o) {
         o->pdynmax[c] = dmax(o->pdynmax[c], p_dyn);
         o->mod_vel_max[c] = dmax(o->mod_vel_max[c], mv);
       }
+      if (P->n_thk * P->n_dyn > 0) vuln_cell(o, c, qp[0], p_dyn, 1);
     } else {
       dry_qp(P, qp);
     }
@@ -1952,9 +2100,56 @@ static int setup_phys(oracle_t* o, const SflowParams* p) {
   }
   P->alphastot_min = p->alphastot_min; P->max_packing = p->maximum_solid_packing;
   P->A_drag = p->A_drag; P->B_drag = p->B_drag;
+  /* SOLID_TRANSPORT_PARAMETERS checks (inpout_2d.f90:1818-1990) */
   P->erosion_coeff = p->erosion_coeff;
-  P->erodible_porosity = 0.0; P->T_erodible = 300.0; P->coeff_porosity = 0.0;
-  P->rho_c_sub = p->gas_flag ? p->pres / (p->sp_gas_const_a * 300.0) : p->rho_l;
+  if (p->erosion_coeff < 0.0) return -1;
+  if (p->erosion_coeff == 0.0) {
+    P->erodible_porosity = 0.0;
+    for (int i = 0; i < P->ns; ++i) P->erodible_fract[i] = 1.0 / P->ns;
+    P->T_erodible = 300.0;
+    P->coeff_porosity = 0.0;
+    P->erodible_init = 0.0;
+  } else {
+    if (p->erodible_porosity < 0.0 || p->erodible_porosity > 1.0) return -1;
+    P->erodible_porosity = p->erodible_porosity;
+    P->coeff_porosity = p->erodible_porosity / (1.0 - p->erodible_porosity);
+    if (P->ns == 1) {
+      P->erodible_fract[0] = 1.0;
+    } else {
+      for (int i = 0; i < P->ns; ++i) {
+        if (p->erodible_fract[i] < 0.0) return -1;
+        P->erodible_fract[i] = p->erodible_fract[i];
+      }
+      double sum = sumv(P->erodible_fract, P->ns);
+      if (sum != 1.0)
+        for (int i = 0; i < P->ns; ++i) P->erodible_fract[i] = P->erodible_fract[i] / sum;
+    }
+    if (p->T_erodible < 0.0) return -1;
+    P->T_erodible = p->T_erodible;
+    P->erodible_init = p->initial_erodible_thickness >= 0.0 ? p->initial_erodible_thickness : 0.0;
+  }
+  P->rho_c_sub = p->gas_flag ? p->pres / (p->sp_gas_const_a * P->T_erodible) : p->rho_l;
+  P->erodible_deposit = p->erodible_deposit_flag;
+  P->topo_change = p->topo_change_flag;
+  P->exchange = p->erosion_coeff != 0.0 || p->settling_flag || p->entrainment_flag;
+  /* bottom radial source */
+  P->bottom_source = p->bottom_radial_source_flag;
+  P->n_intervals = p->n_intervals;
+  for (int i = 0; i < p->n_intervals && i < SFLOW_MAX_INTERVALS; ++i) {
+    P->t_intervals[i] = p->t_intervals[i];
+    P->vel_intervals[i] = p->vel_intervals[i];
+  }
+  P->angle_source = p->angle_source;
+  /* VULNERABILITY_TABLE_PARAMETERS (inpout_2d.f90:3808-3866) */
+  P->n_thk = 0; P->n_dyn = 0;
+  for (int i = 0; i < SFLOW_MAX_LEVELS; ++i) {
+    if (p->thickness_levels[i] >= 0.0) P->n_thk++;
+    if (p->dyn_pres_levels[i] >= 0.0) P->n_dyn++;
+  }
+  for (int i = 0; i < P->n_thk; ++i) P->thk_levels[i] = p->thickness_levels[i];
+  for (int i = 0; i < P->n_dyn; ++i) P->dyn_levels[i] = p->dyn_pres_levels[i];
+  if (P->n_thk > 0 && P->n_dyn <= 0) { P->n_dyn = 1; P->dyn_levels[0] = 0.0; }
+  if (P->n_dyn > 0 && P->n_thk <= 0) { P->n_thk = 1; P->thk_levels[0] = 0.0; }
   P->theta = p->theta; P->reconstr_coeff = p->reconstr_coeff;
   for (int i = 0; i < P->nv; ++i) P->limiter[i] = p->limiter[i];
   P->limiter[P->nv] = p->limiter[1];
@@ -2001,7 +2196,10 @@ oracle_t* sflow_oracle_create(const SflowParams* p, const double* B_cent) {
   if (p->comp_cells_y < 5 && p->comp_cells_y != 1) return NULL;
   oracle_t* o = calloc(1, sizeof(oracle_t));
   o->prm = *p;
-  setup_phys(o, p);
+  if (setup_phys(o, p) != 0) {
+    free(o);
+    return NULL;
+  }
   const int nx = p->comp_cells_x, ny = p->comp_cells_y;
   o->nx = nx; o->ny = ny; o->N = nx * ny; o->nix = nx + 1; o->niy = ny + 1;
   o->dx = nx > 1 ? p->cell_size : 1.0;
@@ -2023,9 +2221,17 @@ oracle_t* sflow_oracle_create(const SflowParams* p, const double* B_cent) {
   for (size_t i = 0; i < sizeof(geo) / sizeof(geo[0]); ++i) *geo[i] = xcalloc(N, 8);
   o->gcsx = xcalloc(NX, 8); o->gcsy = xcalloc(NY, 8);
   o->deposit = xcalloc(N * MAXS, 8);
+  o->erosion = xcalloc(N * MAXS, 8);
+  o->erodible = xcalloc(N * MAXS, 8);
+  o->erodible_thk = xcalloc(N, 8);
+  o->B_init = xcalloc(N, 8);
+  o->cell_fract = xcalloc(N, 8);
+  o->nodata = xcalloc(N, 1);
+  o->vuln = xcalloc(N * SFLOW_MAX_LEVELS * SFLOW_MAX_LEVELS, 1);
   o->source_cell = xcalloc(N, sizeof(int));
   o->srcE = xcalloc(N, 1); o->srcW = xcalloc(N, 1); o->srcN = xcalloc(N, 1); o->srcS = xcalloc(N, 1);
   for (size_t i = 0; i < N; ++i) o->B_cent[i] = B_cent ? B_cent[i] : 0.0;
+  memcpy(o->B_init, o->B_cent, sizeof(double) * N);
   o->q = xcalloc(N * nv, 8); o->q0 = xcalloc(N * nv, 8); o->q_fv = xcalloc(N * nv, 8);
   o->qp = xcalloc(N * np, 8);
   for (size_t i = 0; i < N; ++i) o->qp[i * np + 3] = o->P.T_ambient;
@@ -2047,6 +2253,7 @@ oracle_t* sflow_oracle_create(const SflowParams* p, const double* B_cent) {
   topography_reconstruction(o);
   derive_source(o);
   if (o->P.radial_source) init_source(o);
+  if (o->P.bottom_source) compute_cell_fract(o);
   o->t = p->t_start;
   o->dt = o->dt_old = o->dt_old_old = p->dt0;
   o->t_output = p->t_start + p->dt_output;
@@ -2062,7 +2269,8 @@ void sflow_oracle_destroy(oracle_t* o) {
                   o->qL, o->qR, o->qB, o->qT, o->qpL, o->qpR, o->qpB, o->qpT, o->axN, o->axP,
                   o->ayN, o->ayP, o->Hx, o->Hy, o->mask, o->mask_tmp, o->mask_x, o->mask_y,
                   o->j_cent, o->k_cent, o->j_sx, o->k_sx, o->j_sy, o->k_sy, o->hmax, o->pdynmax,
-                  o->mod_vel_max, o->deposit};
+                  o->mod_vel_max, o->deposit, o->erosion, o->erodible, o->erodible_thk, o->B_init,
+                  o->cell_fract, o->nodata, o->vuln};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
   free(o);
 }
@@ -2076,6 +2284,21 @@ int sflow_oracle_set_q(oracle_t* o, const double* q) {
   o->t_output = o->prm.t_start + o->prm.dt_output;
   o->status = 0;
   o->steps = 0;
+  /* a new run: deposit, erosion and the erodible layer as initialised
+   * (inpout_2d.f90:1983-1986), the topography as given */
+  const int ns = o->P.ns;
+  for (size_t c = 0; c < (size_t)o->N; ++c)
+    for (int i = 0; i < ns; ++i) {
+      o->deposit[c * MAXS + i] = 0.0;
+      o->erosion[c * MAXS + i] = 0.0;
+      o->erodible[c * MAXS + i] = o->P.erodible_fract[i] * (1.0 - o->P.erodible_porosity) *
+                                  (o->have_erodible_thk ? o->erodible_thk[c] : o->P.erodible_init);
+    }
+  if (memcmp(o->B_cent, o->B_init, sizeof(double) * o->N) != 0) {
+    memcpy(o->B_cent, o->B_init, sizeof(double) * o->N);
+    topography_reconstruction(o);
+  }
+  memset(o->vuln, 0, (size_t)o->N * SFLOW_MAX_LEVELS * SFLOW_MAX_LEVELS);
   check_solve(o, 1);
   for (int i = 0; i < o->N; ++i) { o->hmax[i] = 0.0; o->pdynmax[i] = 0.0; o->mod_vel_max[i] = 0.0; }
   for (int l = 0; l < o->solve_cells; ++l) {
@@ -2087,6 +2310,7 @@ int sflow_oracle_set_q(oracle_t* o, const double* q) {
       o->hmax[c] = qp[0];
       double mv = sqrt(sq(qp[nv]) + sq(qp[nv + 1]));
       if (qp[0] > 0.001) { o->pdynmax[c] = p_dyn; o->mod_vel_max[c] = mv; }
+      if (o->P.n_thk * o->P.n_dyn > 0) vuln_cell(o, c, qp[0], p_dyn, 0);
     } else {
       for (int i = 0; i < nv; ++i) qp[i] = 0.0;
       qp[3] = o->P.T_ambient;
@@ -2109,6 +2333,7 @@ int sflow_oracle_step(oracle_t* o) {
   o->dt_old = o->dt;
   imex_RK_solver(o);
   update_erosion_deposition(o);
+  if (o->P.topo_change) topography_reconstruction(o);
   o->t = o->t + o->dt;
   post_step(o);
   o->steps++;
@@ -2140,6 +2365,37 @@ void sflow_oracle_get_mask(const oracle_t* o, unsigned char* m) { memcpy(m, o->m
 void sflow_oracle_get_deposit(const oracle_t* o, double* out) {
   for (int i = 0; i < o->P.ns; ++i)
     for (size_t c = 0; c < (size_t)o->N; ++c) out[(size_t)i * o->N + c] = o->deposit[c * MAXS + i];
+}
+
+/* erosion (which 0) or erodible (1), class slowest */
+void sflow_oracle_get_erosion(const oracle_t* o, int which, double* out) {
+  const double* src = which == 0 ? o->erosion : o->erodible;
+  for (int i = 0; i < o->P.ns; ++i)
+    for (size_t c = 0; c < (size_t)o->N; ++c) out[(size_t)i * o->N + c] = src[c * MAXS + i];
+}
+void sflow_oracle_get_topography(const oracle_t* o, double* out) { memcpy(out, o->B_cent, sizeof(double) * o->N); }
+void sflow_oracle_get_cell_fract(const oracle_t* o, double* out) {
+  memcpy(out, o->cell_fract, sizeof(double) * o->N);
+}
+/* the erodible layer thickness per cell (erodible_init); used from the next
+ * sflow_oracle_set_q */
+void sflow_oracle_set_erodible(oracle_t* o, const double* thk) {
+  memcpy(o->erodible_thk, thk, sizeof(double) * o->N);
+  o->have_erodible_thk = 1;
+}
+void sflow_oracle_set_nodata(oracle_t* o, const unsigned char* nodata) {
+  for (int i = 0; i < o->N; ++i) o->nodata[i] = nodata ? (nodata[i] != 0) : 0;
+}
+void sflow_oracle_vuln_size(const oracle_t* o, int* n_thk, int* n_dyn) {
+  *n_thk = o->P.n_thk;
+  *n_dyn = o->P.n_dyn;
+}
+/* n_thk*n_dyn planes of nx*ny bytes */
+void sflow_oracle_get_vuln(const oracle_t* o, unsigned char* out) {
+  const int ne = o->P.n_thk * o->P.n_dyn;
+  for (int e = 0; e < ne; ++e)
+    for (size_t c = 0; c < (size_t)o->N; ++c)
+      out[(size_t)e * o->N + c] = o->vuln[c * SFLOW_MAX_LEVELS * SFLOW_MAX_LEVELS + e];
 }
 
 /* which: 0 Bx_geom 1 By_geom 2 Bxx 3 Bxy 4 Byy 5 grav_coeff 6 dgc/dx 7 dgc/dy

@@ -105,7 +105,7 @@ def test_boundary_condition_rules(tmp_path):
 @pytest.mark.parametrize("edit, msg", [
     ("N_RK = 2", "N_RK = 2, FOO = 3"),
     ("ENERGY_FLAG = T", "ENERGY_FLAG = T, PORE_PRESSURE_FLAG = T"),
-    ("EROSION_COEFF = 0.D0", "EROSION_COEFF = 0.D0, ERODIBLE_DEPOSIT_FLAG = T"),
+    ("EROSION_COEFF = 0.D0", "EROSION_COEFF = 0.D0, ERODIBLE_FILE = 'layer.asc'"),
     ("HALPHAS_BCE(2)%VALUE = 0.5", "HALPHAS_BCE(2)%VALUE = 0.5, ALPHAG_BCE%FLAG = 1"),
     ("RESTART = .TRUE.", "RESTART = .FALSE."),
     ("H_BCS%FLAG = 1,", ""),
