@@ -69,6 +69,7 @@ class Batch : public BatchBase {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
     if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
+    if (mem_limit_ > 0 && held_ + need > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
 
     std::unique_ptr<Solver<R>> sv(new Solver<R>(hs, tile_h_));
     int rc = sv->init();
@@ -133,6 +134,8 @@ class Batch : public BatchBase {
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
     ++g->launches;
+    s.bytes = sv->device_bytes() + (int64_t)sizeof(uint32_t) * tiles + tiles;
+    held_ += s.bytes;
     s.solver = std::move(sv);
     s.done = false;
     g->tiles_live += tiles;
@@ -332,6 +335,8 @@ class Batch : public BatchBase {
       return SFLOW_ECUDA;
     }
     s->solver.reset();
+    held_ -= s->bytes;
+    s->bytes = 0;
     cudaFree(s->cand);
     s->cand = nullptr;
     cudaFree(s->tile_seed);
@@ -364,6 +369,11 @@ class Batch : public BatchBase {
 
   // Tile height of every run admitted from now on; only while the batch
   // holds no run (the groups' lists and graphs are made for one height).
+  int set_memory_limit(int64_t bytes) override {
+    if (bytes < 0) { err_ = "memory limit must be >= 0"; return SFLOW_EINVAL; }
+    mem_limit_ = bytes;
+    return SFLOW_OK;
+  }
   int set_tile_shape(int th) override {
     if (th == tile_h_) return SFLOW_OK;
     if (!tile_h_built<R>(th)) { err_ = "no kernels built for this tile height"; return SFLOW_EINVAL; }
@@ -394,12 +404,15 @@ class Batch : public BatchBase {
 
  private:
   static constexpr int64_t kReserve = (int64_t)1 << 30;   // device memory kept free
+  int64_t mem_limit_ = 0;   // cap on the resident runs' device bytes (0: none)
+  int64_t held_ = 0;        // device bytes of the resident runs
 
   struct Slot {
     std::unique_ptr<Solver<R>> solver;
     uint32_t* cand = nullptr;
     uint8_t* tile_seed = nullptr;
     int64_t tiles = 0;
+    int64_t bytes = 0;   // device bytes the run holds
     unsigned gen = 0;
     bool done = false;
     int rec = -1;

@@ -218,6 +218,11 @@ int sflow_batch_set_tile_shape(sflow_batch* b, int32_t tile_h) {
   BATCH_FORWARD(b, b->impl->set_tile_shape(tile_h));
 }
 
+int sflow_batch_set_memory_limit(sflow_batch* b, int64_t bytes) {
+  BATCH_CHECK(b);
+  BATCH_FORWARD(b, b->impl->set_memory_limit(bytes));
+}
+
 int sflow_batch_get_tile_shape(const sflow_batch* b, int32_t* tile_h) {
   if (!b || !b->impl) return fail(SFLOW_EINVAL, "null batch");
   if (!tile_h) return fail(SFLOW_EINVAL, "tile_h is NULL");

@@ -128,6 +128,7 @@ class BatchBase {
   virtual int64_t launches() const = 0;
   virtual int tile_shape() const = 0;
   virtual int set_tile_shape(int tile_h) = 0;
+  virtual int set_memory_limit(int64_t bytes) = 0;
   virtual const char* error() const = 0;
 };
 

@@ -144,7 +144,7 @@ __device__ __forceinline__ long long order_key(double x) {
 }
 
 __device__ __forceinline__ bool running(const RunState* st) {
-  return order_key(st->t) < order_key(st->t_stop) && st->steps < st->step_limit;
+  return order_key(st->t) < order_key(st->t_stop) && st->steps < st->step_limit && !(st->status & SFLOW_S_FATAL);
 }
 
 __device__ __forceinline__ unsigned long long dbits(double x) {

@@ -962,6 +962,74 @@ __device__ __forceinline__ double rcp64(double x) {
   return r;
 }
 
+// The same root with every coefficient formed in FP64 from the FP32 state
+// (entering through f2d_exact) and Newton iterated in FP64 with its FP64
+// derivative to a relative step of 4 ulp (the reference's TOLX is the
+// FP64 epsilon, solver_2d.f90:1826, 1984-1990), started from the explicit
+// quadratic root; the result is rounded to float once.
+template <int NS>
+__device__ __noinline__ float reduced_friction_solve_fp64(const Phys<float>& P, const Phys<double>& PD,
+                                                           float Bx, float By, const float* q, double dta,
+                                                           float Sf, float e1, float e2, int& iters) {
+  constexpr int ns = NS;
+  const double q1 = f2d_exact(q[0]), inv_q1 = 1.0 / q1;
+  double xs_tot = 0.0, dcp = 0.0, dinv = 0.0;
+#pragma unroll
+  for (int i = 0; i < ns; ++i) {
+    const double xs = f2d_exact(q[4 + i]) * inv_q1;
+    xs_tot += xs;
+    dcp += xs * PD.sp_heat_s[i];
+    dinv += xs * PD.inv_rho_s[i];
+  }
+  const double xc = 1.0 - xs_tot;
+  const double cmix = dcp + xc * (PD.gas ? PD.sp_heat_a : PD.sp_heat_l);
+  double phi;
+  if (q1 > PD.eps_sing_d) {
+    phi = inv_q1;
+  } else {
+    const double sc = q1 * PD.inv_eps_sing;
+    phi = PD.sqrt2 * sc * PD.inv_eps_sing / sqrt(1.0 + (sc * sc) * (sc * sc));
+  }
+  double kappa2 = 1.0;
+  if (PD.slope_corr) {
+    const double w = f2d_exact(e1) * f2d_exact(Bx) + f2d_exact(e2) * f2d_exact(By);
+    kappa2 = 1.0 + w * w;
+  }
+  const double cgeo = (PD.rheo_model == 1) ? PD.grav * sqrt(kappa2) * phi * phi / PD.xi
+                                           : PD.friction_factor * kappa2 * phi * phi;
+  const bool gas = PD.gas;
+  const bool varT = gas && PD.energy && (q1 > PD.eps_sing_d);
+  const double icm = 1.0 / (q1 * cmix);
+  const double a_T = (q1 > PD.eps_sing_d) ? f2d_exact(q[3]) * icm : PD.T_ambient;
+  const double b_T = varT ? 0.5 * inv_q1 * icm : 0.0;
+  const double c_inv = gas ? xc * PD.sp_gas_const_a * PD.inv_pres : 0.0;
+  const double base_inv = gas ? dinv : dinv + xc * PD.inv_rho_l;
+  const double rho_a = (PD.rheo_model == 1) ? PD.rho_a_amb : 0.0;
+  const double S = f2d_exact(Sf);
+  auto Kd = [&](double sv, double& dK) -> double {
+    double T = a_T - b_T * sv * sv, dT = -2.0 * b_T * sv;
+    if (T <= 0.0) { T = PD.T_ambient; dT = 0.0; }
+    const double rho_m = 1.0 / (base_inv + c_inv * T);
+    dK = cgeo * (-rho_m * rho_m * c_inv * dT);
+    return cgeo * (rho_m - rho_a);
+  };
+  double dK;
+  double K = Kd(S, dK);
+  double sd = 2.0 * S / (1.0 + sqrt(fmax(1.0 + 4.0 * dta * K * S, 0.0)));
+  int it = 0;
+  for (; it < 12; ++it) {
+    K = Kd(sd, dK);
+    const double g = sd + dta * K * sd * sd - S;
+    const double gd = 1.0 + dta * (dK * sd * sd + 2.0 * K * sd);
+    const double ds = g / gd;
+    sd -= ds;
+    if (!(fabs(ds) > 4.0 * kEps * sd)) { ++it; break; }
+  }
+  iters = it;
+  const long long sb = __double_as_longlong(sd);
+  return (sb > 0 && sb <= 0x7ff0000000000000ll) ? d2f_rn(sd) : 0.0f;
+}
+
 template <int NS>
 __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, const Phys<double>& PD,
                                                         float Bx, float By,
@@ -1013,6 +1081,7 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, co
     dK = cgeo * (-rho_m * rho_m * c_inv * dT);
     return cgeo * (rho_m - rho_a);
   };
+  if (PD.newton64) return reduced_friction_solve_fp64<NS>(P, PD, Bx, By, q, dta, S, e1, e2, iters);
   const float dtaf = d2f_rn(dta);
   float dKf;
   float K = Kf(S, dKf);

@@ -746,7 +746,7 @@ class Solver : public SolverBase {
       }
       SFLOW_CU(cudaMemcpyAsync(&hst_, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
       SFLOW_CU(cudaStreamSynchronize(stream_));
-      if (!(hst_.t < stop) || hst_.steps >= limit) break;
+      if (!(hst_.t < stop) || hst_.steps >= limit || (hst_.status & SFLOW_S_FATAL)) break;
     }
     return s ? stats(s) : SFLOW_OK;
   }
@@ -1107,6 +1107,7 @@ class Solver : public SolverBase {
     P.topo_change = p.topo_change_flag ? 1 : 0;
     P.bottom_source = p.bottom_radial_source_flag ? 1 : 0;
     P.exchange = hs_.exchange;
+    P.newton64 = p.fp32_newton_fp64 ? 1 : 0;
     P.nodata = 0;
     for (size_t c = 0; c < hs_.cflags.size(); ++c)
       if (hs_.cflags[c] & kFlagNodata) { P.nodata = 1; break; }

@@ -39,6 +39,7 @@ struct Phys {
   // bottom radial source (constitutive_2d.f90:3149-3307)
   int bottom_source;
   int nodata;     // some cell is B_nodata (emptied by the assembly)
+  int newton64;   // FP32 form: implicit friction solve with FP64 coefficients and iterations
   int exchange;   // update_erosion_deposition_cell runs: settling, entrainment or erosion
   // vulnerability table (IMEX_SfloW2D.f90:351, 489): levels as R (for the
   // FP32 form the smallest float not below the FP64 level, so that a float

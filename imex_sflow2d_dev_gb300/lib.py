@@ -116,6 +116,7 @@ def load(build_if_missing=True):
         "sflow_get_tile_shape": (C.c_int, [vp, C.POINTER(i32)]),
         "sflow_autotune": (C.c_int, [vp, i64, C.POINTER(i32), dp, i32]),
         "sflow_batch_set_tile_shape": (C.c_int, [vp, i32]),
+        "sflow_batch_set_memory_limit": (C.c_int, [vp, i64]),
         "sflow_batch_get_tile_shape": (C.c_int, [vp, C.POINTER(i32)]),
     }
     for name, (res, args) in sigs.items():
@@ -149,7 +150,7 @@ def exported_symbols():
             "sflow_batch_launch", "sflow_batch_wait", "sflow_batch_dry_border_updates",
             "sflow_dry_border_updates", "sflow_download_erosion", "sflow_download_erodible",
             "sflow_set_erodible", "sflow_download_topography", "sflow_set_nodata",
-            "sflow_vuln_table_size", "sflow_download_vuln_table"]
+            "sflow_vuln_table_size", "sflow_download_vuln_table", "sflow_batch_set_memory_limit"]
 
 
 TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
@@ -440,6 +441,9 @@ class Solver:
         _check(self.lib.sflow_status(self.h, C.byref(f)))
         return f.value
 
+    def clear_status(self):
+        _check(self.lib.sflow_clear_status(self.h))
+
     def counters(self):
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
         d = C.c_int32()
@@ -702,3 +706,8 @@ class Batch:
     def set_tile_shape(self, tile_h):
         """Tile height of the runs admitted from now on (no run may be live)."""
         _check(self.lib.sflow_batch_set_tile_shape(self.h, int(tile_h)))
+
+    def set_memory_limit(self, nbytes):
+        """Cap on the device bytes of the resident runs (0: none); a submit
+        past it returns None (SFLOW_EBUSY)."""
+        _check(self.lib.sflow_batch_set_memory_limit(self.h, int(nbytes)))

@@ -25,6 +25,8 @@ S_LOW_T = 0x8
 S_SOLID_GT_MASS = 0x10
 S_NEWTON_MAXIT = 0x20
 S_EROSION = 0x40
+# a run stops at the end of the step that raised one of these
+S_FATAL = S_NAN | S_NEG_H | S_NEG_ALPHA | S_EROSION
 
 STATUS_NAMES = {
     S_NAN: "NaN", S_NEG_H: "negative thickness", S_NEG_ALPHA: "negative solid mass",
@@ -82,6 +84,7 @@ class SflowParams(C.Structure):
         ("bottom_radial_source_flag", C.c_int32), ("n_intervals", C.c_int32),
         ("angle_source", C.c_double),
         ("t_intervals", C.c_double * MAX_INTERVALS), ("vel_intervals", C.c_double * MAX_INTERVALS),
+        ("fp32_newton_fp64", C.c_int32), ("pad2", C.c_int32),
     ]
 
     @property
@@ -117,10 +120,11 @@ def params_to_dict(p):
 
 def params_from_dict(d):
     """SflowParams from params_to_dict output; keys the dict does not hold
-    (fields added after it was made) keep the defaults."""
+    (fields added after it was made) keep the defaults, and the ABI version
+    is this library's."""
     p = default_params()
     for name, _ in SflowParams._fields_:
-        if name not in d:
+        if name not in d or name == "abi_version":
             continue
         v = d[name]
         if name == "bc":

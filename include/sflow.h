@@ -60,6 +60,10 @@ extern "C" {
 #define SFLOW_S_SOLID_GT_MASS 0x10u /* sum solids > q1 (solver_2d.f90:1562)   */
 #define SFLOW_S_NEWTON_MAXIT 0x20u  /* Newton hit max_nl_iter                 */
 #define SFLOW_S_EROSION 0x40u     /* erosion-step consistency check tripped   */
+/* A run stops at the end of the step that raised one of these (where the
+ * reference pauses on READ(*,*)); sflow_clear_status lets it continue.
+ * The other bits are reported and the run goes on. */
+#define SFLOW_S_FATAL (SFLOW_S_NAN | SFLOW_S_NEG_H | SFLOW_S_NEG_ALPHA | SFLOW_S_EROSION)
 
 /* ---- precision of the state and of the explicit (bulk) arithmetic -------- */
 #define SFLOW_PREC_FP64 0   /* plain form: everything FP64                      */
@@ -130,9 +134,9 @@ typedef struct {
   double rho_s[SFLOW_MAX_SOLID], diam_s[SFLOW_MAX_SOLID], sp_heat_s[SFLOW_MAX_SOLID];
   int32_t settling_flag, collective_settling_flag;
   double alphastot_min, maximum_solid_packing, A_drag, B_drag;
-  double erosion_coeff;         /* only 0 is supported */
+  double erosion_coeff;         /* erosion rate coefficient (constitutive_2d.f90:4732) */
 
-  /* RADIAL_SOURCE_PARAMETERS (lateral ring inlet) */
+  /* RADIAL_SOURCE_PARAMETERS (lateral ring inlet; also the bottom source) */
   double x_source, y_source, r_source, r2_source;
   double vel_source, T_source, h_source, mfr_source;
   double alphas_source[SFLOW_MAX_SOLID];
@@ -168,6 +172,12 @@ typedef struct {
   int32_t bottom_radial_source_flag, n_intervals;
   double angle_source;
   double t_intervals[SFLOW_MAX_INTERVALS], vel_intervals[SFLOW_MAX_INTERVALS];
+  /* SFLOW_PREC_FP32 only: 1 forms the implicit friction step's
+   * coefficients and iterates its Newton solve in FP64 (from the FP32
+   * state, to a 4-ulp step); 0 (default) iterates in FP32 and finishes with
+   * one FP64 Newton step */
+  int32_t fp32_newton_fp64;
+  int32_t pad2;
 } SflowParams;
 
 /* Fill p with the defaults of init_param (src/inpout_2d.f90:408-985). */
@@ -366,7 +376,8 @@ const char* sflow_log_sums_noalloc_error(void);
  * Each run follows the N_RK = 2 time step of sflow_step exactly (bitwise the
  * same result as its own handle, alone or in any mix).  Runs can be
  * submitted and collected between sflow_batch_advance calls (continuous
- * batching); a run stops at its t_end or after max_steps steps.
+ * batching); a run stops at its t_end, after max_steps steps or at a
+ * SFLOW_S_FATAL status (its co-resident runs go on unaffected).
  *
  *   sflow_batch_create   precision SFLOW_PREC_FP32 or _FP64 of every run;
  *                        max_runs slots per class count; max_cells bounds
@@ -424,6 +435,9 @@ int sflow_batch_collect(sflow_batch* b, int32_t run_id, double* q_aos);
 int32_t sflow_batch_live(const sflow_batch* b);
 int64_t sflow_batch_launch_count(const sflow_batch* b);
 int sflow_batch_set_tile_shape(sflow_batch* b, int32_t tile_h);
+/* Caps the device bytes the batch's resident runs may hold (0: no cap but
+ * the free memory); a submit that would exceed it answers SFLOW_EBUSY. */
+int sflow_batch_set_memory_limit(sflow_batch* b, int64_t bytes);
 int sflow_batch_get_tile_shape(const sflow_batch* b, int32_t* tile_h);
 
 /*

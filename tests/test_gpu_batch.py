@@ -279,3 +279,75 @@ def test_setups_launch_wait_and_timed_advance_give_the_same_runs():
         assert c["cell_updates"] == cu and c["steps"] == steps
         assert 0 <= b.dry_border_updates(i) <= cu
     b.close()
+
+
+def test_failing_runs_stop_and_the_others_are_unaffected():
+    """A run whose initial state holds a NaN, and one with a negative depth
+    (host-injected), stop after their first step with SFLOW_S_NAN /
+    SFLOW_S_NEG_H (SFLOW_S_FATAL), report done and can be collected; the
+    co-resident runs end bitwise equal to their solo results (FP64)."""
+    from imex_sflow2d_dev_gb300.params import S_FATAL, S_NAN, S_NEG_H
+    runs = _mix()
+    b = L.Batch(PREC_FP64, max_runs=8)
+    ids = [b.submit(p, B, W.to_aos(q)) for p, B, q in runs]
+    p, B, q = W.dam_break(nx=64, ny=48, t_end=100.0)
+    bad_nan = W.to_aos(q).copy().reshape(48, 64, p.n_vars)
+    bad_nan[20, 30, 1] = np.nan
+    bad_neg = W.to_aos(q).copy().reshape(48, 64, p.n_vars)
+    bad_neg[24, 10, 0] = -1.0
+    r_nan = b.submit(p, B, bad_nan.reshape(-1))
+    r_neg = b.submit(p, B, bad_neg.reshape(-1))
+    assert None not in ids and r_nan is not None and r_neg is not None
+    b.advance(12)
+    for rid, bit in ((r_nan, S_NAN), (r_neg, S_NEG_H)):
+        st, done = b.poll(rid)
+        assert done and (st.status & bit) and (st.status & S_FATAL)
+        assert st.steps == 1
+        assert b.collect(rid).size == p.n_vars * 64 * 48
+    b.advance(18)
+    for rid, (p, B, q) in zip(ids, runs):
+        st, done = b.poll(rid)
+        assert st.status == 0
+        ref, _ = _alone(p, B, q, 30, PREC_FP64)
+        same_run(b.collect(rid), ref, PREC_FP64, p.n_vars)
+    b.close()
+
+
+def test_single_run_stops_at_a_fatal_status():
+    """sflow_advance returns at a SFLOW_S_FATAL status instead of stepping
+    on; sflow_clear_status lets the run continue."""
+    from imex_sflow2d_dev_gb300.params import S_NEG_H
+    p, B, q = W.dam_break(nx=64, ny=48, t_end=100.0)
+    bad = W.to_aos(q).copy().reshape(48, 64, p.n_vars)
+    bad[24, 10, 0] = -1.0
+    s = L.Solver(p, B)
+    s.upload_q(bad.reshape(-1))
+    st = s.advance(max_steps=50)
+    assert st.status & S_NEG_H and st.steps == 1
+    st = s.advance(max_steps=5)
+    assert st.steps == 1                      # still stopped
+    s.clear_status()
+    st = s.advance(max_steps=5)
+    assert st.steps > 1
+    s.close()
+
+
+def test_memory_limit_hook_gives_ebusy():
+    """sflow_batch_set_memory_limit: a submit past the cap answers
+    SFLOW_EBUSY (None) and leaves the batch usable."""
+    runs = _mix()
+    p, B, q = runs[0]
+    b = L.Batch(PREC_FP32, max_runs=4)
+    b.set_memory_limit(1)
+    assert b.submit(p, B, W.to_aos(q)) is None
+    b.set_memory_limit(0)
+    r0 = b.submit(p, B, W.to_aos(q))
+    assert r0 is not None
+    b.set_memory_limit(1)
+    assert b.submit(p, B, W.to_aos(q)) is None
+    b.advance(5)
+    ref, _ = _alone(p, B, q, 5, PREC_FP32)
+    same_run(b.collect(r0), ref, PREC_FP32, p.n_vars)
+    b.set_memory_limit(0)
+    assert b.submit(p, B, W.to_aos(q)) is not None
+    b.close()

@@ -176,3 +176,17 @@ def test_ensemble_member_2000_steps_fp64_matches_oracle(member):
 def test_ensemble_member_2000_steps_fp32_error_against_oracle(member):
     p, B, q, steps = W.ensemble_params(member, PREC_FP32, 2000)
     _check_fp32(p, B, q, ("ens", member), steps=steps)
+
+
+@pytest.mark.parametrize("newton64", [0, 1])
+def test_fp32_newton_forms_error_against_oracle(newton64):
+    """The FP32 form's implicit friction solve with FP32 iterations and one
+    FP64 correction (0, the default) and with FP64 coefficients and FP64
+    iterations (1, fp32_newton_fp64): both within the FP32 bounds against the
+    oracle on a developed current (Voellmy friction, slope correction) over
+    60 steps."""
+    p, B, _ = W.pyroclastic(nx=384, ny=384, dx=26.0, settling=False, t_end=1.0e9)
+    q = W.developed_current_state(p, B)
+    p.fp32_newton_fp64 = newton64
+    errs = _check_fp32(p, B, q, ("newton", 384), steps=60)
+    assert errs["h"][0] > 0.0
