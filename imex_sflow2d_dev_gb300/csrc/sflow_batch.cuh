@@ -27,6 +27,7 @@ template <class R>
 class Batch : public BatchBase {
  public:
   static constexpr int kChunk = 16;
+  static constexpr int kStepLaunches = 4;   // k_b_cand, k_b_mask, k_b_flux (+ clock), k_b_stage2
 
   Batch(int max_runs, int64_t max_tiles) : max_runs_(max_runs), max_tiles_(max_tiles) {}
   ~Batch() override {
@@ -167,8 +168,9 @@ class Batch : public BatchBase {
   }
 
   // `steps` batch steps launched one by one without programmatic dependent
-  // launch, with events between the five kernels; ms5 gets the summed
-  // device time of k_b_cand, k_b_mask, k_b_flux, k_b_dt, k_b_stage2 over
+  // launch, with events between the four kernels; ms5 gets the summed
+  // device time of k_b_cand, k_b_mask, k_b_flux, (0: the clock update is
+  // k_b_flux's last block), k_b_stage2 over
   // the steps and the groups
   int profile_kernels(int64_t steps, int* finished, double* ms5) override {
     if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
@@ -189,7 +191,7 @@ class Batch : public BatchBase {
           ms5[i] += f;
         }
         if (e != cudaSuccess) { err_ = cudaGetErrorString(e); rc = SFLOW_ECUDA; }
-        g->launches += 5;
+        g->launches += kStepLaunches;
       }
     }
     for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
@@ -230,13 +232,13 @@ class Batch : public BatchBase {
         }
         cudaError_t e = cudaGraphLaunch(g->graph_exec, g->stream);
         if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
-        g->launches += 5 * kChunk;
+        g->launches += kStepLaunches * kChunk;
         left -= kChunk;
       }
       for (; left > 0; --left) {
         cudaError_t e = g->tab.b_step(g->args, g->stream, g->grids, g->smem_flux, g->lim, g->pdl, nullptr);
         if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
-        g->launches += 5;
+        g->launches += kStepLaunches;
       }
     }
     launched_ = true;
@@ -270,8 +272,11 @@ class Batch : public BatchBase {
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(g->h_summary, g->d_summary, sizeof(BatchSummary) * max_runs_,
                             cudaMemcpyDeviceToHost, g->stream);
+      BatchCtl ctl;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&ctl, g->d_ctl, sizeof(ctl), cudaMemcpyDeviceToHost, g->stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
       if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
+      if (ctl.overflow) { err_ = "active-cell list overflow (internal error)"; return SFLOW_ECUDA; }
       ++g->launches;
       g->tiles_draining = 0;   // entries of collected runs left the lists
       for (int i = 0; i < max_runs_; ++i) {
@@ -429,6 +434,7 @@ class Batch : public BatchBase {
     BatchCtl* d_ctl = nullptr;
     unsigned long long *d_list0 = nullptr, *d_list1 = nullptr, *d_cand = nullptr;
     unsigned long long *d_dlist0 = nullptr, *d_dlist1 = nullptr;
+    unsigned* d_cells = nullptr;
     BatchSummary* d_summary = nullptr;
     BatchSummary* h_summary = nullptr;
     BatchArgs<R> args;
@@ -469,7 +475,7 @@ class Batch : public BatchBase {
       }
       if (graph_exec) cudaGraphExecDestroy(graph_exec);
       if (graph) cudaGraphDestroy(graph);
-      void* bufs[9] = {d_args, d_runs, d_ctl, d_list0, d_list1, d_dlist0, d_dlist1, d_cand, d_summary};
+      void* bufs[10] = {d_args, d_runs, d_ctl, d_list0, d_list1, d_dlist0, d_dlist1, d_cand, d_cells, d_summary};
       for (void* p : bufs)
         if (p) cudaFree(p);
       if (h_summary) cudaFreeHost(h_summary);
@@ -519,6 +525,10 @@ class Batch : public BatchBase {
     if ((e = cudaMalloc((void**)&g->d_cand, lb)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&g->d_dlist0, lb)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&g->d_dlist1, lb)) != cudaSuccess) return fail(e);
+    // active cells: at most every cell of the tiles the active list holds
+    const size_t cap = (size_t)max_tiles_ * TX * tile_h_;
+    if (cap > 0xffffffffull) { err_ = "max_cells too large for the active-cell list"; g->release(); return nullptr; }
+    if ((e = cudaMalloc((void**)&g->d_cells, sizeof(unsigned) * cap)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&g->d_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
     if ((e = cudaMallocHost((void**)&g->h_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
     g->args.args = g->d_args;
@@ -529,6 +539,8 @@ class Batch : public BatchBase {
     g->args.cand = g->d_cand;
     g->args.dlist0 = g->d_dlist0;
     g->args.dlist1 = g->d_dlist1;
+    g->args.cells = g->d_cells;
+    g->args.cells_cap = (unsigned)cap;
     g->args.summary = g->d_summary;
     g->args.max_runs = max_runs_;
     groups_[ns] = std::move(g);

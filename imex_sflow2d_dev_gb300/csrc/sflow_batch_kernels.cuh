@@ -1,7 +1,7 @@
 // sflow_batch_kernels.cuh -- many independent runs advanced together.
 //
 // Every run keeps its own state, geometry, RunState and kernel arguments
-// (KArgs) in device memory.  One batch step is five launches for all runs
+// (KArgs) in device memory.  One batch step is four launches for all runs
 // of a solid-class count together:
 //
 //   k_b_cand    from the active tiles of the previous step (list L[pp]):
@@ -11,9 +11,13 @@
 //               time factor)
 //   k_b_mask    check_solve on the candidate tiles; tiles with an active
 //               cell -> list L[pp^1]
-//   k_b_flux    k_flux on L[pp^1] (persistent blocks, dynamic tile fetch)
-//   k_b_dt      k_dt of every live run (one thread per run); pp ^= 1
-//   k_b_stage2  k_stage2 on L[pp]
+//   k_b_flux    k_flux on L[pp^1] (persistent blocks, dynamic tile fetch);
+//               its last block to finish advances every live run's clock
+//               (dt_update) and flips pp
+//   k_b_stage2  k_stage2 on the active cells of L[pp]: k_b_mask lists
+//               them (entry = list position << 9 | cell in the tile), so
+//               the warps of the pointwise stage carry active cells only
+//               instead of the mostly idle lanes of sparse tiles
 //
 // Why candidates suffice: a cell outside the active set is not updated, so
 // a wet cell (a check_solve seed) was active in the previous step; active
@@ -63,6 +67,9 @@ struct BatchCtl {
   unsigned pp;         // list read by k_b_cand
   unsigned work[3];    // dynamic tile counters of k_b_mask, k_b_flux, k_b_stage2
   unsigned steps;      // batch steps done
+  unsigned ncells;     // entries in the active-cell list (k_b_mask -> k_b_stage2)
+  unsigned overflow;   // set when the active-cell list was too short (never expected)
+  unsigned flux_done;  // blocks of k_b_flux that have finished (0 between kernels)
 };
 
 // per-slot summary copied to the host after a batch advance
@@ -86,11 +93,14 @@ struct BatchArgs {
   unsigned long long* dlist0;
   unsigned long long* dlist1;
   unsigned long long* cand;
+  unsigned* cells;           // active cells of the tiles of the active list
+  unsigned cells_cap;        // entries the cell list holds
   BatchSummary* summary;     // [max_runs]
   int max_runs;
 };
 
 constexpr int kBatchCandThreads = 256;
+constexpr int kBatchStageThreads = 256;
 
 __device__ __forceinline__ int entry_slot(unsigned long long e) { return (int)(e >> 48); }
 __device__ __forceinline__ unsigned entry_gen(unsigned long long e) { return (unsigned)(e >> 32) & 0xffffu; }
@@ -142,10 +152,11 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
   const unsigned n = ctl->count[pp], nd = ctl->dcount[pp];
   const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned G = gridDim.x * blockDim.x;
-  unsigned long long* Ldout = pp ? b.dlist0 : b.dlist1;   // cleared by k_b_dt
+  unsigned long long* Ldout = pp ? b.dlist0 : b.dlist1;   // cleared by the clock update
   if (gt == 0) {
     ctl->count[pp ^ 1u] = 0u;
     ctl->work[0] = 0u;
+    ctl->ncells = 0u;
   }
   for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
     const BatchRun br = b.runs[r];
@@ -229,6 +240,8 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
 template <class R, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
   __shared__ unsigned s_idx[2];
+  __shared__ unsigned s_wcnt[TH];
+  __shared__ unsigned s_base[2];
   step_kernel_entry();
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
@@ -245,12 +258,31 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArg
     const KArgs<R>& a = b.args[slot];
     const BatchRun& br = b.runs[slot];
     if (threadIdx.x == 0) br.cand[tile] = 0u;
-    // k_b_cand listed only running runs, and no run's clock moves before k_b_dt
+    // k_b_cand listed only running runs, and no run's clock moves before k_b_flux ends
     const int tx = (int)(tile % (unsigned)br.tiles_x), ty = (int)(tile / (unsigned)br.tiles_x);
-    const int code = mask_tile<R, TH>(a, 0, tx, ty, br.tiles_x, true);
-    if (code == 1 && threadIdx.x == 0) {
-      const unsigned pos = atomicAdd(&ctl->count[pp ^ 1u], 1u);
-      out[pos] = e;
+    int act = 0;
+    const int code = mask_tile<R, TH>(a, 0, tx, ty, br.tiles_x, true, &act);
+    if (code == 1) {
+      // the tile into the active list, its active cells into the cell list
+      // (one thread per cell of the tile: thread = row * 32 + column)
+      const int lane = threadIdx.x % TX, warp = threadIdx.x / TX;
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (lane == 0) s_wcnt[warp] = __popc(bal);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (int w = 0; w < TH; ++w) { const unsigned c = s_wcnt[w]; s_wcnt[w] = tot; tot += c; }
+        const unsigned pos = atomicAdd(&ctl->count[pp ^ 1u], 1u);
+        out[pos] = e;
+        s_base[0] = pos;
+        s_base[1] = atomicAdd(&ctl->ncells, tot);
+        if (s_base[1] + tot > b.cells_cap) ctl->overflow = 1u;
+        a.tile_wet[tile] = 0;   // the stage kernel ORs the wet bits of the step in
+      }
+      __syncthreads();
+      const unsigned idx = s_base[1] + s_wcnt[warp] + __popc(bal & ((1u << lane) - 1u));
+      if (act && idx < b.cells_cap) b.cells[idx] = (s_base[0] << 9) | (unsigned)threadIdx.x;
+      __syncthreads();   // s_wcnt / s_base are reused by the next tile
     } else if (code == TILE_DRY_BORDER && threadIdx.x == 0) {
       const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
       dout[pos] = e;
@@ -258,6 +290,26 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArg
     } else if (code == 0 && threadIdx.x == 0) {
       a.tile_wet[tile] = 0;   // an inactive tile holds no mass
     }
+  }
+}
+
+// dt_update of every live run, then the list parity flips (one block)
+template <class R>
+__device__ __forceinline__ void batch_clock(const BatchArgs<R>& b) {
+  for (unsigned r = threadIdx.x; r < (unsigned)b.max_runs; r += blockDim.x) {
+    const BatchRun& br = b.runs[r];
+    if (br.live) dt_update(br.st, br.max_dt);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    BatchCtl* ctl = b.ctl;
+    ctl->pp ^= 1u;
+    // the next step's k_b_cand and k_b_mask append dry-border tiles to the
+    // lists this step read (k_b_cand carries tiles there while it runs, so
+    // the count is cleared here, not by it)
+    ctl->dcount[ctl->pp ^ 1u] = 0u;
+    ctl->ncand = 0u;
+    ctl->steps += 1u;
   }
 }
 
@@ -295,54 +347,70 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FL
     flux_tile<R, NS, LIM, TH>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
                      smem_raw);
   }
+  // the last block to finish advances every run's clock
+  if (last_block_of(&ctl->flux_done, gridDim.x)) batch_clock(b);
 }
 
-template <class R>
-__global__ void __launch_bounds__(kBatchCandThreads) k_b_dt(BatchArgs<R> b) {
-  step_kernel_entry();
-  const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned G = gridDim.x * blockDim.x;
-  for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
-    const BatchRun& br = b.runs[r];
-    if (br.live) dt_update(br.st, br.max_dt);
-  }
-  if (gt == 0) {
-    BatchCtl* ctl = b.ctl;
-    ctl->pp ^= 1u;
-    // the next step's k_b_cand and k_b_mask append dry-border tiles to the
-    // lists this step read (k_b_cand carries tiles there while it runs, so
-    // the count is cleared here, not by it)
-    ctl->dcount[ctl->pp ^ 1u] = 0u;
-    ctl->ncand = 0u;
-    ctl->steps += 1u;
-  }
-}
 
+// One active cell per thread from the cell list (grid-stride; the warps'
+// lanes are all active cells, whatever the tiles' density).  The cell's
+// run arguments come straight from the argument table (L1-cached).  Each
+// wet cell ORs its tile's wet bits (TW_*) in with one atomic on the word
+// holding the tile's byte; the Newton counters are summed per run over the
+// lanes of a warp that share it.
 template <class R, int NS, int TH>
-__global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, TileShape<TH>::STAGE_MIN_BLOCKS)
-    k_b_stage2(BatchArgs<R> b) {
-  __shared__ unsigned s_idx[2];
+__global__ void __launch_bounds__(kBatchStageThreads, sizeof(R) == 4 ? 4 : 1) k_b_stage2(BatchArgs<R> b) {
   step_kernel_entry();
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
   const unsigned long long* L = pp ? b.list1 : b.list0;
-  const unsigned n = ctl->count[pp];
-  TileQueue tq{&ctl->work[2], s_idx};
-  for (unsigned i = tq.first(); i < n; i = tq.next()) {
-    tq.prefetch();
-    const unsigned long long e = L[i];
-    const int slot = entry_slot(e);
-    const unsigned tile = entry_tile(e);
-    // the run's arguments straight from the argument table (L1-cached);
-    // unlike the flux kernel's, the stage code reads them few times per tile
-    const KArgs<R>& a = b.args[slot];
-    if (!a.st->run_step) continue;
-    if (a.tile_active[tile] == 2) {   // dry without ring cells (flux_tile)
-      if (threadIdx.x == 0) a.tile_wet[tile] = 0;
-      continue;
+  const unsigned n = min(ctl->ncells, b.cells_cap);
+  const unsigned stride = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  for (unsigned i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n; i0 += stride) {
+    const unsigned i = i0 + lane;
+    const bool have = i < n;
+    int slot = -1, nit = 0;
+    unsigned status = 0;
+    if (have) {
+      const unsigned c = b.cells[i];
+      const unsigned long long e = L[c >> 9];
+      slot = entry_slot(e);
+      const unsigned tile = entry_tile(e);
+      const KArgs<R>& a = b.args[slot];
+      // a tile the flux kernel found dry (code 2) is left unchanged
+      if (a.st->run_step && a.tile_active[tile] != 2) {
+        const int cl = (int)(c & 511u) % TX, row = (int)(c & 511u) / TX;
+        const int tiles_x = (a.g.nx + TX - 1) / TX;
+        const int j = (int)(tile % (unsigned)tiles_x) * TX + cl, k = (int)(tile / (unsigned)tiles_x) * TH + row;
+        if (stage2_cell<R, NS>(a, -1, j, k, status, nit)) {
+          const unsigned bits = TW_ANY | (cl < 2 ? TW_W : 0u) | (cl >= TX - 2 ? TW_E : 0u) |
+                                (row < 2 ? TW_S : 0u) | (row >= TH - 2 ? TW_N : 0u);
+          uint8_t* wb = a.tile_wet + tile;
+          unsigned* word = reinterpret_cast<unsigned*>(reinterpret_cast<uintptr_t>(wb) & ~(uintptr_t)3);
+          atomicOr(word, bits << (8u * (unsigned)(reinterpret_cast<uintptr_t>(wb) & 3u)));
+        }
+      }
     }
-    const int tiles_x = (a.g.nx + TX - 1) / TX;
-    stage2_tile<R, NS, TH>(a, -1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x));
+    // Newton counters and status per run: the lanes of one run together
+    const unsigned grp = __match_any_sync(0xffffffffu, slot);
+    const int leader = __ffs(grp) - 1;
+    int sum = 0, mx = 0;
+    unsigned st_or = 0;
+    for (unsigned m = grp; m; m &= m - 1u) {
+      const int src = __ffs(m) - 1;
+      sum += __shfl_sync(grp, nit, src);
+      mx = max(mx, __shfl_sync(grp, nit, src));
+      st_or |= __shfl_sync(grp, status, src);
+    }
+    if (lane == leader && slot >= 0) {
+      RunState* st = b.args[slot].st;
+      if (st_or) atomicOr(&st->status, st_or);
+      if (sum > 0) {
+        atomicAdd((unsigned long long*)&st->newton_iters, (unsigned long long)sum);
+        atomicMax(&st->newton_max, mx);
+      }
+    }
   }
 }
 

@@ -3,8 +3,9 @@
 // One driver iteration (IMEX_SfloW2D.f90:395-505) with N_RK = 2 runs as
 //   k_mask    check_solve: active-cell mask, per-tile activity, cell count
 //   k_flux    reconstruction + KT speeds/fluxes + divergence + explicit
-//             sources at q0 (stage 1 == timestep state) and the CFL minimum
-//   k_dt      dt from the CFL minimum and the driver's clamps; t += dt
+//             sources at q0 (stage 1 == timestep state) and the CFL minimum;
+//             its last block takes dt from the CFL minimum and the driver's
+//             clamps and advances the clock
 //   k_stage2  stage 2 pointwise: semi-implicit friction, implicit Newton,
 //             assembly + positivity fixes, erosion/deposition epilogue,
 //             post-step maxima
@@ -222,7 +223,7 @@ constexpr uint8_t TILE_DRY_BORDER = 3;
 // Returns the tile code (block-uniform).
 template <class R, int TH>
 __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int tx, int ty, int tiles_x,
-                                         bool mark_dry = false) {
+                                         bool mark_dry = false, int* act_out = nullptr) {
   constexpr int TY = TH, MRY = TH + 2 * MASK_HALO;
   constexpr int RPW = (MRY + TH - 1) / TH;   // frame rows per warp (TH warps)
   __shared__ unsigned long long srow[MRY];   // bit x: seed at frame column x
@@ -307,6 +308,7 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
     if (act && a.pd.radial_source && (a.cflags[c] & F_SC_MASK) == 1) act = 0;
     a.mask[c] = (uint8_t)act;
   }
+  if (act_out) *act_out = act;
   int cnt = __syncthreads_count(act);
   int code = cnt > 0 ? 1 : 0;
   if (code && mark_dry && !solve_all) {
@@ -1088,22 +1090,8 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
   }
 }
 
-template <class R, int NS, int LIM, int TH>
-__global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
-                                                       R* __restrict__ rout, int want_dt) {
-  step_kernel_entry();
-  const RunState* st = a.st;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  // the timestep pass runs before k_dt advances the clock; the later stage
-  // fluxes of a step run after it and follow its run_step decision
-  if (want_dt ? !running(st) : !st->run_step) return;
-  const uint8_t ta = a.tile_active[blockIdx.y * gridDim.x + blockIdx.x];
-  if (ta == 0 || ta == TILE_DRY_BORDER) return;
-  flux_tile<R, NS, LIM, TH>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
-}
-
 // ---------------------------------------------------------------------------
-// k_dt: dt of this step (timestep + IMEX_SfloW2D.f90:417-439), one thread.
+// dt of this step (timestep + IMEX_SfloW2D.f90:417-439), one thread.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   if (!running(st)) { st->run_step = 0; return; }
@@ -1129,6 +1117,46 @@ __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   st->cells_total += (long long)cells;
   st->border_total += (long long)atomicExch(&st->border_acc[p], 0ull);
   st->steps += 1;
+}
+
+// The timestep pass's clock update folded into its last block: every block
+// counts itself out after its CFL minimum (thread 0's atomicMin, fenced);
+// the block that completes the count has seen every block's minimum and
+// advances the clock (dt_update), which needs no launch of its own.
+// No block waits for another.
+__device__ __forceinline__ bool last_block_of(unsigned* done, unsigned nblocks) {
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(done, 1u);
+    s_last = (prev == nblocks - 1u);
+    if (s_last) {
+      *done = 0u;
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  return s_last != 0;
+}
+
+template <class R, int NS, int LIM, int TH>
+// want_dt: 0 a stage flux; 1 the timestep pass (CFL minimum); 2 the
+// timestep pass whose last block also advances the clock
+__global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
+                                                       R* __restrict__ rout, int want_dt) {
+  step_kernel_entry();
+  RunState* st = a.st;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // the timestep pass runs before the clock advances; the later stage
+  // fluxes of a step run after it and follow its run_step decision
+  if (want_dt ? running(st) : st->run_step) {
+    const uint8_t ta = a.tile_active[blockIdx.y * gridDim.x + blockIdx.x];
+    if (ta != 0 && ta != TILE_DRY_BORDER)
+      flux_tile<R, NS, LIM, TH>(a, qin, rout, want_dt != 0, blockIdx.x, blockIdx.y, smem_raw);
+  }
+  if (want_dt == 2 && last_block_of(&st->flux_done, gridDim.x * gridDim.y) && threadIdx.x == 0)
+    dt_update(st, a.g.max_dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -1191,11 +1219,6 @@ __global__ void __launch_bounds__(256) k_topography(KArgs<R> a) {
     geo[6][c] = (R)__dmul_rn(gc2, __dadd_rn(__dmul_rn(bx, bxx), __dmul_rn(by, bxy)));
     geo[7][c] = (R)__dmul_rn(gc2, __dadd_rn(__dmul_rn(bx, bxy), __dmul_rn(by, byy)));
   }
-}
-
-static __global__ void k_dt(RunState* st, double max_dt) {
-  step_kernel_entry();
-  dt_update(st, max_dt);
 }
 
 // The physical variables of a cell's current state, kept between the
@@ -1359,6 +1382,22 @@ __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const G
     const R pdyn = qc_to_qp<R, NS>(P, q, qp);
     Mixt<R> m = mixt_var<R, NS>(P, qp, false);
     red_grav = m.red_grav;
+    // FP32 form: a cell of particle-free gas at T_ambient -- also a film
+    // just filled from a neighbour whose energy came out below its kinetic
+    // energy, for which qc_to_qp takes T = T_ambient as the reference's
+    // r_phys_var does -- is ambient air, whose reduced gravity the FP64 form
+    // computes as exactly 0 and lifts off.  In FP32, rho_c = 1/(R T/p) can
+    // land an ulp above rho_a_amb and keep the film, with an arbitrary
+    // velocity (measured on the 1024^2 current with settling: a 5e-5 kg/m^2
+    // film at 2e4 m/s).  Such a cell is lifted off here too.
+    if constexpr (sizeof(R) == 4) {
+      if (P.gas && qp[3] == P.T_ambient) {
+        R ssum = R(0);
+#pragma unroll
+        for (int i = 0; i < ns; ++i) ssum += q[4 + i];
+        if (ssum == R(0)) red_grav = R(0);
+      }
+    }
     if (cq && red_grav > R(0)) {
 #pragma unroll
       for (int i = 0; i < nv + 2; ++i) cq->qp[i] = qp[i];

@@ -173,7 +173,7 @@ static cudaError_t tab_b_setup(size_t smem_flux, int* grids) {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_b_flux<R, NS, -1, TH>, TileShape<TH>::FLUX_THREADS,
                                                     smem_flux);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_b_stage2<R, NS, TH>, TileShape<TH>::STAGE_THREADS, 0);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_b_stage2<R, NS, TH>, kBatchStageThreads, 0);
   if (e != cudaSuccess) return e;
   grids[0] = sms * 4;
   grids[1] = sms * (occ[0] > 0 ? occ[0] : 1);
@@ -197,10 +197,10 @@ static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* 
     else e = launch_step_kernel(k_b_flux<R, NS, -1, TH>, dim3(grids[2]), T, smem_flux, s, pdl, b);
   }
   if (e == cudaSuccess) e = rec(3);
-  if (e == cudaSuccess) e = launch_step_kernel(k_b_dt<R>, dim3(1), dim3(kBatchCandThreads), 0, s, pdl, b);
+  // (the clock update is the flux kernel's last block: this interval stays empty)
   if (e == cudaSuccess) e = rec(4);
   if (e == cudaSuccess)
-    e = launch_step_kernel(k_b_stage2<R, NS, TH>, dim3(grids[3]), dim3(TileShape<TH>::STAGE_THREADS), 0, s, pdl, b);
+    e = launch_step_kernel(k_b_stage2<R, NS, TH>, dim3(grids[3]), dim3(kBatchStageThreads), 0, s, pdl, b);
   if (e == cudaSuccess) e = rec(5);
   return e;
 }
