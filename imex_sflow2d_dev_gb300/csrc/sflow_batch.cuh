@@ -27,7 +27,7 @@ template <class R>
 class Batch : public BatchBase {
  public:
   static constexpr int kChunk = 16;
-  static constexpr int kStepLaunches = 4;   // k_b_cand, k_b_mask, k_b_flux (+ clock), k_b_stage2
+  static constexpr int kStepLaunches = 5;   // k_b_cand, k_b_mask, k_b_flux, k_b_dt, k_b_stage2
 
   Batch(int max_runs, int64_t max_tiles) : max_runs_(max_runs), max_tiles_(max_tiles) {}
   ~Batch() override {
@@ -168,9 +168,8 @@ class Batch : public BatchBase {
   }
 
   // `steps` batch steps launched one by one without programmatic dependent
-  // launch, with events between the four kernels; ms5 gets the summed
-  // device time of k_b_cand, k_b_mask, k_b_flux, (0: the clock update is
-  // k_b_flux's last block), k_b_stage2 over
+  // launch, with events between the five kernels; ms5 gets the summed
+  // device time of k_b_cand, k_b_mask, k_b_flux, k_b_dt, k_b_stage2 over
   // the steps and the groups
   int profile_kernels(int64_t steps, int* finished, double* ms5) override {
     if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
@@ -434,7 +433,7 @@ class Batch : public BatchBase {
     BatchCtl* d_ctl = nullptr;
     unsigned long long *d_list0 = nullptr, *d_list1 = nullptr, *d_cand = nullptr;
     unsigned long long *d_dlist0 = nullptr, *d_dlist1 = nullptr;
-    unsigned* d_cells = nullptr;
+    unsigned long long* d_cells = nullptr;
     BatchSummary* d_summary = nullptr;
     BatchSummary* h_summary = nullptr;
     BatchArgs<R> args;
@@ -528,7 +527,7 @@ class Batch : public BatchBase {
     // active cells: at most every cell of the tiles the active list holds
     const size_t cap = (size_t)max_tiles_ * TX * tile_h_;
     if (cap > 0xffffffffull) { err_ = "max_cells too large for the active-cell list"; g->release(); return nullptr; }
-    if ((e = cudaMalloc((void**)&g->d_cells, sizeof(unsigned) * cap)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&g->d_cells, sizeof(unsigned long long) * cap)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&g->d_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
     if ((e = cudaMallocHost((void**)&g->h_summary, sizeof(BatchSummary) * max_runs_)) != cudaSuccess) return fail(e);
     g->args.args = g->d_args;

@@ -1,7 +1,7 @@
 // sflow_batch_kernels.cuh -- many independent runs advanced together.
 //
 // Every run keeps its own state, geometry, RunState and kernel arguments
-// (KArgs) in device memory.  One batch step is four launches for all runs
+// (KArgs) in device memory.  One batch step is five launches for all runs
 // of a solid-class count together:
 //
 //   k_b_cand    from the active tiles of the previous step (list L[pp]):
@@ -11,11 +11,10 @@
 //               time factor)
 //   k_b_mask    check_solve on the candidate tiles; tiles with an active
 //               cell -> list L[pp^1]
-//   k_b_flux    k_flux on L[pp^1] (persistent blocks, dynamic tile fetch);
-//               its last block to finish advances every live run's clock
-//               (dt_update) and flips pp
+//   k_b_flux    k_flux on L[pp^1] (persistent blocks, dynamic tile fetch)
+//   k_b_dt      k_dt of every live run (one thread per run); pp ^= 1
 //   k_b_stage2  k_stage2 on the active cells of L[pp]: k_b_mask lists
-//               them (entry = list position << 9 | cell in the tile), so
+//               them (entry = slot | tile | cell in the tile), so
 //               the warps of the pointwise stage carry active cells only
 //               instead of the mostly idle lanes of sparse tiles
 //
@@ -69,7 +68,6 @@ struct BatchCtl {
   unsigned steps;      // batch steps done
   unsigned ncells;     // entries in the active-cell list (k_b_mask -> k_b_stage2)
   unsigned overflow;   // set when the active-cell list was too short (never expected)
-  unsigned flux_done;  // blocks of k_b_flux that have finished (0 between kernels)
 };
 
 // per-slot summary copied to the host after a batch advance
@@ -93,7 +91,7 @@ struct BatchArgs {
   unsigned long long* dlist0;
   unsigned long long* dlist1;
   unsigned long long* cand;
-  unsigned* cells;           // active cells of the tiles of the active list
+  unsigned long long* cells; // active cells: slot (16 bits) | tile (39) | cell in the tile (9)
   unsigned cells_cap;        // entries the cell list holds
   BatchSummary* summary;     // [max_runs]
   int max_runs;
@@ -152,7 +150,7 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
   const unsigned n = ctl->count[pp], nd = ctl->dcount[pp];
   const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned G = gridDim.x * blockDim.x;
-  unsigned long long* Ldout = pp ? b.dlist0 : b.dlist1;   // cleared by the clock update
+  unsigned long long* Ldout = pp ? b.dlist0 : b.dlist1;   // cleared by k_b_dt
   if (gt == 0) {
     ctl->count[pp ^ 1u] = 0u;
     ctl->work[0] = 0u;
@@ -240,8 +238,6 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
 template <class R, int TH>
 __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
   __shared__ unsigned s_idx[2];
-  __shared__ unsigned s_wcnt[TH];
-  __shared__ unsigned s_base[2];
   step_kernel_entry();
   BatchCtl* ctl = b.ctl;
   const unsigned pp = ctl->pp;
@@ -258,31 +254,33 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArg
     const KArgs<R>& a = b.args[slot];
     const BatchRun& br = b.runs[slot];
     if (threadIdx.x == 0) br.cand[tile] = 0u;
-    // k_b_cand listed only running runs, and no run's clock moves before k_b_flux ends
+    // k_b_cand listed only running runs, and no run's clock moves before k_b_dt
     const int tx = (int)(tile % (unsigned)br.tiles_x), ty = (int)(tile / (unsigned)br.tiles_x);
     int act = 0;
     const int code = mask_tile<R, TH>(a, 0, tx, ty, br.tiles_x, true, &act);
     if (code == 1) {
       // the tile into the active list, its active cells into the cell list
-      // (one thread per cell of the tile: thread = row * 32 + column)
-      const int lane = threadIdx.x % TX, warp = threadIdx.x / TX;
-      const unsigned bal = __ballot_sync(0xffffffffu, act);
-      if (lane == 0) s_wcnt[warp] = __popc(bal);
-      __syncthreads();
+      // (one thread per cell of the tile: thread = row * 32 + column), one
+      // atomic per warp holding active cells
       if (threadIdx.x == 0) {
-        unsigned tot = 0;
-        for (int w = 0; w < TH; ++w) { const unsigned c = s_wcnt[w]; s_wcnt[w] = tot; tot += c; }
         const unsigned pos = atomicAdd(&ctl->count[pp ^ 1u], 1u);
         out[pos] = e;
-        s_base[0] = pos;
-        s_base[1] = atomicAdd(&ctl->ncells, tot);
-        if (s_base[1] + tot > b.cells_cap) ctl->overflow = 1u;
         a.tile_wet[tile] = 0;   // the stage kernel ORs the wet bits of the step in
       }
-      __syncthreads();
-      const unsigned idx = s_base[1] + s_wcnt[warp] + __popc(bal & ((1u << lane) - 1u));
-      if (act && idx < b.cells_cap) b.cells[idx] = (s_base[0] << 9) | (unsigned)threadIdx.x;
-      __syncthreads();   // s_wcnt / s_base are reused by the next tile
+      const int lane = threadIdx.x % TX;
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (bal) {
+        const unsigned nw = __popc(bal);
+        unsigned base = 0;
+        if (lane == 0) {
+          base = atomicAdd(&ctl->ncells, nw);
+          if (base + nw > b.cells_cap) ctl->overflow = 1u;
+        }
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const unsigned idx = base + __popc(bal & ((1u << lane) - 1u));
+        if (act && idx < b.cells_cap)
+          b.cells[idx] = (e & 0xffff000000000000ull) | ((unsigned long long)tile << 9) | (unsigned)threadIdx.x;
+      }
     } else if (code == TILE_DRY_BORDER && threadIdx.x == 0) {
       const unsigned pos = atomicAdd(&ctl->dcount[pp ^ 1u], 1u);
       dout[pos] = e;
@@ -290,26 +288,6 @@ __global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArg
     } else if (code == 0 && threadIdx.x == 0) {
       a.tile_wet[tile] = 0;   // an inactive tile holds no mass
     }
-  }
-}
-
-// dt_update of every live run, then the list parity flips (one block)
-template <class R>
-__device__ __forceinline__ void batch_clock(const BatchArgs<R>& b) {
-  for (unsigned r = threadIdx.x; r < (unsigned)b.max_runs; r += blockDim.x) {
-    const BatchRun& br = b.runs[r];
-    if (br.live) dt_update(br.st, br.max_dt);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    BatchCtl* ctl = b.ctl;
-    ctl->pp ^= 1u;
-    // the next step's k_b_cand and k_b_mask append dry-border tiles to the
-    // lists this step read (k_b_cand carries tiles there while it runs, so
-    // the count is cleared here, not by it)
-    ctl->dcount[ctl->pp ^ 1u] = 0u;
-    ctl->ncand = 0u;
-    ctl->steps += 1u;
   }
 }
 
@@ -347,10 +325,29 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS, TileShape<TH>::FL
     flux_tile<R, NS, LIM, TH>(a, a.q, a.rd, 1, (int)(tile % (unsigned)tiles_x), (int)(tile / (unsigned)tiles_x),
                      smem_raw);
   }
-  // the last block to finish advances every run's clock
-  if (last_block_of(&ctl->flux_done, gridDim.x)) batch_clock(b);
 }
 
+
+template <class R>
+__global__ void __launch_bounds__(kBatchCandThreads) k_b_dt(BatchArgs<R> b) {
+  step_kernel_entry();
+  const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned G = gridDim.x * blockDim.x;
+  for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
+    const BatchRun& br = b.runs[r];
+    if (br.live) dt_update(br.st, br.max_dt);
+  }
+  if (gt == 0) {
+    BatchCtl* ctl = b.ctl;
+    ctl->pp ^= 1u;
+    // the next step's k_b_cand and k_b_mask append dry-border tiles to the
+    // lists this step read (k_b_cand carries tiles there while it runs, so
+    // the count is cleared here, not by it)
+    ctl->dcount[ctl->pp ^ 1u] = 0u;
+    ctl->ncand = 0u;
+    ctl->steps += 1u;
+  }
+}
 
 // One active cell per thread from the cell list (grid-stride; the warps'
 // lanes are all active cells, whatever the tiles' density).  The cell's
@@ -362,8 +359,6 @@ template <class R, int NS, int TH>
 __global__ void __launch_bounds__(kBatchStageThreads, sizeof(R) == 4 ? 4 : 1) k_b_stage2(BatchArgs<R> b) {
   step_kernel_entry();
   BatchCtl* ctl = b.ctl;
-  const unsigned pp = ctl->pp;
-  const unsigned long long* L = pp ? b.list1 : b.list0;
   const unsigned n = min(ctl->ncells, b.cells_cap);
   const unsigned stride = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
@@ -373,10 +368,10 @@ __global__ void __launch_bounds__(kBatchStageThreads, sizeof(R) == 4 ? 4 : 1) k_
     int slot = -1, nit = 0;
     unsigned status = 0;
     if (have) {
-      const unsigned c = b.cells[i];
-      const unsigned long long e = L[c >> 9];
-      slot = entry_slot(e);
-      const unsigned tile = entry_tile(e);
+      const unsigned long long ce = b.cells[i];
+      slot = entry_slot(ce);
+      const unsigned tile = (unsigned)((ce >> 9) & 0x7fffffffffull);
+      const unsigned c = (unsigned)(ce & 511u);
       const KArgs<R>& a = b.args[slot];
       // a tile the flux kernel found dry (code 2) is left unchanged
       if (a.st->run_step && a.tile_active[tile] != 2) {

@@ -114,8 +114,7 @@ class BatchBase {
   // the same with the device time of the steps (CUDA events across the
   // groups' streams) in *ms
   virtual int advance_timed(int64_t steps, int* finished, double* ms) = 0;
-  // steps one by one with the device time of each kernel (5 slots: cand,
-  // mask, flux, clock = 0, stage)
+  // steps one by one with the device time of each of the five kernels
   virtual int profile_kernels(int64_t steps, int* finished, double* ms5) = 0;
   // asynchronous form of advance: launch returns at once, wait synchronises
   virtual int launch(int64_t steps) = 0;

@@ -3,9 +3,8 @@
 // One driver iteration (IMEX_SfloW2D.f90:395-505) with N_RK = 2 runs as
 //   k_mask    check_solve: active-cell mask, per-tile activity, cell count
 //   k_flux    reconstruction + KT speeds/fluxes + divergence + explicit
-//             sources at q0 (stage 1 == timestep state) and the CFL minimum;
-//             its last block takes dt from the CFL minimum and the driver's
-//             clamps and advances the clock
+//             sources at q0 (stage 1 == timestep state) and the CFL minimum
+//   k_dt      dt from the CFL minimum and the driver's clamps; t += dt
 //   k_stage2  stage 2 pointwise: semi-implicit friction, implicit Newton,
 //             assembly + positivity fixes, erosion/deposition epilogue,
 //             post-step maxima
@@ -1091,7 +1090,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// dt of this step (timestep + IMEX_SfloW2D.f90:417-439), one thread.
+// k_dt: dt of this step (timestep + IMEX_SfloW2D.f90:417-439), one thread.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   if (!running(st)) { st->run_step = 0; return; }
@@ -1119,44 +1118,23 @@ __device__ __forceinline__ void dt_update(RunState* st, double max_dt) {
   st->steps += 1;
 }
 
-// The timestep pass's clock update folded into its last block: every block
-// counts itself out after its CFL minimum (thread 0's atomicMin, fenced);
-// the block that completes the count has seen every block's minimum and
-// advances the clock (dt_update), which needs no launch of its own.
-// No block waits for another.
-__device__ __forceinline__ bool last_block_of(unsigned* done, unsigned nblocks) {
-  __shared__ int s_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(done, 1u);
-    s_last = (prev == nblocks - 1u);
-    if (s_last) {
-      *done = 0u;
-      __threadfence();
-    }
-  }
-  __syncthreads();
-  return s_last != 0;
+static __global__ void k_dt(RunState* st, double max_dt) {
+  step_kernel_entry();
+  dt_update(st, max_dt);
 }
 
 template <class R, int NS, int LIM, int TH>
-// want_dt: 0 a stage flux; 1 the timestep pass (CFL minimum); 2 the
-// timestep pass whose last block also advances the clock
 __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS) k_flux(KArgs<R> a, const R* __restrict__ qin,
                                                        R* __restrict__ rout, int want_dt) {
   step_kernel_entry();
-  RunState* st = a.st;
+  const RunState* st = a.st;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // the timestep pass runs before the clock advances; the later stage
+  // the timestep pass runs before k_dt advances the clock; the later stage
   // fluxes of a step run after it and follow its run_step decision
-  if (want_dt ? running(st) : st->run_step) {
-    const uint8_t ta = a.tile_active[blockIdx.y * gridDim.x + blockIdx.x];
-    if (ta != 0 && ta != TILE_DRY_BORDER)
-      flux_tile<R, NS, LIM, TH>(a, qin, rout, want_dt != 0, blockIdx.x, blockIdx.y, smem_raw);
-  }
-  if (want_dt == 2 && last_block_of(&st->flux_done, gridDim.x * gridDim.y) && threadIdx.x == 0)
-    dt_update(st, a.g.max_dt);
+  if (want_dt ? !running(st) : !st->run_step) return;
+  const uint8_t ta = a.tile_active[blockIdx.y * gridDim.x + blockIdx.x];
+  if (ta == 0 || ta == TILE_DRY_BORDER) return;
+  flux_tile<R, NS, LIM, TH>(a, qin, rout, want_dt, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -1321,8 +1299,9 @@ __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const G
     qp[3] = P.T_ambient;
   }
   if (cq) cq->valid = false;
+  unsigned dep_limited = 0u;
   mass_exchange<R, NS>(P, qp, geo.Bx, geo.By, dt, P.erosion_coeff > R(0) ? ex.erodible : nullptr, dep, ex.ers,
-                       eqn, ex.topo);
+                       eqn, ex.topo, sizeof(R) == 4 ? &dep_limited : nullptr);
   if (P.bottom_source && ex.bf > R(0)) {
     // the part of the cell inside the bottom source exchanges nothing
     const R out_frac = R(1) - ex.bf;
@@ -1338,6 +1317,15 @@ __device__ __forceinline__ unsigned erosion_deposition(const Phys<R>& P, const G
 #pragma unroll
   for (int i = 0; i < ns; ++i) q[4 + i] = rmax(R(0), q[4 + i]);
   if constexpr (sizeof(R) == 4) {
+    // FP32 form: a class whose deposition took the limiter r_h alpha/dt
+    // settles out entirely -- zero in exact arithmetic; the FP32 sum leaves
+    // a few ulp of its old mass (an alpha of ~1e-9 where the FP64 form
+    // keeps ~1e-18), which is cleared
+    if (!(P.bottom_source && ex.bf > R(0))) {
+#pragma unroll
+      for (int i = 0; i < ns; ++i)
+        if (((dep_limited >> i) & 1u) && ex.ers[i] == R(0)) q[4 + i] = R(0);
+    }
     // FP32 form: when the limited deposition and carrier loss remove the
     // whole mass (exactly zero in exact arithmetic), the sum leaves a
     // rounding residual of a few ulp of the old mass, with a momentum

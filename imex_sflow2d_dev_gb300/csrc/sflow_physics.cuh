@@ -865,7 +865,8 @@ __device__ __forceinline__ R settling_velocity(const Phys<R>& P, R diam, R rhos,
 // T_erodible to the cell's T just before this use).
 template <class R, int NS>
 __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R Bx, R By, R dt,
-                                              const R* erodible, R* dep, R* ers, R* eqn, R& topo) {
+                                              const R* erodible, R* dep, R* ers, R* eqn, R& topo,
+                                              unsigned* dep_limited = nullptr) {
   constexpr int ns = NS, nv = 4 + NS;
   for (int i = 0; i < ns; ++i) { dep[i] = R(0); ers[i] = R(0); }
   for (int i = 0; i < nv; ++i) eqn[i] = R(0);
@@ -900,7 +901,9 @@ __device__ __forceinline__ void mass_exchange(const Phys<R>& P, const R* qpj, R 
       R sv = settling_velocity<R>(P, P.diam_s[i], P.rho_s[i], m.rho_c, inv_kin_visc);
       dep[i] = al[i] * sv * R(1);
       dep[i] = dep[i] * rpow<R>(R(1) - rmin(R(1), at / alpha_max), hind_exp);
-      dep[i] = rmin(dep[i], r_h * al[i] / dt);
+      const R cap = r_h * al[i] / dt;
+      if (dep_limited && !(dep[i] < cap)) *dep_limited |= 1u << i;   // the whole class settles out
+      dep[i] = rmin(dep[i], cap);
     }
   }
   for (int i = 0; i < ns; ++i) sdep += dep[i];
@@ -1015,7 +1018,9 @@ __device__ __noinline__ float reduced_friction_solve_fp64(const Phys<float>& P, 
   };
   double dK;
   double K = Kd(S, dK);
-  double sd = 2.0 * S / (1.0 + sqrt(fmax(1.0 + 4.0 * dta * K * S, 0.0)));
+  const double disc = 1.0 + 4.0 * dta * K * S;
+  if (!(disc >= 0.0)) { iters = 0; return Sf; }   // no real root (see reduced_friction_solve)
+  double sd = 2.0 * S / (1.0 + sqrt(disc));
   int it = 0;
   for (; it < 12; ++it) {
     K = Kd(sd, dK);
@@ -1085,9 +1090,16 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, co
   const float dtaf = d2f_rn(dta);
   float dKf;
   float K = Kf(S, dKf);
-  float s = 2.0f * S / (1.0f + sqrtf(fmaxf(1.0f + 4.0f * dtaf * K * S, 0.0f)));
+  // K < 0 (a mixture lighter than the ambient: the buoyancy-reduced
+  // friction changes sign) with 1 + 4 dt a K S < 0 leaves g without a real
+  // root: the friction step keeps the predictor's momentum (taking the
+  // clamped quadratic instead doubled a film's momentum every step)
+  const float disc = 1.0f + 4.0f * dtaf * K * S;
+  if (!(disc >= 0.0f)) return S;
+  float s = 2.0f * S / (1.0f + sqrtf(disc));
   float gdf = 1.0f + 2.0f * dtaf * K * s;
   if (varT) {
+    const float s0 = s, gd0 = gdf;
     for (int it = 0; it < 8; ++it) {
       K = Kf(s, dKf);
       const float gv = s + dtaf * K * s * s - S;
@@ -1096,6 +1108,8 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, co
       s -= ds;
       if (!(fabsf(ds) > 1.0e-7f * s)) break;
     }
+    // the root lies in (0, 2S] (K > 0: below S; K < 0: at most 2S)
+    if (!(s > 0.0f && s <= 2.0f * S)) { s = s0; gdf = gd0; }
   }
   // One FP64 Newton step from the FP32 root: the residual g(s) in FP64
   // (rho_m to ~1e-14 by one refinement of the float reciprocal), the

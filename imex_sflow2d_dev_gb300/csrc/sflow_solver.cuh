@@ -365,8 +365,11 @@ class Solver : public SolverBase {
       SFLOW_CU(cudaEventRecord(ev_[0], stream_));
       SFLOW_CU(launch_mask(2));
       SFLOW_CU(cudaEventRecord(ev_[1], stream_));
-      SFLOW_CU(launch_flux(2));   // the clock update is the flux kernel's last block
+      SFLOW_CU(launch_flux(1));
       SFLOW_CU(cudaEventRecord(ev_[2], stream_));
+      SFLOW_CU(launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt));
+      ++launches_;
+      SFLOW_CU(cudaGetLastError());
       SFLOW_CU(cudaEventRecord(ev_[3], stream_));
       SFLOW_CU(launch_stage2(-1));
       SFLOW_CU(cudaEventRecord(ev_[4], stream_));
@@ -878,8 +881,8 @@ class Solver : public SolverBase {
 
   int steps_launches() const {
     const int topo = Bc_ ? 1 : 0;
-    if (hs_.nrk == 2) return 3 + topo;
-    int n = 2 + hs_.nrk + 1 + topo;
+    if (hs_.nrk == 2) return 4 + topo;
+    int n = 3 + hs_.nrk + 1 + topo;
     const bool fused0 = hs_.a_dirk[0] == 0.0 && hs_.omega_tilde[0] > 0.0;
     for (int i = 0; i < hs_.nrk; ++i)
       if (hs_.omega_tilde[i] > 0.0 && !(i == 0 && fused0)) ++n;
@@ -1239,7 +1242,11 @@ class Solver : public SolverBase {
     cudaError_t e;
     if (hs_.nrk == 2) {
       e = launch_mask(2);
-      if (e == cudaSuccess) e = launch_flux(2);   // its last block advances the clock
+      if (e == cudaSuccess) e = launch_flux(1);
+      if (e == cudaSuccess) {
+        e = launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt);
+        ++launches_;
+      }
       if (e == cudaSuccess) e = launch_stage2(-1);
     } else {
       e = launch_step_general();
@@ -1259,7 +1266,10 @@ class Solver : public SolverBase {
     cudaError_t e = launch_mask(0);
     if (e != cudaSuccess) return e;
     ++launches_;
-    e = tab_.flux(ka_, grid, smem_flux_, stream_, q_, fused0 ? rd_ : nullptr, 2);   // + the clock
+    e = tab_.flux(ka_, grid, smem_flux_, stream_, q_, fused0 ? rd_ : nullptr, 1);
+    if (e != cudaSuccess) return e;
+    e = launch_step_kernel(k_dt, dim3(1), dim3(1), 0, stream_, ka_.g.pdl, st_, hs_.p.max_dt);
+    ++launches_;
     if (e != cudaSuccess) return e;
     for (int i = 0; i < hs_.nrk; ++i) {
       ++launches_;

@@ -36,8 +36,7 @@ struct KernelTable {
   cudaError_t (*b_setup)(size_t smem_flux, int* grids) = nullptr;
   // lim = 1: every run of the group uses minmod for every variable
   // pdl: launch with programmatic dependent launch; ev: NULL, or 6 events
-  // recorded before, between and after the four kernels (the fourth
-  // interval, the clock update inside k_b_flux, is empty)
+  // recorded before, between and after the five kernels
   cudaError_t (*b_step)(const BatchArgs<R>&, cudaStream_t, const int* grids, size_t smem_flux, int lim,
                         int pdl, cudaEvent_t* ev) = nullptr;
   cudaError_t (*b_admit)(const BatchArgs<R>&, cudaStream_t, int slot, unsigned gen, unsigned ntiles) = nullptr;

@@ -197,7 +197,7 @@ static cudaError_t tab_b_step(const BatchArgs<R>& b, cudaStream_t s, const int* 
     else e = launch_step_kernel(k_b_flux<R, NS, -1, TH>, dim3(grids[2]), T, smem_flux, s, pdl, b);
   }
   if (e == cudaSuccess) e = rec(3);
-  // (the clock update is the flux kernel's last block: this interval stays empty)
+  if (e == cudaSuccess) e = launch_step_kernel(k_b_dt<R>, dim3(1), dim3(kBatchCandThreads), 0, s, pdl, b);
   if (e == cudaSuccess) e = rec(4);
   if (e == cudaSuccess)
     e = launch_step_kernel(k_b_stage2<R, NS, TH>, dim3(grids[3]), dim3(kBatchStageThreads), 0, s, pdl, b);

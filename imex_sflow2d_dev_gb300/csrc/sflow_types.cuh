@@ -105,10 +105,6 @@ struct RunState {
   // active cells of dry border tiles (tile code 3: counted, not computed)
   unsigned long long border_acc[2];
   long long border_total;
-  // blocks of the timestep pass that have finished (the last one advances
-  // the clock; 0 between kernels)
-  unsigned flux_done;
-  unsigned pad3;
 };
 
 }  // namespace sflow

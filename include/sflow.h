@@ -419,9 +419,8 @@ int sflow_batch_advance(sflow_batch* b, int64_t steps, int32_t* finished);
  * batch's streams) in *device_ms */
 int sflow_batch_advance_timed(sflow_batch* b, int64_t steps, int32_t* finished, double* device_ms);
 /* `steps` batch steps launched one at a time with CUDA events between the
- * four kernels of a step; ms5 = summed device ms of k_b_cand, k_b_mask,
- * k_b_flux, 0 (the clock update runs in k_b_flux's last block),
- * k_b_stage2 (for the benchmark's per-kernel roofline) */
+ * five kernels of a step; ms5 = summed device ms of k_b_cand, k_b_mask,
+ * k_b_flux, k_b_dt, k_b_stage2 (for the benchmark's per-kernel roofline) */
 int sflow_batch_profile_kernels(sflow_batch* b, int64_t steps, int32_t* finished, double* ms5);
 int sflow_batch_poll(sflow_batch* b, int32_t run_id, SflowStepStats* stats, int32_t* done);
 int sflow_batch_counters(sflow_batch* b, int32_t run_id, int64_t* cell_updates, int64_t* steps);
