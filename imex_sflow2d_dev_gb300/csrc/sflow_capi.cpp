@@ -301,6 +301,8 @@ void sflow_default_params(SflowParams* p) {
   for (int i = 0; i < SFLOW_MAX_INTERVALS; ++i) p->t_intervals[i] = p->vel_intervals[i] = -1.0;
 }
 
+static int create_from(const SflowParams* p, HostSetup& s, sflow_handle** out);
+
 int sflow_create(const SflowParams* p, const double* B_cent, sflow_handle** out) {
   if (!out) return fail(SFLOW_EINVAL, "out is NULL");
   *out = nullptr;
@@ -308,6 +310,22 @@ int sflow_create(const SflowParams* p, const double* B_cent, sflow_handle** out)
   std::string err;
   int rc = sflow::host_setup(p, B_cent, s, err);
   if (rc != SFLOW_OK) return fail(rc, err);
+  return create_from(p, s, out);
+}
+
+int sflow_create_rows(const SflowParams* p, const double* B_cent, int32_t k0, int32_t rows, int32_t own_lo,
+                      int32_t own_hi, sflow_handle** out) {
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  *out = nullptr;
+  HostSetup s;
+  std::string err;
+  int rc = sflow::host_setup_rows(p, B_cent, k0, rows, own_lo, own_hi, s, err);
+  if (rc != SFLOW_OK) return fail(rc, err);
+  return create_from(p, s, out);
+}
+
+static int create_from(const SflowParams* p, HostSetup& s, sflow_handle** out) {
+  std::string err;
   SolverBase* sv = (p->precision == SFLOW_PREC_FP32) ? sflow::make_solver_fp32(s, err)
                                                      : sflow::make_solver_fp64(s, err);
   if (!sv) return fail(SFLOW_ECUDA, err.empty() ? "device set-up failed" : err);
@@ -398,6 +416,18 @@ int sflow_upload_deposit(sflow_handle* h, const double* in) {
   CHECK_HANDLE(h);
   if (!in) return fail(SFLOW_EINVAL, "in is NULL");
   FORWARD(h->solver->upload_deposit(in));
+}
+
+int sflow_get_rows(sflow_handle* h, int32_t k_lo, int32_t n, double* out) {
+  CHECK_HANDLE(h);
+  if (!out) return fail(SFLOW_EINVAL, "out is NULL");
+  FORWARD(h->solver->get_rows(k_lo, n, out));
+}
+
+int sflow_put_rows(sflow_handle* h, int32_t k_lo, int32_t n, const double* in) {
+  CHECK_HANDLE(h);
+  if (!in) return fail(SFLOW_EINVAL, "in is NULL");
+  FORWARD(h->solver->put_rows(k_lo, n, in));
 }
 
 int sflow_download_erosion(sflow_handle* h, double* out) {

@@ -42,6 +42,9 @@ struct HostSetup {
   double thk_levels[SFLOW_MAX_LEVELS] = {0}, dyn_levels[SFLOW_MAX_LEVELS] = {0};
   // topography (B_cent), row-major
   std::vector<double> B;
+  // row slab of a larger domain (host_setup_rows): rows row0 .. row0+ny-1
+  // of it, of which own_lo .. own_hi-1 (local) are this domain's own
+  int row0 = 0, own_lo = 0, own_hi = 0;
 };
 
 constexpr uint8_t kFlagNodata = 0x40;   // B_nodata cell
@@ -49,6 +52,12 @@ constexpr uint8_t kFlagBottom = 0x80;   // cell fraction of the bottom source > 
 
 // Validates p and fills s; returns 0 or SFLOW_EINVAL with a message in err.
 int host_setup(const SflowParams* p, const double* B_cent, HostSetup& s, std::string& err);
+// host_setup of the whole domain, then only rows k0 .. k0+rows-1 kept (every
+// derived field computed on the whole domain, so a slab's cells carry the
+// same topography terms, inlet geometry and flags as in the whole run);
+// own_lo .. own_hi-1 are the slab's own rows (local indices)
+int host_setup_rows(const SflowParams* p, const double* B_cent, int k0, int rows, int own_lo, int own_hi,
+                    HostSetup& s, std::string& err);
 
 // Reference mixt_var (constitutive_2d.f90:1342-1492) in FP64 on the host,
 // used for constants of the run (inlet state).
@@ -78,6 +87,9 @@ class SolverBase {
   virtual int set_erodible(const double* thickness) = 0;
   virtual int set_nodata(const uint8_t* nodata) = 0;
   virtual int vuln_table(int* n_thk, int* n_dyn, uint8_t* out) = 0;
+  // rows k_lo .. k_lo+n-1 of the conservative state, reference layout
+  virtual int get_rows(int k_lo, int n, double* out) = 0;
+  virtual int put_rows(int k_lo, int n, const double* in) = 0;
   virtual int upload_maps(const double* h, const double* p, const double* v) = 0;
   virtual int set_output_time(double t_output) = 0;
   virtual int check_solve(int solve_all) = 0;

@@ -165,13 +165,20 @@ __device__ __forceinline__ R xcomp(const Grid<R>& g, int j) {
 }
 template <class R>
 __device__ __forceinline__ R ystag(const Grid<R>& g, int k) {
+  k += g.k_off;
   if constexpr (sizeof(R) == 8) return g.y0 + (double)k * g.dy;
   else return g.y0r + (R)k * g.rdy;
 }
 template <class R>
 __device__ __forceinline__ R ycomp(const Grid<R>& g, int k) {
+  k += g.k_off;
   if constexpr (sizeof(R) == 8) return 0.5 * ((g.y0 + (double)k * g.dy) + (g.y0 + (double)(k + 1) * g.dy));
   else return g.y0r + ((R)k + 0.5f) * g.rdy;
+}
+// the row is one this domain owns (row slabs; always true for a whole domain)
+template <class R>
+__device__ __forceinline__ bool owned_row(const Grid<R>& g, int k) {
+  return g.whole || (k >= g.own_lo && k < g.own_hi);
 }
 
 template <class R>
@@ -308,8 +315,14 @@ __device__ __forceinline__ int mask_tile(const KArgs<R>& a, int solve_all, int t
     a.mask[c] = (uint8_t)act;
   }
   if (act_out) *act_out = act;
-  int cnt = __syncthreads_count(act);
-  int code = cnt > 0 ? 1 : 0;
+  int cnt, code;
+  if (g.whole) {
+    cnt = __syncthreads_count(act);
+    code = cnt > 0 ? 1 : 0;
+  } else {
+    cnt = __syncthreads_count(act && owned_row(g, k));
+    code = __syncthreads_or(act) ? 1 : 0;
+  }
   if (code && mark_dry && !solve_all) {
     unsigned spec = 0u;
 #pragma unroll
@@ -1058,7 +1071,7 @@ __device__ __forceinline__ void flux_tile(const KArgs<R>& a, const R* __restrict
         }
         if (rout) rout[i * g.plane + c] = d - e[i];
       }
-      if (want_dt && !tile_dry) {
+      if (want_dt && !tile_dry && owned_row(g, k)) {
         R ax = rmax(sAx[cy * (TX + 1) + cx], sAx[cy * (TX + 1) + cx + 1]);
         R ay = (g.ny > 1) ? rmax(sAy[cy * TX + cx], sAy[(cy + 1) * TX + cx]) : R(0);
         if constexpr (sizeof(R) == 8) {
@@ -1735,8 +1748,9 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, sizeof(R) == 4 ?
   if (ta == 0 || ta == 2 || ta == TILE_DRY_BORDER) return;   // inactive, or left unchanged (k_flux, k_mask)
   unsigned status = 0;
   int nit = 0;
-  int wet = stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, blockIdx.y * 8 + threadIdx.x / TX,
-                               status, nit);
+  const int kk = blockIdx.y * 8 + threadIdx.x / TX;
+  int wet = stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, kk, status, nit);
+  if (!owned_row(a.g, kk)) { status = 0u; nit = 0; }   // halo rows of a row slab
   newton_stats<R>(a.st, status, nit, nit);
   if (mode < 0) {
     // wet flag of the tile for the next check_solve (buffer of the new
@@ -1789,6 +1803,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage(KArgs<R>
         }
       }
       status |= stage_cell<R, NS>(a, geo, q0, s1, s2, dt, a.tableau_ad[irk * 4 + irk], qg, rn, nit);
+      if (!owned_row(g, k)) { status = 0u; nit = 0; }   // halo rows of a row slab
 #pragma unroll
       for (int i = 0; i < nv; ++i) {
         a.qs[i * g.plane + c] = qg[i];
@@ -1840,6 +1855,7 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_assemble(KArgs
       CellQp<R, NS> cq;
       status |= assemble_fixes<R, NS>(a.pr, q, &cq);
       status |= cell_exchange<R, NS>(a, c, dt, q, &cq);
+      if (!owned_row(g, k)) status = 0u;   // halo rows of a row slab
 #pragma unroll
       for (int i = 0; i < nv; ++i) a.q[i * g.plane + c] = q[i];
       post_step_maps<R, NS>(a, c, q, &cq);

@@ -8,6 +8,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "sflow_host.h"
 
@@ -501,6 +502,33 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   }
   ring_source(s);
   if (p.bottom_radial_source_flag) cell_fractions(s);
+  s.row0 = 0;
+  s.own_lo = 0;
+  s.own_hi = s.ny;
+  return SFLOW_OK;
+}
+
+int host_setup_rows(const SflowParams* p, const double* B, int k0, int rows, int own_lo, int own_hi,
+                    HostSetup& s, std::string& err) {
+  int rc = host_setup(p, B, s, err);
+  if (rc != SFLOW_OK) return rc;
+  const int nx = s.nx, ny = s.ny;
+  if (ny == 1) { err = "row slabs need comp_cells_y > 1"; return SFLOW_EINVAL; }
+  if (k0 < 0 || rows < 5 || k0 + rows > ny) { err = "row slab outside the domain (or under 5 rows)"; return SFLOW_EINVAL; }
+  if (own_lo < 0 || own_hi > rows || own_lo >= own_hi) { err = "own rows outside the slab"; return SFLOW_EINVAL; }
+  auto cut = [&](auto& v) {
+    using V = typename std::decay<decltype(v)>::type;
+    if (v.empty()) return;
+    V w(v.begin() + (size_t)k0 * nx, v.begin() + (size_t)(k0 + rows) * nx);
+    v.swap(w);
+  };
+  cut(s.Bx); cut(s.By); cut(s.Bxx); cut(s.Bxy); cut(s.Byy); cut(s.gc); cut(s.dgcx); cut(s.dgcy);
+  cut(s.cflags); cut(s.arc_perim); cut(s.arc_nx); cut(s.arc_ny); cut(s.cell_fract); cut(s.B);
+  s.ny = rows;
+  s.p.comp_cells_y = rows;   // y0 stays: coordinates count rows from the whole domain's edge
+  s.row0 = k0;
+  s.own_lo = own_lo;
+  s.own_hi = own_hi;
   return SFLOW_OK;
 }
 

@@ -541,6 +541,35 @@ class Solver : public SolverBase {
     return SFLOW_OK;
   }
 
+  // rows k_lo .. k_lo+n-1 of q in the reference layout ([row][j][var])
+  int get_rows(int k_lo, int n, double* out) override {
+    if (k_lo < 0 || n < 0 || k_lo + n > hs_.ny) { err_ = "rows outside the domain"; return SFLOW_EINVAL; }
+    const int nx = hs_.nx, nv = hs_.nv;
+    std::vector<R> buf((size_t)n * nx);
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    for (int i = 0; i < nv; ++i) {
+      SFLOW_CU(cudaMemcpy2D(buf.data(), sizeof(R) * nx, q_ + (size_t)i * plane_ + (size_t)k_lo * pitch_,
+                            sizeof(R) * pitch_, sizeof(R) * nx, n, cudaMemcpyDeviceToHost));
+      for (size_t c = 0; c < (size_t)n * nx; ++c) out[c * nv + i] = (double)buf[c];
+    }
+    return SFLOW_OK;
+  }
+  int put_rows(int k_lo, int n, const double* in) override {
+    if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
+    if (k_lo < 0 || n < 0 || k_lo + n > hs_.ny) { err_ = "rows outside the domain"; return SFLOW_EINVAL; }
+    const int nx = hs_.nx, nv = hs_.nv;
+    std::vector<R> buf((size_t)n * nx);
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    for (int i = 0; i < nv; ++i) {
+      for (size_t c = 0; c < (size_t)n * nx; ++c) buf[c] = (R)in[c * nv + i];
+      SFLOW_CU(cudaMemcpy2D(q_ + (size_t)i * plane_ + (size_t)k_lo * pitch_, sizeof(R) * pitch_, buf.data(),
+                            sizeof(R) * nx, sizeof(R) * nx, n, cudaMemcpyHostToDevice));
+    }
+    SFLOW_CU(reset_wet_flags());
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
+
   int set_output_time(double t_output) override {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
     SFLOW_CU(cudaMemcpyAsync(&st_->t_output, &t_output, sizeof(double), cudaMemcpyHostToDevice, stream_));
@@ -1159,6 +1188,10 @@ class Solver : public SolverBase {
         ka_.bc.flag[sd][i] = p.bc[sd][i].flag;
         ka_.bc.value[sd][i] = (R)p.bc[sd][i].value;
       }
+    g.k_off = hs_.row0;
+    g.own_lo = hs_.own_lo;
+    g.own_hi = hs_.own_hi;
+    g.whole = (hs_.own_lo == 0 && hs_.own_hi == hs_.ny) ? 1 : 0;
     g.dry_bc = 1;
     for (int sd = 0; sd < 4; ++sd) {
       if ((sd < 2 && hs_.nx < 2) || (sd >= 2 && hs_.ny < 2)) continue;

@@ -101,6 +101,7 @@ __global__ void k_stats_partial(KArgs<R> a, double* __restrict__ part) {
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
        c += (int64_t)gridDim.x * blockDim.x) {
     int j = (int)(c % g.nx), k = (int)(c / g.nx);
+    if (!owned_row(g, k)) continue;   // halo rows of a row slab
     int64_t d = cidx(g, j, k);
     R q[nv];
     for (int i = 0; i < nv; ++i) q[i] = a.q[i * g.plane + d];

@@ -77,6 +77,11 @@ struct Grid {
   int dry_bc;       // every boundary condition is (Neumann, 0): a dry inside keeps dry ghosts
   int lim_all;      // the limiter of every variable when they are all equal, else -1
   int pdl;          // launch the step kernels with programmatic dependent launch
+  // rows of a larger domain (row slabs): this domain's row k is row
+  // k + k_off of the whole one (coordinates); the CFL minimum, the active
+  // counts, the status bits and the log sums take only rows own_lo .. own_hi-1
+  int k_off, own_lo, own_hi;
+  int whole;        // own_lo == 0 && own_hi == ny
 };
 
 // Device-resident run state (one per domain).

@@ -83,6 +83,9 @@ def load(build_if_missing=True):
         "sflow_upload_deposit": (C.c_int, [vp, dp]),
         "sflow_upload_maps": (C.c_int, [vp, dp, dp, dp]),
         "sflow_set_output_time": (C.c_int, [vp, C.c_double]),
+        "sflow_create_rows": (C.c_int, [P, dp, i32, i32, i32, i32, C.POINTER(vp)]),
+        "sflow_get_rows": (C.c_int, [vp, i32, i32, dp]),
+        "sflow_put_rows": (C.c_int, [vp, i32, i32, dp]),
         "sflow_download_erosion": (C.c_int, [vp, dp]),
         "sflow_download_erodible": (C.c_int, [vp, dp]),
         "sflow_set_erodible": (C.c_int, [vp, dp]),
@@ -150,7 +153,8 @@ def exported_symbols():
             "sflow_batch_launch", "sflow_batch_wait", "sflow_batch_dry_border_updates",
             "sflow_dry_border_updates", "sflow_download_erosion", "sflow_download_erodible",
             "sflow_set_erodible", "sflow_download_topography", "sflow_set_nodata",
-            "sflow_vuln_table_size", "sflow_download_vuln_table", "sflow_batch_set_memory_limit"]
+            "sflow_vuln_table_size", "sflow_download_vuln_table", "sflow_batch_set_memory_limit",
+            "sflow_create_rows", "sflow_get_rows", "sflow_put_rows"]
 
 
 TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
@@ -323,7 +327,10 @@ class Solver:
     """One domain on the GPU.  Method names follow the reference driver's
     call sites (src/IMEX_SfloW2D.f90:395-505)."""
 
-    def __init__(self, params, B_cent):
+    def __init__(self, params, B_cent, rows=None):
+        """rows = (k0, n, own_lo, own_hi): a row slab of the domain (rows
+        k0 .. k0+n-1, own rows own_lo .. own_hi-1 local), see
+        sflow_create_rows; B_cent is then the whole domain's."""
         self.lib = load()
         self.p = params.copy()
         self.nx, self.ny = params.comp_cells_x, params.comp_cells_y
@@ -332,8 +339,26 @@ class Solver:
         if B.size != self.nx * self.ny:
             raise ValueError("B_cent must have nx*ny values")
         h = C.c_void_p()
-        _check(self.lib.sflow_create(C.byref(self.p), _dp(B), C.byref(h)))
+        if rows is None:
+            _check(self.lib.sflow_create(C.byref(self.p), _dp(B), C.byref(h)))
+        else:
+            k0, n, lo, hi = (int(x) for x in rows)
+            _check(self.lib.sflow_create_rows(C.byref(self.p), _dp(B), k0, n, lo, hi, C.byref(h)))
+            self.ny = n
+            self.p.comp_cells_y = n
         self.h = h
+
+    def get_rows(self, k_lo, n):
+        """Rows k_lo .. k_lo+n-1 of q (local rows), reference layout."""
+        out = np.empty(n * self.nx * self.nv)
+        _check(self.lib.sflow_get_rows(self.h, int(k_lo), int(n), _dp(out)))
+        return out
+
+    def put_rows(self, k_lo, n, q_rows):
+        q = np.ascontiguousarray(q_rows, dtype=np.float64).reshape(-1)
+        if q.size != n * self.nx * self.nv:
+            raise ValueError("q_rows must have n*nx*n_vars values")
+        _check(self.lib.sflow_put_rows(self.h, int(k_lo), int(n), _dp(q)))
 
     def close(self):
         if getattr(self, "h", None):

@@ -553,6 +553,29 @@ int sflow_set_nodata(sflow_handle* h, const uint8_t* nodata);
 int sflow_vuln_table_size(sflow_handle* h, int32_t* n_thk, int32_t* n_dyn);
 int sflow_download_vuln_table(sflow_handle* h, uint8_t* out);
 
+/*
+ * Row slabs of one domain (domain decomposition by rows).  A slab handle
+ * holds rows k0 .. k0+rows-1 of the whole domain described by p and B_cent
+ * (the whole DEM: topography terms, inlet geometry and flags are derived on
+ * the whole domain, then cut), of which the local rows own_lo .. own_hi-1
+ * are its own: only they enter its CFL minimum (sflow_timestep), its
+ * active-cell counts, status bits and log sums.  The other rows are halo:
+ * they are computed from the slab's data alone (artificial edges take the
+ * domain's boundary conditions) and must be refreshed from the neighbours
+ * before each step.  With N_RK = 2 one refresh per step suffices: the flux
+ * pass runs once, at the step's start, and reads q up to 2 cells away, and
+ * the active mask of those cells reads q up to 2 further; a halo of 4 rows
+ * each side gives every own cell the whole domain's update (bitwise), with
+ * dt = the minimum over the slabs of sflow_timestep and the driver's clamps
+ * applied on the host, through the per-call entry points.
+ *   sflow_get_rows / sflow_put_rows  rows k_lo .. k_lo+n-1 of q (local),
+ *                                    reference layout, for the exchange
+ */
+int sflow_create_rows(const SflowParams* p, const double* B_cent, int32_t k0, int32_t rows, int32_t own_lo,
+                      int32_t own_hi, sflow_handle** out);
+int sflow_get_rows(sflow_handle* h, int32_t k_lo, int32_t n, double* out);
+int sflow_put_rows(sflow_handle* h, int32_t k_lo, int32_t n, const double* in);
+
 /* Build information ("fp64+fp32 sm_103a ..."). */
 const char* sflow_build_info(void);
 
