@@ -299,6 +299,7 @@ void sflow_default_params(SflowParams* p) {
   p->erodible_porosity = p->T_erodible = p->initial_erodible_thickness = -1.0;
   for (int i = 0; i < SFLOW_MAX_SOLID; ++i) p->erodible_fract[i] = -1.0;
   for (int i = 0; i < SFLOW_MAX_INTERVALS; ++i) p->t_intervals[i] = p->vel_intervals[i] = -1.0;
+  p->mu_s = p->mu_2 = p->I_0 = p->muI_inf = -1.0;
 }
 
 static int create_from(const SflowParams* p, HostSetup& s, sflow_handle** out);

@@ -432,9 +432,9 @@ static const Key kKeys[] = {
     XK("RHEOLOGY_PARAMETERS", "KAPPA", K_ACCEPT), XK("RHEOLOGY_PARAMETERS", "N_TD", K_ACCEPT),
     XK("RHEOLOGY_PARAMETERS", "TAU0", K_ACCEPT), XK("RHEOLOGY_PARAMETERS", "MU_0", K_ACCEPT),
     XK("RHEOLOGY_PARAMETERS", "MU_INF", K_ACCEPT), XK("RHEOLOGY_PARAMETERS", "FR_0", K_ACCEPT),
-    XK("RHEOLOGY_PARAMETERS", "U_W", K_ACCEPT), XK("RHEOLOGY_PARAMETERS", "MU_S", K_ACCEPT),
-    XK("RHEOLOGY_PARAMETERS", "MU_2", K_ACCEPT), XK("RHEOLOGY_PARAMETERS", "I_0", K_ACCEPT),
-    XK("RHEOLOGY_PARAMETERS", "MUI_INF", K_ACCEPT),
+    XK("RHEOLOGY_PARAMETERS", "U_W", K_ACCEPT), PK("RHEOLOGY_PARAMETERS", "MU_S", K_REAL, mu_s),
+    PK("RHEOLOGY_PARAMETERS", "MU_2", K_REAL, mu_2), PK("RHEOLOGY_PARAMETERS", "I_0", K_REAL, I_0),
+    PK("RHEOLOGY_PARAMETERS", "MUI_INF", K_REAL, muI_inf),
     // SOLID_TRANSPORT_PARAMETERS (inpout_2d.f90:1033-1037)
     PA("SOLID_TRANSPORT_PARAMETERS", "RHO_S", K_RARR, rho_s, SFLOW_MAX_SOLID),
     PA("SOLID_TRANSPORT_PARAMETERS", "DIAM_S", K_RARR, diam_s, SFLOW_MAX_SOLID),

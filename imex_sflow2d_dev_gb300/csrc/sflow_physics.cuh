@@ -511,7 +511,8 @@ __device__ __forceinline__ double source_time_coeff(const double* tp, double pi_
 }
 
 // ---------------------------------------------------------------------------
-// constitutive_2d.f90:4027-4547 eval_nh_semi_impl_terms (rheology 1); FP64
+// constitutive_2d.f90:4027-4547 eval_nh_semi_impl_terms: the Coulomb term of
+// rheology 1 and the mu(I) rheology 11 (4384-4458)
 // ---------------------------------------------------------------------------
 template <class R, int NS>
 __device__ __forceinline__ void semi_impl_terms(const Phys<R>& P, const Geo<R>& g, const R* qpj,
@@ -529,6 +530,41 @@ __device__ __forceinline__ void semi_impl_terms(const Phys<R>& P, const Geo<R>& 
     tt = rmax(R(0), tt);
     si[1] = si[1] - tt * r_u / mod_vel;
     si[2] = si[2] - tt * r_v / mod_vel;
+  } else if (P.rheo_model == 11 && mod_vel > R(0)) {
+    // grain diameter and density: Sauter mean and volume-weighted mean
+    // (sauter_diameter, average_density_solids, constitutive_2d.f90:387-416)
+    constexpr int ns = NS;
+    R diam, rho_p;
+    if (ns > 1) {
+      R al[kMaxSolid], sa = R(0);
+      for (int i = 0; i < ns; ++i) { al[i] = P.alpha ? qpj[4 + i] : qpj[4 + i] / qpj[0]; sa += al[i]; }
+      if (sa < P.thr_eps) {
+        R sd = R(0), sr = R(0);
+        for (int i = 0; i < ns; ++i) { sd += P.diam_s[i]; sr += P.rho_s[i]; }
+        diam = sd / R(ns);
+        rho_p = sr / R(ns);
+      } else {
+        R sdi = R(0), sar = R(0);
+        for (int i = 0; i < ns; ++i) { sdi += al[i] / P.diam_s[i]; sar += al[i] * P.rho_s[i]; }
+        diam = sa / sdi;
+        rho_p = sar / sa;
+      }
+    } else {
+      diam = P.diam_s[0];
+      rho_p = P.rho_s[0];
+    }
+    const R hh = (r_h < P.thr_eps) ? P.thr_eps : r_h;   // EPSILON(1.0_wp), exact in both forms
+    R centr = P.curv ? (g.Bxx * sq(r_u) + cst<R>(2.0) * g.Bxy * r_u * r_v + g.Byy * sq(r_v)) : R(0);
+    R vert = m.rho_m * (m.red_grav + centr) * hh;
+    vert = rmax(vert, R(0));
+    R eff = rmax(R(0), vert * sqrt(g.gc));
+    if (eff < P.thr_eps) eff = P.thr_eps;
+    const R shear = cst<R>(2.5) * mod_vel / (hh * sqrt(g.gc));
+    const R I = diam * shear / sqrt(eff / rho_p);
+    const R mu_I = (P.mu_s * P.I_0 + P.mu_2 * I + P.muI_inf * (I * I)) / (P.I_0 + I);
+    const R tt = mu_I * eff;
+    si[1] = si[1] - tt * (r_u / mod_vel);
+    si[2] = si[2] - tt * (r_v / mod_vel);
   }
 }
 
@@ -1047,7 +1083,7 @@ __device__ __forceinline__ float reduced_friction_solve(const Phys<float>& P, co
   const float iS = 1.0f / S;
   e1 = q[1] * iS;
   e2 = q[2] * iS;
-  if (!P.rheo || !(q[0] > P.thr_eps)) return S;
+  if (!P.rheo || P.rheo_model == 11 || !(q[0] > P.thr_eps)) return S;   // model 11: no implicit friction
   const float q1 = q[0], inv_q1 = 1.0f / q1;
   float xs_tot = 0.0f, dcp = 0.0f, dinv = 0.0f;
 #pragma unroll

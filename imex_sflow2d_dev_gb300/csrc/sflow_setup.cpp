@@ -317,7 +317,16 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   if (p.n_rk < 1 || p.n_rk > 4) { err = "N_RK must be 1, 2, 3 or 4"; return SFLOW_EINVAL; }
   if (p.gas_flag && p.liquid_flag) { err = "gas carrier with a liquid phase is not supported"; return SFLOW_EINVAL; }
   if (!p.gas_flag && !p.liquid_flag) { err = "one of gas_flag / liquid_flag must be set"; return SFLOW_EINVAL; }
-  if (p.rheology_flag && p.rheology_model != 1 && p.rheology_model != 6) { err = "rheology_model must be 1 or 6"; return SFLOW_EINVAL; }
+  if (p.rheology_flag && p.rheology_model != 1 && p.rheology_model != 6 && p.rheology_model != 11) {
+    err = "rheology_model must be 1, 6 or 11";
+    return SFLOW_EINVAL;
+  }
+  if (p.rheology_flag && p.rheology_model == 11 &&
+      (p.mu_s < 0.0 || p.mu_2 < 0.0 || p.I_0 < 0.0 || p.muI_inf < 0.0)) {
+    // inpout_2d.f90:3592-3611
+    err = "rheology_model 11 needs mu_s, mu_2, I_0 and muI_inf >= 0";
+    return SFLOW_EINVAL;
+  }
   if (p.erosion_coeff < 0.0) { err = "erosion_coeff must be >= 0"; return SFLOW_EINVAL; }
   if (p.solver_scheme != SFLOW_SCHEME_KT && p.solver_scheme != SFLOW_SCHEME_UP) {
     err = "SOLVER_SCHEME must be KT or UP";

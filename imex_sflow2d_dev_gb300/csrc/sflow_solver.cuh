@@ -1125,6 +1125,7 @@ class Solver : public SolverBase {
     P.cell_area = (T)(hs_.dx * hs_.dy);
     P.src_rho_m = (T)hs_.src_rho_m; P.src_cp_mix = (T)hs_.src_cp_mix;
     P.mu = (T)p.mu; P.xi = (T)p.xi; P.friction_factor = (T)p.friction_factor;
+    P.mu_s = (T)p.mu_s; P.mu_2 = (T)p.mu_2; P.I_0 = (T)p.I_0; P.muI_inf = (T)p.muI_inf;
     P.kin_visc_c = (T)hs_.kin_visc_c; P.loss_rate = (T)p.loss_rate;
     P.alphastot_min = (T)p.alphastot_min; P.max_packing = (T)p.maximum_solid_packing;
     P.A_drag = (T)p.A_drag; P.B_drag = (T)p.B_drag;

@@ -30,6 +30,7 @@ struct Phys {
   R src_rho_m, src_cp_mix;    // mixt_var of the inlet state (constant per run)
   // FP64-only physics (semi-implicit, Newton, mass exchange)
   R mu, xi, friction_factor, kin_visc_c, loss_rate;
+  R mu_s, mu_2, I_0, muI_inf;   // mu(I) rheology (model 11)
   R diam_s[kMaxSolid];
   R alphastot_min, max_packing, A_drag, B_drag, coeff_porosity, rho_c_sub, T_erodible,
       erodible_porosity;

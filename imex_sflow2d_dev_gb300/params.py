@@ -85,6 +85,7 @@ class SflowParams(C.Structure):
         ("angle_source", C.c_double),
         ("t_intervals", C.c_double * MAX_INTERVALS), ("vel_intervals", C.c_double * MAX_INTERVALS),
         ("fp32_newton_fp64", C.c_int32), ("pad2", C.c_int32),
+        ("mu_s", C.c_double), ("mu_2", C.c_double), ("I_0", C.c_double), ("muI_inf", C.c_double),
     ]
 
     @property

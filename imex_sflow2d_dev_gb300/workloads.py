@@ -352,6 +352,40 @@ def eroding_dam_break(nx=120, ny=60, dx=2.0, precision=PREC_FP64, t_end=12.0, de
     return p, B, q
 
 
+def granular_slide(nx=120, ny=64, dx=2.0, precision=PREC_FP64, t_end=20.0, n_solid=1):
+    """A dense granular column (solid fraction 0.5, 1 mm grains) released
+    on a 35-degree slope into a run-out flat, with the mu(I) rheology 11
+    (mu_s 0.48, mu_2 0.73, I_0 0.279, muI_inf 0.005) and slope correction;
+    air carrier at ambient temperature."""
+    p = default_params()
+    p.precision = precision
+    p.comp_cells_x, p.comp_cells_y, p.cell_size = nx, ny, dx
+    p.x0 = p.y0 = 0.0
+    p.n_solid = n_solid
+    p.gas_flag, p.liquid_flag, p.energy_flag = 1, 0, 1
+    p.rheology_flag, p.rheology_model = 1, 11
+    p.mu_s, p.mu_2, p.I_0, p.muI_inf = 0.48, 0.73, 0.279, 0.005
+    p.slope_correction_flag = 1
+    _gas_common(p)
+    for i, (rho, d) in enumerate([(2500.0, 1.0e-3), (1800.0, 4.0e-3), (2700.0, 5.0e-4)][:n_solid]):
+        p.rho_s[i], p.diam_s[i], p.sp_heat_s[i] = rho, d, 1100.0
+    p.n_rk = 2
+    p.cfl, p.dt0, p.max_dt = 0.24, 1.0e-3, 1.0
+    p.set_bc_all(1, 0.0)
+    p.t_start, p.t_end = 0.0, t_end
+    p.dt_output = 2.0 * (p.t_end - p.t_start)
+    x = (np.arange(nx) + 0.5) * dx
+    y = (np.arange(ny) + 0.5) * dx
+    xb = 0.6 * nx * dx
+    z = np.where(x < xb, np.tan(np.radians(35.0)) * (xb - x), 0.0)
+    B = np.broadcast_to(z[None, :], (ny, nx)).copy()
+    r2 = (x[None, :] - 0.15 * nx * dx) ** 2 + (y[:, None] - 0.5 * ny * dx) ** 2
+    h = np.where(r2 <= (0.2 * ny * dx) ** 2, 2.0, 0.0)
+    alphas = [0.5 / n_solid] * n_solid
+    q = rest_state_q(p, h, 300.0, alphas)
+    return p, B, q
+
+
 def developed_current_state(p, B, radius=3500.0, h_max=3.0, u_max=15.0, T=950.0, seed=11):
     """A spread gas-particle current over the cone, as a seeded stand-in for
     the state of the pyroclastic run a few minutes after the inlet opened:

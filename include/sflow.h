@@ -178,6 +178,10 @@ typedef struct {
    * one FP64 Newton step */
   int32_t fp32_newton_fp64;
   int32_t pad2;
+  /* RHEOLOGY_PARAMETERS of the mu(I) rheology (rheology_model = 11,
+   * constitutive_2d.f90:4384-4458): static and high-I friction, reference
+   * inertial number, high-I regularisation; -1 = not given */
+  double mu_s, mu_2, I_0, muI_inf;
 } SflowParams;
 
 /* Fill p with the defaults of init_param (src/inpout_2d.f90:408-985). */

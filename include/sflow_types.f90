@@ -104,6 +104,10 @@ MODULE sflow_types
      REAL(C_DOUBLE) :: vel_intervals(SFLOW_MAX_INTERVALS)
      INTEGER(C_INT32_T) :: fp32_newton_fp64
      INTEGER(C_INT32_T) :: pad2
+     REAL(C_DOUBLE) :: mu_s
+     REAL(C_DOUBLE) :: mu_2
+     REAL(C_DOUBLE) :: I_0
+     REAL(C_DOUBLE) :: muI_inf
   END TYPE sflow_params
 
   TYPE, BIND(C) :: sflow_step_stats

@@ -114,6 +114,7 @@ typedef struct {
   int gas, liquid, energy, alpha, rheo, rheo_model, slope_corr, curv;
   int settling, entrain, collective, radial_source, scheme;
   double grav, mu, xi, friction_factor;
+  double mu_s, mu_2, I_0, muI_inf; /* mu(I) rheology 11 */
   double pres, inv_pres, sp_heat_a, sp_gas_const_a, T_ambient, rho_a_amb;
   double kin_visc_c;
   double rho_l, inv_rho_l, sp_heat_l, loss_rate;
@@ -537,6 +538,41 @@ static void semi_impl_terms(const phys_t* P, double Bx, double By, double Bxx, d
       tt = dmax(0.0, tt);
       si[1] = si[1] - tt * r_u / mod_vel;
       si[2] = si[2] - tt * r_v / mod_vel;
+    }
+  } else if (P->rheo_model == 11) {
+    /* constitutive_2d.f90:4384-4458, mu(I) rheology */
+    if (mod_vel > 0.0) {
+      const int ns = P->ns;
+      double diam, rho_p;
+      if (ns > 1) {
+        double al[MAXS];
+        for (int i = 0; i < ns; ++i) al[i] = P->alpha ? qpj[4 + i] : qpj[4 + i] / qpj[0];
+        /* sauter_diameter, average_density_solids (constitutive_2d.f90:387-416) */
+        if (sumv(al, ns) < EPS) {
+          diam = sumv(P->diam_s, ns) / ns;
+          rho_p = sumv(P->rho_s, ns) / ns;
+        } else {
+          double q[MAXS], r[MAXS];
+          for (int i = 0; i < ns; ++i) { q[i] = al[i] / P->diam_s[i]; r[i] = al[i] * P->rho_s[i]; }
+          diam = sumv(al, ns) / sumv(q, ns);
+          rho_p = sumv(r, ns) / sumv(al, ns);
+        }
+      } else {
+        diam = P->diam_s[0];
+        rho_p = P->rho_s[0];
+      }
+      if (r_h < EPS) r_h = EPS;
+      double centr = P->curv ? (Bxx * sq(r_u) + 2.0 * Bxy * r_u * r_v + Byy * sq(r_v)) : 0.0;
+      double vert = m.rho_m * (m.red_grav + centr) * r_h;
+      vert = dmax(vert, 0.0);
+      double eff = dmax(0.0, vert * sqrt(gc));
+      if (eff < EPS) eff = EPS;
+      double shear = 5.0 / 2.0 * mod_vel / (r_h * sqrt(gc));
+      double I = diam * shear / sqrt(eff / rho_p);
+      double mu_I = (P->mu_s * P->I_0 + P->mu_2 * I + P->muI_inf * (I * I)) / (P->I_0 + I);
+      double tt = mu_I * eff;
+      si[1] = si[1] - tt * (r_u / mod_vel);
+      si[2] = si[2] - tt * (r_v / mod_vel);
     }
   }
 }
@@ -2087,6 +2123,7 @@ static int setup_phys(oracle_t* o, const SflowParams* p) {
   P->collective = p->collective_settling_flag; P->radial_source = p->radial_source_flag;
   P->scheme = p->solver_scheme;
   P->grav = p->grav; P->mu = p->mu; P->xi = p->xi; P->friction_factor = p->friction_factor;
+  P->mu_s = p->mu_s; P->mu_2 = p->mu_2; P->I_0 = p->I_0; P->muI_inf = p->muI_inf;
   P->pres = p->pres; P->inv_pres = 1.0 / p->pres;
   P->sp_heat_a = p->sp_heat_a; P->sp_gas_const_a = p->sp_gas_const_a; P->T_ambient = p->T_ambient;
   P->rho_a_amb = p->pres / (p->sp_gas_const_a * p->T_ambient);

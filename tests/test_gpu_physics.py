@@ -1,5 +1,5 @@
-"""Erosion with topography change, the bottom radial source, B_nodata cells
-and the vulnerability table on the GPU against the oracle (the C
+"""Erosion with topography change, the bottom radial source, B_nodata cells,
+the vulnerability table and the mu(I) rheology on the GPU against the oracle (the C
 restatement of the reference time step), through the C ABI.
 
 Tolerances, written in each test:
@@ -151,3 +151,16 @@ def test_batch_rejects_single_run_physics():
                 b.submit(p, B, W.to_aos(q), max_steps=10)
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("n_solid", [1, 3])
+def test_mu_i_rheology_fp64_matches_oracle(n_solid):
+    p, B, q = W.granular_slide(n_solid=n_solid)
+    o, g = _compare_fp64(p, B, q, steps=300)
+    qo = W.from_aos(o["q"], p.n_vars, p.comp_cells_x, p.comp_cells_y)
+    assert np.abs(qo[1]).max() > 0.0   # it slides
+
+
+def test_mu_i_rheology_fp32_error_against_oracle():
+    p, B, q = W.granular_slide()
+    _compare_fp32(p, B, q, steps=300)
