@@ -42,7 +42,9 @@ def main():
         ids = [b.submit(p, B, W.to_aos(q), max_steps=st) for p, B, q, st in members]
         b.advance(a.steps)
         cu = sum(b.counters(i)["cell_updates"] for i in ids)
-        print(f"ensemble runs={a.ensemble} cells={cells} steps={a.steps} cell_updates={cu}")
+        border = sum(b.dry_border_updates(i) for i in ids)
+        print(f"ensemble runs={a.ensemble} cells={cells} steps={a.steps} cell_updates={cu} "
+              f"dry_border_updates={border} computed_cell_updates={cu - border}")
         b.close()
         return
     prec = PREC_FP32 if a.precision == "fp32" else PREC_FP64
