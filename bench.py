@@ -778,7 +778,7 @@ def run_gb300(args, d):
                  "mask": 4 + 1 + 1, "cand": 0, "dt": 0}
     launch_s = kms[dom] / 1e3 / 16
     achieved = alg_bytes[dom] * computed_launch / launch_s / 1e9
-    prof = read_profile("k_b_flux_ensemble_256") if dom == "flux" else None
+    prof = read_profile("k_b_flux_ensemble_64") if dom == "flux" else None
     traffic = (prof["dram_bytes_per_computed_cell"] * computed_launch
                if prof and prof.get("dram_bytes_per_computed_cell") else None)
     roofline = {"bound": "hbm", "kernel": "k_b_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -788,6 +788,9 @@ def run_gb300(args, d):
                 "kernel_ms_per_step": {k: v / 16 for k, v in kms.items()},
                 "kernel_share": {k: v / sum(kms.values()) for k, v in kms.items()},
                 "profile_window": f"16 batch steps from step {ENS_STEPS // 2}, events between kernels"}
+    if prof:
+        roofline["traffic_source"] = (f"profiles/k_b_flux_ensemble_64.json: ncu DRAM bytes per computed cell "
+                                      f"({prof['tile']} tiles) x computed cells of this launch")
     if prof and prof.get("warp_inst_per_computed_cell") and prof.get("issue_peak_warp_inst_per_s"):
         roofline["issue_frac"] = (prof["warp_inst_per_computed_cell"] * computed_launch / launch_s
                                   / prof["issue_peak_warp_inst_per_s"])
@@ -866,7 +869,7 @@ def main():
     ap.add_argument("--large-steps", type=int, default=10)
     ap.add_argument("--tune-steps", type=int, default=64,
                     help="steps per tile height of the autotuners (0: default 32x8 tiles)")
-    ap.add_argument("--tile-h", type=int, default=0, choices=[0, 8, 16],
+    ap.add_argument("--tile-h", type=int, default=0, choices=[0, 8, 16, 4],
                     help="FP32 tile height of the ensemble without the autotuner (0: autotune)")
     args = ap.parse_args()
     if args.warmup < 3:

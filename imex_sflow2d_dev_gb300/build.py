@@ -27,12 +27,15 @@ UNITS = [
     ("sflow_k_fp64_ns2.cu", FP64),
     ("sflow_k_fp32_ns2.cu", FP32),
     ("sflow_k_fp32_ns2_t16.cu", FP32),
+    ("sflow_k_fp32_ns2_t4.cu", FP32),
     ("sflow_k_fp64_ns3.cu", FP64),
     ("sflow_k_fp32_ns3.cu", FP32),
     ("sflow_k_fp32_ns3_t16.cu", FP32),
+    ("sflow_k_fp32_ns3_t4.cu", FP32),
     ("sflow_k_fp64_ns1.cu", FP64),
     ("sflow_k_fp32_ns1.cu", FP32),
     ("sflow_k_fp32_ns1_t16.cu", FP32),
+    ("sflow_k_fp32_ns1_t4.cu", FP32),
     ("sflow_noalloc.cu", FP64),
     ("sflow_fp64.cu", FP64),
     ("sflow_fp32.cu", FP32),

@@ -38,7 +38,7 @@
 // so a slot can be reused at once after its run is collected.
 //
 // The per-cell arithmetic is the single-run code (mask_tile, flux_tile,
-// stage2_tile) on the run's own arguments, so a run gives bit-identical
+// stage2_cell) on the run's own arguments, so a run gives bit-identical
 // results alone, with the single-run solver, and in any mix.
 #pragma once
 #include <cuda_runtime.h>

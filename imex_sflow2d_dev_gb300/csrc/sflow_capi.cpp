@@ -250,9 +250,10 @@ int sflow_eval_math(int32_t which, int64_t n, const double* x, const double* y, 
 int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count) {
   if (!count) return fail(SFLOW_EINVAL, "count is NULL");
   if (precision != SFLOW_PREC_FP32 && precision != SFLOW_PREC_FP64) return fail(SFLOW_EINVAL, "unknown precision");
-  const int32_t fp32[2] = {8, 16}, fp64[1] = {8};
+  // the compiled heights, in the autotuner's candidate order
+  const int32_t fp32[3] = {8, 16, 4}, fp64[1] = {8};
   const int32_t* v = (precision == SFLOW_PREC_FP32) ? fp32 : fp64;
-  const int32_t n = (precision == SFLOW_PREC_FP32) ? 2 : 1;
+  const int32_t n = (precision == SFLOW_PREC_FP32) ? 3 : 1;
   for (int32_t i = 0; i < n && i < capacity && heights; ++i) heights[i] = v[i];
   *count = n;
   return SFLOW_OK;

@@ -1700,40 +1700,6 @@ __device__ __forceinline__ int stage2_cell(const KArgs<R>& a, int mode, int j, i
 // neighbours across those edges can gain active cells.  0xff: unknown.
 constexpr uint8_t TW_ANY = 1, TW_W = 2, TW_E = 4, TW_S = 8, TW_N = 16;
 
-// A whole 32 x TH tile with 32 x 8 threads, 8 rows at a time (batched
-// runs), then the tile's wet byte for the candidate rule (mode -1).
-template <class R, int NS, int TH>
-__device__ __forceinline__ void stage2_tile(const KArgs<R>& a, int mode, int tx, int ty) {
-  static_assert(TH % 8 == 0, "stage tiles are processed 8 rows at a time");
-  __shared__ unsigned s_bits[8];
-  unsigned status = 0;
-  int nit_sum = 0, nit_max = 0;
-  unsigned bits = 0;
-  const int lane = threadIdx.x % TX;
-#pragma unroll 1
-  for (int r0 = 0; r0 < TH; r0 += 8) {
-    int nit = 0;
-    const int row = r0 + threadIdx.x / TX;
-    const int wet = stage2_cell<R, NS>(a, mode, tx * TX + lane, ty * TH + row, status, nit);
-    if (wet)
-      bits |= TW_ANY | (lane < 2 ? TW_W : 0u) | (lane >= TX - 2 ? TW_E : 0u) | (row < 2 ? TW_S : 0u) |
-              (row >= TH - 2 ? TW_N : 0u);
-    nit_sum += nit;
-    nit_max = max(nit_max, nit);
-  }
-  newton_stats<R>(a.st, status, nit_sum, nit_max);
-  if (mode < 0) {
-    bits = __reduce_or_sync(0xffffffffu, bits);
-    if (lane == 0) s_bits[threadIdx.x / TX] = bits;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned b = 0;
-      for (int w = 0; w < 8; ++w) b |= s_bits[w];
-      a.tile_wet[ty * a.g.tiles_x + tx] = (uint8_t)b;
-    }
-  }
-}
-
 // single run: one block per 32 x 8 cells (grid tiles_x x ceil(ny/8)); the
 // activity byte is the one of the 32 x TH tile holding the block.  The FP32
 // form is compiled for 6 resident blocks per SM (40 registers): the kernel
@@ -1743,22 +1709,33 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS, sizeof(R) == 4 ?
     k_stage2(KArgs<R> a, int mode) {
   step_kernel_entry();
   if (!a.st->run_step) return;
-  const int tile = (blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x;
-  const uint8_t ta = a.tile_active[tile];
-  if (ta == 0 || ta == 2 || ta == TILE_DRY_BORDER) return;   // inactive, or left unchanged (k_flux, k_mask)
+  const int kk = blockIdx.y * 8 + threadIdx.x / TX;
+  // inactive, or left unchanged (k_flux's dry tiles, k_mask's dry border)
+  auto skipped = [](uint8_t ta) { return ta == 0 || ta == 2 || ta == TILE_DRY_BORDER; };
+  int tile;
+  bool run = true;
+  if constexpr (TH >= 8) {
+    tile = (blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x;
+    if (skipped(a.tile_active[tile])) return;
+  } else {
+    // 32 x 4 tiles: the block's two halves belong to two tiles
+    tile = (kk / TH) * gridDim.x + blockIdx.x;
+    run = kk < a.g.ny && !skipped(a.tile_active[tile]);
+  }
   unsigned status = 0;
   int nit = 0;
-  const int kk = blockIdx.y * 8 + threadIdx.x / TX;
-  int wet = stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, kk, status, nit);
+  int wet = run ? stage2_cell<R, NS>(a, mode, blockIdx.x * TX + threadIdx.x % TX, kk, status, nit) : 0;
   if (!owned_row(a.g, kk)) { status = 0u; nit = 0; }   // halo rows of a row slab
   newton_stats<R>(a.st, status, nit, nit);
   if (mode < 0) {
     // wet flag of the tile for the next check_solve (buffer of the new
     // step count's parity; set only, the check_solve of this step cleared it)
-    wet = __syncthreads_or(wet);
-    if (wet && threadIdx.x == 0) {
-      const int nt = gridDim.x * a.g.tiles_y;
-      a.tile_wet_step[(unsigned)(a.st->steps & 1) * nt + tile] = 1;
+    const int nt = gridDim.x * a.g.tiles_y;
+    if constexpr (TH >= 8) {
+      wet = __syncthreads_or(wet);
+      if (wet && threadIdx.x == 0) a.tile_wet_step[(unsigned)(a.st->steps & 1) * nt + tile] = 1;
+    } else {
+      if (wet) a.tile_wet_step[(unsigned)(a.st->steps & 1) * nt + tile] = 1;
     }
   }
 }
@@ -1775,13 +1752,15 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_stage(KArgs<R>
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
   if (!st->run_step) return;
-  if (!a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x]) return;
+  if constexpr (TH >= 8) {
+    if (!a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x]) return;
+  }
   const Grid<R>& g = a.g;
   const int j = blockIdx.x * TX + threadIdx.x % TX;
   const int k = blockIdx.y * 8 + threadIdx.x / TX;
   unsigned status = 0;
   int nit = 0;
-  if (j < g.nx && k < g.ny) {
+  if (j < g.nx && k < g.ny && (TH >= 8 || a.tile_active[(k / TH) * gridDim.x + blockIdx.x])) {
     const int64_t c = cidx(g, j, k);
     if (a.mask[c]) {
       const double dt = st->dt;
@@ -1821,12 +1800,14 @@ __global__ void __launch_bounds__(TileShape<TH>::STAGE_THREADS) k_assemble(KArgs
   constexpr int nv = 4 + NS;
   RunState* st = a.st;
   if (!st->run_step) return;
-  if (!a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x]) return;
+  if constexpr (TH >= 8) {
+    if (!a.tile_active[(blockIdx.y * 8 / TH) * gridDim.x + blockIdx.x]) return;
+  }
   const Grid<R>& g = a.g;
   const int j = blockIdx.x * TX + threadIdx.x % TX;
   const int k = blockIdx.y * 8 + threadIdx.x / TX;
   unsigned status = 0;
-  if (j < g.nx && k < g.ny) {
+  if (j < g.nx && k < g.ny && (TH >= 8 || a.tile_active[(k / TH) * gridDim.x + blockIdx.x])) {
     const int64_t c = cidx(g, j, k);
     if (a.mask[c]) {
       const double dt = st->dt;

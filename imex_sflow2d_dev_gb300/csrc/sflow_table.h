@@ -52,13 +52,13 @@ void fill_tile_entries(KernelTable<R>& t);
 constexpr int kMinSolidBuilt = 1;
 constexpr int kMaxSolidBuilt = 3;
 
-// tile heights the autotuner tries, and those with compiled kernels: 8 and
-// 16 for the FP32 bulk form, 8 for the FP64 plain form
-constexpr int kTileCandidates = 2;
-constexpr int kTileCandidate[kTileCandidates] = {8, 16};
+// tile heights the autotuner tries, and those with compiled kernels: 8, 16
+// and 4 for the FP32 bulk form, 8 for the FP64 plain form
+constexpr int kTileCandidates = 3;
+constexpr int kTileCandidate[kTileCandidates] = {8, 16, 4};
 template <class R>
 inline bool tile_h_built(int th) {
-  return th == 8 || (std::is_same<R, float>::value && th == 16);
+  return th == 8 || (std::is_same<R, float>::value && (th == 16 || th == 4));
 }
 
 template <class R, int NS>
@@ -66,6 +66,7 @@ inline void fill_tiles(KernelTable<R>& t, int th) {
   if (th == 8) fill_tile_entries<R, NS, 8>(t);
   if constexpr (std::is_same<R, float>::value) {
     if (th == 16) fill_tile_entries<R, NS, 16>(t);
+    if (th == 4) fill_tile_entries<R, NS, 4>(t);
   }
 }
 

@@ -157,7 +157,7 @@ def exported_symbols():
             "sflow_create_rows", "sflow_get_rows", "sflow_put_rows"]
 
 
-TILE_CANDIDATES = (8, 16)   # the candidate order of sflow_autotune
+TILE_CANDIDATES = (8, 16, 4)   # the candidate order of sflow_autotune
 
 
 def check_conversions(n=1 << 22, seed=12345):

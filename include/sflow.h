@@ -285,7 +285,7 @@ int64_t sflow_device_bytes(const sflow_handle* h);
  * run over cells: the tiling is how this library maps the step onto the
  * GPU).  The tiled kernels work on tiles of 32 x tile_h cells; the results
  * of a step are the same for every tile height.  Heights with compiled
- * kernels: 8 and 16 in the FP32 bulk form, 8 in the FP64 plain form
+ * kernels: 8, 16 and 4 in the FP32 bulk form, 8 in the FP64 plain form
  * (sflow_tile_shapes lists them; the default is 8).
  *
  * sflow_set_tile_shape  switch a run between steps (SFLOW_EINVAL for a
@@ -295,7 +295,7 @@ int64_t sflow_device_bytes(const sflow_handle* h);
  *                       height, times them with CUDA events, keeps the
  *                       fastest per active-cell update and returns it in
  *                       *best; ms_per_mcu[i] (n entries, candidates in the
- *                       order of sflow_tile_shapes' full list 8, 16) gets
+ *                       order of sflow_tile_shapes' full list 8, 16, 4) gets
  *                       the ms per 10^6 cell updates, -1 where not
  *                       compiled or nothing ran.  The steps advance the run.
  * sflow_batch_set_tile_shape  height of the batch's runs; only while the
@@ -313,7 +313,7 @@ int sflow_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
  * arguments (y only for pow).  For tests of those functions. */
 int sflow_eval_math(int32_t which, int64_t n, const double* x, const double* y, double* out);
 
-#define SFLOW_TILE_CANDIDATES 2
+#define SFLOW_TILE_CANDIDATES 3
 int sflow_tile_shapes(int32_t precision, int32_t* heights, int32_t capacity, int32_t* count);
 int sflow_set_tile_shape(sflow_handle* h, int32_t tile_h);
 int sflow_get_tile_shape(const sflow_handle* h, int32_t* tile_h);

@@ -30,6 +30,8 @@ def _load(timing=False):
     lib.sflow_oracle_create.argtypes = [vp, dp]
     lib.sflow_oracle_destroy.argtypes = [vp]
     lib.sflow_oracle_set_q.argtypes = [vp, dp]
+    lib.sflow_oracle_replace_q.argtypes = [vp, dp]
+    lib.sflow_oracle_replace_q.restype = None
     lib.sflow_oracle_step.argtypes = [vp]
     lib.sflow_oracle_run.restype = ip
     lib.sflow_oracle_run.argtypes = [vp, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
@@ -140,6 +142,12 @@ class Oracle:
         q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
         assert q.size == self.nx * self.ny * self.nv
         self.lib.sflow_oracle_set_q(self.h, _dp(q))
+
+    def replace_q(self, q_aos):
+        """Replace q in place, keeping the time, dt history and maps."""
+        q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
+        assert q.size == self.nx * self.ny * self.nv
+        self.lib.sflow_oracle_replace_q(self.h, _dp(q))
 
     def step(self):
         return self.lib.sflow_oracle_step(self.h)

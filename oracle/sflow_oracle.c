@@ -2313,6 +2313,13 @@ void sflow_oracle_destroy(oracle_t* o) {
 }
 
 /* IMEX_SfloW2D.f90:263-368: init check_solve(.TRUE.), initial qp and maxima */
+/* Replace the conserved variables in place, keeping the time, dt history
+ * and every map (test hook: perturbs a running state, e.g. rounds it to
+ * FP32 to measure how the run responds to rounding of the state). */
+void sflow_oracle_replace_q(oracle_t* o, const double* q) {
+  memcpy(o->q, q, sizeof(double) * o->N * o->P.nv);
+}
+
 int sflow_oracle_set_q(oracle_t* o, const double* q) {
   const int nv = o->P.nv, np = nv + 2;
   memcpy(o->q, q, sizeof(double) * o->N * nv);

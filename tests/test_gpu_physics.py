@@ -162,5 +162,30 @@ def test_mu_i_rheology_fp64_matches_oracle(n_solid):
 
 
 def test_mu_i_rheology_fp32_error_against_oracle():
+    """The granular slide is ill-conditioned: the mu(I) friction of a cell
+    near rest points along u/|u| whatever |u|, and the mass creeps where
+    friction and gravity nearly balance.  The oracle itself, with its state
+    rounded to FP32 after every step, departs from its unrounded run by
+    ~4e-4 (L1) after 300 steps.  The bar is that rounding band: the FP32
+    form's error per variable <= 2 x the band's (L1 and Linf), i.e. the
+    FP32 arithmetic adds nothing beyond the rounding of the stored state."""
     p, B, q = W.granular_slide()
-    _compare_fp32(p, B, q, steps=300)
+    steps = 300
+    pp = p.copy()
+    pp.precision = PREC_FP64
+    ref, rnd = oracle.Oracle(pp, B), oracle.Oracle(pp, B)
+    ref.set_q(W.to_aos(q))
+    rnd.set_q(W.to_aos(q))
+    ref.run(max_steps=steps)
+    for _ in range(steps):
+        rnd.run(max_steps=1)
+        rnd.replace_q(rnd.q().astype(np.float32).astype(np.float64))
+    band = _field_errors(p, rnd.qp(), ref.qp())
+    g = _gpu(p, B, q, PREC_FP32, steps)
+    assert g["st"].status & ~S_LOW_T == 0, g["st"].status
+    errs = _field_errors(p, g["qp"], ref.qp())
+    ref.close()
+    rnd.close()
+    for n, (l1, linf) in errs.items():
+        assert l1 <= 2.0 * band[n][0] + 1e-6, (n, l1, band[n])
+        assert linf <= 2.0 * band[n][1] + 1e-5, (n, linf, band[n])

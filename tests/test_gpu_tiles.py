@@ -58,7 +58,7 @@ def _same(a, b):
 
 
 def test_compiled_heights():
-    assert L.tile_shapes(PREC_FP32) == [8, 16]
+    assert L.tile_shapes(PREC_FP32) == [8, 16, 4]
     assert L.tile_shapes(PREC_FP64) == [8]
 
 
@@ -68,14 +68,17 @@ def test_tile_heights_give_identical_results(shape):
     p, B, q = _developed(nx, ny, dx, settling=True, entrainment=True)
     ref = _run(p, B, q, 12, [8] * 12)
     _same(ref, _run(p, B, q, 12, [16] * 12))
+    _same(ref, _run(p, B, q, 12, [4] * 12))
     # switched between steps
-    _same(ref, _run(p, B, q, 12, [8, 16, 16, 8, 16, 8, 8, 16, 16, 16, 8, 16]))
+    _same(ref, _run(p, B, q, 12, [8, 16, 4, 8, 16, 8, 4, 4, 16, 16, 8, 16]))
 
 
 def test_tile_heights_general_tableau():
     p, B, q = _developed(96, 80, 12.0, settling=False)
     p.n_rk = 3
-    _same(_run(p, B, q, 6, [8] * 6), _run(p, B, q, 6, [16] * 6))
+    ref = _run(p, B, q, 6, [8] * 6)
+    _same(ref, _run(p, B, q, 6, [16] * 6))
+    _same(ref, _run(p, B, q, 6, [4] * 6))
 
 
 def test_fp64_form_has_one_height():
@@ -96,10 +99,10 @@ def test_autotune_steps_are_ordinary_steps():
     s = L.Solver(p, B)
     s.upload_q(W.to_aos(q))
     best, tab = s.autotune(16)
-    assert best in (8, 16) and s.tile_shape() == best
-    assert set(tab) == {8, 16} and all(v > 0 for v in tab.values())
+    assert best in (8, 16, 4) and s.tile_shape() == best
+    assert set(tab) == {8, 16, 4} and all(v > 0 for v in tab.values())
     n = s.counters()["steps"]
-    assert n == 2 * (16 + 16)
+    assert n == 3 * (16 + 16)
     got = s.download_q()
     s.close()
     r = L.Solver(p, B)
@@ -141,5 +144,5 @@ def test_tune_batch_picks_a_compiled_height():
     members = [(p, B, W.to_aos(q)) for p, B, q in
                (_developed(128, 96, 10.0, settling=False), _developed(96, 128, 12.0, settling=False))]
     best, rates = A.tune_batch(PREC_FP32, members, steps=32)
-    assert best in (8, 16) and set(rates) == {8, 16}
+    assert best in (8, 16, 4) and set(rates) == {8, 16, 4}
     assert all(v > 0 for v in rates.values())

@@ -201,3 +201,20 @@ def test_bottom_source_parameter_checks(edit):
     edit(p)
     with pytest.raises(L.SflowError):
         L.host_scalars(p, B)
+
+
+def test_oracle_replace_q_keeps_the_run():
+    """replace_q with the run's own state continues the run bit for bit
+    (it keeps the time, dt history and maps, unlike set_q)."""
+    p, B, q = W.granular_slide(nx=48, ny=32)
+    a, b = oracle.Oracle(p, B), oracle.Oracle(p, B)
+    a.set_q(W.to_aos(q))
+    b.set_q(W.to_aos(q))
+    a.run(max_steps=20)
+    for _ in range(20):
+        b.run(max_steps=1)
+        b.replace_q(b.q())
+    assert np.array_equal(a.q(), b.q())
+    assert a.stats().t == b.stats().t and a.stats().steps == b.stats().steps
+    a.close()
+    b.close()
