@@ -8,7 +8,8 @@ per-run Voellmy mu in [0.05, 0.3] and xi in [200, 2000], inlet radius
 0.005-0.05 of 2 classes, settling on (workloads.ensemble_params), each run
 2000 steps from the empty state with N_RK = 2, KT fluxes, minmod.  All runs
 are resident together and advanced by the batch engine (persistent kernels
-over a device-built tile queue, CUDA graphs of 16 steps).
+over a device-built tile queue and active-cell list, CUDA graphs of 16
+steps).
 
 One bench step is one chunk of 2000 / K batch steps (every run advances
 that many time steps), so the K timed steps cover the runs' 2000 steps.
@@ -28,6 +29,10 @@ Metric: cell-updates/s = sum over runs and steps of the active cells
                -funroll-all-loops) on a bounded sample of the ensemble, one
                single-threaded process per member on the host cores, as the
                reference runs ensembles (one job per process)
+  error_vs_oracle  FP32 against the oracle (FP64) on the 8 smallest members
+               after their 2000 steps, per member; for a member above the
+               1e-4 L1 bar on h, the oracle's own FP32 rounding band (its
+               run with the state rounded to FP32 after every step)
 The working set (every run's state, increments, topography and maps,
 ~6 GB) and the per-step traffic of the active tiles (~1.4 M cells x ~150 B)
 exceed the 129 MB L2, so no flush is needed between steps.
@@ -66,6 +71,7 @@ METRIC = ("cell-updates/s (batched FP32 vs plain FP64 GPU, ≤1e-4 L1 err) ; "
           "p50/p99 solve latency")
 UNIT = "cell-updates/s"
 ENS_RUNS, ENS_STEPS = 256, 2000
+H_L1_BAR = 1e-4                # the relative L1 bar on h of the FP32 form against the oracle
 WORKLOAD = (f"batched ensemble: {ENS_RUNS} ring-inlet runs x {ENS_STEPS} steps, sides 128-1024 "
             "log-uniform, dx 5-20 m, own cone+fBm DEMs, per-run mu/xi/inlet draws, 2 classes, N_RK=2")
 CPU_SAMPLE_EVERY = 16          # cpu sample: members 0, 16, 32, ...
@@ -320,6 +326,26 @@ def _oracle_member_worker(index):
     o = oracle.Oracle(p, B)
     o.set_q(W.to_aos(q))
     o.run(max_steps=steps)
+    qo = o.q()
+    o.close()
+    return index, qo
+
+
+def _band_member_worker(index):
+    """The FP32 rounding band of one member: the oracle's parity build run
+    over the member's 2000 steps with its state rounded to FP32 after every
+    step (one host core); returns (index, q).  Its distance from the
+    unrounded oracle run is the error any form that stores the state in
+    FP32 carries on this member, before its own arithmetic adds any."""
+    import oracle
+    oracle.set_threads(1)
+    p, B, q, steps = W.ensemble_params(index, PREC_FP64, ENS_STEPS)
+    o = oracle.Oracle(p, B)
+    o.set_q(W.to_aos(q))
+    for _ in range(steps):
+        if o.run(max_steps=1)[0] == 0:
+            break
+        o.replace_q(o.q().astype(np.float32).astype(np.float64))
     qo = o.q()
     o.close()
     return index, qo
@@ -762,6 +788,13 @@ def run_gb300(args, d):
             p, B = members64[k][0], members64[k][1]
             err_oracle.append(field_errors(p, qp_of_state(p, B, q32[k]), qp_of_state(p, B, orc[k])))
             err_fp64.append(float(np.abs(q64[k] - orc[k]).max() / max(np.abs(orc[k]).max(), 1e-300)))
+    # members above the h bar: the oracle's own FP32 rounding band (spawned
+    # processes, while the GPU runs the e2e and profile legs)
+    over = [k for k, e in zip(err_members, err_oracle) if e["h"]["l1_rel"] > H_L1_BAR]
+    band_res = None
+    if over:
+        pool = mp.get_context("spawn").Pool(processes=len(over))
+        band_res = pool.map_async(_band_member_worker, over)
 
     # e2e through the C ABI from host buffers
     e2e = ensemble_e2e(lib, members32, K, chunk, th)
@@ -795,6 +828,18 @@ def run_gb300(args, d):
         roofline["issue_frac"] = (prof["warp_inst_per_computed_cell"] * computed_launch / launch_s
                                   / prof["issue_peak_warp_inst_per_s"])
     log(f"profile {roofline['kernel_ms_per_step']}")
+
+    per_member = {}
+    for k, e in zip(err_members, err_oracle):
+        per_member[str(k)] = {"h_l1": e["h"]["l1_rel"], "h_linf": e["h"]["linf_rel"]}
+    if band_res is not None:
+        for k, qb in band_res.get():
+            p, B = members64[k][0], members64[k][1]
+            band = field_errors(p, qp_of_state(p, B, qb), qp_of_state(p, B, orc[k]))
+            per_member[str(k)]["fp32_rounding_band_h_l1"] = band["h"]["l1_rel"]
+            per_member[str(k)]["fp32_rounding_band_h_linf"] = band["h"]["linf_rel"]
+        pool.close()
+        pool.join()
 
     cur = None
     if d.rank == 0 and args.current_steps > 0:
@@ -832,6 +877,12 @@ def run_gb300(args, d):
             "speedup_fp32_over_fp64": value / value64 if value64 else None,
             "error_vs_oracle": ({"members": err_members, "steps": ENS_STEPS,
                                  "fp32_worst": worst(err_oracle),
+                                 "h_l1_bar": H_L1_BAR,
+                                 "members_within_h_bar": sum(e["h"]["l1_rel"] <= H_L1_BAR for e in err_oracle),
+                                 "per_member": per_member,
+                                 "band_note": "fp32_rounding_band_*: the oracle with its state rounded to FP32 "
+                                              "after every step against the unrounded oracle (members above "
+                                              "the bar only)",
                                  "fp64_max_rel_q": max(err_fp64) if err_fp64 else None}
                                 if err_oracle else None),
             "autotune": tuned,

@@ -189,3 +189,20 @@ def test_mu_i_rheology_fp32_error_against_oracle():
     for n, (l1, linf) in errs.items():
         assert l1 <= 2.0 * band[n][0] + 1e-6, (n, l1, band[n])
         assert linf <= 2.0 * band[n][1] + 1e-5, (n, linf, band[n])
+
+
+def test_mu_i_rheology_batch_equals_single_run():
+    """Granular slides (mu(I) rheology 11, 1 and 3 classes) batched beside
+    a ring-inlet current: each run equals its single-run handle bit for bit
+    in the plain FP64 form (the batch and the handle share the per-cell
+    code; the FP32 slide is too ill-conditioned for a last-bit comparison
+    of two compilations)."""
+    runs = [W.granular_slide(n_solid=1), W.granular_slide(nx=96, ny=40, n_solid=3),
+            W.pyroclastic(nx=80, ny=80, dx=20.0, settling=True)]
+    b = L.Batch(PREC_FP64, max_runs=4, max_cells=1 << 20)
+    ids = [b.submit(p, B, W.to_aos(q)) for p, B, q in runs]
+    b.advance(120)
+    for (p, B, q), rid in zip(runs, ids):
+        g = _gpu(p, B, q, PREC_FP64, 120)
+        np.testing.assert_array_equal(b.collect(rid), g["q"])
+    b.close()
