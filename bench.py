@@ -21,7 +21,8 @@ Metric: cell-updates/s = sum over runs and steps of the active cells
   fp64_plain   the same ensemble in the plain FP64 form (same batch
                engine), the same K steps: the same-workload comparator
   e2e          the same ensemble through the C ABI from host buffers:
-               sflow_batch_submit of every run (host set-up, upload),
+               sflow_batch_submit_many of every run (host set-ups on the
+               host's threads, uploads in order),
                the K steps, sflow_batch_collect with the download of every
                run's q, host wall clock
   cpu_baseline the oracle (C restatement of the reference time step) built
@@ -368,12 +369,9 @@ def ensemble_batch(lib, precision, members, tile_h):
 
 
 def ensemble_submit(b, members):
-    ids = []
-    for p, B, q, st in members:
-        rid = b.submit(p, B, W.to_aos(q), max_steps=st)
-        if rid is None:
-            raise RuntimeError("ensemble member not admitted")
-        ids.append(rid)
+    ids = b.submit_many([(p, B, W.to_aos(q), st) for p, B, q, st in members])
+    if any(rid is None for rid in ids):
+        raise RuntimeError("ensemble member not admitted")
     return ids
 
 
@@ -430,12 +428,9 @@ def ensemble_e2e(lib, members, K, chunk, tile_h):
     b = ensemble_batch(lib, PREC_FP32, members, tile_h)
     qs = [W.to_aos(q) for _, _, q, _ in members]
     t0 = time.perf_counter()
-    ids = []
-    for (p, B, _, st), qa in zip(members, qs):
-        rid = b.submit(p, B, qa, max_steps=st)
-        if rid is None:
-            raise RuntimeError("ensemble member not admitted")
-        ids.append(rid)
+    ids = b.submit_many([(p, B, qa, st) for (p, B, _, st), qa in zip(members, qs)])
+    if any(rid is None for rid in ids):
+        raise RuntimeError("ensemble member not admitted")
     for _ in range(K):
         b.advance(chunk)
     cu = 0
@@ -449,8 +444,9 @@ def ensemble_e2e(lib, members, K, chunk, tile_h):
     in_bytes = sum(qa.nbytes + B.size * 8 for (p, B, _, _), qa in zip(members, qs))
     return {"value": cu / wall, "unit": UNIT, "h2d_bytes_per_step": in_bytes / K,
             "d2h_bytes_per_step": out_bytes / K, "seconds": wall, "steps": K,
-            "path": "sflow_batch_submit (host set-up + upload) of every run, sflow_batch_advance, "
-                    "sflow_batch_collect with q download; host buffers, wall clock"}
+            "path": "sflow_batch_submit_many (host set-ups on the host's threads, uploads in order) of "
+                    "every run, sflow_batch_advance, sflow_batch_collect with q download; host buffers, "
+                    "wall clock", "host_threads": os.cpu_count()}
 
 
 def warm_up(lib, precision, members, tile_h, steps):

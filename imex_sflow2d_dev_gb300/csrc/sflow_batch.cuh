@@ -44,7 +44,7 @@ class Batch : public BatchBase {
   }
   std::string err_;
 
-  int submit(const HostSetup& hs, const double* q_aos, int64_t max_steps, int* id) override {
+  int submit(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* id) override {
     if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     if (hs.nrk != 2) { err_ = "batched runs use the N_RK = 2 tableau"; return SFLOW_EINVAL; }
     if (hs.ns < kMinSolidBuilt || hs.ns > kMaxSolidBuilt) { err_ = "n_solid out of range"; return SFLOW_EINVAL; }
@@ -72,12 +72,14 @@ class Batch : public BatchBase {
     if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
     if (mem_limit_ > 0 && held_ + need > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
 
-    std::unique_ptr<Solver<R>> sv(new Solver<R>(hs, tile_h_));
+    const int ns = hs.ns;
+    const double t_end = hs.p.t_end, max_dt = hs.p.max_dt;
+    std::unique_ptr<Solver<R>> sv(new Solver<R>(std::move(hs), tile_h_));
     int rc = sv->init();
     if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
     rc = sv->upload(q_aos);
     if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
-    rc = sv->limits(hs.p.t_end, max_steps > 0 ? max_steps : -1);
+    rc = sv->limits(t_end, max_steps > 0 ? max_steps : -1);
     if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
     sv->trim_stage();
     uint32_t* cand = nullptr;
@@ -113,7 +115,7 @@ class Batch : public BatchBase {
     br.tiles_y = sv->tiles_y();
     br.gen = s.gen;
     br.live = 1;
-    br.max_dt = hs.p.max_dt;
+    br.max_dt = max_dt;
     const KArgs<R> ka = sv->kargs();
     if (ka.g.lim_all != 1 && g->lim == 1) {
       // the group needs the generic limiter kernel from now on: re-capture
@@ -142,7 +144,7 @@ class Batch : public BatchBase {
     g->tiles_live += tiles;
     g->live += 1;
     const int rid = (int)recs_.size();
-    recs_.push_back(Rec{hs.ns, slot, true});
+    recs_.push_back(Rec{ns, slot, true});
     s.rec = rid;
     *id = rid;
     return SFLOW_OK;

@@ -1,7 +1,12 @@
 // sflow_capi.cpp -- the extern "C" boundary declared in include/sflow.h.
+#include <algorithm>
+#include <condition_variable>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sflow.h"
@@ -96,7 +101,7 @@ int sflow_batch_submit(sflow_batch* b, const SflowParams* p, const double* B_cen
   int rc = sflow::host_setup(p, B_cent, s, err);
   if (rc != SFLOW_OK) return fail(rc, err);
   int id = -1;
-  rc = b->impl->submit(s, q_aos, max_steps, &id);
+  rc = b->impl->submit(std::move(s), q_aos, max_steps, &id);
   if (rc < 0) return fail(rc, b->impl->error());
   *run_id = id;
   return SFLOW_OK;
@@ -125,9 +130,107 @@ int sflow_batch_submit_setup(sflow_batch* b, const sflow_setup* s, const double*
   if (!s || !q_aos || !run_id) return fail(SFLOW_EINVAL, "NULL argument");
   if (s->hs.p.precision != b->precision) return fail(SFLOW_EINVAL, "run precision differs from the batch precision");
   int id = -1;
-  const int rc = b->impl->submit(s->hs, q_aos, max_steps, &id);
+  HostSetup copy = s->hs;   // a setup can be submitted again
+  const int rc = b->impl->submit(std::move(copy), q_aos, max_steps, &id);
   if (rc < 0) return fail(rc, b->impl->error());
   *run_id = id;
+  return SFLOW_OK;
+}
+
+int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params, const double* const* B_cent,
+                            const double* const* q_aos, const int64_t* max_steps, int32_t* run_ids,
+                            int32_t threads) {
+  BATCH_CHECK(b);
+  if (n < 0) return fail(SFLOW_EINVAL, "n must be >= 0");
+  if (n > 0 && (!params || !B_cent || !q_aos || !run_ids)) return fail(SFLOW_EINVAL, "NULL argument");
+  for (int32_t i = 0; i < n; ++i) run_ids[i] = -1;
+  if (n == 0) return SFLOW_OK;
+  int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+  nt = std::min(std::max(1, std::min(nt, 64)), (int)n);
+  const int window = 2 * nt;
+
+  // set-ups made by the workers in place, taken in run order by this thread
+  struct Item {
+    HostSetup hs;
+    int rc = SFLOW_OK;
+    std::string err;
+    bool ready = false;
+  };
+  std::vector<Item> items((size_t)n);
+  auto make = [&](int i, Item& it) {
+    try {
+      if (!B_cent[i] || !q_aos[i]) {
+        it.rc = SFLOW_EINVAL;
+        it.err = "NULL argument";
+      } else if (params[i].precision != b->precision) {
+        it.rc = SFLOW_EINVAL;
+        it.err = "run precision differs from the batch precision";
+      } else {
+        it.rc = sflow::host_setup(&params[i], B_cent[i], it.hs, it.err);
+      }
+    } catch (const std::bad_alloc&) {
+      it.hs = HostSetup();
+      it.rc = SFLOW_ENOMEM;
+      it.err = "host allocation failed";
+    }
+  };
+  std::mutex mu;
+  std::condition_variable cv_ready, cv_room;
+  int next = 0, taken = 0;
+  auto work = [&]() {
+    for (;;) {
+      int i;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_room.wait(lk, [&] { return next >= n || next < taken + window; });
+        if (next >= n) return;
+        i = next++;
+      }
+      Item tmp;
+      make(i, tmp);
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        items[(size_t)i] = std::move(tmp);
+        items[(size_t)i].ready = true;
+      }
+      cv_ready.notify_all();
+    }
+  };
+  std::vector<std::thread> pool;
+  try {
+    for (int t = 0; t < nt; ++t) pool.emplace_back(work);
+  } catch (const std::exception&) {
+    // fewer threads than asked (at worst none: the set-ups are made below)
+  }
+  int first_rc = SFLOW_OK;
+  std::string first_err;
+  for (int32_t i = 0; i < n; ++i) {
+    Item it;
+    if (pool.empty()) {
+      make(i, it);
+    } else {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_ready.wait(lk, [&] { return items[(size_t)i].ready; });
+      it = std::move(items[(size_t)i]);
+      items[(size_t)i] = Item();
+      taken = i + 1;
+    }
+    cv_room.notify_all();
+    int rc = it.rc;
+    std::string err = it.err;
+    if (rc == SFLOW_OK) {
+      int id = -1;
+      rc = b->impl->submit(std::move(it.hs), q_aos[i], max_steps ? max_steps[i] : 0, &id);
+      if (rc < 0) err = b->impl->error();
+      else run_ids[i] = id;
+    }
+    if (rc < 0 && first_rc == SFLOW_OK) {
+      first_rc = rc;
+      first_err = "run " + std::to_string(i) + ": " + err;
+    }
+  }
+  for (auto& t : pool) t.join();
+  if (first_rc != SFLOW_OK) return fail(first_rc, first_err);
   return SFLOW_OK;
 }
 

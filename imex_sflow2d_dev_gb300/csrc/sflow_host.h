@@ -121,7 +121,8 @@ SolverBase* make_solver_fp32(const HostSetup& s, std::string& err);
 class BatchBase {
  public:
   virtual ~BatchBase() {}
-  virtual int submit(const HostSetup& hs, const double* q_aos, int64_t max_steps, int* id) = 0;
+  // takes hs over (its host arrays move into the run)
+  virtual int submit(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* id) = 0;
   virtual int advance(int64_t steps, int* finished) = 0;
   // the same with the device time of the steps (CUDA events across the
   // groups' streams) in *ms

@@ -111,7 +111,11 @@ template <class R>
 class Solver : public SolverBase {
  public:
   explicit Solver(const HostSetup& s, int tile_h = kTileHDefault) : hs_(s), tile_h_(tile_h) {
-    tab_ = kernel_table<R>(s.ns, tile_h);
+    tab_ = kernel_table<R>(hs_.ns, tile_h);
+  }
+  // takes the set-up's host arrays over instead of copying them
+  explicit Solver(HostSetup&& s, int tile_h) : hs_(std::move(s)), tile_h_(tile_h) {
+    tab_ = kernel_table<R>(hs_.ns, tile_h);
   }
   ~Solver() override { release(); }
 

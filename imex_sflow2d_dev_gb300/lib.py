@@ -102,6 +102,8 @@ def load(build_if_missing=True):
         "sflow_setup_create": (C.c_int, [P, dp, C.POINTER(vp)]),
         "sflow_setup_destroy": (None, [vp]),
         "sflow_batch_submit_setup": (C.c_int, [vp, vp, dp, i64, C.POINTER(i32)]),
+        "sflow_batch_submit_many": (C.c_int, [vp, i32, P, C.POINTER(dp), C.POINTER(dp), C.POINTER(i64),
+                                               C.POINTER(i32), i32]),
         "sflow_batch_launch": (C.c_int, [vp, i64]),
         "sflow_batch_wait": (C.c_int, [vp, C.POINTER(i32)]),
         "sflow_batch_dry_border_updates": (C.c_int, [vp, i32, C.POINTER(i64)]),
@@ -149,7 +151,7 @@ def exported_symbols():
             "sflow_set_tile_shape", "sflow_get_tile_shape", "sflow_autotune",
             "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape", "sflow_check_conversions",
             "sflow_eval_math", "sflow_batch_advance_timed", "sflow_batch_profile_kernels",
-            "sflow_setup_create", "sflow_setup_destroy", "sflow_batch_submit_setup",
+            "sflow_setup_create", "sflow_setup_destroy", "sflow_batch_submit_setup", "sflow_batch_submit_many",
             "sflow_batch_launch", "sflow_batch_wait", "sflow_batch_dry_border_updates",
             "sflow_dry_border_updates", "sflow_download_erosion", "sflow_download_erodible",
             "sflow_set_erodible", "sflow_download_topography", "sflow_set_nodata",
@@ -656,6 +658,45 @@ class Batch:
         _check(rc)
         self._shape[rid.value] = p.n_vars * p.comp_cells_x * p.comp_cells_y
         return rid.value
+
+    def submit_many(self, runs, threads=0):
+        """Submit [(params, B_cent, q_aos, max_steps)] at once, the host
+        set-ups on `threads` host threads (0: every hardware thread) while
+        the runs are uploaded in order (sflow_batch_submit_many).  Returns
+        the run ids, None for a run not admitted for want of room (EBUSY);
+        any other failure raises SflowError, whose run_ids attribute holds
+        the ids of the runs that were admitted."""
+        n = len(runs)
+        m = max(n, 1)
+        ps = (SflowParams * m)()
+        Bs, qs, keep = (C.POINTER(C.c_double) * m)(), (C.POINTER(C.c_double) * m)(), []
+        ms = (C.c_int64 * m)()
+        for i, (params, B_cent, q_aos, max_steps) in enumerate(runs):
+            p = params.copy()
+            p.precision = self.precision
+            B = np.ascontiguousarray(B_cent, dtype=np.float64).reshape(-1)
+            q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
+            if B.size != p.comp_cells_x * p.comp_cells_y:
+                raise ValueError("B_cent must have nx*ny values")
+            if q.size != p.n_vars * p.comp_cells_x * p.comp_cells_y:
+                raise ValueError("q must have n_vars*nx*ny values")
+            ps[i] = p
+            Bs[i], qs[i], ms[i] = _dp(B), _dp(q), int(max_steps or 0)
+            keep.append((B, q, p))
+        ids = (C.c_int32 * m)()
+        rc = self.lib.sflow_batch_submit_many(self.h, n, ps, Bs, qs, ms, ids, int(threads))
+        out = []
+        for i in range(n):
+            rid = ids[i]
+            if rid >= 0:
+                p = keep[i][2]
+                self._shape[rid] = p.n_vars * p.comp_cells_x * p.comp_cells_y
+            out.append(rid if rid >= 0 else None)
+        if rc < 0 and rc != EBUSY:
+            err = SflowError(rc, self.lib.sflow_last_error().decode())
+            err.run_ids = out
+            raise err
+        return out
 
     def advance(self, steps):
         f = C.c_int32(0)

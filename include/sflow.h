@@ -412,6 +412,19 @@ int sflow_setup_create(const SflowParams* p, const double* B_cent, sflow_setup**
 void sflow_setup_destroy(sflow_setup* s);
 int sflow_batch_submit_setup(sflow_batch* b, const sflow_setup* s, const double* q_aos, int64_t max_steps,
                              int32_t* run_id);
+/* n runs at once: params[i], B_cent[i], q_aos[i] and max_steps[i] (NULL:
+ * no step limit) as for sflow_batch_submit.  The host set-ups run on
+ * `threads` host threads (<= 0: the host's hardware threads, at most 64)
+ * while the calling thread uploads, in order, the runs whose set-up is done;
+ * at most 2 x threads set-ups are held at a time.  run_ids[i] receives the
+ * run id, or -1 when run i was not admitted.  Returns SFLOW_OK when every run
+ * was admitted, else the code of the first failure in run order
+ * (sflow_last_error names the run); the runs that could be admitted are
+ * admitted either way.  The runs give the same results as sequential
+ * sflow_batch_submit calls. */
+int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params, const double* const* B_cent,
+                            const double* const* q_aos, const int64_t* max_steps, int32_t* run_ids,
+                            int32_t threads);
 /* Asynchronous sflow_batch_advance: sflow_batch_launch enqueues `steps`
  * batch steps and returns at once; sflow_batch_wait waits for them and
  * reports finished runs.  Between the two only host work is allowed: every

@@ -351,3 +351,49 @@ def test_memory_limit_hook_gives_ebusy():
     b.set_memory_limit(0)
     assert b.submit(p, B, W.to_aos(q)) is not None
     b.close()
+
+
+@pytest.mark.parametrize("threads", [1, 4, 0])
+def test_submit_many_equals_sequential_submits(threads):
+    """sflow_batch_submit_many (host set-ups on worker threads, uploads in
+    order) admits the runs a sequential submit would, with the same results
+    (FP64 form: bitwise)."""
+    runs = _mix()
+    ref = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 22)
+    rids = [ref.submit(p, B, W.to_aos(q), max_steps=30) for p, B, q in runs]
+    ref.advance(40)
+    b = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 22)
+    ids = b.submit_many([(p, B, W.to_aos(q), 30) for p, B, q in runs], threads=threads)
+    assert all(i is not None for i in ids)
+    b.advance(40)
+    for rid, i in zip(rids, ids):
+        np.testing.assert_array_equal(b.collect(i), ref.collect(rid))
+    b.close()
+    ref.close()
+
+
+def test_submit_many_reports_the_first_failure_and_admits_the_rest():
+    runs = _mix()
+    bad = runs[2][0].copy()
+    bad.n_rk = 3                       # batched runs use the N_RK = 2 tableau
+    items = [(p, B, W.to_aos(q), 0) for p, B, q in runs]
+    items[2] = (bad, runs[2][1], W.to_aos(runs[2][2]), 0)
+    b = L.Batch(PREC_FP32, max_runs=8, max_cells=1 << 22)
+    with pytest.raises(L.SflowError) as ei:
+        b.submit_many(items, threads=3)
+    assert "run 2" in str(ei.value)
+    ids = ei.value.run_ids
+    assert ids[2] is None and all(ids[i] is not None for i in (0, 1, 3, 4))
+    assert b.live() == 4
+    b.close()
+
+
+def test_submit_many_without_room_returns_none():
+    # one solid class: the runs share the class count's two slots
+    runs = [W.dam_break(nx=64, ny=48, t_end=100.0), W.dam_break(nx=40, ny=200, t_end=100.0),
+            W.dam_break(nx=50, ny=50, t_end=100.0)]
+    b = L.Batch(PREC_FP32, max_runs=2, max_cells=1 << 22)
+    ids = b.submit_many([(p, B, W.to_aos(q), 0) for p, B, q in runs])
+    assert ids[0] is not None and ids[1] is not None and ids[2] is None
+    assert b.submit_many([]) == []
+    b.close()
