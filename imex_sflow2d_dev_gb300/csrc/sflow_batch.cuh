@@ -67,9 +67,16 @@ class Batch : public BatchBase {
     }
     const int64_t need = Solver<R>::batch_bytes(hs, tile_h_) +
                          (int64_t)sizeof(double) * hs.nx * hs.ny * (hs.nv + 3);   // staging, freed after upload
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
-    if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
+    // free device memory: queried at every submit, or tracked across a bulk
+    // admission (re-queried every 32 admissions and near the need)
+    if (!bulk_ || !free_known_ || since_query_ >= 32 || free_est_ < need + kReserve + (int64_t(4) << 30)) {
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
+      free_est_ = (int64_t)free_b;
+      free_known_ = bulk_;
+      since_query_ = 0;
+    }
+    if (free_est_ < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
     if (mem_limit_ > 0 && held_ + need > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
 
     const int ns = hs.ns;
@@ -139,6 +146,8 @@ class Batch : public BatchBase {
     ++g->launches;
     s.bytes = sv->device_bytes() + (int64_t)sizeof(uint32_t) * tiles + tiles;
     held_ += s.bytes;
+    free_est_ -= s.bytes;
+    ++since_query_;
     s.solver = std::move(sv);
     s.done = false;
     g->tiles_live += tiles;
@@ -148,6 +157,11 @@ class Batch : public BatchBase {
     s.rec = rid;
     *id = rid;
     return SFLOW_OK;
+  }
+
+  void set_bulk(bool on) override {
+    bulk_ = on;
+    free_known_ = false;
   }
 
   int advance(int64_t steps, int* finished) override { return advance_impl(steps, finished, nullptr); }
@@ -412,6 +426,10 @@ class Batch : public BatchBase {
   static constexpr int64_t kReserve = (int64_t)1 << 30;   // device memory kept free
   int64_t mem_limit_ = 0;   // cap on the resident runs' device bytes (0: none)
   int64_t held_ = 0;        // device bytes of the resident runs
+  bool bulk_ = false;       // inside sflow_batch_submit_many
+  bool free_known_ = false; // free_est_ holds a query of this bulk admission
+  int64_t free_est_ = 0;    // free device memory (last query minus admitted runs since)
+  int since_query_ = 0;     // admissions since that query
 
   struct Slot {
     std::unique_ptr<Solver<R>> solver;

@@ -204,6 +204,7 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
   }
   int first_rc = SFLOW_OK;
   std::string first_err;
+  b->impl->set_bulk(true);
   for (int32_t i = 0; i < n; ++i) {
     Item it;
     if (pool.empty()) {
@@ -229,6 +230,7 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
       first_err = "run " + std::to_string(i) + ": " + err;
     }
   }
+  b->impl->set_bulk(false);
   for (auto& t : pool) t.join();
   if (first_rc != SFLOW_OK) return fail(first_rc, first_err);
   return SFLOW_OK;

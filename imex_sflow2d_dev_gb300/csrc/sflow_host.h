@@ -123,6 +123,10 @@ class BatchBase {
   virtual ~BatchBase() {}
   // takes hs over (its host arrays move into the run)
   virtual int submit(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* id) = 0;
+  // bulk admission (sflow_batch_submit_many): the free device memory is
+  // queried once and tracked across the submits while on, re-queried
+  // every 32 admissions and whenever the estimate nears the run's need
+  virtual void set_bulk(bool on) = 0;
   virtual int advance(int64_t steps, int* finished) = 0;
   // the same with the device time of the steps (CUDA events across the
   // groups' streams) in *ms

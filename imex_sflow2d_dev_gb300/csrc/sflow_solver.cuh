@@ -76,6 +76,43 @@ __global__ void __launch_bounds__(kHostChunk) k_host_planes_to_aos(const R* __re
   for (int i = threadIdx.x; i < nval; i += kHostChunk) aos[c0 * nv + i] = sbuf[i];
 }
 
+// One FP64 plane of the host layout (nx x ny, row-major) into a pitched
+// device plane of R, the pad columns zeroed; `src` is host memory the device
+// reads directly (pageable memory on a system with pageable access, or
+// mapped pinned memory) or a device buffer.
+template <class R>
+__global__ void k_plane_to_pitched(const double* __restrict__ src, R* __restrict__ dst, int nx, int ny, int pitch) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)pitch * ny) return;
+  const int j = (int)(c % pitch), k = (int)(c / pitch);
+  dst[c] = (j < nx) ? (R)src[(int64_t)k * nx + j] : R(0);
+}
+
+// Whether kernels on `dev` may read and write pageable host memory (a
+// Grace-Blackwell node with address translation services); queried once
+// per device.
+inline bool pageable_access(int dev) {
+  static int cached[64];   // 0 unknown, 1 no, 2 yes
+  if (dev < 0 || dev >= 64) return false;
+  if (!cached[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    cached[dev] = v ? 2 : 1;
+  }
+  return cached[dev] == 2;
+}
+inline bool pageable_access() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return pageable_access(dev);
+}
+
 template <class R>
 __global__ void k_map_to_host(const R* __restrict__ m, double* __restrict__ out, int nx, int ny,
                               int pitch) {
@@ -129,6 +166,15 @@ class Solver : public SolverBase {
     tiles_x_ = (nx + TX - 1) / TX;
     tiles_y_ = (ny + tile_h_ - 1) / tile_h_;
     SFLOW_CU(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    // one allocation for the buffers below (alloc() carves it; anything it
+    // cannot hold gets its own cudaMalloc)
+    arena_cap_ = init_bytes();
+    if (cudaMalloc((void**)&arena_, arena_cap_) != cudaSuccess) {
+      cudaGetLastError();
+      arena_ = nullptr;
+      arena_cap_ = 0;
+    }
+    arena_used_ = 0;
     SFLOW_CU(alloc((void**)&q_, sizeof(R) * plane_ * nv));
     const int nstage = (hs_.nrk == 2) ? 1 : hs_.nrk;
     SFLOW_CU(alloc((void**)&rd_, sizeof(R) * plane_ * nv * nstage));
@@ -201,8 +247,32 @@ class Solver : public SolverBase {
     std::memset(&hst_, 0, sizeof(hst_));
     init_state_host();
     limits_known_ = false;
+    SFLOW_CU(cudaStreamSynchronize(stream_));   // plane uploads read the set-up's host arrays
     SFLOW_CU(cudaMemcpy(st_, &hst_, sizeof(RunState), cudaMemcpyHostToDevice));
     return SFLOW_OK;
+  }
+
+  // device bytes of init()'s allocations, each rounded as alloc() rounds
+  size_t init_bytes() const {
+    auto A = [](size_t b) { return (b + kArenaAlign - 1) / kArenaAlign * kArenaAlign; };
+    const size_t P = (size_t)plane_, nv = (size_t)hs_.nv, ns = (size_t)hs_.ns;
+    const size_t nstage = (hs_.nrk == 2) ? 1 : (size_t)hs_.nrk;
+    const size_t tiles = (size_t)tiles_x_ * tiles_y_;
+    size_t b = A(sizeof(R) * P * nv) + A(sizeof(R) * P * nv * nstage);
+    if (hs_.nrk != 2) b += A(sizeof(R) * P * nv * nstage) + A(sizeof(R) * P * nv);
+    b += (size_t)(hs_.p.curvature_term_flag ? 8 : 5) * A(sizeof(R) * P);
+    b += A(P) + A(sizeof(R) * P * 3) + A(P);                        // flags, arc, mask
+    b += A(tiles) + A(3 * tiles) + A(tiles) + A(tiles * sizeof(uint16_t));
+    b += 3 * A(sizeof(R) * P);                                      // maxima
+    if (hs_.exchange) b += A(sizeof(double) * P * ns);
+    if (hs_.p.erosion_coeff > 0.0 || (hs_.p.erodible_deposit_flag && hs_.exchange))
+      b += 2 * A(sizeof(double) * P * ns);
+    if (hs_.p.topo_change_flag && hs_.exchange) b += A(sizeof(double) * P);
+    if (hs_.p.bottom_radial_source_flag)
+      b += A(sizeof(R) * P) + A(sizeof(double) * (1 + 2 * (size_t)SFLOW_MAX_INTERVALS));
+    if (hs_.n_thk * hs_.n_dyn > 0) b += A(sizeof(uint32_t) * P * (size_t)((hs_.n_thk * hs_.n_dyn + 31) / 32));
+    b += A(sizeof(RunState)) + A(sizeof(double) * 4 * 1024) + A(sizeof(double) * 4);
+    return b;
   }
 
   // --- used by the batch engine ----------------------------------------------
@@ -271,9 +341,7 @@ class Solver : public SolverBase {
   int upload(const double* q_aos) override {
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     const size_t N = (size_t)nx * ny;
-    SFLOW_CU(ensure_stage());
-    SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
-    k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
+    SFLOW_CU(layout_in(q_aos));
     ++launches_;
     SFLOW_CU(cudaGetLastError());
     init_state_host();
@@ -293,6 +361,27 @@ class Solver : public SolverBase {
   // space; on a Grace-Blackwell node the layout kernels then read or write
   // it over NVLink-C2C directly, with no staging copy.  Other host memory
   // goes through the device staging buffer and the copy engines.
+  // q (host layout) into the state planes: the device reads the host array
+  // itself when it can (mapped pinned memory; pageable memory on a system
+  // with pageable access), else through the staging buffer
+  cudaError_t layout_in(const double* q_aos) {
+    const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
+    const size_t N = (size_t)nx * ny;
+    const double* src = mapped_host(q_aos);
+    if (!src && pageable_access()) src = q_aos;
+    if (src) {
+      k_host_aos_to_planes<R><<<(unsigned)((N + kHostChunk - 1) / kHostChunk), kHostChunk,
+                                sizeof(double) * kHostChunk * nv, stream_>>>(src, q_, nv, nx, ny, pitch_, plane_);
+      return cudaGetLastError();
+    }
+    cudaError_t e = ensure_stage();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_);
+    if (e != cudaSuccess) return e;
+    k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
+    return cudaGetLastError();
+  }
+
   static const double* mapped_host(const void* p) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -307,15 +396,8 @@ class Solver : public SolverBase {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
     const int nx = hs_.nx, ny = hs_.ny, nv = hs_.nv;
     const size_t N = (size_t)nx * ny;
-    const double* src = mapped_host(q_aos);
-    if (src) {
-      k_host_aos_to_planes<R><<<(unsigned)((N + kHostChunk - 1) / kHostChunk), kHostChunk,
-                                sizeof(double) * kHostChunk * nv, stream_>>>(src, q_, nv, nx, ny, pitch_, plane_);
-    } else {
-      SFLOW_CU(ensure_stage());
-      SFLOW_CU(cudaMemcpyAsync(stage_aos_, q_aos, sizeof(double) * N * nv, cudaMemcpyHostToDevice, stream_));
-      k_aos_to_planes<R><<<(unsigned)((N + 255) / 256), 256, 0, stream_>>>(stage_aos_, q_, nv, nx, ny, pitch_, plane_);
-    }
+    (void)N;
+    SFLOW_CU(layout_in(q_aos));
     SFLOW_CU(reset_wet_flags());
     ++launches_;
     SFLOW_CU(cudaGetLastError());
@@ -861,6 +943,8 @@ class Solver : public SolverBase {
   double *stage_aos_ = nullptr, *stat_part_ = nullptr, *stat_out_ = nullptr;
   int nstat_blocks_ = 0;
   std::vector<void*> allocs_;
+  char* arena_ = nullptr;   // one allocation carved by alloc()
+  size_t arena_cap_ = 0, arena_used_ = 0;
   int64_t bytes_ = 0, launches_ = 0;
   KArgs<R> ka_;
   size_t smem_flux_ = 0;
@@ -928,7 +1012,18 @@ class Solver : public SolverBase {
     return b;
   }
 
+  static constexpr size_t kArenaAlign = 256;
+  bool in_arena(const void* p) const {
+    return arena_ && (const char*)p >= arena_ && (const char*)p < arena_ + arena_cap_;
+  }
   cudaError_t alloc(void** p, size_t bytes) {
+    const size_t a = (bytes + kArenaAlign - 1) / kArenaAlign * kArenaAlign;
+    if (arena_ && arena_used_ + a <= arena_cap_) {
+      *p = arena_ + arena_used_;
+      arena_used_ += a;
+      bytes_ += (int64_t)bytes;
+      return cudaSuccess;
+    }
     cudaError_t e = cudaMalloc(p, bytes);
     if (e == cudaSuccess) {
       allocs_.push_back(*p);
@@ -982,6 +1077,10 @@ class Solver : public SolverBase {
     return cudaMemsetAsync(tile_wet_ + n, 0xff, 2 * n, stream_);
   }
   void free_tracked(void* p, size_t bytes) {
+    if (in_arena(p)) {   // arena space is not reused; freed with the arena
+      bytes_ -= (int64_t)bytes;
+      return;
+    }
     for (auto it = allocs_.begin(); it != allocs_.end(); ++it)
       if (*it == p) {
         allocs_.erase(it);
@@ -1011,6 +1110,8 @@ class Solver : public SolverBase {
     if (flush_buf_) cudaFree(flush_buf_);
     for (void* p : allocs_) cudaFree(p);
     allocs_.clear();
+    if (arena_) cudaFree(arena_);
+    arena_ = nullptr;
     if (stage_aos_) cudaFree(stage_aos_);
     stage_aos_ = nullptr;
     if (stream_) cudaStreamDestroy(stream_);
@@ -1025,7 +1126,17 @@ class Solver : public SolverBase {
     return e;
   }
 
+  // a per-cell FP64 host plane into a pitched device plane of R: read and
+  // converted by the device where it can read host memory (asynchronous on
+  // the run's stream; `src` must stay unchanged until the stream is
+  // synchronised), else converted here and copied
   cudaError_t put_plane(R* dst, const std::vector<double>& src) {
+    if (pageable_access() && src.size() == (size_t)hs_.nx * hs_.ny) {
+      k_plane_to_pitched<R><<<(unsigned)(((size_t)plane_ + 255) / 256), 256, 0, stream_>>>(
+          src.data(), dst, hs_.nx, hs_.ny, pitch_);
+      ++launches_;
+      return cudaGetLastError();
+    }
     std::vector<R> buf((size_t)plane_, R(0));
     for (int k = 0; k < hs_.ny; ++k)
       for (int j = 0; j < hs_.nx; ++j) buf[(size_t)k * pitch_ + j] = (R)src[(size_t)k * hs_.nx + j];
