@@ -9,12 +9,14 @@ on the workload and is measured, not guessed:
 
   * a single run: ``Solver.autotune(steps)`` (C ABI ``sflow_autotune``)
     times graph-replayed steps of the run itself with every compiled height
-    and keeps the fastest per active-cell update.  The results of a step do
-    not depend on the height, so the tuning steps are ordinary steps.
+    and keeps the fastest per active-cell update (a height other than the
+    default 32 x 8 only when it is more than 2 % faster).  The results of a
+    step do not depend on the height, so the tuning steps are ordinary
+    steps.
   * a batch: ``tune_batch`` advances a sample of the batch's runs in a
     scratch batch once per height and returns the height with the most
-    cell-updates/s; the real batch is then made with
-    ``Batch.set_tile_shape``.
+    cell-updates/s (with the same 2 % margin); the real batch is then made
+    with ``Batch.set_tile_shape``.
 
 ``TuneCache`` keeps the choices in a JSON file keyed by device, precision,
 solid classes and a size class, so a service tunes a workload class once.
@@ -22,7 +24,6 @@ solid classes and a size class, so a service tunes a workload class once.
 import json
 import math
 import os
-import time
 
 from . import lib as L
 
@@ -38,11 +39,13 @@ def tune_solver(solver, steps=64):
     return solver.autotune(steps)
 
 
-def tune_batch(precision, members, steps=128, warm=16, heights=None, max_cells=None):
+def tune_batch(precision, members, steps=128, warm=16, heights=None, max_cells=None, margin=0.02):
     """Time `members` ((params, B_cent, q_aos) triples) in a scratch batch
     once per tile height: `warm` untimed batch steps, then `steps` timed
-    ones (host clock around the synchronising advance call).  Returns
-    (best height, {height: cell-updates/s})."""
+    ones (device time of the steps, CUDA events).  The first height (the
+    default, 32 x 8) is kept unless another one is faster by more than
+    `margin` (a near tie is measurement noise, not a better shape).
+    Returns (chosen height, {height: cell-updates/s})."""
     heights = list(heights or L.tile_shapes(precision))
     cells = sum(p.comp_cells_x * p.comp_cells_y for p, _, _ in members)
     if max_cells is None:
@@ -60,14 +63,15 @@ def tune_batch(precision, members, steps=128, warm=16, heights=None, max_cells=N
                 ids.append(rid)
             b.advance(warm)
             c0 = sum(b.counters(i)["cell_updates"] for i in ids)
-            t0 = time.perf_counter()
-            b.advance(steps)
-            dt = time.perf_counter() - t0
+            _, ms = b.advance_timed(steps)
             c1 = sum(b.counters(i)["cell_updates"] for i in ids)
-            rates[th] = (c1 - c0) / dt if dt > 0 else 0.0
+            rates[th] = (c1 - c0) / (ms * 1e-3) if ms > 0 else 0.0
         finally:
             b.close()
-    best = max(rates, key=rates.get)
+    best = heights[0]
+    for th in heights[1:]:
+        if rates[th] > rates[best] * (1.0 + margin):
+            best = th
     return best, rates
 
 

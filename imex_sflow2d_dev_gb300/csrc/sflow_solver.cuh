@@ -789,6 +789,7 @@ class Solver : public SolverBase {
   // update.  The steps are real steps of the run (the results are the same
   // with every height); ms_per_mcu[i] receives the time per 10^6 cell
   // updates of candidate i of kTileCandidates (-1 when not compiled).
+  static constexpr double kTuneMargin = 0.02;
   int autotune(int64_t steps, int* best, double* ms_per_mcu) override {
     if (!uploaded_) { err_ = "no state uploaded"; return SFLOW_ESTATE; }
     if (steps < 1) { err_ = "autotune needs at least one step per tile height"; return SFLOW_EINVAL; }
@@ -821,7 +822,10 @@ class Solver : public SolverBase {
       const long long cells = h1.cells_total - h0.cells_total;
       if (cells <= 0) continue;   // the run stopped: nothing measured
       ms_per_mcu[i] = (double)m / ((double)cells * 1.0e-6);
-      if (best_v < 0.0 || ms_per_mcu[i] < best_v) {
+      // a later candidate must beat the best so far by more than 2 %: a
+      // near tie is measurement noise, and the first candidate (32 x 8) is
+      // the default
+      if (best_v < 0.0 || ms_per_mcu[i] < best_v * (1.0 - kTuneMargin)) {
         best_v = ms_per_mcu[i];
         best_th = th;
       }

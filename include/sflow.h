@@ -293,8 +293,9 @@ int64_t sflow_device_bytes(const sflow_handle* h);
  * sflow_autotune        runs `steps_per_shape` steps of the run (after one
  *                       untimed 16-step graph chunk) with each candidate
  *                       height, times them with CUDA events, keeps the
- *                       fastest per active-cell update and returns it in
- *                       *best; ms_per_mcu[i] (n entries, candidates in the
+ *                       fastest per active-cell update (a later candidate
+ *                       only when it is more than 2 % faster than the best
+ *                       before it) and returns it in *best; ms_per_mcu[i] (n entries, candidates in the
  *                       order of sflow_tile_shapes' full list 8, 16, 4) gets
  *                       the ms per 10^6 cell updates, -1 where not
  *                       compiled or nothing ran.  The steps advance the run.
