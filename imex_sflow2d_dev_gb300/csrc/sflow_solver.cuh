@@ -90,10 +90,13 @@ __global__ void k_plane_to_pitched(const double* __restrict__ src, R* __restrict
 
 // Whether kernels on `dev` may read and write pageable host memory (a
 // Grace-Blackwell node with address translation services); queried once
-// per device.
+// per device.  SFLOW_HOST_READS=0 in the environment turns the direct
+// reads off (uploads then go through the staging buffer).
 inline bool pageable_access(int dev) {
   static int cached[64];   // 0 unknown, 1 no, 2 yes
   if (dev < 0 || dev >= 64) return false;
+  const char* env = std::getenv("SFLOW_HOST_READS");
+  if (env && env[0] == '0') return false;
   if (!cached[dev]) {
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {

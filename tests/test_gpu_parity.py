@@ -419,3 +419,36 @@ def test_launches_without_programmatic_dependency_give_the_same_bits(precision, 
     assert sa.t == sn.t
     np.testing.assert_array_equal(a, n)
     np.testing.assert_array_equal(ab, nb)
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_FP32])
+def test_uploads_through_staging_give_the_same_bits(precision, monkeypatch):
+    """Where the device reads pageable host memory itself (Grace nodes), the
+    state and the set-up planes are read and converted by kernels straight
+    from host memory; SFLOW_HOST_READS=0 sends them through the staging
+    buffer and host conversion instead.  Both give the same device state,
+    so the same bits after 30 steps, for a handle and for submit_many."""
+    p, B, q = _pyro(settling=True, entrainment=True)
+    p.precision = precision
+    qa = W.to_aos(q)
+
+    def run():
+        s = L.Solver(p, B)
+        s.upload_q(qa)
+        s.advance(max_steps=30)
+        out = s.download_q()
+        s.close()
+        b = L.Batch(precision, max_runs=2, max_cells=1 << 20)
+        rid = b.submit_many([(p, B, qa, 0)])[0]
+        b.advance(30)
+        outb = b.collect(rid)
+        b.close()
+        return out, outb
+
+    direct = run()
+    monkeypatch.setenv("SFLOW_HOST_READS", "0")
+    staged = run()
+    np.testing.assert_array_equal(direct[0], staged[0])
+    np.testing.assert_array_equal(direct[1], staged[1])
+    if precision == PREC_FP64:
+        np.testing.assert_array_equal(direct[0], direct[1])   # handle and batch
