@@ -103,6 +103,20 @@ def test_fp64_variants_curvature_arc_rheology6_bcs():
     assert max(err) <= FP64_TOL, err
 
 
+@pytest.mark.parametrize("limiters", [(0, 0, 0, 0, 0, 0), (6, 7, 6, 7, 0, 6), (7, 6, 1, 0, 7, 2)])
+def test_fp64_first_order_and_one_sided_limiters(limiters):
+    """Limiter 0 (no reconstruction: first order), 6 and 7 (the forward and
+    backward differences, limit() of geometry_2d.f90) on the GPU against the
+    oracle, mixed per variable with the others."""
+    p, B, q = _pyro(nx=72, ny=64, dx=20.0, settling=True)
+    for i, lim in enumerate(limiters):
+        p.limiter[i] = lim
+    o, s = run_pair(p, B, q, 40)
+    err = rel_err(s.download_q(), o.q(), p.n_vars, p.comp_cells_x, p.comp_cells_y)
+    assert max(err) <= FP64_TOL, err
+    assert s.stats().status == o.stats().status == 0
+
+
 def test_fp64_dam_break_is_bitwise_equal():
     p, B, q = W.dam_break(nx=64, ny=48, t_end=100.0)
     o, s = run_pair(p, B, q, 40)
