@@ -23,6 +23,7 @@ struct sflow_batch {
 
 struct sflow_setup {
   HostSetup hs;
+  bool spent = false;   // its arrays went to a run (sflow_batch_submit_setup_take)
 };
 
 struct sflow_handle {
@@ -128,6 +129,7 @@ int sflow_batch_submit_setup(sflow_batch* b, const sflow_setup* s, const double*
                              int32_t* run_id) {
   BATCH_CHECK(b);
   if (!s || !q_aos || !run_id) return fail(SFLOW_EINVAL, "NULL argument");
+  if (s->spent) return fail(SFLOW_EINVAL, "the setup was handed to a run");
   if (s->hs.p.precision != b->precision) return fail(SFLOW_EINVAL, "run precision differs from the batch precision");
   int id = -1;
   HostSetup copy = s->hs;   // a setup can be submitted again
@@ -233,6 +235,22 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
   b->impl->set_bulk(false);
   for (auto& t : pool) t.join();
   if (first_rc != SFLOW_OK) return fail(first_rc, first_err);
+  return SFLOW_OK;
+}
+
+int sflow_batch_submit_setup_take(sflow_batch* b, sflow_setup* s, const double* q_aos, int64_t max_steps,
+                                  int32_t* run_id) {
+  BATCH_CHECK(b);
+  if (!s || !q_aos || !run_id) return fail(SFLOW_EINVAL, "NULL argument");
+  if (s->spent) return fail(SFLOW_EINVAL, "the setup was handed to a run");
+  if (s->hs.p.precision != b->precision) return fail(SFLOW_EINVAL, "run precision differs from the batch precision");
+  const size_t n = (size_t)s->hs.nx * s->hs.ny;
+  int id = -1;
+  const int rc = b->impl->submit(std::move(s->hs), q_aos, max_steps, &id);
+  // the arrays move into the run once admission passed (B is always set up)
+  if (rc == SFLOW_OK || s->hs.B.size() != n) s->spent = true;
+  if (rc < 0) return fail(rc, b->impl->error());
+  *run_id = id;
   return SFLOW_OK;
 }
 

@@ -102,6 +102,7 @@ def load(build_if_missing=True):
         "sflow_setup_create": (C.c_int, [P, dp, C.POINTER(vp)]),
         "sflow_setup_destroy": (None, [vp]),
         "sflow_batch_submit_setup": (C.c_int, [vp, vp, dp, i64, C.POINTER(i32)]),
+        "sflow_batch_submit_setup_take": (C.c_int, [vp, vp, dp, i64, C.POINTER(i32)]),
         "sflow_batch_submit_many": (C.c_int, [vp, i32, P, C.POINTER(dp), C.POINTER(dp), C.POINTER(i64),
                                                C.POINTER(i32), i32]),
         "sflow_batch_launch": (C.c_int, [vp, i64]),
@@ -151,7 +152,7 @@ def exported_symbols():
             "sflow_set_tile_shape", "sflow_get_tile_shape", "sflow_autotune",
             "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape", "sflow_check_conversions",
             "sflow_eval_math", "sflow_batch_advance_timed", "sflow_batch_profile_kernels",
-            "sflow_setup_create", "sflow_setup_destroy", "sflow_batch_submit_setup", "sflow_batch_submit_many",
+            "sflow_setup_create", "sflow_setup_destroy", "sflow_batch_submit_setup", "sflow_batch_submit_many", "sflow_batch_submit_setup_take",
             "sflow_batch_launch", "sflow_batch_wait", "sflow_batch_dry_border_updates",
             "sflow_dry_border_updates", "sflow_download_erosion", "sflow_download_erodible",
             "sflow_set_erodible", "sflow_download_topography", "sflow_set_nodata",
@@ -645,14 +646,18 @@ class Batch:
         self._shape[rid.value] = p.n_vars * p.comp_cells_x * p.comp_cells_y
         return rid.value
 
-    def submit_setup(self, setup, q_aos, max_steps=0):
-        """submit() of a run prepared as a Setup (the GPU part only)."""
+    def submit_setup(self, setup, q_aos, max_steps=0, take=False):
+        """submit() of a run prepared as a Setup (the GPU part only).  With
+        take=True the setup's host arrays move into the run (no copy) and an
+        admitted setup is spent (sflow_batch_submit_setup_take); a setup
+        that was not admitted (None) can be submitted again."""
         p = setup.p
         q = np.ascontiguousarray(q_aos, dtype=np.float64).reshape(-1)
         if q.size != p.n_vars * p.comp_cells_x * p.comp_cells_y:
             raise ValueError("q must have n_vars*nx*ny values")
         rid = C.c_int32(-1)
-        rc = self.lib.sflow_batch_submit_setup(self.h, setup.h, _dp(q), int(max_steps), C.byref(rid))
+        fn = self.lib.sflow_batch_submit_setup_take if take else self.lib.sflow_batch_submit_setup
+        rc = fn(self.h, setup.h, _dp(q), int(max_steps), C.byref(rid))
         if rc == EBUSY:
             return None
         _check(rc)

@@ -6,7 +6,8 @@ the host: sflow_setup_create, which needs no GPU), while the GPU advances
 the resident runs.  At every chunk boundary the loop admits the prepared
 requests in arrival order while the batch accepts them -- a free slot,
 tile-list capacity and free device memory, checked by
-sflow_batch_submit_setup, which answers SFLOW_EBUSY otherwise -- launches
+sflow_batch_submit_setup_take, which answers SFLOW_EBUSY otherwise and
+otherwise hands the prepared host arrays to the run without a copy -- launches
 `chunk` batch steps of every resident run (one CUDA-graph replay per
 solid-class count, the groups on their own streams; sflow_batch_launch
 returns at once), waits for the device (sflow_batch_wait; the worker
@@ -76,7 +77,7 @@ class RequestLoop:
                 while queue and queue[0][1].done():
                     r, fut = queue[0]
                     setup, prep_s = fut.result()
-                    bid = self.batch.submit_setup(setup, r.q_aos, max_steps=r.max_steps)
+                    bid = self.batch.submit_setup(setup, r.q_aos, max_steps=r.max_steps, take=True)
                     if bid is None:
                         if not live:
                             raise RuntimeError(f"request {r.rid} does not fit an empty batch")

@@ -413,6 +413,13 @@ int sflow_setup_create(const SflowParams* p, const double* B_cent, sflow_setup**
 void sflow_setup_destroy(sflow_setup* s);
 int sflow_batch_submit_setup(sflow_batch* b, const sflow_setup* s, const double* q_aos, int64_t max_steps,
                              int32_t* run_id);
+/* sflow_batch_submit_setup that hands the setup's host arrays over to the
+ * run instead of copying them (for a request loop that submits each setup
+ * once).  After SFLOW_OK the setup is spent: only sflow_setup_destroy may
+ * follow.  After SFLOW_EBUSY or an argument error it is unchanged and can
+ * be submitted again; after a device failure it is spent. */
+int sflow_batch_submit_setup_take(sflow_batch* b, sflow_setup* s, const double* q_aos, int64_t max_steps,
+                                  int32_t* run_id);
 /* n runs at once: params[i], B_cent[i], q_aos[i] and max_steps[i] (NULL:
  * no step limit) as for sflow_batch_submit.  The host set-ups run on
  * `threads` host threads (<= 0: the host's hardware threads, at most 64)

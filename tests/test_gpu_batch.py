@@ -397,3 +397,31 @@ def test_submit_many_without_room_returns_none():
     assert ids[0] is not None and ids[1] is not None and ids[2] is None
     assert b.submit_many([]) == []
     b.close()
+
+
+def test_submit_setup_take_hands_the_setup_over_once():
+    """sflow_batch_submit_setup_take: the run equals one submitted from a
+    copy of the setup (FP64: bitwise); a setup the batch could not admit
+    (EBUSY) stays usable; an admitted one is spent."""
+    p, B, q = _pyro(80, 64, 15.0, settling=True)
+    qa = W.to_aos(q)
+    ref = L.Batch(PREC_FP64, max_runs=2, max_cells=1 << 20)
+    rr = ref.submit(p, B, qa)
+    ref.advance(25)
+    b = L.Batch(PREC_FP64, max_runs=1, max_cells=1 << 20)
+    s1, s2 = L.Setup(p, B, precision=PREC_FP64), L.Setup(p, B, precision=PREC_FP64)
+    r1 = b.submit_setup(s1, qa, take=True)
+    assert r1 is not None
+    with pytest.raises(L.SflowError):
+        b.submit_setup(s1, qa, take=True)        # spent
+    assert b.submit_setup(s2, qa, take=True) is None   # no slot: s2 unchanged
+    b.advance(25)
+    np.testing.assert_array_equal(b.collect(r1), ref.collect(rr))
+    r2 = b.submit_setup(s2, qa, take=True)       # admitted now
+    assert r2 is not None
+    b.advance(25)
+    np.testing.assert_array_equal(b.collect(r2), _alone(p, B, q, 25, PREC_FP64)[0])
+    s1.close()
+    s2.close()
+    b.close()
+    ref.close()
