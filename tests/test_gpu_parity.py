@@ -14,7 +14,7 @@ import pytest
 import oracle
 from imex_sflow2d_dev_gb300 import lib as L
 from imex_sflow2d_dev_gb300 import workloads as W
-from imex_sflow2d_dev_gb300.params import (PREC_FP32, PREC_FP64, S_NAN, S_NEG_H, SflowStepStats)
+from imex_sflow2d_dev_gb300.params import (PREC_FP32, PREC_FP64, S_FATAL, S_NAN, S_NEG_H, SflowStepStats)
 
 pytestmark = pytest.mark.gpu
 
@@ -107,14 +107,45 @@ def test_fp64_variants_curvature_arc_rheology6_bcs():
 def test_fp64_first_order_and_one_sided_limiters(limiters):
     """Limiter 0 (no reconstruction: first order), 6 and 7 (the forward and
     backward differences, limit() of geometry_2d.f90) on the GPU against the
-    oracle, mixed per variable with the others."""
+    oracle, mixed per variable with the others.  The unlimited one-sided
+    slopes make this current unstable after ~25 steps (negative solid mass,
+    see the next test), so the comparison is at step 20."""
     p, B, q = _pyro(nx=72, ny=64, dx=20.0, settling=True)
     for i, lim in enumerate(limiters):
         p.limiter[i] = lim
-    o, s = run_pair(p, B, q, 40)
+    o, s = run_pair(p, B, q, 20)
     err = rel_err(s.download_q(), o.q(), p.n_vars, p.comp_cells_x, p.comp_cells_y)
     assert max(err) <= FP64_TOL, err
     assert s.stats().status == o.stats().status == 0
+
+
+def test_fp64_stops_where_the_oracle_first_fails():
+    """With forward / backward-difference slopes the current goes unstable:
+    the oracle first reports fatal status bits (negative solid mass, the
+    erosion-step check) at some step.  The GPU run stops after that same
+    step with the same bits and the same state (it advances no further)."""
+    p, B, q = _pyro(nx=72, ny=64, dx=20.0, settling=True)
+    for i, lim in enumerate((6, 7, 6, 7, 0, 6)):
+        p.limiter[i] = lim
+    o = oracle.Oracle(p, B)
+    o.set_q(W.to_aos(q))
+    n_fatal = None
+    for n in range(1, 61):
+        o.step()
+        if o.stats().status & S_FATAL:
+            n_fatal = n
+            break
+    assert n_fatal is not None
+    s = L.Solver(p, B)
+    s.upload_q(W.to_aos(q))
+    st = s.advance(max_steps=60)
+    so = o.stats()
+    assert st.status == so.status and st.status & S_FATAL
+    assert st.steps == so.steps == n_fatal and st.t == so.t
+    err = rel_err(s.download_q(), o.q(), p.n_vars, p.comp_cells_x, p.comp_cells_y)
+    assert max(err) <= FP64_TOL, err
+    s.close()
+    o.close()
 
 
 def test_fp64_dam_break_is_bitwise_equal():
