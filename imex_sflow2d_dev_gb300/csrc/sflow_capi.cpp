@@ -168,7 +168,9 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
         it.rc = SFLOW_EINVAL;
         it.err = "run precision differs from the batch precision";
       } else {
-        it.rc = sflow::host_setup(&params[i], B_cent[i], it.hs, it.err);
+        // topography terms on the device (Solver::init): the host part is
+        // then validation, inlet geometry and flags
+        it.rc = sflow::host_setup(&params[i], B_cent[i], it.hs, it.err, false);
       }
     } catch (const std::bad_alloc&) {
       it.hs = HostSetup();

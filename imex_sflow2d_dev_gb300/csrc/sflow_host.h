@@ -51,7 +51,11 @@ constexpr uint8_t kFlagNodata = 0x40;   // B_nodata cell
 constexpr uint8_t kFlagBottom = 0x80;   // cell fraction of the bottom source > 0
 
 // Validates p and fills s; returns 0 or SFLOW_EINVAL with a message in err.
-int host_setup(const SflowParams* p, const double* B_cent, HostSetup& s, std::string& err);
+// host_topography = false leaves the topography terms (Bx ... dgcy) empty:
+// the solver then derives them from B on the device (the same arithmetic,
+// operation by operation), which is how batched runs are set up in bulk.
+int host_setup(const SflowParams* p, const double* B_cent, HostSetup& s, std::string& err,
+               bool host_topography = true);
 // host_setup of the whole domain, then only rows k0 .. k0+rows-1 kept (every
 // derived field computed on the whole domain, so a slab's cells carry the
 // same topography terms, inlet geometry and flags as in the whole run);

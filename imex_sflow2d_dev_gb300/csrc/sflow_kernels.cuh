@@ -1151,30 +1151,22 @@ __global__ void __launch_bounds__(TileShape<TH>::FLUX_THREADS) k_flux(KArgs<R> a
 }
 
 // ---------------------------------------------------------------------------
-// k_topography: topography_reconstruction (geometry_2d.f90:555-895) after
-// the topography changed (TOPO_CHANGE_FLAG, IMEX_SfloW2D.f90:445): 5-point
-// centred slopes and curvatures of B on cells 3 .. n-2, the two-cell frame
-// copied from the nearest computed row / column (a clamped index), then the
-// slope factor and its derivatives.  FP64 with every product and sum
-// rounded on its own (the host's order), written to the topography planes
-// in R.  One thread per cell.
+// topography_reconstruction (geometry_2d.f90:555-895): 5-point centred
+// slopes and curvatures of B on cells 3 .. n-2, the two-cell frame copied
+// from the nearest computed row / column (a clamped index), then the slope
+// factor and its derivatives.  FP64 with every product and sum rounded on
+// its own (the host's order, sflow_setup.cpp), written to the topography
+// planes in R; B is a pitched FP64 plane.  One thread per cell.
 // ---------------------------------------------------------------------------
 template <class R>
-__global__ void __launch_bounds__(256) k_topography(KArgs<R> a) {
-  step_kernel_entry();
-  const Grid<R>& g = a.g;
-  if (!a.st->run_step) return;
-  const int64_t n = (int64_t)g.nx * g.ny;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int j = (int)(i % g.nx), k = (int)(i / g.nx);
-  const int jj = j < 2 ? 2 : (j > g.nx - 3 ? g.nx - 3 : j);
-  const int kk = g.ny == 1 ? 0 : (k < 2 ? 2 : (k > g.ny - 3 ? g.ny - 3 : k));
+__device__ __forceinline__ void topography_cell(const double* __restrict__ B, int nx, int ny, int64_t pitch,
+                                                double dx, double dy, bool slope_corr, R* const* geo,
+                                                int j, int k, int64_t c) {
+  const int jj = j < 2 ? 2 : (j > nx - 3 ? nx - 3 : j);
+  const int kk = ny == 1 ? 0 : (k < 2 ? 2 : (k > ny - 3 ? ny - 3 : k));
   const double c1[5] = {-2.0, -1.0, 0.0, 1.0, 2.0};
   const double c2[5] = {2.0, -1.0, -2.0, -1.0, 2.0};
-  const double dx = g.dx, dy = g.dy;
-  const double* B = a.Bc;
-  auto Bat = [&](int x, int y) { return B[cidx(g, x, y)]; };
+  auto Bat = [&](int x, int y) { return B[(int64_t)y * pitch + x]; };
   double px = 0.0, py = 0.0, sxx = 0.0, syy = 0.0, ws = 0.0;
   for (int m = 0; m < 5; ++m) {
     px = __dadd_rn(px, __dmul_rn(c1[m], Bat(jj + m - 2, kk)));
@@ -1183,7 +1175,7 @@ __global__ void __launch_bounds__(256) k_topography(KArgs<R> a) {
   double bx, by, bxx, byy, bxy;
   bx = __ddiv_rn(px, __dmul_rn(10.0, dx));
   bxx = __ddiv_rn(sxx, __dmul_rn(7.0, __dmul_rn(dx, dx)));
-  if (g.ny == 1) {
+  if (ny == 1) {
     by = __ddiv_rn(0.0, __dmul_rn(10.0, dy));
     byy = __ddiv_rn(0.0, __dmul_rn(7.0, __dmul_rn(dy, dy)));
     bxy = 0.0;
@@ -1198,12 +1190,10 @@ __global__ void __launch_bounds__(256) k_topography(KArgs<R> a) {
     byy = __ddiv_rn(syy, __dmul_rn(7.0, __dmul_rn(dy, dy)));
     bxy = __ddiv_rn(ws, __dmul_rn(__dmul_rn(10.0, dx), __dmul_rn(10.0, dy)));
   }
-  const int64_t c = cidx(g, j, k);
-  R* const* geo = const_cast<R* const*>(a.geo);
   geo[0][c] = (R)bx;
   geo[1][c] = (R)by;
   if (geo[2]) { geo[2][c] = (R)bxx; geo[3][c] = (R)bxy; geo[4][c] = (R)byy; }
-  if (a.pd.slope_corr) {
+  if (slope_corr) {
     const double gc = __ddiv_rn(1.0, __dadd_rn(__dadd_rn(1.0, __dmul_rn(bx, bx)), __dmul_rn(by, by)));
     const double gc2 = __dmul_rn(-2.0, __dmul_rn(gc, gc));
     geo[5][c] = (R)gc;
@@ -1212,6 +1202,47 @@ __global__ void __launch_bounds__(256) k_topography(KArgs<R> a) {
   }
 }
 
+// after the topography changed (TOPO_CHANGE_FLAG, IMEX_SfloW2D.f90:445)
+template <class R>
+__global__ void __launch_bounds__(256) k_topography(KArgs<R> a) {
+  step_kernel_entry();
+  const Grid<R>& g = a.g;
+  if (!a.st->run_step) return;
+  const int64_t n = (int64_t)g.nx * g.ny;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j = (int)(i % g.nx), k = (int)(i / g.nx);
+  topography_cell<R>(a.Bc, g.nx, g.ny, g.pitch, (double)g.dx, (double)g.dy, a.pd.slope_corr,
+                     const_cast<R* const*>(a.geo), j, k, cidx(g, j, k));
+}
+
+// the eight topography planes (Bx, By, Bxx, Bxy, Byy, gc, dgcx, dgcy; the
+// curvature ones null without the curvature term) as a kernel argument
+template <class R>
+struct TopoPlanes {
+  R* p[8];
+};
+
+// at creation, from B in a pitched FP64 plane: the slope factor is 1 and its
+// derivatives 0 without the slope correction (the host's initial values)
+template <class R>
+__global__ void __launch_bounds__(256) k_topography_setup(const double* __restrict__ B, int nx, int ny,
+                                                          int64_t pitch, double dx, double dy, int slope_corr,
+                                                          TopoPlanes<R> geo) {
+  const int64_t n = (int64_t)nx * ny;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j = (int)(i % nx), k = (int)(i / nx);
+  const int64_t c = (int64_t)k * pitch + j;
+  topography_cell<R>(B, nx, ny, pitch, dx, dy, slope_corr != 0, geo.p, j, k, c);
+  if (!slope_corr) {
+    geo.p[5][c] = R(1);
+    geo.p[6][c] = R(0);
+    geo.p[7][c] = R(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // The physical variables of a cell's current state, kept between the
 // assembly fixes, the erosion/deposition step and the post-step maxima of
 // one step so that qc_to_qp of an unchanged state is not evaluated again

@@ -296,7 +296,7 @@ static void cell_fractions(HostSetup& s) {
   }
 }
 
-int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::string& err) {
+int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::string& err, bool host_topography) {
   if (!pin) { err = "params is NULL"; return SFLOW_EINVAL; }
   s.p = *pin;
   SflowParams& p = s.p;
@@ -445,7 +445,7 @@ int host_setup(const SflowParams* pin, const double* B, HostSetup& s, std::strin
   }
 
   if (!B) { err = "B_cent is NULL"; return SFLOW_EINVAL; }
-  topography(s, B);
+  if (host_topography) topography(s, B);
   s.B.assign(B, B + (size_t)s.nx * s.ny);
 
   // inlet (radial ring / bottom source) constants

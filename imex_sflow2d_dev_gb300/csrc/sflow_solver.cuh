@@ -181,7 +181,6 @@ class Solver : public SolverBase {
     SFLOW_CU(alloc((void**)&q_, sizeof(R) * plane_ * nv));
     const int nstage = (hs_.nrk == 2) ? 1 : hs_.nrk;
     SFLOW_CU(alloc((void**)&rd_, sizeof(R) * plane_ * nv * nstage));
-    SFLOW_CU(cudaMemset(rd_, 0, sizeof(R) * plane_ * nv * nstage));
     if (hs_.nrk != 2) {
       SFLOW_CU(alloc((void**)&rn_, sizeof(R) * plane_ * nv * nstage));
       SFLOW_CU(cudaMemset(rn_, 0, sizeof(R) * plane_ * nv * nstage));
@@ -190,11 +189,28 @@ class Solver : public SolverBase {
     }
     for (int i = 0; i < 8; ++i) geo_[i] = nullptr;
     const std::vector<double>* gsrc[8] = {&hs_.Bx, &hs_.By, &hs_.Bxx, &hs_.Bxy, &hs_.Byy, &hs_.gc, &hs_.dgcx, &hs_.dgcy};
+    const bool device_topo = hs_.Bx.empty();
     for (int i = 0; i < 8; ++i) {
       if ((i >= 2 && i <= 4) && !hs_.p.curvature_term_flag) continue;
       SFLOW_CU(alloc((void**)&geo_[i], sizeof(R) * plane_));
-      SFLOW_CU(put_plane(geo_[i], *gsrc[i]));
+      if (!device_topo) SFLOW_CU(put_plane(geo_[i], *gsrc[i]));
     }
+    if (device_topo) {
+      // B (pitched FP64) in the stage-residual buffer, which is cleared
+      // right after: sizeof(R) * nv >= 8 bytes per cell
+      if (hs_.B.size() != (size_t)nx * ny) { err_ = "set-up without topography"; return SFLOW_EINVAL; }
+      double* Bp = reinterpret_cast<double*>(rd_);
+      SFLOW_CU(cudaMemcpy2DAsync(Bp, sizeof(double) * pitch_, hs_.B.data(), sizeof(double) * nx,
+                                 sizeof(double) * nx, ny, cudaMemcpyHostToDevice, stream_));
+      TopoPlanes<R> tp;
+      for (int i = 0; i < 8; ++i) tp.p[i] = geo_[i];
+      const int64_t n = (int64_t)nx * ny;
+      k_topography_setup<R><<<(unsigned)((n + 255) / 256), 256, 0, stream_>>>(
+          Bp, nx, ny, (int64_t)pitch_, hs_.dx, hs_.dy, hs_.p.slope_correction_flag ? 1 : 0, tp);
+      ++launches_;
+      SFLOW_CU(cudaGetLastError());
+    }
+    SFLOW_CU(cudaMemsetAsync(rd_, 0, sizeof(R) * plane_ * nv * nstage, stream_));
     SFLOW_CU(alloc((void**)&cflags_, plane_));
     SFLOW_CU(put_flags());
     SFLOW_CU(alloc((void**)&arc_, sizeof(R) * plane_ * 3));
@@ -1190,6 +1206,16 @@ class Solver : public SolverBase {
   cudaError_t reset_topography() {
     cudaError_t e = cudaStreamSynchronize(stream_);
     if (e == cudaSuccess) e = put_plane_d(Bc_, hs_.B);
+    if (e == cudaSuccess && hs_.Bx.empty()) {
+      // a set-up without host topography terms: derive them from Bc_
+      TopoPlanes<R> tp;
+      for (int i = 0; i < 8; ++i) tp.p[i] = geo_[i];
+      const int64_t n = (int64_t)hs_.nx * hs_.ny;
+      k_topography_setup<R><<<(unsigned)((n + 255) / 256), 256, 0, stream_>>>(
+          Bc_, hs_.nx, hs_.ny, (int64_t)pitch_, hs_.dx, hs_.dy, hs_.p.slope_correction_flag ? 1 : 0, tp);
+      ++launches_;
+      return cudaGetLastError();
+    }
     const std::vector<double>* gsrc[8] = {&hs_.Bx, &hs_.By, &hs_.Bxx, &hs_.Bxy, &hs_.Byy, &hs_.gc, &hs_.dgcx, &hs_.dgcy};
     for (int i = 0; i < 8 && e == cudaSuccess; ++i)
       if (geo_[i]) e = put_plane(geo_[i], *gsrc[i]);

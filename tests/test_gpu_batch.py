@@ -353,16 +353,22 @@ def test_memory_limit_hook_gives_ebusy():
     b.close()
 
 
-@pytest.mark.parametrize("threads", [1, 4, 0])
-def test_submit_many_equals_sequential_submits(threads):
-    """sflow_batch_submit_many (host set-ups on worker threads, uploads in
-    order) admits the runs a sequential submit would, with the same results
-    (FP64 form: bitwise)."""
+@pytest.mark.parametrize("threads,precision", [(1, PREC_FP64), (4, PREC_FP64), (0, PREC_FP64), (0, PREC_FP32)])
+def test_submit_many_equals_sequential_submits(threads, precision):
+    """sflow_batch_submit_many (host set-ups on worker threads, the
+    topography terms derived on the device, uploads in order) admits the
+    runs a sequential submit (topography terms from the host) would, with
+    the same results bit for bit: the device repeats the host's topography
+    arithmetic operation by operation, and both forms run the same batch
+    kernels."""
     runs = _mix()
-    ref = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 22)
+    pc, Bc, qc = _pyro(72, 64, 20.0, settling=False)
+    pc.curvature_term_flag = 1           # the curvature planes too
+    runs.append((pc, Bc, qc))
+    ref = L.Batch(precision, max_runs=8, max_cells=1 << 22)
     rids = [ref.submit(p, B, W.to_aos(q), max_steps=30) for p, B, q in runs]
     ref.advance(40)
-    b = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 22)
+    b = L.Batch(precision, max_runs=8, max_cells=1 << 22)
     ids = b.submit_many([(p, B, W.to_aos(q), 30) for p, B, q in runs], threads=threads)
     assert all(i is not None for i in ids)
     b.advance(40)
