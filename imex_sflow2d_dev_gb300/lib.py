@@ -752,15 +752,24 @@ class Batch:
         _check(self.lib.sflow_batch_counters(self.h, rid, C.byref(a), C.byref(b)))
         return {"cell_updates": a.value, "steps": b.value}
 
-    def download(self, rid):
-        out = np.empty(self._shape[rid])
+    def download(self, rid, out=None):
+        """The run's q (reference layout), into `out` when given (a float64
+        array of the run's size, e.g. a view of pinned host memory)."""
+        out = self._out(rid, out)
         _check(self.lib.sflow_batch_download(self.h, rid, _dp(out)))
         return out
 
-    def collect(self, rid, want_q=True):
-        out = np.empty(self._shape[rid]) if want_q else None
+    def collect(self, rid, want_q=True, out=None):
+        out = self._out(rid, out) if want_q else None
         _check(self.lib.sflow_batch_collect(self.h, rid, _dp(out) if want_q else None))
         del self._shape[rid]
+        return out
+
+    def _out(self, rid, out):
+        if out is None:
+            return np.empty(self._shape[rid])
+        if out.dtype != np.float64 or out.size != self._shape[rid] or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float64 array of the run's size")
         return out
 
     def live(self):
