@@ -443,19 +443,23 @@ def ensemble_e2e(lib, members, K, chunk, tile_h):
     ids = b.submit_many([(p, B, qa, st) for (p, B, _, st), qa in zip(members, qs)])
     if any(rid is None for rid in ids):
         raise RuntimeError("ensemble member not admitted")
+    t1 = time.perf_counter()
     for _ in range(K):
         b.advance(chunk)
+    t2 = time.perf_counter()
     cu = 0
     out_bytes = 0
     for rid, o in zip(ids, outs):
         cu += b.counters(rid)["cell_updates"]
         q = b.collect(rid, want_q=True, out=o)
         out_bytes += q.nbytes
-    wall = time.perf_counter() - t0
+    t3 = time.perf_counter()
+    wall = t3 - t0
     b.close()
     in_bytes = sum(qa.nbytes + B.size * 8 for (p, B, _, _), qa in zip(members, qs))
     return {"value": cu / wall, "unit": UNIT, "h2d_bytes_per_step": in_bytes / K,
             "d2h_bytes_per_step": out_bytes / K, "seconds": wall, "steps": K,
+            "split_s": {"submit": t1 - t0, "steps": t2 - t1, "collect": t3 - t2},
             "path": "sflow_batch_submit_many (host set-ups on the host's threads, uploads in order) of "
                     "every run, sflow_batch_advance, sflow_batch_collect with q download; q in and out "
                     "through pinned host buffers, topography from pageable host arrays; wall clock",
