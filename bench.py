@@ -802,17 +802,18 @@ def run_gb300(args, d):
             p, B = members64[k][0], members64[k][1]
             err_oracle.append(field_errors(p, qp_of_state(p, B, q32[k]), qp_of_state(p, B, orc[k])))
             err_fp64.append(float(np.abs(q64[k] - orc[k]).max() / max(np.abs(orc[k]).max(), 1e-300)))
+
+    # e2e through the C ABI from host buffers
+    e2e = ensemble_e2e(lib, members32, K, chunk, th)
+    log(f"ensemble e2e {e2e['value']:.3e}")
+
     # members above the h bar: the oracle's own FP32 rounding band (spawned
-    # processes, while the GPU runs the e2e and profile legs)
+    # processes, while the GPU runs the legs below)
     over = [k for k, e in zip(err_members, err_oracle) if e["h"]["l1_rel"] > H_L1_BAR]
     band_res = None
     if over:
         pool = mp.get_context("spawn").Pool(processes=len(over))
         band_res = pool.map_async(_band_member_worker, over)
-
-    # e2e through the C ABI from host buffers
-    e2e = ensemble_e2e(lib, members32, K, chunk, th)
-    log(f"ensemble e2e {e2e['value']:.3e}")
 
     # per-kernel device times of the developed ensemble and the roofline of
     # its dominant kernel (algorithmic bytes per computed cell: the dry
