@@ -1166,12 +1166,15 @@ class Solver : public SolverBase {
     return cudaMemcpy(dst, buf.data(), sizeof(R) * plane_, cudaMemcpyHostToDevice);
   }
 
+  // the flag bytes into their pitched plane (pad columns zero), in order
+  // with the run's stream and finished on return
   cudaError_t put_flags() {
     const int nx = hs_.nx, ny = hs_.ny;
-    std::vector<uint8_t> f((size_t)plane_, 0);
-    for (int k = 0; k < ny; ++k)
-      for (int j = 0; j < nx; ++j) f[(size_t)k * pitch_ + j] = hs_.cflags[(size_t)k * nx + j];
-    return cudaMemcpy(cflags_, f.data(), plane_, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemsetAsync(cflags_, 0, plane_, stream_);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(cflags_, pitch_, hs_.cflags.data(), nx, nx, ny, cudaMemcpyHostToDevice, stream_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+    return e;
   }
   cudaError_t put_plane_d(double* dst, const std::vector<double>& src) {
     std::vector<double> buf((size_t)plane_, 0.0);
