@@ -235,8 +235,11 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
 // the ring flag, four pointers), so they come straight from the argument
 // table in global memory (L1-cached) instead of a shared-memory copy of the
 // whole KArgs per run change: candidate lists interleave the runs' tiles.
+// Compiled for 8 resident blocks per SM (32 x 8 tiles: 64 warps, the
+// SM's limit): more candidate tiles' frame loads in flight; measured 9 %
+// faster than the 6 blocks the registers allowed unbounded.
 template <class R, int TH>
-__global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
+__global__ void __launch_bounds__(TileShape<TH>::MASK_THREADS, 2048 / TileShape<TH>::MASK_THREADS) k_b_mask(BatchArgs<R> b) {
   __shared__ unsigned s_idx[2];
   step_kernel_entry();
   BatchCtl* ctl = b.ctl;
