@@ -15,6 +15,7 @@
 
 #include <cstdlib>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -29,7 +30,12 @@ class Batch : public BatchBase {
   static constexpr int kChunk = 16;
   static constexpr int kStepLaunches = 5;   // k_b_cand, k_b_mask, k_b_flux, k_b_dt, k_b_stage2
 
-  Batch(int max_runs, int64_t max_tiles) : max_runs_(max_runs), max_tiles_(max_tiles) {}
+  Batch(int max_runs, int64_t max_tiles) : max_runs_(max_runs), max_tiles_(max_tiles) {
+    if (cudaGetDevice(&dev_) != cudaSuccess) {
+      cudaGetLastError();
+      dev_ = 0;
+    }
+  }
   ~Batch() override {
     for (auto& g : groups_)
       if (g) g->release();
@@ -44,86 +50,111 @@ class Batch : public BatchBase {
   }
   std::string err_;
 
-  int submit(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* id) override {
-    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
-    if (hs.nrk != 2) { err_ = "batched runs use the N_RK = 2 tableau"; return SFLOW_EINVAL; }
-    if (hs.ns < kMinSolidBuilt || hs.ns > kMaxSolidBuilt) { err_ = "n_solid out of range"; return SFLOW_EINVAL; }
+  // A run's device state built off the batch's tables (sflow_batch_submit
+  // builds it in place; sflow_batch_submit_many on its worker threads).
+  struct Prepared : PreparedRun {
+    std::unique_ptr<Solver<R>> sv;
+    uint32_t* cand = nullptr;      // per-tile candidate flags (zeroed)
+    uint8_t* tile_seed = nullptr;  // per-tile seed flags
+    int64_t tiles = 0;
+    int ns = 0;
+    double max_dt = 0.0;
+    ~Prepared() override {
+      if (cand) cudaFree(cand);
+      if (tile_seed) cudaFree(tile_seed);
+    }
+  };
+
+  // what a run must satisfy whatever the batch holds
+  int check_run(const HostSetup& hs, std::string& err) const {
+    if (hs.nrk != 2) { err = "batched runs use the N_RK = 2 tableau"; return SFLOW_EINVAL; }
+    if (hs.ns < kMinSolidBuilt || hs.ns > kMaxSolidBuilt) { err = "n_solid out of range"; return SFLOW_EINVAL; }
     if (hs.p.erosion_coeff != 0.0 || hs.p.bottom_radial_source_flag || hs.n_thk * hs.n_dyn > 0) {
       // their per-step work (source factors, topography) and results
       // (erosion, vulnerability table) belong to the single-run solver
-      err_ = "erosion, the bottom radial source and the vulnerability table run on the single-run solver";
+      err = "erosion, the bottom radial source and the vulnerability table run on the single-run solver";
       return SFLOW_EINVAL;
     }
-    Group* g = group(hs.ns);
+    return SFLOW_OK;
+  }
+  int64_t run_tiles(const HostSetup& hs) const {
+    return (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + tile_h_ - 1) / tile_h_);
+  }
+  static int64_t run_need(const HostSetup& hs, int tile_h) {
+    return Solver<R>::batch_bytes(hs, tile_h) +
+           (int64_t)sizeof(double) * hs.nx * hs.ny * (hs.nv + 3);   // staging, freed after upload
+  }
+
+  // Builds the run's device state: solver, upload of q, limits, the
+  // candidate and seed flags.  Touches no table of the batch, so worker
+  // threads may run it for different runs at once.
+  std::unique_ptr<Prepared> build(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* rc,
+                                  std::string& err) const {
+    std::unique_ptr<Prepared> pr(new Prepared());
+    pr->ns = hs.ns;
+    pr->max_dt = hs.p.max_dt;
+    pr->tiles = run_tiles(hs);
+    const double t_end = hs.p.t_end;
+    pr->sv.reset(new Solver<R>(std::move(hs), tile_h_));
+    Solver<R>& sv = *pr->sv;
+    *rc = sv.init();
+    if (*rc == SFLOW_OK) *rc = sv.upload(q_aos);
+    if (*rc == SFLOW_OK) *rc = sv.limits(t_end, max_steps > 0 ? max_steps : -1);
+    if (*rc != SFLOW_OK) {
+      err = sv.err_;
+      return nullptr;
+    }
+    sv.trim_stage();
+    const std::vector<uint8_t> ts = sv.tile_seed_host();
+    if (cudaMalloc((void**)&pr->cand, sizeof(uint32_t) * pr->tiles) != cudaSuccess ||
+        cudaMalloc((void**)&pr->tile_seed, ts.size()) != cudaSuccess) {
+      cudaGetLastError();
+      *rc = SFLOW_ENOMEM;
+      err = "cudaMalloc failed";
+      return nullptr;
+    }
+    if (cudaMemsetAsync(pr->cand, 0, sizeof(uint32_t) * pr->tiles, sv.stream()) != cudaSuccess ||
+        cudaMemcpyAsync(pr->tile_seed, ts.data(), ts.size(), cudaMemcpyHostToDevice, sv.stream()) != cudaSuccess ||
+        cudaStreamSynchronize(sv.stream()) != cudaSuccess) {
+      *rc = SFLOW_ECUDA;
+      err = "cudaMemcpy failed";
+      return nullptr;
+    }
+    return pr;
+  }
+
+  // The run joins the batch: a free slot, list capacity and the memory
+  // limit are checked, then its arguments go into the device tables.
+  int admit(std::unique_ptr<Prepared> pr, int* id) {
+    Group* g = group(pr->ns);
     if (!g) return SFLOW_ECUDA;
     int slot = -1;
     for (int i = 0; i < max_runs_; ++i)
       if (!g->slots[i].solver) { slot = i; break; }
     if (slot < 0) { err_ = "no free run slot"; return SFLOW_EBUSY; }
-    const int64_t tiles = (int64_t)((hs.nx + TX - 1) / TX) * ((hs.ny + tile_h_ - 1) / tile_h_);
+    const int64_t tiles = pr->tiles;
     if (g->tiles_live + g->tiles_draining + tiles > max_tiles_) {
       err_ = "tile-list capacity of the batch is in use";
       return SFLOW_EBUSY;
     }
-    const int64_t need = Solver<R>::batch_bytes(hs, tile_h_) +
-                         (int64_t)sizeof(double) * hs.nx * hs.ny * (hs.nv + 3);   // staging, freed after upload
-    // free device memory: queried at every submit, or tracked across a bulk
-    // admission (re-queried every 32 admissions and near the need)
-    if (!bulk_ || !free_known_ || since_query_ >= 32 || free_est_ < need + kReserve + (int64_t(4) << 30)) {
-      size_t free_b = 0, total_b = 0;
-      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
-      free_est_ = (int64_t)free_b;
-      free_known_ = bulk_;
-      since_query_ = 0;
-    }
-    if (free_est_ < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
-    if (mem_limit_ > 0 && held_ + need > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
-
-    const int ns = hs.ns;
-    const double t_end = hs.p.t_end, max_dt = hs.p.max_dt;
-    std::unique_ptr<Solver<R>> sv(new Solver<R>(std::move(hs), tile_h_));
-    int rc = sv->init();
-    if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
-    rc = sv->upload(q_aos);
-    if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
-    rc = sv->limits(t_end, max_steps > 0 ? max_steps : -1);
-    if (rc != SFLOW_OK) { err_ = sv->err_; return rc; }
-    sv->trim_stage();
-    uint32_t* cand = nullptr;
-    if (cudaMalloc((void**)&cand, sizeof(uint32_t) * tiles) != cudaSuccess) { err_ = "cudaMalloc failed"; return SFLOW_ENOMEM; }
-    if (cudaMemset(cand, 0, sizeof(uint32_t) * tiles) != cudaSuccess) {
-      cudaFree(cand);
-      err_ = "cudaMemset failed";
-      return SFLOW_ECUDA;
-    }
-    uint8_t* tile_seed = nullptr;
-    {
-      const std::vector<uint8_t> ts = sv->tile_seed_host();
-      if (cudaMalloc((void**)&tile_seed, ts.size()) != cudaSuccess) { cudaFree(cand); err_ = "cudaMalloc failed"; return SFLOW_ENOMEM; }
-      if (cudaMemcpy(tile_seed, ts.data(), ts.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
-        cudaFree(cand);
-        cudaFree(tile_seed);
-        err_ = "cudaMemcpy failed";
-        return SFLOW_ECUDA;
-      }
-    }
+    Solver<R>& sv = *pr->sv;
+    const int64_t bytes = sv.device_bytes() + (int64_t)sizeof(uint32_t) * tiles + tiles;
+    if (mem_limit_ > 0 && held_ + bytes > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
+    if (g->smem_flux < sv.smem_flux()) { err_ = "flux shared memory mismatch"; return SFLOW_EINVAL; }
     Slot& s = g->slots[slot];
-    s.gen = (s.gen + 1u) & 0xffffu;
-    s.cand = cand;
-    s.tile_seed = tile_seed;
-    s.tiles = tiles;
+    const unsigned gen = (s.gen + 1u) & 0xffffu;
     BatchRun br;
-    br.st = sv->state_dev();
-    br.cand = cand;
-    br.tile_wet = sv->tile_wet_dev();
-    br.tile_count = sv->tile_count_dev();
-    br.tile_seed = tile_seed;
-    br.tiles_x = sv->tiles_x();
-    br.tiles_y = sv->tiles_y();
-    br.gen = s.gen;
+    br.st = sv.state_dev();
+    br.cand = pr->cand;
+    br.tile_wet = sv.tile_wet_dev();
+    br.tile_count = sv.tile_count_dev();
+    br.tile_seed = pr->tile_seed;
+    br.tiles_x = sv.tiles_x();
+    br.tiles_y = sv.tiles_y();
+    br.gen = gen;
     br.live = 1;
-    br.max_dt = max_dt;
-    const KArgs<R> ka = sv->kargs();
+    br.max_dt = pr->max_dt;
+    const KArgs<R> ka = sv.kargs();
     if (ka.g.lim_all != 1 && g->lim == 1) {
       // the group needs the generic limiter kernel from now on: re-capture
       g->lim = -1;
@@ -132,36 +163,106 @@ class Batch : public BatchBase {
       g->graph_exec = nullptr;
       g->graph = nullptr;
     }
-    if (g->smem_flux < sv->smem_flux()) { err_ = "flux shared memory mismatch"; cudaFree(cand); return SFLOW_EINVAL; }
     // the batch stream is idle here (every advance ends synchronised)
     if (cudaMemcpy(g->d_args + slot, &ka, sizeof(ka), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(g->d_runs + slot, &br, sizeof(br), cudaMemcpyHostToDevice) != cudaSuccess) {
-      cudaFree(cand);
       err_ = "cudaMemcpy failed";
       return SFLOW_ECUDA;
     }
-    cudaError_t e = g->tab.b_admit(g->args, g->stream, slot, s.gen, (unsigned)tiles);
+    cudaError_t e = g->tab.b_admit(g->args, g->stream, slot, gen, (unsigned)tiles);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) { err_ = cudaGetErrorString(e); return SFLOW_ECUDA; }
     ++g->launches;
-    s.bytes = sv->device_bytes() + (int64_t)sizeof(uint32_t) * tiles + tiles;
+    s.gen = gen;
+    s.cand = pr->cand;
+    s.tile_seed = pr->tile_seed;
+    pr->cand = nullptr;
+    pr->tile_seed = nullptr;
+    s.tiles = tiles;
+    s.bytes = bytes;
     held_ += s.bytes;
-    free_est_ -= s.bytes;
-    ++since_query_;
-    s.solver = std::move(sv);
+    s.solver = std::move(pr->sv);
     s.done = false;
     g->tiles_live += tiles;
     g->live += 1;
     const int rid = (int)recs_.size();
-    recs_.push_back(Rec{ns, slot, true});
+    recs_.push_back(Rec{pr->ns, slot, true});
     s.rec = rid;
     *id = rid;
     return SFLOW_OK;
   }
 
+  int submit(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* id) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
+    int rc = check_run(hs, err_);
+    if (rc != SFLOW_OK) return rc;
+    // admission before anything is allocated: slot, list capacity, memory
+    Group* g = group(hs.ns);
+    if (!g) return SFLOW_ECUDA;
+    bool free_slot = false;
+    for (int i = 0; i < max_runs_ && !free_slot; ++i) free_slot = !g->slots[i].solver;
+    if (!free_slot) { err_ = "no free run slot"; return SFLOW_EBUSY; }
+    if (g->tiles_live + g->tiles_draining + run_tiles(hs) > max_tiles_) {
+      err_ = "tile-list capacity of the batch is in use";
+      return SFLOW_EBUSY;
+    }
+    const int64_t need = run_need(hs, tile_h_);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
+    if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
+    if (mem_limit_ > 0 && held_ + need > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
+    std::unique_ptr<Prepared> pr = build(std::move(hs), q_aos, max_steps, &rc, err_);
+    if (!pr) return rc;
+    return admit(std::move(pr), id);
+  }
+
+  // sflow_batch_submit_many: prepare() on worker threads (each bound to the
+  // batch's device), commit() in run order on the submitting thread.  A
+  // worker builds a run only while the device has room for it (free memory
+  // minus the reserve), so runs built ahead never exhaust the device.
+  std::unique_ptr<PreparedRun> prepare(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* rc,
+                                       std::string* err) override {
+    *rc = check_run(hs, *err);
+    if (*rc != SFLOW_OK) return nullptr;
+    *rc = reserve_room(run_need(hs, tile_h_), *err);
+    if (*rc != SFLOW_OK) return nullptr;
+    return build(std::move(hs), q_aos, max_steps, rc, *err);
+  }
+  int commit(std::unique_ptr<PreparedRun> pr, int* id) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
+    std::unique_ptr<Prepared> p(static_cast<Prepared*>(pr.release()));
+    return admit(std::move(p), id);
+  }
+  void bind_thread() override { cudaSetDevice(dev_); }
+
+  // Room on the device for a run built by prepare(): the free memory is
+  // queried once per bulk submission, every 32 builds and whenever the
+  // estimate nears the need; each build takes its need off the estimate.
+  int reserve_room(int64_t need, std::string& err) {
+    std::lock_guard<std::mutex> lk(room_mu_);
+    if (room_free_ < 0 || room_since_ >= 32 || room_free_ < need + kReserve + (int64_t(4) << 30)) {
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        err = "cudaMemGetInfo failed";
+        return SFLOW_ECUDA;
+      }
+      room_free_ = (int64_t)free_b;
+      room_since_ = 0;
+    }
+    if (room_free_ < need + kReserve) {
+      err = "not enough free device memory for the run now";
+      return SFLOW_EBUSY;
+    }
+    room_free_ -= need;
+    ++room_since_;
+    return SFLOW_OK;
+  }
+
   void set_bulk(bool on) override {
-    bulk_ = on;
-    free_known_ = false;
+    std::lock_guard<std::mutex> lk(room_mu_);
+    (void)on;
+    room_free_ = -1;   // a new bulk submission queries afresh
   }
 
   int advance(int64_t steps, int* finished) override { return advance_impl(steps, finished, nullptr); }
@@ -426,10 +527,9 @@ class Batch : public BatchBase {
   static constexpr int64_t kReserve = (int64_t)1 << 30;   // device memory kept free
   int64_t mem_limit_ = 0;   // cap on the resident runs' device bytes (0: none)
   int64_t held_ = 0;        // device bytes of the resident runs
-  bool bulk_ = false;       // inside sflow_batch_submit_many
-  bool free_known_ = false; // free_est_ holds a query of this bulk admission
-  int64_t free_est_ = 0;    // free device memory (last query minus admitted runs since)
-  int since_query_ = 0;     // admissions since that query
+  std::mutex room_mu_;      // reserve_room(), called by prepare() on worker threads
+  int64_t room_free_ = -1;  // free device memory: last query minus the needs built since (-1: query)
+  int room_since_ = 0;      // builds since that query
 
   struct Slot {
     std::unique_ptr<Solver<R>> solver;
@@ -568,6 +668,7 @@ class Batch : public BatchBase {
 
   int max_runs_;
   int64_t max_tiles_;
+  int dev_ = 0;                      // the device the batch lives on
   int tile_h_ = kTileHDefault;
   cudaStream_t tstream_ = nullptr;   // timing stream of advance_timed
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evg_[kMaxSolidBuilt + 1] = {};

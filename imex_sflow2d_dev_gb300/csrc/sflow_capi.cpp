@@ -151,9 +151,10 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
   nt = std::min(std::max(1, std::min(nt, 64)), (int)n);
   const int window = 2 * nt;
 
-  // set-ups made by the workers in place, taken in run order by this thread
+  // Each run is set up on the host and built on the device by a worker
+  // (BatchBase::prepare), then admitted in run order by this thread.
   struct Item {
-    HostSetup hs;
+    std::unique_ptr<sflow::PreparedRun> run;
     int rc = SFLOW_OK;
     std::string err;
     bool ready = false;
@@ -161,6 +162,7 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
   std::vector<Item> items((size_t)n);
   auto make = [&](int i, Item& it) {
     try {
+      HostSetup hs;
       if (!B_cent[i] || !q_aos[i]) {
         it.rc = SFLOW_EINVAL;
         it.err = "NULL argument";
@@ -169,11 +171,15 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
         it.err = "run precision differs from the batch precision";
       } else {
         // topography terms on the device (Solver::init): the host part is
-        // then validation, inlet geometry and flags
-        it.rc = sflow::host_setup(&params[i], B_cent[i], it.hs, it.err, false);
+        // validation, inlet geometry and flags
+        it.rc = sflow::host_setup(&params[i], B_cent[i], hs, it.err, false);
+      }
+      if (it.rc == SFLOW_OK) {
+        it.run = b->impl->prepare(std::move(hs), q_aos[i], max_steps ? max_steps[i] : 0, &it.rc, &it.err);
+        if (!it.run && it.rc == SFLOW_OK) it.rc = SFLOW_ECUDA;
       }
     } catch (const std::bad_alloc&) {
-      it.hs = HostSetup();
+      it.run.reset();
       it.rc = SFLOW_ENOMEM;
       it.err = "host allocation failed";
     }
@@ -182,6 +188,7 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
   std::condition_variable cv_ready, cv_room;
   int next = 0, taken = 0;
   auto work = [&]() {
+    b->impl->bind_thread();
     for (;;) {
       int i;
       {
@@ -200,15 +207,15 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
       cv_ready.notify_all();
     }
   };
+  b->impl->set_bulk(true);
   std::vector<std::thread> pool;
   try {
     for (int t = 0; t < nt; ++t) pool.emplace_back(work);
   } catch (const std::exception&) {
-    // fewer threads than asked (at worst none: the set-ups are made below)
+    // fewer threads than asked (at worst none: the runs are made below)
   }
   int first_rc = SFLOW_OK;
   std::string first_err;
-  b->impl->set_bulk(true);
   for (int32_t i = 0; i < n; ++i) {
     Item it;
     if (pool.empty()) {
@@ -225,7 +232,7 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
     std::string err = it.err;
     if (rc == SFLOW_OK) {
       int id = -1;
-      rc = b->impl->submit(std::move(it.hs), q_aos[i], max_steps ? max_steps[i] : 0, &id);
+      rc = b->impl->commit(std::move(it.run), &id);
       if (rc < 0) err = b->impl->error();
       else run_ids[i] = id;
     }
@@ -234,8 +241,8 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
       first_err = "run " + std::to_string(i) + ": " + err;
     }
   }
-  b->impl->set_bulk(false);
   for (auto& t : pool) t.join();
+  b->impl->set_bulk(false);
   if (first_rc != SFLOW_OK) return fail(first_rc, first_err);
   return SFLOW_OK;
 }

@@ -1,6 +1,7 @@
 // sflow_host.h -- host-side set-up shared by the FP64 and FP32 solvers.
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -121,15 +122,29 @@ class SolverBase {
 SolverBase* make_solver_fp64(const HostSetup& s, std::string& err);
 SolverBase* make_solver_fp32(const HostSetup& s, std::string& err);
 
+// A batched run whose device state is built but which has not joined the
+// batch yet (BatchBase::prepare / commit).
+struct PreparedRun {
+  virtual ~PreparedRun() {}
+};
+
 // Many independent runs advanced together (sflow_batch.cuh).
 class BatchBase {
  public:
   virtual ~BatchBase() {}
+  // sflow_batch_submit_many: prepare() builds a run's device state and may
+  // run on several threads at once (each first calls bind_thread() to
+  // select the batch's device); commit() admits prepared runs in order on
+  // the submitting thread.  A prepared run that is not admitted (SFLOW_EBUSY
+  // and the like) is released with its unique_ptr.
+  virtual std::unique_ptr<PreparedRun> prepare(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* rc,
+                                               std::string* err) = 0;
+  virtual int commit(std::unique_ptr<PreparedRun> pr, int* id) = 0;
+  virtual void bind_thread() = 0;
   // takes hs over (its host arrays move into the run)
   virtual int submit(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* id) = 0;
-  // bulk admission (sflow_batch_submit_many): the free device memory is
-  // queried once and tracked across the submits while on, re-queried
-  // every 32 admissions and whenever the estimate nears the run's need
+  // start (on) or end of a bulk submission: prepare() then tracks the free
+  // device memory across its builds from one fresh query
   virtual void set_bulk(bool on) = 0;
   virtual int advance(int64_t steps, int* finished) = 0;
   // the same with the device time of the steps (CUDA events across the

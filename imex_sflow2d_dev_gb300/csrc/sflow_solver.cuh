@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
@@ -93,19 +94,21 @@ __global__ void k_plane_to_pitched(const double* __restrict__ src, R* __restrict
 // per device.  SFLOW_HOST_READS=0 in the environment turns the direct
 // reads off (uploads then go through the staging buffer).
 inline bool pageable_access(int dev) {
-  static int cached[64];   // 0 unknown, 1 no, 2 yes
+  static std::atomic<int> cached[64];   // 0 unknown, 1 no, 2 yes (any thread)
   if (dev < 0 || dev >= 64) return false;
   const char* env = std::getenv("SFLOW_HOST_READS");
   if (env && env[0] == '0') return false;
-  if (!cached[dev]) {
+  int c = cached[dev].load(std::memory_order_relaxed);
+  if (!c) {
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
       cudaGetLastError();
       v = 0;
     }
-    cached[dev] = v ? 2 : 1;
+    c = v ? 2 : 1;
+    cached[dev].store(c, std::memory_order_relaxed);
   }
-  return cached[dev] == 2;
+  return c == 2;
 }
 inline bool pageable_access() {
   int dev = 0;
