@@ -58,7 +58,9 @@ class Batch : public BatchBase {
     uint8_t* tile_seed = nullptr;  // per-tile seed flags
     int64_t tiles = 0;
     int ns = 0;
-    double max_dt = 0.0;
+    double max_dt = 0.0, t_end = 0.0;
+    int64_t max_steps = 0;
+    const double* q_pending = nullptr;   // q still to upload (admit does it)
     ~Prepared() override {
       if (cand) cudaFree(cand);
       if (tile_seed) cudaFree(tile_seed);
@@ -88,18 +90,25 @@ class Batch : public BatchBase {
   // Builds the run's device state: solver, upload of q, limits, the
   // candidate and seed flags.  Touches no table of the batch, so worker
   // threads may run it for different runs at once.
+  // defer_upload leaves the upload of q (and the limits) to admit(): the
+  // device reads pageable host memory fastest from one thread at a time
   std::unique_ptr<Prepared> build(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* rc,
-                                  std::string& err) const {
+                                  std::string& err, bool defer_upload = false) const {
     std::unique_ptr<Prepared> pr(new Prepared());
     pr->ns = hs.ns;
     pr->max_dt = hs.p.max_dt;
+    pr->t_end = hs.p.t_end;
+    pr->max_steps = max_steps;
     pr->tiles = run_tiles(hs);
-    const double t_end = hs.p.t_end;
     pr->sv.reset(new Solver<R>(std::move(hs), tile_h_));
     Solver<R>& sv = *pr->sv;
     *rc = sv.init();
-    if (*rc == SFLOW_OK) *rc = sv.upload(q_aos);
-    if (*rc == SFLOW_OK) *rc = sv.limits(t_end, max_steps > 0 ? max_steps : -1);
+    if (*rc == SFLOW_OK && defer_upload) {
+      pr->q_pending = q_aos;
+    } else {
+      if (*rc == SFLOW_OK) *rc = sv.upload(q_aos);
+      if (*rc == SFLOW_OK) *rc = sv.limits(pr->t_end, max_steps > 0 ? max_steps : -1);
+    }
     if (*rc != SFLOW_OK) {
       err = sv.err_;
       return nullptr;
@@ -126,6 +135,14 @@ class Batch : public BatchBase {
   // The run joins the batch: a free slot, list capacity and the memory
   // limit are checked, then its arguments go into the device tables.
   int admit(std::unique_ptr<Prepared> pr, int* id) {
+    if (pr->q_pending) {
+      Solver<R>& sv = *pr->sv;
+      int rc = sv.upload(pr->q_pending);
+      if (rc == SFLOW_OK) rc = sv.limits(pr->t_end, pr->max_steps > 0 ? pr->max_steps : -1);
+      if (rc != SFLOW_OK) { err_ = sv.err_; return rc; }
+      sv.trim_stage();
+      pr->q_pending = nullptr;
+    }
     Group* g = group(pr->ns);
     if (!g) return SFLOW_ECUDA;
     int slot = -1;
@@ -226,7 +243,7 @@ class Batch : public BatchBase {
     if (*rc != SFLOW_OK) return nullptr;
     *rc = reserve_room(run_need(hs, tile_h_), *err);
     if (*rc != SFLOW_OK) return nullptr;
-    return build(std::move(hs), q_aos, max_steps, rc, *err);
+    return build(std::move(hs), q_aos, max_steps, rc, *err, !Solver<R>::is_mapped_host(q_aos));
   }
   int commit(std::unique_ptr<PreparedRun> pr, int* id) override {
     if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }

@@ -404,6 +404,8 @@ class Solver : public SolverBase {
     return cudaGetLastError();
   }
 
+  // host memory the device reads or writes through its own mapping (pinned)
+  static bool is_mapped_host(const void* p) { return mapped_host(p) != nullptr; }
   static const double* mapped_host(const void* p) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
