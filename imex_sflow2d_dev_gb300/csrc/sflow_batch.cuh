@@ -59,8 +59,6 @@ class Batch : public BatchBase {
     int64_t tiles = 0;
     int ns = 0;
     double max_dt = 0.0, t_end = 0.0;
-    int64_t max_steps = 0;
-    const double* q_pending = nullptr;   // q still to upload (admit does it)
     ~Prepared() override {
       if (cand) cudaFree(cand);
       if (tile_seed) cudaFree(tile_seed);
@@ -90,25 +88,18 @@ class Batch : public BatchBase {
   // Builds the run's device state: solver, upload of q, limits, the
   // candidate and seed flags.  Touches no table of the batch, so worker
   // threads may run it for different runs at once.
-  // defer_upload leaves the upload of q (and the limits) to admit(): the
-  // device reads pageable host memory fastest from one thread at a time
   std::unique_ptr<Prepared> build(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* rc,
-                                  std::string& err, bool defer_upload = false) const {
+                                  std::string& err) const {
     std::unique_ptr<Prepared> pr(new Prepared());
     pr->ns = hs.ns;
     pr->max_dt = hs.p.max_dt;
     pr->t_end = hs.p.t_end;
-    pr->max_steps = max_steps;
     pr->tiles = run_tiles(hs);
     pr->sv.reset(new Solver<R>(std::move(hs), tile_h_));
     Solver<R>& sv = *pr->sv;
     *rc = sv.init();
-    if (*rc == SFLOW_OK && defer_upload) {
-      pr->q_pending = q_aos;
-    } else {
-      if (*rc == SFLOW_OK) *rc = sv.upload(q_aos);
-      if (*rc == SFLOW_OK) *rc = sv.limits(pr->t_end, max_steps > 0 ? max_steps : -1);
-    }
+    if (*rc == SFLOW_OK) *rc = sv.upload(q_aos);
+    if (*rc == SFLOW_OK) *rc = sv.limits(pr->t_end, max_steps > 0 ? max_steps : -1);
     if (*rc != SFLOW_OK) {
       err = sv.err_;
       return nullptr;
@@ -135,14 +126,6 @@ class Batch : public BatchBase {
   // The run joins the batch: a free slot, list capacity and the memory
   // limit are checked, then its arguments go into the device tables.
   int admit(std::unique_ptr<Prepared> pr, int* id) {
-    if (pr->q_pending) {
-      Solver<R>& sv = *pr->sv;
-      int rc = sv.upload(pr->q_pending);
-      if (rc == SFLOW_OK) rc = sv.limits(pr->t_end, pr->max_steps > 0 ? pr->max_steps : -1);
-      if (rc != SFLOW_OK) { err_ = sv.err_; return rc; }
-      sv.trim_stage();
-      pr->q_pending = nullptr;
-    }
     Group* g = group(pr->ns);
     if (!g) return SFLOW_ECUDA;
     int slot = -1;
@@ -224,9 +207,15 @@ class Batch : public BatchBase {
       return SFLOW_EBUSY;
     }
     const int64_t need = run_need(hs, tile_h_);
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
-    if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
+    if (bulk_) {
+      // inside sflow_batch_submit_many: the shared estimate of reserve_room
+      rc = reserve_room(need, err_);
+      if (rc != SFLOW_OK) return rc;
+    } else {
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { err_ = "cudaMemGetInfo failed"; return SFLOW_ECUDA; }
+      if ((int64_t)free_b < need + kReserve) { err_ = "not enough free device memory for the run now"; return SFLOW_EBUSY; }
+    }
     if (mem_limit_ > 0 && held_ + need > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
     std::unique_ptr<Prepared> pr = build(std::move(hs), q_aos, max_steps, &rc, err_);
     if (!pr) return rc;
@@ -243,7 +232,7 @@ class Batch : public BatchBase {
     if (*rc != SFLOW_OK) return nullptr;
     *rc = reserve_room(run_need(hs, tile_h_), *err);
     if (*rc != SFLOW_OK) return nullptr;
-    return build(std::move(hs), q_aos, max_steps, rc, *err, !Solver<R>::is_mapped_host(q_aos));
+    return build(std::move(hs), q_aos, max_steps, rc, *err);
   }
   int commit(std::unique_ptr<PreparedRun> pr, int* id) override {
     if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
@@ -251,6 +240,7 @@ class Batch : public BatchBase {
     return admit(std::move(p), id);
   }
   void bind_thread() override { cudaSetDevice(dev_); }
+  bool device_mapped(const void* p) const override { return Solver<R>::is_mapped_host(p); }
 
   // Room on the device for a run built by prepare(): the free memory is
   // queried once per bulk submission, every 32 builds and whenever the
@@ -278,7 +268,7 @@ class Batch : public BatchBase {
 
   void set_bulk(bool on) override {
     std::lock_guard<std::mutex> lk(room_mu_);
-    (void)on;
+    bulk_ = on;
     room_free_ = -1;   // a new bulk submission queries afresh
   }
 
@@ -544,6 +534,7 @@ class Batch : public BatchBase {
   static constexpr int64_t kReserve = (int64_t)1 << 30;   // device memory kept free
   int64_t mem_limit_ = 0;   // cap on the resident runs' device bytes (0: none)
   int64_t held_ = 0;        // device bytes of the resident runs
+  bool bulk_ = false;       // inside sflow_batch_submit_many (set_bulk)
   std::mutex room_mu_;      // reserve_room(), called by prepare() on worker threads
   int64_t room_free_ = -1;  // free device memory: last query minus the needs built since (-1: query)
   int room_since_ = 0;      // builds since that query

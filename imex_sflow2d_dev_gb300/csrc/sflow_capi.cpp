@@ -154,13 +154,14 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
   // Each run is set up on the host and built on the device by a worker
   // (BatchBase::prepare), then admitted in run order by this thread.
   struct Item {
-    std::unique_ptr<sflow::PreparedRun> run;
+    std::unique_ptr<sflow::PreparedRun> run;   // built on the device (pinned q)
+    HostSetup hs;                              // host set-up only (other q)
     int rc = SFLOW_OK;
     std::string err;
     bool ready = false;
   };
   std::vector<Item> items((size_t)n);
-  auto make = [&](int i, Item& it) {
+  auto make = [&](int i, Item& it, bool build) {
     try {
       HostSetup hs;
       if (!B_cent[i] || !q_aos[i]) {
@@ -174,12 +175,15 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
         // validation, inlet geometry and flags
         it.rc = sflow::host_setup(&params[i], B_cent[i], hs, it.err, false);
       }
-      if (it.rc == SFLOW_OK) {
+      if (it.rc == SFLOW_OK && build && b->impl->device_mapped(q_aos[i])) {
         it.run = b->impl->prepare(std::move(hs), q_aos[i], max_steps ? max_steps[i] : 0, &it.rc, &it.err);
         if (!it.run && it.rc == SFLOW_OK) it.rc = SFLOW_ECUDA;
+      } else if (it.rc == SFLOW_OK) {
+        it.hs = std::move(hs);
       }
     } catch (const std::bad_alloc&) {
       it.run.reset();
+      it.hs = HostSetup();
       it.rc = SFLOW_ENOMEM;
       it.err = "host allocation failed";
     }
@@ -198,7 +202,7 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
         i = next++;
       }
       Item tmp;
-      make(i, tmp);
+      make(i, tmp, true);
       {
         std::lock_guard<std::mutex> lk(mu);
         items[(size_t)i] = std::move(tmp);
@@ -219,7 +223,7 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
   for (int32_t i = 0; i < n; ++i) {
     Item it;
     if (pool.empty()) {
-      make(i, it);
+      make(i, it, false);
     } else {
       std::unique_lock<std::mutex> lk(mu);
       cv_ready.wait(lk, [&] { return items[(size_t)i].ready; });
@@ -232,7 +236,8 @@ int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params
     std::string err = it.err;
     if (rc == SFLOW_OK) {
       int id = -1;
-      rc = b->impl->commit(std::move(it.run), &id);
+      rc = it.run ? b->impl->commit(std::move(it.run), &id)
+                  : b->impl->submit(std::move(it.hs), q_aos[i], max_steps ? max_steps[i] : 0, &id);
       if (rc < 0) err = b->impl->error();
       else run_ids[i] = id;
     }

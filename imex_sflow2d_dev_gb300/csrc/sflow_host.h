@@ -141,6 +141,10 @@ class BatchBase {
                                                std::string* err) = 0;
   virtual int commit(std::unique_ptr<PreparedRun> pr, int* id) = 0;
   virtual void bind_thread() = 0;
+  // host memory the device maps (pinned): runs whose q lives there are
+  // built on worker threads; the device reads other host memory fastest
+  // from one thread at a time, so those runs are built by the submitter
+  virtual bool device_mapped(const void* p) const = 0;
   // takes hs over (its host arrays move into the run)
   virtual int submit(HostSetup&& hs, const double* q_aos, int64_t max_steps, int* id) = 0;
   // start (on) or end of a bulk submission: prepare() then tracks the free
