@@ -89,6 +89,15 @@ __global__ void k_plane_to_pitched(const double* __restrict__ src, R* __restrict
   dst[c] = (j < nx) ? (R)src[(int64_t)k * nx + j] : R(0);
 }
 
+// The same for a byte plane (the cell flags).
+static __global__ void k_bytes_to_pitched(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, int nx, int ny,
+                                          int pitch) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)pitch * ny) return;
+  const int j = (int)(c % pitch), k = (int)(c / pitch);
+  dst[c] = (j < nx) ? src[(int64_t)k * nx + j] : (uint8_t)0;
+}
+
 // Whether kernels on `dev` may read and write pageable host memory (a
 // Grace-Blackwell node with address translation services); queried once
 // per device.  SFLOW_HOST_READS=0 in the environment turns the direct
@@ -203,8 +212,15 @@ class Solver : public SolverBase {
       // right after: sizeof(R) * nv >= 8 bytes per cell
       if (hs_.B.size() != (size_t)nx * ny) { err_ = "set-up without topography"; return SFLOW_EINVAL; }
       double* Bp = reinterpret_cast<double*>(rd_);
-      SFLOW_CU(cudaMemcpy2DAsync(Bp, sizeof(double) * pitch_, hs_.B.data(), sizeof(double) * nx,
-                                 sizeof(double) * nx, ny, cudaMemcpyHostToDevice, stream_));
+      if (pageable_access()) {
+        k_plane_to_pitched<double><<<(unsigned)(((size_t)plane_ + 255) / 256), 256, 0, stream_>>>(
+            hs_.B.data(), Bp, nx, ny, pitch_);
+        ++launches_;
+        SFLOW_CU(cudaGetLastError());
+      } else {
+        SFLOW_CU(cudaMemcpy2DAsync(Bp, sizeof(double) * pitch_, hs_.B.data(), sizeof(double) * nx,
+                                   sizeof(double) * nx, ny, cudaMemcpyHostToDevice, stream_));
+      }
       TopoPlanes<R> tp;
       for (int i = 0; i < 8; ++i) tp.p[i] = geo_[i];
       const int64_t n = (int64_t)nx * ny;
@@ -1172,13 +1188,23 @@ class Solver : public SolverBase {
   }
 
   // the flag bytes into their pitched plane (pad columns zero), in order
-  // with the run's stream and finished on return
+  // with the run's stream and finished on return: read by the device from
+  // the host array where it can, else laid out here and copied
   cudaError_t put_flags() {
     const int nx = hs_.nx, ny = hs_.ny;
-    cudaError_t e = cudaMemsetAsync(cflags_, 0, plane_, stream_);
-    if (e == cudaSuccess)
-      e = cudaMemcpy2DAsync(cflags_, pitch_, hs_.cflags.data(), nx, nx, ny, cudaMemcpyHostToDevice, stream_);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+    if (pageable_access()) {
+      k_bytes_to_pitched<<<(unsigned)(((size_t)plane_ + 255) / 256), 256, 0, stream_>>>(hs_.cflags.data(), cflags_,
+                                                                                      nx, ny, pitch_);
+      ++launches_;
+      cudaError_t e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+      return e;
+    }
+    std::vector<uint8_t> f((size_t)plane_, 0);
+    for (int k = 0; k < ny; ++k)
+      for (int j = 0; j < nx; ++j) f[(size_t)k * pitch_ + j] = hs_.cflags[(size_t)k * nx + j];
+    cudaError_t e = cudaStreamSynchronize(stream_);
+    if (e == cudaSuccess) e = cudaMemcpy(cflags_, f.data(), plane_, cudaMemcpyHostToDevice);
     return e;
   }
   cudaError_t put_plane_d(double* dst, const std::vector<double>& src) {
