@@ -156,7 +156,11 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
     ctl->work[0] = 0u;
     ctl->ncells = 0u;
   }
-  for (unsigned r = gt; r < (unsigned)b.max_runs; r += G) {
+  // Three independent loops on disjoint threads so that their latencies
+  // overlap: the candidate expansion on threads 0 .. 9n-1, the dry border
+  // strips on the threads after those, the per-run work (an FP64 cosine per
+  // run) on the last threads of the grid.
+  for (unsigned r = G - 1u - gt; r < (unsigned)b.max_runs; r += G) {
     const BatchRun br = b.runs[r];
     if (!br.live) continue;
     RunState* st = br.st;
@@ -199,7 +203,8 @@ __global__ void __launch_bounds__(kBatchCandThreads) k_b_cand(BatchArgs<R> b) {
   // is a candidate of this step then and must not be listed twice.  Else it
   // is its own candidate (it holds no mass, so it dilates only as a
   // tile_seed tile).
-  for (unsigned k = gt; k < nd; k += G) {
+  const unsigned base = (n * 9u < G) ? n * 9u : 0u;
+  for (unsigned k = (gt >= base) ? gt - base : gt + (G - base); k < nd; k += G) {
     const unsigned long long e = Ld[k];
     const int slot = entry_slot(e);
     const BatchRun& br = b.runs[slot];
