@@ -422,14 +422,15 @@ int sflow_batch_submit_setup_take(sflow_batch* b, sflow_setup* s, const double* 
                                   int32_t* run_id);
 /* n runs at once: params[i], B_cent[i], q_aos[i] and max_steps[i] (NULL:
  * no step limit) as for sflow_batch_submit.  The host set-ups run on
- * `threads` host threads (<= 0: the host's hardware threads, at most 64)
- * while the calling thread uploads, in order, the runs whose set-up is done;
- * at most 2 x threads set-ups are held at a time.  run_ids[i] receives the
- * run id, or -1 when run i was not admitted.  Returns SFLOW_OK when every run
- * was admitted, else the code of the first failure in run order
- * (sflow_last_error names the run); the runs that could be admitted are
- * admitted either way.  The runs give the same results as sequential
- * sflow_batch_submit calls. */
+ * `threads` host threads (<= 0: the host's hardware threads, at most 64),
+ * which also build on the device the runs whose q is in pinned (page-locked)
+ * host memory; the calling thread builds the others and admits every run in
+ * order.  At most 2 x threads runs are held ahead at a time, each only while
+ * the device has room for it.  run_ids[i] receives the run id, or -1 when
+ * run i was not admitted.  Returns SFLOW_OK when every run was admitted,
+ * else the code of the first failure in run order (sflow_last_error names
+ * the run); the runs that could be admitted are admitted either way.  The
+ * runs give the same results as sequential sflow_batch_submit calls. */
 int sflow_batch_submit_many(sflow_batch* b, int32_t n, const SflowParams* params, const double* const* B_cent,
                             const double* const* q_aos, const int64_t* max_steps, int32_t* run_ids,
                             int32_t threads);
