@@ -56,12 +56,15 @@ class Batch : public BatchBase {
     std::unique_ptr<Solver<R>> sv;
     uint32_t* cand = nullptr;      // per-tile candidate flags (zeroed)
     uint8_t* tile_seed = nullptr;  // per-tile seed flags
+    bool flags_owned = false;      // own allocations (else in the solver's)
     int64_t tiles = 0;
     int ns = 0;
     double max_dt = 0.0, t_end = 0.0;
     ~Prepared() override {
-      if (cand) cudaFree(cand);
-      if (tile_seed) cudaFree(tile_seed);
+      if (flags_owned) {
+        if (cand) cudaFree(cand);
+        if (tile_seed) cudaFree(tile_seed);
+      }
     }
   };
 
@@ -97,6 +100,8 @@ class Batch : public BatchBase {
     pr->tiles = run_tiles(hs);
     pr->sv.reset(new Solver<R>(std::move(hs), tile_h_));
     Solver<R>& sv = *pr->sv;
+    sv.reserve_extra(sizeof(uint32_t) * (size_t)pr->tiles);
+    sv.reserve_extra((size_t)pr->tiles);
     *rc = sv.init();
     if (*rc == SFLOW_OK) *rc = sv.upload(q_aos);
     if (*rc == SFLOW_OK) *rc = sv.limits(pr->t_end, max_steps > 0 ? max_steps : -1);
@@ -106,12 +111,20 @@ class Batch : public BatchBase {
     }
     sv.trim_stage();
     const std::vector<uint8_t> ts = sv.tile_seed_host();
-    if (cudaMalloc((void**)&pr->cand, sizeof(uint32_t) * pr->tiles) != cudaSuccess ||
-        cudaMalloc((void**)&pr->tile_seed, ts.size()) != cudaSuccess) {
-      cudaGetLastError();
-      *rc = SFLOW_ENOMEM;
-      err = "cudaMalloc failed";
-      return nullptr;
+    pr->cand = static_cast<uint32_t*>(sv.carve(sizeof(uint32_t) * pr->tiles));
+    pr->tile_seed = static_cast<uint8_t*>(sv.carve(ts.size()));
+    if (!pr->cand || !pr->tile_seed) {
+      // no room left in the run's allocation: allocations of their own
+      pr->cand = nullptr;
+      pr->tile_seed = nullptr;
+      pr->flags_owned = true;
+      if (cudaMalloc((void**)&pr->cand, sizeof(uint32_t) * pr->tiles) != cudaSuccess ||
+          cudaMalloc((void**)&pr->tile_seed, ts.size()) != cudaSuccess) {
+        cudaGetLastError();
+        *rc = SFLOW_ENOMEM;
+        err = "cudaMalloc failed";
+        return nullptr;
+      }
     }
     if (cudaMemsetAsync(pr->cand, 0, sizeof(uint32_t) * pr->tiles, sv.stream()) != cudaSuccess ||
         cudaMemcpyAsync(pr->tile_seed, ts.data(), ts.size(), cudaMemcpyHostToDevice, sv.stream()) != cudaSuccess ||
@@ -138,7 +151,7 @@ class Batch : public BatchBase {
       return SFLOW_EBUSY;
     }
     Solver<R>& sv = *pr->sv;
-    const int64_t bytes = sv.device_bytes() + (int64_t)sizeof(uint32_t) * tiles + tiles;
+    const int64_t bytes = sv.device_bytes() + (pr->flags_owned ? (int64_t)sizeof(uint32_t) * tiles + tiles : 0);
     if (mem_limit_ > 0 && held_ + bytes > mem_limit_) { err_ = "the batch's memory limit is in use"; return SFLOW_EBUSY; }
     if (g->smem_flux < sv.smem_flux()) { err_ = "flux shared memory mismatch"; return SFLOW_EINVAL; }
     Slot& s = g->slots[slot];
@@ -176,6 +189,7 @@ class Batch : public BatchBase {
     s.gen = gen;
     s.cand = pr->cand;
     s.tile_seed = pr->tile_seed;
+    s.flags_owned = pr->flags_owned;
     pr->cand = nullptr;
     pr->tile_seed = nullptr;
     s.tiles = tiles;
@@ -462,13 +476,16 @@ class Batch : public BatchBase {
       err_ = "cudaMemcpy failed";
       return SFLOW_ECUDA;
     }
-    s->solver.reset();
+    if (s->flags_owned) {
+      cudaFree(s->cand);
+      cudaFree(s->tile_seed);
+    }
+    s->solver.reset();   // frees the run's allocation (flags included unless owned)
     held_ -= s->bytes;
     s->bytes = 0;
-    cudaFree(s->cand);
     s->cand = nullptr;
-    cudaFree(s->tile_seed);
     s->tile_seed = nullptr;
+    s->flags_owned = false;
     g->tiles_live -= s->tiles;
     g->tiles_draining += s->tiles;
     g->live -= 1;
@@ -543,6 +560,7 @@ class Batch : public BatchBase {
     std::unique_ptr<Solver<R>> solver;
     uint32_t* cand = nullptr;
     uint8_t* tile_seed = nullptr;
+    bool flags_owned = false;   // cand / tile_seed allocated on their own
     int64_t tiles = 0;
     int64_t bytes = 0;   // device bytes the run holds
     unsigned gen = 0;
@@ -594,11 +612,14 @@ class Batch : public BatchBase {
     void release() {
       if (stream) cudaStreamSynchronize(stream);
       for (auto& s : slots) {
+        if (s.flags_owned) {
+          if (s.cand) cudaFree(s.cand);
+          if (s.tile_seed) cudaFree(s.tile_seed);
+        }
         s.solver.reset();
-        if (s.cand) cudaFree(s.cand);
-        if (s.tile_seed) cudaFree(s.tile_seed);
         s.cand = nullptr;
         s.tile_seed = nullptr;
+        s.flags_owned = false;
       }
       if (graph_exec) cudaGraphExecDestroy(graph_exec);
       if (graph) cudaGraphDestroy(graph);

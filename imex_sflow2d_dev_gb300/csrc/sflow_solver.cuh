@@ -310,7 +310,18 @@ class Solver : public SolverBase {
       b += A(sizeof(R) * P) + A(sizeof(double) * (1 + 2 * (size_t)SFLOW_MAX_INTERVALS));
     if (hs_.n_thk * hs_.n_dyn > 0) b += A(sizeof(uint32_t) * P * (size_t)((hs_.n_thk * hs_.n_dyn + 31) / 32));
     b += A(sizeof(RunState)) + A(sizeof(double) * 4 * 1024) + A(sizeof(double) * 4);
-    return b;
+    return b + extra_bytes_;
+  }
+  // room in the run's allocation for buffers its owner adds after init()
+  // (the batch's per-tile flags): call before init(); carve() hands it out
+  void reserve_extra(size_t bytes) { extra_bytes_ += (bytes + kArenaAlign - 1) / kArenaAlign * kArenaAlign; }
+  void* carve(size_t bytes) {
+    const size_t a = (bytes + kArenaAlign - 1) / kArenaAlign * kArenaAlign;
+    if (!arena_ || arena_used_ + a > arena_cap_) return nullptr;
+    void* p = arena_ + arena_used_;
+    arena_used_ += a;
+    bytes_ += (int64_t)bytes;
+    return p;
   }
 
   // --- used by the batch engine ----------------------------------------------
@@ -988,7 +999,7 @@ class Solver : public SolverBase {
   int nstat_blocks_ = 0;
   std::vector<void*> allocs_;
   char* arena_ = nullptr;   // one allocation carved by alloc()
-  size_t arena_cap_ = 0, arena_used_ = 0;
+  size_t arena_cap_ = 0, arena_used_ = 0, extra_bytes_ = 0;
   int64_t bytes_ = 0, launches_ = 0;
   KArgs<R> ka_;
   size_t smem_flux_ = 0;
