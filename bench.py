@@ -21,9 +21,9 @@ Metric: cell-updates/s = sum over runs and steps of the active cells
   fp64_plain   the same ensemble in the plain FP64 form (same batch
                engine), the same K steps: the same-workload comparator
   e2e          the same ensemble through the C ABI from host buffers:
-               sflow_batch_submit_many of every run (host set-ups on the
-               host's threads, uploads in order),
-               the K steps, sflow_batch_collect with the download of every
+               sflow_batch_submit_many of every run (host set-ups and
+               device builds on the host's threads),
+               the K steps, sflow_batch_collect_many with the download of every
                run's q, host wall clock
   cpu_baseline the oracle (C restatement of the reference time step) built
                with the reference's compiler flags (-fopenmp -Ofast
@@ -447,12 +447,9 @@ def ensemble_e2e(lib, members, K, chunk, tile_h):
     for _ in range(K):
         b.advance(chunk)
     t2 = time.perf_counter()
-    cu = 0
-    out_bytes = 0
-    for rid, o in zip(ids, outs):
-        cu += b.counters(rid)["cell_updates"]
-        q = b.collect(rid, want_q=True, out=o)
-        out_bytes += q.nbytes
+    cu = sum(b.counters(rid)["cell_updates"] for rid in ids)
+    qs_out = b.collect_many(ids, outs=outs)
+    out_bytes = sum(q.nbytes for q in qs_out)
     t3 = time.perf_counter()
     wall = t3 - t0
     b.close()
@@ -460,9 +457,9 @@ def ensemble_e2e(lib, members, K, chunk, tile_h):
     return {"value": cu / wall, "unit": UNIT, "h2d_bytes_per_step": in_bytes / K,
             "d2h_bytes_per_step": out_bytes / K, "seconds": wall, "steps": K,
             "split_s": {"submit": t1 - t0, "steps": t2 - t1, "collect": t3 - t2},
-            "path": "sflow_batch_submit_many (host set-ups on the host's threads, uploads in order) of "
-                    "every run, sflow_batch_advance, sflow_batch_collect with q download; q in and out "
-                    "through pinned host buffers, topography from pageable host arrays; wall clock",
+            "path": "sflow_batch_submit_many (host set-ups and device builds on the host's threads) of "
+                    "every run, sflow_batch_advance, sflow_batch_collect_many with every q downloaded; q in "
+                    "and out through pinned host buffers, topography from pageable host arrays; wall clock",
             "host_threads": os.cpu_count()}
 
 

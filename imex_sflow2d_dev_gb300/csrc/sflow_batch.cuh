@@ -13,9 +13,12 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -500,6 +503,62 @@ class Batch : public BatchBase {
       g->tiles_draining = 0;
     }
     return SFLOW_OK;
+  }
+
+  int collect_many(int n, const int32_t* ids, double* const* q_aos, int threads, int32_t* status) override {
+    if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
+    std::vector<Solver<R>*> sv((size_t)n, nullptr);
+    int first = SFLOW_OK;
+    std::string first_err;
+    auto note = [&](int i, int rc, const std::string& e) {
+      status[i] = rc;
+      if (rc < 0 && first == SFLOW_OK) {
+        first = rc;
+        first_err = "run " + std::to_string(ids[i]) + ": " + e;
+      }
+    };
+    for (int i = 0; i < n; ++i) {
+      status[i] = SFLOW_OK;
+      for (int j = 0; j < i; ++j)
+        if (ids[j] == ids[i]) { note(i, SFLOW_EINVAL, "run id given twice"); break; }
+      if (status[i] != SFLOW_OK) continue;
+      Slot* s = lookup(ids[i]);
+      if (!s) note(i, SFLOW_EINVAL, err_);
+      else sv[(size_t)i] = s->solver.get();
+    }
+    // downloads: independent solvers, their own streams
+    std::vector<int> drc((size_t)n, SFLOW_OK);
+    std::vector<std::string> derr((size_t)n);
+    std::atomic<int> next{0};
+    auto work = [&]() {
+      cudaSetDevice(dev_);
+      for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+        if (!sv[(size_t)i] || !q_aos || !q_aos[i]) continue;
+        drc[(size_t)i] = sv[(size_t)i]->download(q_aos[i]);
+        if (drc[(size_t)i] != SFLOW_OK) derr[(size_t)i] = sv[(size_t)i]->error();
+      }
+    };
+    const int nt = std::max(1, std::min(threads > 0 ? threads : (int)std::thread::hardware_concurrency(),
+                                        std::min(n, 64)));
+    std::vector<std::thread> pool;
+    try {
+      for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    } catch (const std::exception&) {
+      // fewer threads: this one takes the rest
+    }
+    work();
+    for (auto& t : pool) t.join();
+    for (int i = 0; i < n; ++i) {
+      if (!sv[(size_t)i]) continue;
+      if (drc[(size_t)i] != SFLOW_OK) {
+        note(i, drc[(size_t)i], derr[(size_t)i]);
+        continue;
+      }
+      const int rc = collect(ids[i], nullptr);
+      if (rc != SFLOW_OK) note(i, rc, err_);
+    }
+    if (first != SFLOW_OK) err_ = first_err;
+    return first;
   }
 
   int download(int id, double* q_aos) override {

@@ -268,6 +268,17 @@ int sflow_batch_submit_setup_take(sflow_batch* b, sflow_setup* s, const double* 
   return SFLOW_OK;
 }
 
+int sflow_batch_collect_many(sflow_batch* b, int32_t n, const int32_t* ids, double* const* q_aos, int32_t threads,
+                             int32_t* status) {
+  BATCH_CHECK(b);
+  if (n < 0) return fail(SFLOW_EINVAL, "n must be >= 0");
+  if (n > 0 && (!ids || !status)) return fail(SFLOW_EINVAL, "NULL argument");
+  if (n == 0) return SFLOW_OK;
+  const int rc = b->impl->collect_many(n, ids, q_aos, threads, status);
+  if (rc < 0) return fail(rc, b->impl->error());
+  return SFLOW_OK;
+}
+
 int sflow_batch_launch(sflow_batch* b, int64_t steps) {
   BATCH_CHECK(b);
   if (steps < 0) return fail(SFLOW_EINVAL, "steps must be >= 0");

@@ -164,6 +164,9 @@ class BatchBase {
   virtual int border_updates(int id, int64_t* n) = 0;
   virtual int download(int id, double* q_aos) = 0;
   virtual int collect(int id, double* q_aos) = 0;
+  // collect() of n runs: the downloads on `threads` host threads (each run
+  // on its own stream), the slots freed in order; status[i] per run
+  virtual int collect_many(int n, const int32_t* ids, double* const* q_aos, int threads, int32_t* status) = 0;
   virtual int live() const = 0;
   virtual int64_t launches() const = 0;
   virtual int tile_shape() const = 0;

@@ -103,6 +103,7 @@ def load(build_if_missing=True):
         "sflow_setup_destroy": (None, [vp]),
         "sflow_batch_submit_setup": (C.c_int, [vp, vp, dp, i64, C.POINTER(i32)]),
         "sflow_batch_submit_setup_take": (C.c_int, [vp, vp, dp, i64, C.POINTER(i32)]),
+        "sflow_batch_collect_many": (C.c_int, [vp, i32, C.POINTER(i32), C.POINTER(dp), i32, C.POINTER(i32)]),
         "sflow_batch_submit_many": (C.c_int, [vp, i32, P, C.POINTER(dp), C.POINTER(dp), C.POINTER(i64),
                                                C.POINTER(i32), i32]),
         "sflow_batch_launch": (C.c_int, [vp, i64]),
@@ -153,6 +154,7 @@ def exported_symbols():
             "sflow_batch_set_tile_shape", "sflow_batch_get_tile_shape", "sflow_check_conversions",
             "sflow_eval_math", "sflow_batch_advance_timed", "sflow_batch_profile_kernels",
             "sflow_setup_create", "sflow_setup_destroy", "sflow_batch_submit_setup", "sflow_batch_submit_many", "sflow_batch_submit_setup_take",
+            "sflow_batch_collect_many",
             "sflow_batch_launch", "sflow_batch_wait", "sflow_batch_dry_border_updates",
             "sflow_dry_border_updates", "sflow_download_erosion", "sflow_download_erodible",
             "sflow_set_erodible", "sflow_download_topography", "sflow_set_nodata",
@@ -764,6 +766,31 @@ class Batch:
         _check(self.lib.sflow_batch_collect(self.h, rid, _dp(out) if want_q else None))
         del self._shape[rid]
         return out
+
+    def collect_many(self, rids, outs=None, want_q=True, threads=0):
+        """collect() of several runs at once (sflow_batch_collect_many: the
+        downloads on host threads).  outs: optional arrays (one per run) to
+        receive q.  Returns the q arrays (None where want_q is False); a
+        failure raises SflowError."""
+        n = len(rids)
+        m = max(n, 1)
+        ids = (C.c_int32 * m)(*[int(r) for r in rids])
+        ptrs = (C.POINTER(C.c_double) * m)()
+        res = []
+        for i, rid in enumerate(rids):
+            if want_q:
+                o = self._out(rid, outs[i] if outs is not None else None)
+                ptrs[i] = _dp(o)
+                res.append(o)
+            else:
+                res.append(None)
+        status = (C.c_int32 * m)()
+        rc = self.lib.sflow_batch_collect_many(self.h, n, ids, ptrs if want_q else None, int(threads), status)
+        for i, rid in enumerate(rids):
+            if status[i] == 0:
+                self._shape.pop(rid, None)
+        _check(rc)
+        return res
 
     def _out(self, rid, out):
         if out is None:

@@ -420,6 +420,14 @@ int sflow_batch_submit_setup(sflow_batch* b, const sflow_setup* s, const double*
  * be submitted again; after a device failure it is spent. */
 int sflow_batch_submit_setup_take(sflow_batch* b, sflow_setup* s, const double* q_aos, int64_t max_steps,
                                   int32_t* run_id);
+/* sflow_batch_collect of n runs: q_aos[i] receives run ids[i]'s q (q_aos
+ * NULL or q_aos[i] NULL: no download); the downloads run on `threads` host
+ * threads (<= 0: the host's hardware threads, at most 64), the slots are
+ * freed in order.  status[i] receives each run's result; returns SFLOW_OK or
+ * the first failure (sflow_last_error names the run id); a run whose
+ * download failed is not collected. */
+int sflow_batch_collect_many(sflow_batch* b, int32_t n, const int32_t* ids, double* const* q_aos, int32_t threads,
+                             int32_t* status);
 /* n runs at once: params[i], B_cent[i], q_aos[i] and max_steps[i] (NULL:
  * no step limit) as for sflow_batch_submit.  The host set-ups run on
  * `threads` host threads (<= 0: the host's hardware threads, at most 64),

@@ -431,3 +431,25 @@ def test_submit_setup_take_hands_the_setup_over_once():
     s2.close()
     b.close()
     ref.close()
+
+
+def test_collect_many_equals_collect():
+    """sflow_batch_collect_many (downloads on host threads) returns what a
+    collect of each run returns, frees the slots, and names a bad id."""
+    runs = _mix()
+    a = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 22)
+    b = L.Batch(PREC_FP64, max_runs=8, max_cells=1 << 22)
+    ia = [a.submit(p, B, W.to_aos(q)) for p, B, q in runs]
+    ib = [b.submit(p, B, W.to_aos(q)) for p, B, q in runs]
+    a.advance(30)
+    b.advance(30)
+    ref = [a.collect(r) for r in ia]
+    got = b.collect_many(ib, threads=3)
+    for x, y in zip(got, ref):
+        np.testing.assert_array_equal(x, y)
+    assert b.live() == 0
+    with pytest.raises(L.SflowError) as ei:
+        b.collect_many([ib[0]])                  # already collected
+    assert str(ib[0]) in str(ei.value)
+    a.close()
+    b.close()
