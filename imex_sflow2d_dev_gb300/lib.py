@@ -778,12 +778,12 @@ class Batch:
         ptrs = (C.POINTER(C.c_double) * m)()
         res = []
         for i, rid in enumerate(rids):
-            if want_q:
+            if want_q and rid in self._shape:
                 o = self._out(rid, outs[i] if outs is not None else None)
                 ptrs[i] = _dp(o)
                 res.append(o)
             else:
-                res.append(None)
+                res.append(None)   # no download (an unknown id is reported by the call)
         status = (C.c_int32 * m)()
         rc = self.lib.sflow_batch_collect_many(self.h, n, ids, ptrs if want_q else None, int(threads), status)
         for i, rid in enumerate(rids):
