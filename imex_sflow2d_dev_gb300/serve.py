@@ -11,7 +11,8 @@ otherwise hands the prepared host arrays to the run without a copy -- launches
 `chunk` batch steps of every resident run (one CUDA-graph replay per
 solid-class count, the groups on their own streams; sflow_batch_launch
 returns at once), waits for the device (sflow_batch_wait; the worker
-threads keep preparing meanwhile) and collects the runs that have stopped.
+threads keep preparing meanwhile) and collects the runs that have stopped
+(sflow_batch_collect_many).
 A request that arrives while others are on the GPU joins them at the next
 chunk boundary; its state stays resident until it is collected.
 
@@ -99,13 +100,14 @@ class RequestLoop:
                 self.batch.launch(self.chunk)
                 finished = self.batch.wait()
                 if finished:
-                    for bid in [b for b in live if self.batch.done(b)]:
+                    done = [b for b in live if self.batch.done(b)]
+                    stats = [(self.batch.counters(b), self.batch.poll(b)[0]) for b in done]
+                    qs = self.batch.collect_many(done, want_q=self.keep)
+                    t_fin = time.perf_counter() - t0
+                    for bid, (c, st), q in zip(done, stats, qs):
                         r = live.pop(bid)
-                        c = self.batch.counters(bid)
-                        st, _ = self.batch.poll(bid)
-                        q = self.batch.collect(bid, want_q=self.keep)
                         rec = recs[r.rid]
-                        rec["finished_s"] = time.perf_counter() - t0
+                        rec["finished_s"] = t_fin
                         rec["tts_s"] = rec["finished_s"] - r.arrival_s
                         rec["steps"] = c["steps"]
                         rec["cell_updates"] = c["cell_updates"]
