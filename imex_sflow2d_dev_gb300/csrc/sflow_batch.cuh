@@ -446,11 +446,11 @@ class Batch : public BatchBase {
     if (launched_) { err_ = "steps are in flight: wait first"; return SFLOW_ESTATE; }
     Slot* s = lookup(id);
     if (!s) return SFLOW_EINVAL;
-    SflowStepStats st;
-    int rc = s->solver->stats(&st);
+    RunState h;
+    int rc = s->solver->run_state(&h);
     if (rc != SFLOW_OK) { err_ = s->solver->error(); return rc; }
-    if (cells) *cells = s->solver->cells_total();
-    if (steps) *steps = st.steps;
+    if (cells) *cells = h.cells_total;
+    if (steps) *steps = h.steps;
     return SFLOW_OK;
   }
 

@@ -964,6 +964,12 @@ class Solver : public SolverBase {
     return SFLOW_OK;
   }
   const char* error() const override { return err_.c_str(); }
+  // the run's device state record (clock, counters, status), one copy
+  int run_state(RunState* h) {
+    SFLOW_CU(cudaMemcpyAsync(h, st_, sizeof(RunState), cudaMemcpyDeviceToHost, stream_));
+    SFLOW_CU(cudaStreamSynchronize(stream_));
+    return SFLOW_OK;
+  }
   int64_t cells_total() override {
     RunState h;
     if (cudaMemcpy(&h, st_, sizeof(RunState), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
