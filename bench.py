@@ -661,13 +661,23 @@ def served_leg(lib, n_requests, rate, probe_steps, tile_h=None):
     arr = W.poisson_arrivals(n_requests, rate)
     reqs = [S.Request(i, arr[i], p, B, q, st, kind) for i, (p, B, q, st, kind) in enumerate(jobs)]
     cells = sum(p.comp_cells_x * p.comp_cells_y for p, *_ in jobs)
+    tuned = None
+    if tile_h is None:
+        # the stream's own tile height, tuned on every 8th job (untimed)
+        from imex_sflow2d_dev_gb300 import autotune as A
+        t0 = time.perf_counter()
+        sample = [(p, B, W.to_aos(q)) for p, B, q, _, _ in jobs[::8]]
+        tile_h, rates = A.tune_batch(PREC_FP32, sample, steps=128, warm=256)
+        tuned = {"tile_h": tile_h, "cell_updates_per_s": {str(k): v for k, v in rates.items()},
+                 "sample": f"{len(sample)} jobs (every 8th), 256 + 128 batch steps per height",
+                 "seconds": time.perf_counter() - t0}
     loop = S.RequestLoop(PREC_FP32, max_runs=64, max_cells=int(cells * 1.2) + 4096, chunk=16,
                          tile_h=tile_h)
     recs = loop.run(reqs)
     launches = loop.batch.launch_count()
     loop.close()
     out = S.summarize(recs)
-    out.update({"rate_per_s": rate, "gpu_launches": launches, "tile_h": tile_h or 8})
+    out.update({"rate_per_s": rate, "gpu_launches": launches, "tile_h": tile_h or 8, "autotune": tuned})
     # one job at a time, plain FP64 form
     t0 = time.perf_counter()
     service = []
@@ -865,7 +875,8 @@ def run_gb300(args, d):
         log(f"large {large['fp32']['value']:.3e}")
     srv = None
     if d.rank == 0 and args.served_requests > 0:
-        srv = served_leg(lib, args.served_requests, args.served_rate, args.served_probe_steps, tile_h=th)
+        srv = served_leg(lib, args.served_requests, args.served_rate, args.served_probe_steps,
+                         tile_h=args.tile_h or (None if args.tune_steps > 0 else 8))
         log(f"served p50 {srv['p50_s']:.2f} p99 {srv['p99_s']:.2f}")
 
     if d.rank == 0:
