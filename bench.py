@@ -663,13 +663,24 @@ def served_leg(lib, n_requests, rate, probe_steps, tile_h=None):
     cells = sum(p.comp_cells_x * p.comp_cells_y for p, *_ in jobs)
     tuned = None
     if tile_h is None:
-        # the stream's own tile height, tuned on every 8th job (untimed)
+        # the stream's own tile height (untimed), tuned on the jobs that
+        # carry most of its work: the largest by cells x steps, up to half
+        # of the stream's cell-steps (at most 12 jobs)
         from imex_sflow2d_dev_gb300 import autotune as A
         t0 = time.perf_counter()
-        sample = [(p, B, W.to_aos(q)) for p, B, q, _, _ in jobs[::8]]
-        tile_h, rates = A.tune_batch(PREC_FP32, sample, steps=128, warm=1000)
+        work = [p.comp_cells_x * p.comp_cells_y * st for p, _, _, st, _ in jobs]
+        order = sorted(range(len(jobs)), key=lambda i: -work[i])
+        pick, acc = [], 0
+        for i in order:
+            if acc >= 0.5 * sum(work) or len(pick) >= 12:
+                break
+            pick.append(i)
+            acc += work[i]
+        sample = [(jobs[i][0], jobs[i][1], W.to_aos(jobs[i][2])) for i in pick]
+        tile_h, rates = A.tune_batch(PREC_FP32, sample, steps=64, warm=256)
         tuned = {"tile_h": tile_h, "cell_updates_per_s": {str(k): v for k, v in rates.items()},
-                 "sample": f"{len(sample)} jobs (every 8th), 1000 + 128 batch steps per height",
+                 "sample": f"the {len(sample)} largest jobs ({acc / sum(work):.0%} of the stream's cell-steps), "
+                           "256 + 64 batch steps per height",
                  "seconds": time.perf_counter() - t0}
     loop = S.RequestLoop(PREC_FP32, max_runs=64, max_cells=int(cells * 1.2) + 4096, chunk=16,
                          tile_h=tile_h)
