@@ -546,7 +546,10 @@ class Batch : public BatchBase {
     } catch (const std::exception&) {
       // fewer threads: this one takes the rest
     }
-    work();
+    int prev_dev = dev_;
+    if (cudaGetDevice(&prev_dev) != cudaSuccess) cudaGetLastError();
+    work();   // this thread too (it selects the batch's device meanwhile)
+    cudaSetDevice(prev_dev);
     for (auto& t : pool) t.join();
     for (int i = 0; i < n; ++i) {
       if (!sv[(size_t)i]) continue;
