@@ -68,11 +68,18 @@ def tune_batch(precision, members, steps=128, warm=16, heights=None, max_cells=N
             rates[th] = (c1 - c0) / (ms * 1e-3) if ms > 0 else 0.0
         finally:
             b.close()
+    return choose(heights, rates, margin), rates
+
+
+def choose(heights, rates, margin=0.02):
+    """The height to keep from measured rates (higher is better): the first
+    height (the default) unless a later one beats the best so far by more
+    than `margin`."""
     best = heights[0]
     for th in heights[1:]:
         if rates[th] > rates[best] * (1.0 + margin):
             best = th
-    return best, rates
+    return best
 
 
 class TuneCache:
